@@ -1,0 +1,300 @@
+"""Benchmark: Lloyd k-means iterations/s on one GB300 (headline), with the
+plain kNN self-join queries/s alongside.
+
+Workload (one "step" = one complete Lloyd k-means call): n=70,000, d=784,
+k=64, each coordinate 0 with probability 0.8 else U{1..255}/255 (synthetic
+stand-in for MNIST), init = 64 seeded distinct rows, 100 fixed iterations.
+The input matrix (219.5 MB) is larger than the 129 MB L2, so no explicit L2
+flush is needed between steps.
+
+Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+Under torchrun (N>1) each rank runs an independent replica ("replicas only";
+the path is a single-device engine) and rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "k-means Lloyd iters/s & kNN queries/s: TC+refine vs plain FP32, 1 GB300; p99"
+N, D, K, ITERS = 70_000, 784, 64, 100
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "_fallback": True}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_lloyd_sample(X, init, iters, threads):
+    """fuel's CPU Lloyd (restated, f32 running sums, host summation order) on
+    the full matrix for a bounded number of iterations; returns seconds."""
+    from oracle import oracle
+    t0 = time.perf_counter()
+    oracle.lloyd(X, K, init, max_iter=iters, order=oracle.host_order(), threads=threads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from fuel_gb300 import workloads
+    from oracle import oracle
+    oracle.build()
+    X, init = workloads.lloyd_sparse(N, D, K)
+    threads = os.cpu_count() or 1
+    sample_iters = 3
+    for _ in range(args.warmup):
+        cpu_lloyd_sample(X, init, sample_iters, threads)
+    times = [cpu_lloyd_sample(X, init, sample_iters, threads) for _ in range(args.steps)]
+    tot = sum(times)
+    value = sample_iters * len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"lloyd k={K} n={N} d={D}", "n": N, "d": D, "k": K,
+                   "sample": f"{sample_iters} Lloyd iterations of the full matrix per step"},
+        "cpu_baseline": {"value": value, "unit": "iters/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample_iters} iterations x {args.steps} steps, restated fuel CPU Lloyd "
+                                   f"(f32 running sums, {oracle.host_order()} summation order)"},
+        "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    from fuel_gb300 import _lib, build, workloads
+
+    world, rank, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+        torch.cuda.set_device(local)
+    build.build()
+    lib = _lib.load()
+    prec = _lib.PRECISION[args.precision]
+    order = _lib.ORDER[_lib.default_order()]
+
+    X, init = workloads.lloyd_sparse(N, D, K)
+    Xd = torch.from_numpy(X).cuda()
+    Cd = torch.from_numpy(init).cuda()
+    oc = torch.empty((K, D), dtype=torch.float32, device="cuda")
+    ol = torch.empty((N,), dtype=torch.int64, device="cuda")
+    # pinned host copies for the end-to-end leg
+    Xh = torch.empty((N, D), dtype=torch.float32, pin_memory=True)
+    Xh.copy_(torch.from_numpy(X))
+    Ch = torch.empty((K, D), dtype=torch.float32, pin_memory=True)
+    Ch.copy_(torch.from_numpy(init))
+    och = torch.empty((K, D), dtype=torch.float32, pin_memory=True)
+    olh = torch.empty((N,), dtype=torch.int64, pin_memory=True)
+
+    def step(device_resident=True):
+        st = _lib.Stats()
+        it = ctypes.c_int32()
+        inert = ctypes.c_double()
+        src = (Xd, Cd, oc, ol) if device_resident else (Xh, Ch, och, olh)
+        _lib.check(lib.fuelg_kmeans_lloyd(_lib.ptr(src[0]), N, D, K, _lib.ptr(src[1]), ITERS, 0.0, prec, order,
+                                          _lib.LLOYD_FIXED_ITERS, _lib.ptr(src[2]), _lib.ptr(src[3]),
+                                          ctypes.byref(it), ctypes.byref(inert), ctypes.byref(st)))
+        assert it.value == ITERS
+        return st, inert.value
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step(True)
+    barrier()
+    with ClockSampler(local) as clk:
+        stats = [step(True) for _ in range(args.steps)]
+    barrier()
+    dev_ms = sum(s.device_ms for s, _ in stats)
+    hot_ms = sum(s.hot_kernel_ms for s, _ in stats)
+    hot_n = sum(s.hot_kernel_launches for s, _ in stats)
+    launches = sum(s.kernel_launches for s, _ in stats)
+    inertia = stats[-1][1]
+
+    # end-to-end through the C ABI with pinned host buffers (copies inside the timed call)
+    for _ in range(max(1, args.warmup // 2)):
+        step(False)
+    barrier()
+    e2e = [step(False) for _ in range(args.steps)]
+    barrier()
+    e2e_ms = sum(s.device_ms for s, _ in e2e)
+    h2d = e2e[0][0].h2d_bytes
+    d2h = e2e[0][0].d2h_bytes
+
+    t_max = dev_ms
+    e2e_max = e2e_ms
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([dev_ms, e2e_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max, e2e_max = float(t[0]), float(t[1])
+    if rank != 0:
+        return
+
+    pk = peaks()
+    value = world * ITERS * args.steps / (t_max / 1e3)
+    e2e_value = world * ITERS * args.steps / (e2e_max / 1e3)
+    # roofline of the hot kernel (the assignment scan): algorithmic bytes per launch =
+    # one read of X (n*d*4) + the centres (k*d*4) + one 8-byte key per point.
+    alg_bytes = N * D * 4 + K * D * 4 + N * 8
+    avg_launch_ms = hot_ms / max(1, hot_n)
+    achieved = alg_bytes / (avg_launch_ms / 1e3) / 1e9
+    hbm_peak = pk.get("hbm_gbs", 6800.0)
+
+    # kNN plain self-join (n=20,000, d=16, k=10) queries/s, device-resident, plain FP32
+    knn = knn_plain_rate(lib, _lib, torch, args)
+
+    # CPU baseline: restated fuel CPU Lloyd on the host cores, bounded sample
+    threads = os.cpu_count() or 1
+    sample_iters = 2
+    cpu_t = cpu_lloyd_sample(X, init, sample_iters, threads)
+    cpu_value = sample_iters / cpu_t
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"lloyd k={K} n={N} d={D}, {ITERS} fixed iterations per step", "n": N, "d": D,
+                   "k": K, "iters_per_step": ITERS, "precision": args.precision,
+                   "summation_order": _lib.default_order(),
+                   "l2": "inputs (219.5 MB) larger than L2; no flush", "parallelism": "replicas"},
+        "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "kernel": "scan_topk_kernel (Lloyd assignment)",
+                     "avg_launch_ms": avg_launch_ms, "peak_source": "measured" if "_fallback" not in pk else
+                     "fallback"},
+        "cpu_baseline": {"value": cpu_value, "unit": "iters/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample_iters} iterations of the full n={N} matrix, restated fuel CPU Lloyd"},
+        "clocks": clk.summary(),
+        "inertia": inertia,
+        "knn_plain": knn,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def knn_plain_rate(lib, _lib, torch, args):
+    from fuel_gb300 import workloads
+    X = workloads.knn_plain()
+    n, d, k = X.shape[0], X.shape[1], 10
+    h = ctypes.c_void_p()
+    _lib.check(lib.fuelg_index_create(_lib.ptr(X), n, d, 0, _lib.ORDER[_lib.default_order()], ctypes.byref(h)))
+    try:
+        Qd = torch.from_numpy(X).cuda()
+        oi = torch.empty((n, k), dtype=torch.int64, device="cuda")
+        od = torch.empty((n, k), dtype=torch.float32, device="cuda")
+        ms = []
+        hot = []
+        for i in range(args.warmup + args.steps):
+            st = _lib.Stats()
+            _lib.check(lib.fuelg_knn(h, _lib.ptr(Qd), n, k, 1, 0, _lib.ptr(oi), _lib.ptr(od), ctypes.byref(st)))
+            if i >= args.warmup:
+                ms.append(st.device_ms)
+                hot.append(st.hot_kernel_ms / max(1, st.hot_kernel_launches))
+        t = sum(ms) / len(ms)
+        return {"workload": "knn self-join n=20000 d=16 k=10 sqeuclidean", "queries_per_s": n / (t / 1e3),
+                "ms_per_call": t, "distance_evals_per_s": n * n / (t / 1e3), "hot_kernel_ms": sum(hot) / len(hot),
+                "precision": "fp32"}
+    finally:
+        lib.fuelg_index_destroy(h)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="fp32")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,565 @@
+// fuelg_api.cu -- the C ABI (include/fuelg.h): handles, staging of host
+// buffers, status codes, cancellation and per-call measurements.
+#include <cstdarg>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/fuelg.h"
+#include "fuelg_common.cuh"
+#include "fuelg_internal.h"
+
+namespace fuelg {
+
+namespace {
+thread_local std::string g_err;
+thread_local int64_t g_launches = 0;
+thread_local HotTimer* g_hot = nullptr;
+std::mutex g_cancel_mu;
+int* g_cancel_host = nullptr;  // pinned + mapped
+int* g_cancel_dev = nullptr;
+}  // namespace
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+}
+const char* last_error() { return g_err.c_str(); }
+void note_launch(int count) { g_launches += count; }
+int64_t launch_count() { return g_launches; }
+HotTimer*& hot_timer() { return g_hot; }
+
+static int ensure_cancel_word() {
+  std::lock_guard<std::mutex> lk(g_cancel_mu);
+  if (g_cancel_host) return ST_OK;
+  int* h = nullptr;
+  cudaError_t e = cudaHostAlloc(&h, sizeof(int), cudaHostAllocMapped | cudaHostAllocPortable);
+  if (e != cudaSuccess) {
+    set_error("cannot allocate the cancel word: %s", cudaGetErrorString(e));
+    return ST_ECUDA;
+  }
+  *h = 0;
+  int* dptr = nullptr;
+  e = cudaHostGetDevicePointer(&dptr, h, 0);
+  if (e != cudaSuccess) {
+    cudaFreeHost(h);
+    set_error("cannot map the cancel word: %s", cudaGetErrorString(e));
+    return ST_ECUDA;
+  }
+  g_cancel_dev = dptr;
+  g_cancel_host = h;
+  return ST_OK;
+}
+int* cancel_word_device() { return g_cancel_dev; }
+bool cancel_requested() { return g_cancel_host && *(volatile int*)g_cancel_host; }
+
+__global__ void widen_labels_kernel(const int32_t* __restrict__ a, int64_t* __restrict__ b, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) b[i] = a[i];
+}
+void widen_labels(const int32_t* a, int64_t* b, int64_t n, cudaStream_t s) {
+  if (n > 0) widen_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, b, n); ::fuelg::note_launch();
+}
+
+}  // namespace fuelg
+
+using namespace fuelg;
+
+struct fuelg_index {
+  int device = 0;
+  int64_t n = 0;
+  int32_t d = 0;
+  int32_t metric = 0;
+  int32_t order = 0;
+  float* X = nullptr;  // device copy [n, d]
+  cudaStream_t stream = nullptr;
+  std::mutex mu;  // calls on one handle are serialised
+};
+
+struct fuelg_range_result {
+  int64_t m = 0, total = 0;
+  int64_t* off = nullptr;  // device
+  int64_t* idx = nullptr;
+  float* dist = nullptr;
+};
+
+namespace {
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// A read-only input view: device pointer used in place, host pointer staged.
+struct InBuf {
+  const void* dptr = nullptr;
+  Scratch own;
+  int64_t h2d = 0;
+  int init(const void* src, size_t bytes, cudaStream_t s) {
+    if (bytes == 0) {
+      dptr = nullptr;
+      return ST_OK;
+    }
+    if (is_device_ptr(src)) {
+      dptr = src;
+      return ST_OK;
+    }
+    FUELG_TRY(own.alloc(bytes, s));
+    FUELG_CUDA(cudaMemcpyAsync(own.p, src, bytes, cudaMemcpyHostToDevice, s));
+    dptr = own.p;
+    h2d = (int64_t)bytes;
+    return ST_OK;
+  }
+};
+
+// An output view: device pointer written in place, host pointer written back.
+struct OutBuf {
+  void* user = nullptr;
+  void* dptr = nullptr;
+  Scratch own;
+  size_t bytes = 0;
+  bool staged = false;
+  int init(void* dst, size_t b, cudaStream_t s) {
+    user = dst;
+    bytes = b;
+    if (b == 0) return ST_OK;
+    if (is_device_ptr(dst)) {
+      dptr = dst;
+      return ST_OK;
+    }
+    FUELG_TRY(own.alloc(b, s));
+    dptr = own.p;
+    staged = true;
+    return ST_OK;
+  }
+  int flush(cudaStream_t s, int64_t* d2h) {
+    if (staged && bytes) {
+      FUELG_CUDA(cudaMemcpyAsync(user, dptr, bytes, cudaMemcpyDeviceToHost, s));
+      if (d2h) *d2h += (int64_t)bytes;
+    }
+    return ST_OK;
+  }
+};
+
+int check_device() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    set_error("no CUDA device is visible; the GB300 engine has no CPU fallback");
+    return ST_ENODEV;
+  }
+  return ST_OK;
+}
+
+int begin_call() {
+  FUELG_TRY(check_device());
+  FUELG_TRY(ensure_cancel_word());
+  *(volatile int*)g_cancel_host = 0;  // py_interruptible resets before running
+  return ST_OK;
+}
+
+int read_dev_status(const int* dstat, cudaStream_t s) {
+  int h = 0;
+  FUELG_CUDA(cudaMemcpyAsync(&h, dstat, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FUELG_CUDA(cudaStreamSynchronize(s));
+  if (h & DEV_CANCELLED) {
+    set_error("interrupted");
+    return ST_ECANCELLED;
+  }
+  if (h & DEV_TIMEOUT) {
+    set_error("a bounded device wait timed out");
+    return ST_ETIMEOUT;
+  }
+  if (h & DEV_BADARG) {
+    set_error("a kernel rejected its arguments");
+    return ST_EINVAL;
+  }
+  return ST_OK;
+}
+
+// Installs a HotTimer for the current call and snapshots the launch counter.
+struct CallMeter {
+  HotTimer ht;
+  int64_t launches0;
+  CallMeter() : launches0(launch_count()) { hot_timer() = &ht; }
+  ~CallMeter() { hot_timer() = nullptr; }
+  void fill(fuelg_stats* st) {
+    if (!st) return;
+    st->hot_kernel_ms = ht.total_ms();
+    st->hot_kernel_launches = ht.count();
+    st->kernel_launches = (int32_t)(launch_count() - launches0);
+  }
+};
+
+struct Timer {
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaStream_t s;
+  explicit Timer(cudaStream_t st) : s(st) {
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+  }
+  double stop() {
+    cudaEventRecord(b, s);
+    cudaEventSynchronize(b);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    return ms;
+  }
+  ~Timer() {
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* fuelg_last_error(void) { return fuelg::last_error(); }
+const char* fuelg_version(void) { return "fuel-gb300 0.1.0 (sm_103a)"; }
+
+int fuelg_device_count(int32_t* out_count) {
+  if (!out_count) {
+    set_error("out_count is NULL");
+    return ST_EINVAL;
+  }
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  *out_count = n;
+  return ST_OK;
+}
+
+int fuelg_cancel(void) {
+  if (g_cancel_host) *(volatile int*)g_cancel_host = 1;
+  return ST_OK;
+}
+int fuelg_reset_cancel(void) {
+  if (g_cancel_host) *(volatile int*)g_cancel_host = 0;
+  return ST_OK;
+}
+
+int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, int32_t order, fuelg_index** out) {
+  if (!out) {
+    set_error("out is NULL");
+    return ST_EINVAL;
+  }
+  *out = nullptr;
+  if (n < 0 || d <= 0 || (n > 0 && !data)) {
+    set_error("invalid index shape n=%lld d=%d", (long long)n, d);
+    return ST_EINVAL;
+  }
+  if (metric != FUELG_METRIC_SQEUCLIDEAN && metric != FUELG_METRIC_EUCLIDEAN) {
+    set_error("unsupported metric %d (the GPU path serves sqeuclidean and euclidean)", metric);
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  FUELG_TRY(begin_call());
+  fuelg_index* ix = new fuelg_index();
+  cudaGetDevice(&ix->device);
+  ix->n = n;
+  ix->d = d;
+  ix->metric = metric;
+  ix->order = order;
+  if (cudaStreamCreateWithFlags(&ix->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ix;
+    set_error("cannot create a stream");
+    return ST_ECUDA;
+  }
+  const size_t bytes = (size_t)n * d * sizeof(float);
+  if (bytes) {
+    if (cudaMalloc(&ix->X, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      cudaStreamDestroy(ix->stream);
+      delete ix;
+      set_error("cannot allocate %zu bytes for the index", bytes);
+      return ST_ENOMEM;
+    }
+    cudaError_t e = cudaMemcpyAsync(ix->X, data, bytes, cudaMemcpyDefault, ix->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
+    if (e != cudaSuccess) {
+      cudaFree(ix->X);
+      cudaStreamDestroy(ix->stream);
+      delete ix;
+      set_error("index upload failed: %s", cudaGetErrorString(e));
+      return ST_ECUDA;
+    }
+  }
+  *out = ix;
+  return ST_OK;
+}
+
+int fuelg_index_destroy(fuelg_index* ix) {
+  if (!ix) return ST_OK;
+  if (ix->X) cudaFree(ix->X);
+  if (ix->stream) cudaStreamDestroy(ix->stream);
+  delete ix;
+  return ST_OK;
+}
+
+int fuelg_index_info(const fuelg_index* ix, int64_t* n, int32_t* d, int32_t* metric, int32_t* order) {
+  if (!ix) {
+    set_error("index is NULL");
+    return ST_EINVAL;
+  }
+  if (n) *n = ix->n;
+  if (d) *d = ix->d;
+  if (metric) *metric = ix->metric;
+  if (order) *order = ix->order;
+  return ST_OK;
+}
+
+int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32_t exclude_mode, int32_t precision,
+              int64_t* out_idx, float* out_dist, fuelg_stats* stats) {
+  if (!ix) {
+    set_error("index is NULL");
+    return ST_EINVAL;
+  }
+  if (m < 0 || k < 0 || (m > 0 && !queries) || (m > 0 && k > 0 && (!out_idx || !out_dist))) {
+    set_error("invalid knn arguments m=%lld k=%d", (long long)m, k);
+    return ST_EINVAL;
+  }
+  if (exclude_mode < FUELG_EXCLUDE_NONE || exclude_mode > FUELG_EXCLUDE_KPLUS1) {
+    set_error("unknown exclude mode %d", exclude_mode);
+    return ST_EINVAL;
+  }
+  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16) {
+    set_error("unknown precision tier %d", precision);
+    return ST_EINVAL;
+  }
+  if (k > 4095) {
+    set_error("k=%d exceeds the supported maximum of 4095", k);
+    return ST_ENOTSUP;
+  }
+  std::lock_guard<std::mutex> lk(ix->mu);
+  FUELG_TRY(begin_call());
+  cudaSetDevice(ix->device);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (m == 0 || k == 0) return ST_OK;
+  cudaStream_t s = ix->stream;
+  const int kk = exclude_mode == FUELG_EXCLUDE_NONE ? k : k + 1;
+  CallMeter meter;
+  Timer tm(s);
+  InBuf q;
+  FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(float), s));
+  OutBuf oi, od;
+  FUELG_TRY(oi.init(out_idx, (size_t)m * k * sizeof(int64_t), s));
+  FUELG_TRY(od.init(out_dist, (size_t)m * k * sizeof(float), s));
+  Scratch keys, dstat;
+  FUELG_TRY(keys.alloc((size_t)m * kk * sizeof(uint64_t), s));
+  FUELG_TRY(dstat.alloc(sizeof(int), s));
+  FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
+  ExactScanParams p;
+  p.A = static_cast<const float*>(q.dptr);
+  p.m = m;
+  p.B = ix->X;
+  p.n = ix->n;
+  p.d = ix->d;
+  p.kind = KIND_KNN;
+  p.order = ix->order;
+  p.metric = ix->metric;
+  p.kk = kk;
+  // Tensor-core tiers are served by the exact path until the screen lands.
+  FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
+  FUELG_TRY(finalize_knn(keys.as<uint64_t>(), m, kk, k, exclude_mode, static_cast<int64_t*>(oi.dptr),
+                         static_cast<float*>(od.dptr), s));
+  int64_t d2h = 0;
+  FUELG_TRY(oi.flush(s, &d2h));
+  FUELG_TRY(od.flush(s, &d2h));
+  const double ms = tm.stop();
+  FUELG_TRY(read_dev_status(dstat.as<int>(), s));
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = q.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = m * ix->n;
+    stats->precision_used = FUELG_PREC_FP32;
+    meter.fill(stats);
+  }
+  return ST_OK;
+}
+
+int fuelg_range(fuelg_index* ix, const float* queries, int64_t m, double radius, int32_t exclude_self,
+                fuelg_range_result** out, fuelg_stats* stats) {
+  if (!ix || !out) {
+    set_error("index or out is NULL");
+    return ST_EINVAL;
+  }
+  *out = nullptr;
+  if (m < 0 || (m > 0 && !queries)) {
+    set_error("invalid range arguments m=%lld", (long long)m);
+    return ST_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(ix->mu);
+  FUELG_TRY(begin_call());
+  cudaSetDevice(ix->device);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaStream_t s = ix->stream;
+  CallMeter meter;
+  Timer tm(s);
+  InBuf q;
+  FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(float), s));
+  Scratch dstat;
+  FUELG_TRY(dstat.alloc(sizeof(int), s));
+  FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
+  ExactScanParams p;
+  p.A = static_cast<const float*>(q.dptr);
+  p.m = m;
+  p.B = ix->X;
+  p.n = ix->n;
+  p.d = ix->d;
+  p.kind = KIND_KNN;
+  p.order = ix->order;
+  p.metric = ix->metric;
+  fuelg_range_result* r = new fuelg_range_result();
+  r->m = m;
+  int st = exact_range(p, (float)radius, exclude_self ? 1 : 0, &r->off, &r->idx, &r->dist, &r->total,
+                       dstat.as<int>(), s);
+  if (st == ST_OK) st = read_dev_status(dstat.as<int>(), s);
+  const double ms = tm.stop();
+  if (st != ST_OK) {
+    fuelg_range_free(r);
+    return st;
+  }
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = q.h2d;
+    stats->distance_evals = 2 * m * ix->n;
+    stats->precision_used = FUELG_PREC_FP32;
+    meter.fill(stats);
+  }
+  *out = r;
+  return ST_OK;
+}
+
+int fuelg_range_size(const fuelg_range_result* r, int64_t* m, int64_t* total) {
+  if (!r) {
+    set_error("range result is NULL");
+    return ST_EINVAL;
+  }
+  if (m) *m = r->m;
+  if (total) *total = r->total;
+  return ST_OK;
+}
+
+int fuelg_range_copy(const fuelg_range_result* r, int64_t* offsets, int64_t* idx, float* dist) {
+  if (!r) {
+    set_error("range result is NULL");
+    return ST_EINVAL;
+  }
+  if (offsets) FUELG_CUDA(cudaMemcpy(offsets, r->off, sizeof(int64_t) * (r->m + 1), cudaMemcpyDefault));
+  if (r->total) {
+    if (idx) FUELG_CUDA(cudaMemcpy(idx, r->idx, sizeof(int64_t) * r->total, cudaMemcpyDefault));
+    if (dist) FUELG_CUDA(cudaMemcpy(dist, r->dist, sizeof(float) * r->total, cudaMemcpyDefault));
+  }
+  return ST_OK;
+}
+
+int fuelg_range_free(fuelg_range_result* r) {
+  if (!r) return ST_OK;
+  if (r->off) cudaFree(r->off);
+  if (r->idx) cudaFree(r->idx);
+  if (r->dist) cudaFree(r->dist);
+  delete r;
+  return ST_OK;
+}
+
+int fuelg_kmeans_lloyd(const float* data, int64_t n, int32_t d, int32_t k, const float* init_centers,
+                       int32_t max_iter, double tol, int32_t precision, int32_t order, int32_t flags,
+                       float* out_centers, int64_t* out_labels, int32_t* out_iters, double* out_inertia,
+                       fuelg_stats* stats) {
+  if (n <= 0 || d <= 0 || k <= 0 || !data || !init_centers || !out_centers || !out_labels) {
+    set_error("invalid lloyd arguments n=%lld d=%d k=%d", (long long)n, d, k);
+    return ST_EINVAL;
+  }
+  if (max_iter < 1) {
+    set_error("max_iter must be >= 1");
+    return ST_EINVAL;
+  }
+  if (!(tol >= 0.0)) {
+    set_error("tol must be >= 0");
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16) {
+    set_error("unknown precision tier %d", precision);
+    return ST_EINVAL;
+  }
+  FUELG_TRY(begin_call());
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaStream_t s;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  CallMeter meter;
+  Timer tm(s);
+  InBuf X, C0;
+  FUELG_TRY(X.init(data, (size_t)n * d * sizeof(float), s));
+  FUELG_TRY(C0.init(init_centers, (size_t)k * d * sizeof(float), s));
+  OutBuf oc, ol;
+  FUELG_TRY(oc.init(out_centers, (size_t)k * d * sizeof(float), s));
+  FUELG_TRY(ol.init(out_labels, (size_t)n * sizeof(int64_t), s));
+  Scratch lab32, dstat;
+  FUELG_TRY(lab32.alloc(sizeof(int32_t) * n, s));
+  FUELG_TRY(dstat.alloc(sizeof(int), s));
+  FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
+  LloydParams p;
+  p.X = static_cast<const float*>(X.dptr);
+  p.n = n;
+  p.d = d;
+  p.k = k;
+  p.init = static_cast<const float*>(C0.dptr);
+  p.max_iter = max_iter;
+  p.tol = tol;
+  p.order = order;
+  p.precision = precision;
+  p.fixed_iters = (flags & FUELG_LLOYD_FIXED_ITERS) ? 1 : 0;
+  LloydResult r;
+  r.centers = static_cast<float*>(oc.dptr);
+  r.labels = lab32.as<int32_t>();
+  FUELG_TRY(lloyd_run(p, &r, dstat.as<int>(), s));
+  // widen labels to int64 (python/kmeans.rs:20: `v as i64`)
+  widen_labels(r.labels, static_cast<int64_t*>(ol.dptr), n, s);
+  FUELG_CUDA(cudaGetLastError());
+  int64_t d2h = 0;
+  FUELG_TRY(oc.flush(s, &d2h));
+  FUELG_TRY(ol.flush(s, &d2h));
+  const double ms = tm.stop();
+  FUELG_TRY(read_dev_status(dstat.as<int>(), s));
+  if (out_iters) *out_iters = r.iters;
+  if (out_inertia) *out_inertia = r.inertia;
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = X.h2d + C0.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = (int64_t)r.iters * n * k;
+    stats->rescored = r.rescored;
+    stats->iterations = r.iters;
+    stats->precision_used = precision;
+    meter.fill(stats);
+  }
+  return ST_OK;
+}
+
+}  // extern "C"
+

@@ -1,0 +1,165 @@
+// fuelg_internal.h -- host-side declarations shared by the engine's
+// translation units (not part of the public C ABI; see include/fuelg.h).
+#pragma once
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <utility>
+#include <vector>
+#include <cuda_runtime.h>
+
+namespace fuelg {
+
+// Status codes mirrored by include/fuelg.h.
+enum Status : int {
+  ST_OK = 0,
+  ST_EINVAL = 1,
+  ST_ENOMEM = 2,
+  ST_ECUDA = 3,
+  ST_ECANCELLED = 4,
+  ST_ENOTSUP = 5,
+  ST_ENODEV = 6,
+  ST_ETIMEOUT = 7,
+};
+
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define FUELG_CUDA(call)                                                                               \
+  do {                                                                                                 \
+    cudaError_t e_ = (call);                                                                           \
+    if (e_ != cudaSuccess) {                                                                           \
+      ::fuelg::set_error("CUDA error %s at %s:%d: %s", cudaGetErrorName(e_), __FILE__, __LINE__,       \
+                         cudaGetErrorString(e_));                                                      \
+      return ::fuelg::ST_ECUDA;                                                                        \
+    }                                                                                                  \
+  } while (0)
+
+#define FUELG_TRY(expr)            \
+  do {                             \
+    int s_ = (expr);               \
+    if (s_ != ::fuelg::ST_OK) return s_; \
+  } while (0)
+
+// Stream-ordered scratch allocations (cudaMallocAsync pool) freed on scope exit.
+struct Scratch {
+  void* p = nullptr;
+  cudaStream_t s = nullptr;
+  Scratch() = default;
+  Scratch(const Scratch&) = delete;
+  Scratch& operator=(const Scratch&) = delete;
+  ~Scratch() {
+    if (p) cudaFreeAsync(p, s);
+  }
+  int alloc(size_t bytes, cudaStream_t stream) {
+    s = stream;
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
+      return ST_ENOMEM;
+    }
+    return ST_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// Per-thread accounting of this library's own kernel launches, and optional
+// CUDA-event timing of the dominant ("hot") kernel of a call, recorded on the
+// stream that kernel is launched on.
+void note_launch(int count = 1);
+int64_t launch_count();
+struct HotTimer {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev;
+  void begin(cudaStream_t s) {
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaEventRecord(a, s);
+    ev.emplace_back(a, b);
+  }
+  void end(cudaStream_t s) { cudaEventRecord(ev.back().second, s); }
+  double total_ms() const {
+    double t = 0;
+    for (auto& e : ev) {
+      float ms = 0.f;
+      cudaEventSynchronize(e.second);
+      cudaEventElapsedTime(&ms, e.first, e.second);
+      t += ms;
+    }
+    return t;
+  }
+  int count() const { return (int)ev.size(); }
+  ~HotTimer() {
+    for (auto& e : ev) {
+      cudaEventDestroy(e.first);
+      cudaEventDestroy(e.second);
+    }
+  }
+};
+// The timer the current call installed for its hot kernel (or nullptr).
+HotTimer*& hot_timer();
+
+// Host-mapped cancel word (pinned, device-visible); set by fuelg_cancel().
+int* cancel_word_device();
+bool cancel_requested();
+
+// Device status word helpers (per call).
+struct DevStatus {
+  int* d = nullptr;
+};
+
+// -------- exact linear-scan top-k (fuelg_knn.cu) ----------------------------
+struct ExactScanParams {
+  const float* A = nullptr;  // queries [m, d] (device)
+  int64_t m = 0;
+  const float* B = nullptr;  // points [n, d] (device)
+  int64_t n = 0;
+  int d = 0;
+  int kind = 0;    // Kind
+  int order = 0;   // Order
+  int metric = 0;  // Metric
+  int kk = 0;      // keys kept per query (k or k+1)
+};
+
+// Top-kk (distance, index) keys per query, sorted ascending, written to
+// out_keys [m, kk] (device).  Unused slots hold ~0ull.
+int exact_topk(const ExactScanParams& p, uint64_t* out_keys, int* dev_status, cudaStream_t stream);
+
+// Turn sorted keys [m, kk] into the reference's (int64 idx, float dist) rows
+// with the given exclude-self mode and -1/+inf padding.
+int finalize_knn(const uint64_t* keys, int64_t m, int kk, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
+                 cudaStream_t stream);
+
+// Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
+int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
+                float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream);
+
+// -------- Lloyd (fuelg_lloyd.cu) -------------------------------------------
+struct LloydParams {
+  const float* X = nullptr;  // [n, d] device
+  int64_t n = 0;
+  int d = 0;
+  int k = 0;
+  const float* init = nullptr;  // [k, d] device
+  int max_iter = 0;
+  double tol = 0.0;
+  int order = 0;
+  int precision = 0;
+  int fixed_iters = 0;  // 1: ignore the changed==0 stop (benchmark mode)
+};
+struct LloydResult {
+  float* centers = nullptr;   // [k, d] device (caller-provided)
+  int32_t* labels = nullptr;  // [n] device (caller-provided)
+  int32_t iters = 0;
+  double inertia = 0.0;
+  int64_t rescored = 0;       // points re-scored exactly (tensor-core tiers)
+  double kernel_ms = 0.0;
+};
+int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_t stream);
+
+}  // namespace fuelg

@@ -1,0 +1,348 @@
+// fuelg_lloyd.cu -- Lloyd k-means (src/cluster/kmeans/lloyd.rs:12-202) on GB300.
+//
+// One iteration = assign + centre update:
+//   assign   every point's nearest centre under the reference's own distance
+//            order (iteration 1: the pairwise kernel order of
+//            vec_pairwise_sqdist, lloyd.rs:76; later iterations: math::sqdist,
+//            lloyd.rs:166-172), first index wins ties (strict '<').  This is
+//            the exact linear-scan top-1 of fuelg_knn.cu with centres as the
+//            index and points as the queries.
+//   update   centre_j = (f32)(sum_j / count_j), sums in FP64 over the members
+//            of cluster j in ascending point order (stable radix sort by
+//            label, then fixed 32-row chunk partials reduced in chunk order):
+//            deterministic and atomics-free on the floating-point path.
+//            Empty clusters keep their centre (lloyd.rs:138-146).
+// The loop stops when no label changed (lloyd.rs:197) or at max_iter
+// (initialisation counts as iteration 1, util.rs:40); the reported inertia is
+// the FP64 sum of squared distances of every point to the centre it was
+// assigned to in the final pass (the f32 `lastsum` of lloyd.rs:196, computed
+// exactly).
+#include <algorithm>
+#include <cmath>
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+#include <vector>
+
+#include "fuelg_common.cuh"
+#include "fuelg_internal.h"
+
+namespace fuelg {
+
+int lloyd_assign_tc(const LloydParams& p, const float* centers, int32_t* labels, int32_t* changed_count,
+                    int64_t* rescored, int* dev_status, cudaStream_t stream);
+
+namespace {
+
+constexpr int kChunk = 32;  // rows per FP64 partial-sum chunk
+
+__global__ void post_assign_kernel(const uint64_t* __restrict__ keys, int64_t n, int32_t* __restrict__ labels,
+                                   int first, int32_t* __restrict__ changed) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int c = 0;
+  if (i < n) {
+    const int32_t a = (int32_t)key_idx(keys[i]);
+    if (first || labels[i] != a) c = 1;
+    labels[i] = a;
+  }
+  c = __syncthreads_count(c);
+  if (threadIdx.x == 0 && c) atomicAdd(changed, c);  // integer: order-independent
+}
+
+__global__ void iota_kernel(int32_t* __restrict__ v, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = (int32_t)i;
+}
+
+__global__ void count_global_kernel(const int32_t* __restrict__ labels, int64_t n, int32_t* __restrict__ counts) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&counts[labels[i]], 1);  // integer: order-independent
+}
+
+__global__ void count_kernel(const int32_t* __restrict__ labels, int64_t n, int k, int32_t* __restrict__ counts) {
+  extern __shared__ int32_t hist[];
+  for (int j = threadIdx.x; j < k; j += blockDim.x) hist[j] = 0;
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&hist[labels[i]], 1);
+  __syncthreads();
+  for (int j = threadIdx.x; j < k; j += blockDim.x)
+    if (hist[j]) atomicAdd(&counts[j], hist[j]);
+}
+
+// Per cluster: member offset, number of 32-row chunks.
+__global__ void chunk_count_kernel(const int32_t* __restrict__ counts, int k, int32_t* __restrict__ nchunks) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < k) nchunks[j] = (counts[j] + kChunk - 1) / kChunk;
+}
+
+__global__ void chunk_table_kernel(const int32_t* __restrict__ chunk_off, const int32_t* __restrict__ nchunks, int k,
+                                   int32_t* __restrict__ chunk_cluster) {
+  const int j = blockIdx.x;
+  for (int c = threadIdx.x; c < nchunks[j]; c += blockDim.x) chunk_cluster[chunk_off[j] + c] = j;
+}
+
+// partial[c][t] = sum over the <=32 member rows of chunk c, in member order.
+__global__ void chunk_sum_kernel(const float* __restrict__ X, int d, const int32_t* __restrict__ perm,
+                                 const int32_t* __restrict__ mem_off, const int32_t* __restrict__ counts,
+                                 const int32_t* __restrict__ chunk_off, const int32_t* __restrict__ chunk_cluster,
+                                 const int32_t* __restrict__ total_chunks, double* __restrict__ partial) {
+  const int c = blockIdx.x;
+  if (c >= *total_chunks) return;  // grid sized for the upper bound n/32 + k + 1
+  const int j = chunk_cluster[c];
+  const int r0 = (c - chunk_off[j]) * kChunk;
+  const int rows = min(kChunk, counts[j] - r0);
+  const int32_t* members = perm + mem_off[j] + r0;
+  __shared__ int32_t mrow[kChunk];
+  if (threadIdx.x < rows) mrow[threadIdx.x] = members[threadIdx.x];
+  __syncthreads();
+  for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < d; t += gridDim.y * blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < rows; r++) s += (double)__ldg(X + (int64_t)mrow[r] * d + t);
+    partial[(int64_t)c * d + t] = s;
+  }
+}
+
+// centre_j[t] = (f32)(sum over chunks of j, in chunk order / count_j); empty clusters keep theirs.
+__global__ void reduce_update_kernel(const double* __restrict__ partial, int d, int k,
+                                     const int32_t* __restrict__ counts, const int32_t* __restrict__ chunk_off,
+                                     const int32_t* __restrict__ nchunks, float* __restrict__ centers) {
+  const int j = blockIdx.x;
+  const int cnt = counts[j];
+  if (cnt == 0) return;
+  const int c0 = chunk_off[j], nc = nchunks[j];
+  for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < d; t += gridDim.y * blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < nc; c++) s += partial[(int64_t)(c0 + c) * d + t];
+    centers[(int64_t)j * d + t] = __double2float_rn(__ddiv_rn(s, (double)cnt));
+  }
+}
+
+// Per-block FP64 partials of sum_i ||x_i - c_{l_i}||^2 (differences in double).
+__global__ void inertia_partial_kernel(const float* __restrict__ X, int64_t n, int d, const float* __restrict__ C,
+                                       const int32_t* __restrict__ labels, double* __restrict__ partial) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int64_t i = (int64_t)blockIdx.x * nw + warp; i < n; i += (int64_t)gridDim.x * nw) {
+    const float* x = X + i * d;
+    const float* c = C + (int64_t)labels[i] * d;
+    double s = 0.0;
+    for (int t = lane; t < d; t += 32) {
+      const double df = (double)x[t] - (double)c[t];
+      s = fma(df, df, s);
+    }
+    acc += s;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < nw; w++) s += red[w];
+    partial[blockIdx.x] = s;
+  }
+}
+
+__global__ void sum_partials_kernel(const double* __restrict__ partial, int nb, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0.0;
+    for (int b = 0; b < nb; b++) s += partial[b];
+    *out = s;
+  }
+}
+
+// FP64 ||C_new - C_old||_F^2 and ||C_old||_F^2 for the tol>0 stop rule
+// (lloyd.rs:136-153).
+__global__ void frob_kernel(const float* __restrict__ Cold, const float* __restrict__ Cnew, int64_t kd,
+                            double* __restrict__ out2) {
+  __shared__ double s1[256], s2[256];
+  double a = 0.0, b = 0.0;
+  for (int64_t e = threadIdx.x; e < kd; e += blockDim.x) {
+    const double o = Cold[e], w = Cnew[e];
+    a += (w - o) * (w - o);
+    b += o * o;
+  }
+  s1[threadIdx.x] = a;
+  s2[threadIdx.x] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double x = 0.0, y = 0.0;
+    for (int t = 0; t < (int)blockDim.x; t++) {
+      x += s1[t];
+      y += s2[t];
+    }
+    out2[0] = x;
+    out2[1] = y;
+  }
+}
+
+int end_bit_for(int k) {
+  int b = 1;
+  while ((1 << b) < k) b++;
+  return b;
+}
+
+}  // namespace
+
+int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_t stream) {
+  const int64_t n = p.n;
+  const int d = p.d, k = p.k;
+  if (n <= 0 || d <= 0 || k <= 0) {
+    set_error("lloyd: n, d and k must be positive (n=%lld d=%d k=%d)", (long long)n, d, k);
+    return ST_EINVAL;
+  }
+  if (n >= (1ll << 31)) {
+    set_error("lloyd: n=%lld exceeds the 2^31-1 row limit", (long long)n);
+    return ST_ENOTSUP;
+  }
+  float* C = r->centers;
+  int32_t* labels = r->labels;
+  FUELG_CUDA(cudaMemcpyAsync(C, p.init, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
+
+  Scratch keys, changed, perm_in, perm, lab_sorted, counts, offs, nchunks, chunk_off, chunk_cluster, partial, tmp,
+      frob, cold, inert_part, inert;
+  const int64_t max_chunks = n / kChunk + k + 1;
+  FUELG_TRY(keys.alloc(sizeof(uint64_t) * n, stream));
+  FUELG_TRY(changed.alloc(sizeof(int32_t) * 2, stream));
+  FUELG_TRY(perm_in.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(perm.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(lab_sorted.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(counts.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(offs.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(nchunks.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(chunk_off.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(chunk_cluster.alloc(sizeof(int32_t) * max_chunks, stream));
+  FUELG_TRY(partial.alloc(sizeof(double) * max_chunks * d, stream));
+  FUELG_TRY(frob.alloc(sizeof(double) * 2, stream));
+  if (p.tol > 0) FUELG_TRY(cold.alloc(sizeof(float) * k * d, stream));
+  const int inert_blocks = 4 * 152;
+  FUELG_TRY(inert_part.alloc(sizeof(double) * inert_blocks, stream));
+  FUELG_TRY(inert.alloc(sizeof(double), stream));
+
+  size_t sort_bytes = 0, scan_bytes = 0;
+  const int ebit = end_bit_for(k);
+  FUELG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, labels, lab_sorted.as<int32_t>(),
+                                             perm_in.as<int32_t>(), perm.as<int32_t>(), (int)n, 0, ebit, stream));
+  FUELG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, counts.as<int32_t>(), offs.as<int32_t>(), k + 1,
+                                           stream));
+  FUELG_TRY(tmp.alloc(std::max(sort_bytes, scan_bytes), stream));
+  iota_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(perm_in.as<int32_t>(), n); ::fuelg::note_launch();
+
+  int32_t* h_changed = nullptr;
+  FUELG_CUDA(cudaMallocHost(&h_changed, sizeof(int32_t)));
+  struct HostFree {
+    void* p;
+    ~HostFree() {
+      if (p) cudaFreeHost(p);
+    }
+  } hf{h_changed};
+
+  cudaEvent_t ev0, ev1;
+  FUELG_CUDA(cudaEventCreate(&ev0));
+  FUELG_CUDA(cudaEventCreate(&ev1));
+  FUELG_CUDA(cudaEventRecord(ev0, stream));
+
+  auto assign = [&](bool first) -> int {
+    FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t) * 2, stream));
+    if (p.precision != 0 && !first) {
+      return lloyd_assign_tc(p, C, labels, changed.as<int32_t>(), &r->rescored, dev_status, stream);
+    }
+    ExactScanParams sp;
+    sp.A = p.X;
+    sp.m = n;
+    sp.B = C;
+    sp.n = k;
+    sp.d = d;
+    sp.kind = first ? KIND_PAIRWISE : KIND_SQDIST;
+    sp.order = p.order;
+    sp.metric = METRIC_SQEUCLIDEAN;
+    sp.kk = 1;
+    FUELG_TRY(exact_topk(sp, keys.as<uint64_t>(), dev_status, stream));
+    post_assign_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(keys.as<uint64_t>(), n, labels, first ? 1 : 0,
+                                                                       changed.as<int32_t>()); ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+    return ST_OK;
+  };
+
+  auto update_centers = [&]() -> int {
+    FUELG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int32_t) * (k + 1), stream));
+    if (k <= 8192) {
+      count_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, sizeof(int32_t) * k, stream>>>(
+          labels, n, k, counts.as<int32_t>()); ::fuelg::note_launch();
+    } else {
+      count_global_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, stream>>>(
+          labels, n, counts.as<int32_t>()); ::fuelg::note_launch();
+    }
+    size_t sb = sort_bytes;
+    FUELG_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, sb, labels, lab_sorted.as<int32_t>(), perm_in.as<int32_t>(),
+                                               perm.as<int32_t>(), (int)n, 0, ebit, stream));
+    size_t scb = scan_bytes;
+    FUELG_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, scb, counts.as<int32_t>(), offs.as<int32_t>(), k + 1, stream));
+    chunk_count_kernel<<<(k + 255) / 256, 256, 0, stream>>>(counts.as<int32_t>(), k, nchunks.as<int32_t>()); ::fuelg::note_launch();
+    FUELG_CUDA(cudaMemsetAsync(nchunks.as<int32_t>() + k, 0, sizeof(int32_t), stream));
+    scb = scan_bytes;
+    FUELG_CUDA(
+        cub::DeviceScan::ExclusiveSum(tmp.p, scb, nchunks.as<int32_t>(), chunk_off.as<int32_t>(), k + 1, stream));
+    chunk_table_kernel<<<k, 128, 0, stream>>>(chunk_off.as<int32_t>(), nchunks.as<int32_t>(), k,
+                                              chunk_cluster.as<int32_t>()); ::fuelg::note_launch();
+    const int ty = (d + 255) / 256;
+    dim3 g1((unsigned)max_chunks, ty);
+    chunk_sum_kernel<<<g1, 256, 0, stream>>>(p.X, d, perm.as<int32_t>(), offs.as<int32_t>(), counts.as<int32_t>(),
+                                             chunk_off.as<int32_t>(), chunk_cluster.as<int32_t>(),
+                                             chunk_off.as<int32_t>() + k, partial.as<double>()); ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+    if (p.tol > 0) FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
+    dim3 g2(k, ty);
+    reduce_update_kernel<<<g2, 256, 0, stream>>>(partial.as<double>(), d, k, counts.as<int32_t>(),
+                                                 chunk_off.as<int32_t>(), nchunks.as<int32_t>(), C); ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+    return ST_OK;
+  };
+
+  const float* inertia_centers = C;
+  FUELG_TRY(assign(true));
+  int iters = 1;
+  while (iters < p.max_iter) {
+    iters++;
+    FUELG_TRY(update_centers());
+    if (p.tol > 0) {
+      frob_kernel<<<1, 256, 0, stream>>>(cold.as<float>(), C, (int64_t)k * d, frob.as<double>()); ::fuelg::note_launch();
+      double h2[2];
+      FUELG_CUDA(cudaMemcpyAsync(h2, frob.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, stream));
+      FUELG_CUDA(cudaStreamSynchronize(stream));
+      const double diff = std::sqrt(h2[0]), oldn = std::sqrt(h2[1]);
+      const double rel = oldn == 0.0 ? diff : diff / oldn;
+      if (rel <= p.tol) {
+        // lloyd.rs:147-152: stop before re-assigning; the returned centres are
+        // the updated ones, labels and inertia stay those of the previous
+        // pass (against the previous centres).
+        inertia_centers = cold.as<float>();
+        break;
+      }
+    }
+    FUELG_TRY(assign(false));
+    if (!p.fixed_iters) {
+      FUELG_CUDA(cudaMemcpyAsync(h_changed, changed.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+      FUELG_CUDA(cudaStreamSynchronize(stream));
+      if (*h_changed == 0) break;
+    }
+  }
+  r->iters = iters;
+  FUELG_CUDA(cudaEventRecord(ev1, stream));
+  inertia_partial_kernel<<<inert_blocks, 256, 0, stream>>>(p.X, n, d, inertia_centers, labels, inert_part.as<double>()); ::fuelg::note_launch();
+  sum_partials_kernel<<<1, 32, 0, stream>>>(inert_part.as<double>(), inert_blocks, inert.as<double>()); ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  double h_inert = 0.0;
+  FUELG_CUDA(cudaMemcpyAsync(&h_inert, inert.p, sizeof(double), cudaMemcpyDeviceToHost, stream));
+  FUELG_CUDA(cudaStreamSynchronize(stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ev0, ev1);
+  r->kernel_ms = ms;
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  r->inertia = h_inert;
+  return ST_OK;
+}
+
+}  // namespace fuelg

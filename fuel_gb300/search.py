@@ -1,0 +1,208 @@
+"""Drop-in for fuel's linear-scan search API on one GB300.
+
+Mirrors ``fuel.search`` (python/fuel/search.py:205-408): ``SearchIndex``,
+``knn_search`` and ``range_search`` keep their names, keyword arguments,
+validation, return types and exclude-self rules.  The scan itself runs in
+libfuelg.so; distances are bit-identical to fuel's f32 distances for the
+chosen summation profile (``order``).
+
+What is served: float32 data, distances ``euclidean``/``l2`` and
+``sqeuclidean``/``squared_euclidean``, the linear scan (``tree`` = ``None``,
+``'auto'``, ``'linear'``, ``'brute'``, ``'bruteforce'``).  Anything else
+raises ``NotImplementedError`` rather than silently running elsewhere.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+_DISTANCE = {
+    "euclidean": "euclidean", "l2": "euclidean",
+    "sqeuclidean": "sqeuclidean", "squared_euclidean": "sqeuclidean",
+}
+# python/fuel/search.py:12-26
+_TREE_NAME_MAP = {
+    "auto": "auto", "vp": "vp", "vptree": "vp", "cover": "cover", "covertree": "cover", "ct": "cover",
+    "ball": "cover", "balltree": "cover", "kd": "kd", "kdtree": "kd", "linear": "linear", "brute": "linear",
+    "bruteforce": "linear",
+}
+
+
+def _ensure_float(data):
+    """python/fuel/_dispatch.py:8-12: non-float input becomes float64."""
+    data = np.asarray(data)
+    if data.dtype not in (np.float32, np.float64):
+        return data.astype(np.float64)
+    return data
+
+
+def _normalize_tree(tree):
+    """python/fuel/search.py:37-47."""
+    if tree is None:
+        return "auto"
+    if not isinstance(tree, str):
+        raise TypeError("tree must be a string or None")
+    key = tree.lower().replace("_", "").replace("-", "")
+    if key in _TREE_NAME_MAP:
+        return _TREE_NAME_MAP[key]
+    raise ValueError(
+        f"unknown tree '{tree}', valid values are 'auto', 'vp', 'kd', 'cover', 'linear', 'vptree', 'ct', "
+        "'covertree', 'brute', or 'brute_force'")
+
+
+def _parse_distance(distance: str) -> str:
+    """python/mod.rs:42-71 for the two metrics this engine serves."""
+    key = str(distance).lower()
+    if key in _DISTANCE:
+        return _DISTANCE[key]
+    raise NotImplementedError(
+        f"distance '{distance}' is not served by the GB300 linear scan (served: euclidean, l2, sqeuclidean, "
+        "squared_euclidean)")
+
+
+def _require_f32(arr, what):
+    if arr.dtype != np.float32:
+        raise NotImplementedError(
+            f"{what} has dtype {arr.dtype}; the GB300 engine serves float32 (cast with .astype(np.float32))")
+
+
+class SearchIndex:
+    """Persistent linear-scan index held in GB300 memory.
+
+    Parameters mirror ``fuel.search.SearchIndex`` (python/fuel/search.py:230).
+    ``precision`` ('fp32' | 'bf16' | 'split_bf16') picks the tier and
+    ``order`` ('arm' | 'x86') the summation profile to reproduce (default: the
+    profile fuel compiles on this host).  ``precompute=K`` is accepted; the
+    exact answer is computed on every call with the k+1 exclude-self rule of
+    the precomputed path (python/search.rs:1163-1170).
+    """
+
+    def __init__(self, data, *, distance="euclidean", tree=None, seed=None, precompute=None, precision="fp32",
+                 order=None):
+        data = _ensure_float(data)
+        if data.ndim != 2:
+            raise ValueError("data must be a 2D array of observations")
+        self.data = data
+        self.distance = distance
+        self.seed = seed
+        self.precompute = precompute
+        self.dtype = data.dtype
+        self.shape = data.shape
+        self.tree = _normalize_tree(tree)
+        if self.tree == "auto":
+            self.tree = "linear"
+        if self.tree != "linear":
+            raise NotImplementedError(
+                f"tree '{tree}' is not served by the GB300 engine; only the exact linear scan is accelerated")
+        self._metric = _parse_distance(distance)
+        _require_f32(data, "data")
+        if precision not in _lib.PRECISION:
+            raise ValueError(f"precision must be one of {sorted(_lib.PRECISION)}")
+        self.precision = precision
+        self.order = order or _lib.default_order()
+        if self.order not in _lib.ORDER:
+            raise ValueError(f"order must be one of {sorted(_lib.ORDER)}")
+        self._source_shape = data.shape
+        self._source_strides = data.strides
+        self._source_ptr = data.__array_interface__["data"][0]
+        lib = _lib.load()
+        host = np.ascontiguousarray(data)
+        handle = ctypes.c_void_p()
+        _lib.check(lib.fuelg_index_create(_lib.ptr(host), host.shape[0], host.shape[1], _lib.METRIC[self._metric],
+                                          _lib.ORDER[self.order], ctypes.byref(handle)))
+        self._handle = handle
+        self.index = self
+        self.last_stats = None
+
+    def __del__(self):
+        h = getattr(self, "_handle", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().fuelg_index_destroy(h)
+            except Exception:
+                pass
+            self._handle = None
+
+    def _same_source(self, query):
+        """python/fuel/search.py:270-275."""
+        return (query.shape == self._source_shape and query.strides == self._source_strides
+                and query.__array_interface__["data"][0] == self._source_ptr)
+
+    def _prepare_query(self, query, exclude_self):
+        query = _ensure_float(query)
+        if query.dtype != self.dtype:
+            query = query.astype(self.dtype)
+        if query.ndim != 2 or query.shape[1] != self.shape[1]:
+            raise ValueError(f"query shape {query.shape} is not compatible with index data shape {self.shape}")
+        if exclude_self is None:
+            exclude_self = self._same_source(query)
+        elif exclude_self and not self._same_source(query):
+            raise ValueError(
+                "exclude_self=True is only supported when query refers to the same underlying array as data")
+        return query, bool(exclude_self)
+
+    def knn(self, query, k, *, exclude_self=None):
+        """(int64[m, k] indices, float32[m, k] distances), -1 / inf padded."""
+        query, exclude_self = self._prepare_query(query, exclude_self)
+        k = int(k)
+        if k < 0:
+            raise OverflowError("can't convert negative int to unsigned")
+        m = query.shape[0]
+        q = np.ascontiguousarray(query)
+        idx = np.empty((m, k), np.int64)
+        dist = np.empty((m, k), np.float32)
+        if exclude_self:
+            mode = _lib.EXCLUDE_KPLUS1 if self.precompute is not None else _lib.EXCLUDE_LINEAR
+        else:
+            mode = _lib.EXCLUDE_NONE
+        st = _lib.Stats()
+        _lib.check(_lib.load().fuelg_knn(self._handle, _lib.ptr(q), m, k, mode, _lib.PRECISION[self.precision],
+                                         _lib.ptr(idx), _lib.ptr(dist), ctypes.byref(st)))
+        self.last_stats = st.as_dict()
+        return idx, dist
+
+    def radius_search(self, query, radius, *, exclude_self=None):
+        """([int64 arrays], [float32 arrays]) per query row, sorted by (distance, index)."""
+        query, exclude_self = self._prepare_query(query, exclude_self)
+        q = np.ascontiguousarray(query)
+        m = q.shape[0]
+        lib = _lib.load()
+        res = ctypes.c_void_p()
+        st = _lib.Stats()
+        _lib.check(lib.fuelg_range(self._handle, _lib.ptr(q), m, float(radius), int(exclude_self),
+                                   ctypes.byref(res), ctypes.byref(st)))
+        try:
+            mm, tot = ctypes.c_int64(), ctypes.c_int64()
+            _lib.check(lib.fuelg_range_size(res, ctypes.byref(mm), ctypes.byref(tot)))
+            off = np.empty(m + 1, np.int64)
+            idx = np.empty(max(1, tot.value), np.int64)
+            dist = np.empty(max(1, tot.value), np.float32)
+            _lib.check(lib.fuelg_range_copy(res, _lib.ptr(off), _lib.ptr(idx), _lib.ptr(dist)))
+        finally:
+            lib.fuelg_range_free(res)
+        self.last_stats = st.as_dict()
+        idx_list = [idx[off[i]:off[i + 1]].copy() for i in range(m)]
+        dist_list = [dist[off[i]:off[i + 1]].copy() for i in range(m)]
+        return idx_list, dist_list
+
+    def __repr__(self):
+        return f"<SearchIndex tree={self.tree!r} dtype={self.dtype!r} shape={self.shape!r}>"
+
+
+def knn_search(data, query, k, *, exclude_self=None, distance="euclidean", tree="auto", seed=None, **kw):
+    """python/fuel/search.py:315-368."""
+    data = _ensure_float(data)
+    query = _ensure_float(query)
+    index = SearchIndex(data, distance=distance, tree=tree, seed=seed, **kw)
+    return index.knn(query, k, exclude_self=exclude_self)
+
+
+def range_search(data, query, radius, *, exclude_self=None, distance="euclidean", tree="auto", seed=None, **kw):
+    """python/fuel/search.py:371-408."""
+    data = _ensure_float(data)
+    query = _ensure_float(query)
+    index = SearchIndex(data, distance=distance, tree=tree, seed=seed, **kw)
+    return index.radius_search(query, radius, exclude_self=exclude_self)

@@ -1,0 +1,133 @@
+/*
+ * fuelg.h -- C ABI of the GB300 engine for kno10/fuel's linear-scan kNN /
+ * range search and Lloyd k-means hot path.
+ *
+ * Plain C: pointers, sizes and status codes; no C++ or torch types.  Every
+ * pointer argument may be a host pointer or a CUDA device pointer (unified
+ * addressing); host buffers are staged through the device by the call.
+ * Every call is synchronous: when it returns, outputs are written.
+ * Calls return FUELG_OK (0) or a status code; fuelg_last_error() then gives a
+ * message for the calling thread.
+ *
+ * Semantics follow the reference exactly:
+ *  - distances use fuel's own summation order for the chosen host profile
+ *    (FUELG_ORDER_ARM = non-x86 builds: src/math/unroll.rs and the portable
+ *    fallback of src/distance/squared_euclidean.rs:99-133;
+ *    FUELG_ORDER_X86 = x86_64 AVX2+FMA builds: src/math/avx2.rs and
+ *    src/distance/squared_euclidean.rs:16-39), so the returned f32 distances
+ *    are bit-identical to fuel's;
+ *  - neighbours are ordered by (distance, index) as DistPair orders them
+ *    (src/api/search.rs:23-30), rows are truncated to k and padded with
+ *    -1 / +inf as knn_results_to_arrays does (python/search.rs:1195-1216).
+ */
+#ifndef FUELG_H
+#define FUELG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define FUELG_OK 0
+#define FUELG_EINVAL 1     /* bad argument (Python: ValueError)               */
+#define FUELG_ENOMEM 2     /* device or host allocation failed                 */
+#define FUELG_ECUDA 3      /* CUDA runtime error (Python: RuntimeError)        */
+#define FUELG_ECANCELLED 4 /* fuelg_cancel() was called (Python: KeyboardInterrupt) */
+#define FUELG_ENOTSUP 5    /* shape or option outside the supported envelope   */
+#define FUELG_ENODEV 6     /* no CUDA device                                   */
+#define FUELG_ETIMEOUT 7   /* a bounded device wait gave up                    */
+
+/* ---- enums --------------------------------------------------------------- */
+#define FUELG_METRIC_SQEUCLIDEAN 0 /* "sqeuclidean" / "squared_euclidean"  */
+#define FUELG_METRIC_EUCLIDEAN 1   /* "euclidean" / "l2": sqrt of the above */
+
+#define FUELG_ORDER_ARM 0 /* fuel built for a non-x86 host (e.g. Grace) */
+#define FUELG_ORDER_X86 1 /* fuel built for x86_64 with AVX2+FMA        */
+
+#define FUELG_EXCLUDE_NONE 0   /* keep self matches                                         */
+#define FUELG_EXCLUDE_LINEAR 1 /* linear-scan index: search k, drop self (python/search.rs:485-488) */
+#define FUELG_EXCLUDE_KPLUS1 2 /* tree / precomputed path: search k+1, drop self (python/search.rs:1163-1170) */
+
+#define FUELG_PREC_FP32 0       /* plain FP32 CUDA-core distances (exact reference order)  */
+#define FUELG_PREC_BF16 1       /* tcgen05 BF16 screen + exact FP32 re-score (d >= 32)     */
+#define FUELG_PREC_SPLIT_BF16 2 /* tcgen05 split-BF16 (hi+lo) screen + exact FP32 re-score */
+
+#define FUELG_LLOYD_FIXED_ITERS 1 /* run exactly max_iter iterations (ignore changed==0 stop) */
+
+typedef struct fuelg_index fuelg_index;
+typedef struct fuelg_range_result fuelg_range_result;
+
+/* Per-call measurements, filled when a non-NULL pointer is passed. */
+typedef struct {
+    double device_ms;       /* device time of the call's kernels (CUDA events)      */
+    int64_t h2d_bytes;      /* host->device bytes copied by the call                */
+    int64_t d2h_bytes;      /* device->host bytes copied by the call                */
+    int64_t distance_evals; /* (query, point) distances formed                       */
+    int64_t rescored;       /* rows re-scored exactly after a tensor-core screen    */
+    int32_t iterations;     /* Lloyd iterations run                                 */
+    int32_t precision_used; /* FUELG_PREC_* actually used                           */
+    double hot_kernel_ms;   /* summed device time of the dominant kernel's launches,
+                               CUDA events on the stream it runs on               */
+    int32_t hot_kernel_launches; /* launches of the dominant kernel               */
+    int32_t kernel_launches;     /* launches of this library's own kernels        */
+} fuelg_stats;
+
+/* Message for the last failing call on this thread ("" if none). */
+const char *fuelg_last_error(void);
+/* Library version string. */
+const char *fuelg_version(void);
+/* Number of visible CUDA devices. */
+int fuelg_device_count(int32_t *out_count);
+
+/* ---- linear-scan index ---------------------------------------------------
+ * Replaces build_linear_scan_f32 (python/search.rs:1353-1370).  Unlike the
+ * reference (whose LinearScanSearcher holds only the distance function,
+ * python/search.rs:516-518) the handle OWNS a device copy of the data, so
+ * repeated queries do not re-upload it. */
+int fuelg_index_create(const float *data, int64_t n, int32_t d, int32_t metric, int32_t order, fuelg_index **out);
+int fuelg_index_destroy(fuelg_index *index);
+int fuelg_index_info(const fuelg_index *index, int64_t *n, int32_t *d, int32_t *metric, int32_t *order);
+
+/* k nearest neighbours of every query row.  Replaces SearchIndex::knn for a
+ * linear index (python/search.rs:560-568 -> linear_scan_knn_batch :471-491 ->
+ * linear_scan_knn, src/api/search.rs:169-184).  out_idx / out_dist are
+ * [m, k] row-major (int64 / f32).  exclude_mode selects the exclude-self rule
+ * (FUELG_EXCLUDE_*), which drops index i from query row i. */
+int fuelg_knn(fuelg_index *index, const float *queries, int64_t m, int32_t k, int32_t exclude_mode, int32_t precision,
+              int64_t *out_idx, float *out_dist, fuelg_stats *stats);
+
+/* All points with distance <= radius (radius is cast to f32 as
+ * python/search.rs:781-783 does), sorted by (distance, index).  Replaces
+ * SearchIndex::radius_search (python/search.rs:776-790 -> linear_scan_range,
+ * src/api/search.rs:154-166).  The result is CSR, owned by the handle *out. */
+int fuelg_range(fuelg_index *index, const float *queries, int64_t m, double radius, int32_t exclude_self,
+                fuelg_range_result **out, fuelg_stats *stats);
+int fuelg_range_size(const fuelg_range_result *res, int64_t *m, int64_t *total);
+/* offsets: [m+1]; idx / dist: [total]. */
+int fuelg_range_copy(const fuelg_range_result *res, int64_t *offsets, int64_t *idx, float *dist);
+int fuelg_range_free(fuelg_range_result *res);
+
+/* Lloyd k-means with fixed initial centres.  Replaces lloyd_f32
+ * (python/kmeans.rs:188-218, 355) -> cluster::kmeans::lloyd
+ * (src/cluster/kmeans/lloyd.rs:118-202) with InitMethod::Fixed
+ * (python/kmeans.rs:111-130).  Centre sums/means are formed in FP64 and
+ * inertia is the FP64 sum of squared distances of the final pass.
+ * out_centers [k, d] f32, out_labels [n] int64. */
+int fuelg_kmeans_lloyd(const float *data, int64_t n, int32_t d, int32_t k, const float *init_centers,
+                       int32_t max_iter, double tol, int32_t precision, int32_t order, int32_t flags,
+                       float *out_centers, int64_t *out_labels, int32_t *out_iters, double *out_inertia,
+                       fuelg_stats *stats);
+
+/* Cooperative cancellation (src/api/mod.rs:29 SHUTDOWN_REQUESTED): running
+ * kernels poll a host-mapped word and stop; the call returns
+ * FUELG_ECANCELLED.  Each call clears the word when it starts, as
+ * py_interruptible does (src/api/parallel.rs:145-173). */
+int fuelg_cancel(void);
+int fuelg_reset_cancel(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FUELG_H */

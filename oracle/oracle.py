@@ -1,0 +1,296 @@
+"""Test-side oracle for fuel's linear-scan kNN / range search and Lloyd k-means.
+
+This module is TEST INFRASTRUCTURE.  Only the tests, ``__graft_entry__.smoke()``
+and the CPU-baseline leg of ``bench.py`` import it, and only as the checker
+(or, for the baseline, as the thing timed on the host cores).  The product
+library (``fuel_gb300``) never imports it.
+
+Two oracles live here:
+
+* ``libfuel_oracle.so`` (``fuel_oracle.c``): a C restatement of fuel's CPU
+  code in fuel's own operation order, for both summation profiles that fuel
+  compiles (``'arm'``: src/math/unroll.rs + the portable distance fallback;
+  ``'x86'``: src/math/avx2.rs + the AVX2/FMA distance kernel).  Its results
+  are bit-identical to what fuel returns on that ISA.
+* an FP64 oracle (numpy): distances formed and summed in double, ordered by
+  (distance, index) exactly like ``DistPair`` (src/api/search.rs:23-30).
+
+Pinned against the reference's own known answers in tests/test_oracle_golden.py.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "libfuel_oracle.so")
+_lib = None
+
+ORDERS = {"arm": 0, "x86": 1}
+KINDS = {"knn": 0, "sqdist": 1, "pairwise": 2, "dot": 3}
+METRICS = {"sqeuclidean": 0, "euclidean": 1}
+EXCLUDE = {"none": 0, "linear": 1, "kplus1": 2}
+
+
+def host_order() -> str:
+    """The summation profile fuel itself compiles on this machine."""
+    m = platform.machine().lower()
+    return "x86" if m in ("x86_64", "amd64") else "arm"
+
+
+def build() -> str:
+    """Compile libfuel_oracle.so in place (gcc, no cmake)."""
+    src = os.path.join(_HERE, "fuel_oracle.c")
+    if (not os.path.exists(_LIB_PATH)) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", _HERE])
+    return _LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    build()
+    lib = ctypes.CDLL(_LIB_PATH)
+    i64, i32, dbl = ctypes.c_int64, ctypes.c_int, ctypes.c_double
+    vp = ctypes.c_void_p
+    lib.fo_dist_f32.restype = ctypes.c_float
+    lib.fo_dist_f32.argtypes = [i32, i32, vp, vp, i64]
+    lib.fo_dist_f64.restype = ctypes.c_double
+    lib.fo_dist_f64.argtypes = [i32, i32, vp, vp, i64]
+    for nm in ("fo_pairwise_sqdist_f32", "fo_pairwise_sqdist_f64"):
+        getattr(lib, nm).restype = None
+        getattr(lib, nm).argtypes = [i32, vp, i64, vp, i64, i64, vp]
+    for nm in ("fo_knn_f32", "fo_knn_f64"):
+        getattr(lib, nm).restype = i32
+        getattr(lib, nm).argtypes = [vp, i64, i64, vp, i64, i64, i32, i32, i32, i32, vp, vp]
+    for nm in ("fo_range_f32", "fo_range_f64"):
+        getattr(lib, nm).restype = i32
+        getattr(lib, nm).argtypes = [vp, i64, i64, vp, i64, dbl, i32, i32, i32, i32,
+                                     ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
+    lib.fo_free.restype = None
+    lib.fo_free.argtypes = [vp]
+    lib.fo_lloyd_f32.restype = i32
+    lib.fo_lloyd_f32.argtypes = [vp, i64, i64, i64, vp, i64, dbl, i32, i32, i32, vp, vp,
+                                 ctypes.POINTER(i64), ctypes.POINTER(dbl), ctypes.POINTER(i64)]
+    lib.fo_lloyd_assign_f32.restype = i32
+    lib.fo_lloyd_assign_f32.argtypes = [vp, i64, i64, i64, vp, i32, i32, i32, vp, vp]
+    _lib = lib
+    return lib
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f(a, dtype):
+    return np.ascontiguousarray(a, dtype=dtype)
+
+
+def dist(kind: str, order: str, a, b) -> float:
+    """One per-pair distance in the reference's operation order."""
+    lib = load()
+    a = np.asarray(a)
+    if a.dtype == np.float64:
+        a, b = _f(a, np.float64), _f(b, np.float64)
+        return float(lib.fo_dist_f64(KINDS[kind], ORDERS[order], _p(a), _p(b), a.shape[0]))
+    a, b = _f(a, np.float32), _f(b, np.float32)
+    return np.float32(lib.fo_dist_f32(KINDS[kind], ORDERS[order], _p(a), _p(b), a.shape[0]))
+
+
+def pairwise_sqdist(p1, p2, order: str | None = None) -> np.ndarray:
+    """math::pairwise_sqdist (src/math/mod.rs) as an [n1, n2] matrix."""
+    lib = load()
+    order = order or host_order()
+    p1 = np.asarray(p1)
+    is64 = p1.dtype == np.float64
+    dt = np.float64 if is64 else np.float32
+    p1, p2 = _f(p1, dt), _f(p2, dt)
+    out = np.empty((p1.shape[0], p2.shape[0]), dtype=dt)
+    fn = lib.fo_pairwise_sqdist_f64 if is64 else lib.fo_pairwise_sqdist_f32
+    fn(ORDERS[order], _p(p1), p1.shape[0], _p(p2), p2.shape[0], p1.shape[1], _p(out))
+    return out
+
+
+def knn(X, Q, k: int, metric: str = "sqeuclidean", order: str | None = None, exclude: str = "none",
+        threads: int = 1):
+    """SearchIndex(tree='linear').knn: (int64[m,k], float[m,k]) with -1/+inf padding."""
+    lib = load()
+    order = order or host_order()
+    X = np.asarray(X)
+    is64 = X.dtype == np.float64
+    dt = np.float64 if is64 else np.float32
+    X, Q = _f(X, dt), _f(Q, dt)
+    m, d = Q.shape
+    idx = np.empty((m, k), dtype=np.int64)
+    dd = np.empty((m, k), dtype=dt)
+    fn = lib.fo_knn_f64 if is64 else lib.fo_knn_f32
+    rc = fn(_p(X), X.shape[0], d, _p(Q), m, k, METRICS[metric], ORDERS[order], EXCLUDE[exclude], threads,
+            _p(idx), _p(dd))
+    if rc != 0:
+        raise ValueError("oracle knn: bad arguments")
+    return idx, dd
+
+
+def range_search(X, Q, radius: float, metric: str = "sqeuclidean", order: str | None = None,
+                 exclude_self: bool = False, threads: int = 1):
+    """linear_scan_range per query row -> CSR (offsets[m+1], idx[], dist[])."""
+    lib = load()
+    order = order or host_order()
+    X = np.asarray(X)
+    is64 = X.dtype == np.float64
+    dt = np.float64 if is64 else np.float32
+    X, Q = _f(X, dt), _f(Q, dt)
+    m, d = Q.shape
+    po, pi, pd = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+    fn = lib.fo_range_f64 if is64 else lib.fo_range_f32
+    fn(_p(X), X.shape[0], d, _p(Q), m, float(radius), METRICS[metric], ORDERS[order], int(exclude_self),
+       threads, ctypes.byref(po), ctypes.byref(pi), ctypes.byref(pd))
+    off = np.ctypeslib.as_array(ctypes.cast(po, ctypes.POINTER(ctypes.c_int64)), shape=(m + 1,)).copy()
+    tot = int(off[-1])
+    if tot:
+        idx = np.ctypeslib.as_array(ctypes.cast(pi, ctypes.POINTER(ctypes.c_int64)), shape=(tot,)).copy()
+        ctyp = ctypes.c_double if is64 else ctypes.c_float
+        dist_ = np.ctypeslib.as_array(ctypes.cast(pd, ctypes.POINTER(ctyp)), shape=(tot,)).copy()
+    else:
+        idx = np.empty(0, np.int64)
+        dist_ = np.empty(0, dt)
+    for p in (po, pi, pd):
+        lib.fo_free(p)
+    return off, idx, dist_
+
+
+def lloyd(X, k: int, init, max_iter: int = 300, tol: float = 0.0, order: str | None = None,
+          threads: int = 1, sums: str = "reference"):
+    """lloyd() with a fixed init array.  sums='reference' reproduces fuel's f32
+    running sums (result depends on `threads`, the rayon thread count);
+    sums='fp64' uses fp64 cluster sums and returns the fp64 inertia."""
+    lib = load()
+    order = order or host_order()
+    X = _f(X, np.float32)
+    init = _f(init, np.float32)
+    n, d = X.shape
+    cent = np.empty((k, d), np.float32)
+    lab = np.empty(n, np.int64)
+    it = ctypes.c_int64()
+    inert = ctypes.c_double()
+    chg = ctypes.c_int64()
+    rc = lib.fo_lloyd_f32(_p(X), n, d, k, _p(init), max_iter, float(tol), ORDERS[order], threads,
+                          0 if sums == "reference" else 1, _p(cent), _p(lab), ctypes.byref(it),
+                          ctypes.byref(inert), ctypes.byref(chg))
+    if rc != 0:
+        raise ValueError("oracle lloyd: bad arguments")
+    return cent, lab, int(it.value), float(inert.value)
+
+
+def lloyd_assign(X, centers, initial: bool = False, order: str | None = None, threads: int = 1):
+    """One assignment pass against fixed centres: (labels int64[n], best f32[n])."""
+    lib = load()
+    order = order or host_order()
+    X = _f(X, np.float32)
+    C = _f(centers, np.float32)
+    n, d = X.shape
+    lab = np.empty(n, np.int64)
+    best = np.empty(n, np.float32)
+    lib.fo_lloyd_assign_f32(_p(X), n, d, C.shape[0], _p(C), int(initial), ORDERS[order], threads, _p(lab),
+                            _p(best))
+    return lab, best
+
+
+# --------------------------------------------------------------------------
+# FP64 oracle
+# --------------------------------------------------------------------------
+
+def sqdist_fp64(X, Q) -> np.ndarray:
+    """Exact-in-double squared distances [m, n]: differences and sums in fp64."""
+    X = np.asarray(X, np.float64)
+    Q = np.asarray(Q, np.float64)
+    out = np.empty((Q.shape[0], X.shape[0]), np.float64)
+    step = max(1, int(2e7 // max(1, X.shape[0] * X.shape[1])))
+    for s in range(0, Q.shape[0], step):
+        diff = Q[s:s + step, None, :] - X[None, :, :]
+        out[s:s + step] = np.einsum("mnd,mnd->mn", diff, diff)
+    return out
+
+
+def knn_fp64(X, Q, k: int, metric: str = "sqeuclidean", exclude_self: bool = False):
+    """Top-k by (fp64 distance, index); exclude_self drops index i for query i
+    after selecting k+1 (the tree-path semantics)."""
+    D = sqdist_fp64(X, Q)
+    if metric == "euclidean":
+        D = np.sqrt(D)
+    m, n = D.shape
+    idx = np.full((m, k), -1, np.int64)
+    dist_ = np.full((m, k), np.inf)
+    ar = np.arange(n)
+    for i in range(m):
+        order_ = np.lexsort((ar, D[i]))
+        if exclude_self:
+            order_ = order_[order_ != i]
+        order_ = order_[:k]
+        idx[i, :len(order_)] = order_
+        dist_[i, :len(order_)] = D[i, order_]
+    return idx, dist_
+
+
+def lloyd_inertia_fp64(X, centers, labels) -> float:
+    X = np.asarray(X, np.float64)
+    C = np.asarray(centers, np.float64)
+    diff = X - C[np.asarray(labels)]
+    return float(np.einsum("nd,nd->", diff, diff))
+
+
+# --------------------------------------------------------------------------
+# Outlier scores from kNN lists (for the ELKI golden vectors)
+# --------------------------------------------------------------------------
+
+def knn_outlier(dist_k: np.ndarray) -> np.ndarray:
+    """kNN outlier score: distance to the k-th neighbour (src/outlier/knn.rs:14-36)."""
+    return np.array([row[np.isfinite(row)][-1] if np.isfinite(row).any() else 0.0 for row in dist_k])
+
+
+def lof(idx: np.ndarray, dist_: np.ndarray) -> np.ndarray:
+    """Local outlier factor from exclusive k-NN lists (src/outlier/lof.rs:38-80)."""
+    n = idx.shape[0]
+    neigh = [[(int(j), float(dv)) for j, dv in zip(idx[i], dist_[i]) if j >= 0] for i in range(n)]
+    kdist = np.array([nb[-1][1] if nb else 0.0 for nb in neigh])
+    lrd = np.empty(n)
+    for i in range(n):
+        if not neigh[i]:
+            lrd[i] = np.inf
+            continue
+        s = 0.0
+        for j, dv in neigh[i]:
+            s += max(kdist[j], dv)
+        lrd[i] = len(neigh[i]) / s if s > 0 else np.inf
+    out = np.empty(n)
+    for i in range(n):
+        if not neigh[i] or np.isinf(lrd[i]):
+            out[i] = 1.0
+        else:
+            s = 0.0
+            for j, _ in neigh[i]:
+                s += lrd[j]
+            out[i] = s / (lrd[i] * len(neigh[i]))
+    return out
+
+
+def knn_with_ties(X, q, k: int, metric: str = "sqeuclidean", order: str | None = None):
+    """The full tie-inclusive linear_scan_knn list for one query (no truncation)."""
+    lib = load()
+    order = order or host_order()
+    X = _f(X, np.float32)
+    q = _f(q, np.float32).ravel()
+    fn = lib.fo_knn_ties_f32
+    fn.restype = ctypes.c_int64
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
+                   ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
+    cap = X.shape[0]
+    idx = np.empty(cap, np.int64)
+    dd = np.empty(cap, np.float32)
+    cnt = fn(_p(X), X.shape[0], X.shape[1], _p(q), k, METRICS[metric], ORDERS[order], cap, _p(idx), _p(dd))
+    return idx[:cnt].copy(), dd[:cnt].copy()

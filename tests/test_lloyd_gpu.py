@@ -1,0 +1,105 @@
+"""Parity of GPU Lloyd k-means with the restated fuel CPU path.
+
+Per iteration (the primary bar): given the same centres, the GPU assignment is
+bit-identical to fuel's (iteration 1 in the vec_pairwise_sqdist order,
+later iterations in the math::sqdist order, strict '<' so the lowest index
+wins ties).  Whole runs: the GPU forms centre sums in FP64, so it is compared
+with the oracle's FP64-sums Lloyd (labels, iteration count, centres within
+1 ulp, inertia within 1e-7 relative) and with fuel's f32-sums Lloyd (labels).
+"""
+import numpy as np
+import pytest
+
+from conftest import threads
+from fuel_gb300 import kmeans, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def ulp_diff(a, b):
+    ai = np.ascontiguousarray(a, np.float32).view(np.int32).astype(np.int64)
+    bi = np.ascontiguousarray(b, np.float32).view(np.int32).astype(np.int64)
+    return np.abs(ai - bi).max() if a.size else 0
+
+
+def mixture(n, d, k, seed):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(-10, 10, size=(k, d))
+    return (c[rng.integers(0, k, n)] + rng.normal(size=(n, d))).astype(np.float32)
+
+
+@pytest.mark.parametrize("order", ["arm", "x86"])
+@pytest.mark.parametrize("d,k", [(2, 4), (3, 7), (8, 16), (32, 10), (64, 33), (784, 64)])
+def test_per_iteration_assignment_bit_exact(gpu, oracle, order, d, k):
+    n = 3000 if d < 784 else 1500
+    X = mixture(n, d, k, d * 100 + k)
+    init = X[np.random.default_rng(1).choice(n, k, replace=False)]
+    for t in (1, 2, 3, 6):
+        r = kmeans(X, k=k, variant="lloyd", max_iter=t, init=init, order=order, fixed_iters=True)
+        lab, _ = oracle.lloyd_assign(X, r.centers, initial=(t == 1), order=order, threads=threads())
+        assert np.array_equal(r.labels, lab), f"iteration {t}: {np.sum(r.labels != lab)} labels differ"
+
+
+@pytest.mark.parametrize("order", ["arm", "x86"])
+def test_full_run_vs_fp64_oracle(gpu, oracle, order):
+    X = mixture(4000, 16, 12, 5)
+    init = X[:12].copy()
+    r = kmeans(X, k=12, variant="lloyd", max_iter=100, init=init, order=order)
+    c, lab, it, inert = oracle.lloyd(X, 12, init, max_iter=100, order=order, sums="fp64", threads=threads())
+    assert r.n_iter == it
+    assert np.array_equal(r.labels, lab)
+    assert ulp_diff(r.centers, c) <= 1
+    assert abs(r.inertia - inert) <= 1e-7 * inert
+    # fuel's own f32-sums trajectory lands on the same partition here
+    c2, lab2, it2, _ = oracle.lloyd(X, 12, init, max_iter=100, order=order, threads=8)
+    assert np.array_equal(r.labels, lab2)
+
+
+def test_lloyd_sparse_config_reduced(gpu, oracle):
+    """The k=64, d=784 sparse 0..255/255 workload at n=7,000, 10 iterations."""
+    X, init = workloads.lloyd_sparse(n=7000)
+    r = kmeans(X, k=64, variant="lloyd", max_iter=10, init=init, fixed_iters=True)
+    c, lab, it, inert = oracle.lloyd(X, 64, init, max_iter=10, sums="fp64", threads=threads())
+    assert r.n_iter == 10
+    assert np.array_equal(r.labels, lab)
+    assert ulp_diff(r.centers, c) <= 1
+    assert abs(r.inertia - inert) <= 1e-7 * inert
+    assert abs(r.inertia - oracle.lloyd_inertia_fp64(X, r.centers, r.labels)) <= 1e-9 * inert
+
+
+def test_fixed_iters_and_stop_rule(gpu):
+    X = mixture(2000, 4, 3, 9)
+    r1 = kmeans(X, k=3, variant="lloyd", max_iter=50, init="first")
+    assert r1.n_iter < 50
+    r2 = kmeans(X, k=3, variant="lloyd", max_iter=50, init="first", fixed_iters=True)
+    assert r2.n_iter == 50
+    assert np.array_equal(r1.labels, r2.labels)
+    r3 = kmeans(X, k=3, variant="lloyd", max_iter=50, init="first", tol=1e-3)
+    assert r3.n_iter <= r1.n_iter
+
+
+def test_edge_cases(gpu, oracle):
+    X = np.array([[0.0], [1.0], [2.0], [10.0]], np.float32)
+    # duplicate initial centre: centre 1 loses every tie and stays empty
+    init = np.array([[1.0], [1.0], [10.0]], np.float32)
+    r = kmeans(X, k=3, variant="lloyd", max_iter=5, init=init)
+    c, lab, it, _ = oracle.lloyd(X, 3, init, max_iter=5, sums="fp64")
+    assert np.array_equal(r.labels, lab) and r.n_iter == it
+    assert r.centers[1, 0] == 1.0
+    # k = 1 and k = n
+    r1 = kmeans(X, k=1, variant="lloyd", init="first")
+    assert (r1.labels == 0).all() and np.isclose(r1.centers[0, 0], 3.25)
+    rn = kmeans(X, k=4, variant="lloyd", init="first")
+    assert rn.labels.tolist() == [0, 1, 2, 3] and rn.inertia == 0.0
+    # max_iter = 1: only the initial assignment, centres are the init
+    r0 = kmeans(X, k=2, variant="lloyd", max_iter=1, init="first")
+    assert r0.n_iter == 1 and np.array_equal(r0.centers, X[:2])
+
+
+def test_deterministic(gpu):
+    X, init = workloads.lloyd_sparse(n=5000)
+    a = kmeans(X, k=64, variant="lloyd", max_iter=5, init=init)
+    b = kmeans(X, k=64, variant="lloyd", max_iter=5, init=init)
+    assert np.array_equal(a.labels, b.labels)
+    assert np.array_equal(a.centers.view(np.uint32), b.centers.view(np.uint32))
+    assert a.inertia == b.inertia
