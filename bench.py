@@ -164,12 +164,13 @@ def run_ours(args):
     och = torch.empty((K, D), dtype=torch.float32, pin_memory=True)
     olh = torch.empty((N,), dtype=torch.int64, pin_memory=True)
 
-    def step(device_resident=True):
+    def step(device_resident=True, precision=None):
         st = _lib.Stats()
         it = ctypes.c_int32()
         inert = ctypes.c_double()
         src = (Xd, Cd, oc, ol) if device_resident else (Xh, Ch, och, olh)
-        _lib.check(lib.fuelg_kmeans_lloyd(_lib.ptr(src[0]), N, D, K, _lib.ptr(src[1]), ITERS, 0.0, prec, order,
+        pr = prec if precision is None else precision
+        _lib.check(lib.fuelg_kmeans_lloyd(_lib.ptr(src[0]), N, D, K, _lib.ptr(src[1]), ITERS, 0.0, pr, order,
                                           _lib.LLOYD_FIXED_ITERS, _lib.ptr(src[2]), _lib.ptr(src[3]),
                                           ctypes.byref(it), ctypes.byref(inert), ctypes.byref(st)))
         assert it.value == ITERS
@@ -188,6 +189,8 @@ def run_ours(args):
         stats = [step(True) for _ in range(args.steps)]
     barrier()
     dev_ms = sum(s.device_ms for s, _ in stats)
+    rescored = sum(s.rescored for s, _ in stats)
+    prec_used = stats[-1][0].precision_used
     hot_ms = sum(s.hot_kernel_ms for s, _ in stats)
     hot_n = sum(s.hot_kernel_launches for s, _ in stats)
     launches = sum(s.kernel_launches for s, _ in stats)
@@ -203,6 +206,16 @@ def run_ours(args):
     h2d = e2e[0][0].h2d_bytes
     d2h = e2e[0][0].d2h_bytes
 
+    # the plain FP32 CUDA-core tier on the same workload, for the TC-vs-plain ratio
+    plain = None
+    if prec != 0:
+        step(True, 0)
+        pst = [step(True, 0) for _ in range(2)]
+        pms = sum(s.device_ms for s, _ in pst)
+        plain = {"iters_per_s": ITERS * len(pst) / (pms / 1e3),
+                 "hot_kernel_ms": sum(s.hot_kernel_ms for s, _ in pst) / max(1, sum(s.hot_kernel_launches
+                                                                                      for s, _ in pst))}
+
     t_max = dev_ms
     e2e_max = e2e_ms
     if world > 1:
@@ -216,9 +229,15 @@ def run_ours(args):
     pk = peaks()
     value = world * ITERS * args.steps / (t_max / 1e3)
     e2e_value = world * ITERS * args.steps / (e2e_max / 1e3)
-    # roofline of the hot kernel (the assignment scan): algorithmic bytes per launch =
+    # roofline of the hot kernel.  Tensor-core tier: one read of the BF16 copy of X
+    # (n*d*2), the BF16 centres (k*d*2) and one int32 label per point.  Plain tier:
     # one read of X (n*d*4) + the centres (k*d*4) + one 8-byte key per point.
-    alg_bytes = N * D * 4 + K * D * 4 + N * 8
+    if prec_used != 0:
+        alg_bytes = N * D * 2 * (2 if prec_used == 2 else 1) + K * D * 2 + N * 4
+        hot_name = "lloyd_tc_kernel (tcgen05 BF16 screen of the Lloyd assignment)"
+    else:
+        alg_bytes = N * D * 4 + K * D * 4 + N * 8
+        hot_name = "scan_topk_kernel (exact FP32 Lloyd assignment)"
     avg_launch_ms = hot_ms / max(1, hot_n)
     achieved = alg_bytes / (avg_launch_ms / 1e3) / 1e9
     hbm_peak = pk.get("hbm_gbs", 6800.0)
@@ -235,7 +254,7 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "bf16+f32" if prec_used else "f32", "data": "synthetic",
         "config": {"workload": f"lloyd k={K} n={N} d={D}, {ITERS} fixed iterations per step", "n": N, "d": D,
                    "k": K, "iters_per_step": ITERS, "precision": args.precision,
                    "summation_order": _lib.default_order(),
@@ -244,13 +263,17 @@ def run_ours(args):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None,
-                     "kernel": "scan_topk_kernel (Lloyd assignment)",
+                     "kernel": hot_name, "alg_bytes_per_launch": alg_bytes,
                      "avg_launch_ms": avg_launch_ms, "peak_source": "measured" if "_fallback" not in pk else
                      "fallback"},
         "cpu_baseline": {"value": cpu_value, "unit": "iters/s", "cores": threads, "kind": "port",
                          "sample": f"{sample_iters} iterations of the full n={N} matrix, restated fuel CPU Lloyd"},
         "clocks": clk.summary(),
         "inertia": inertia,
+        "precision_used": {0: "fp32", 1: "bf16", 2: "split_bf16"}[prec_used],
+        "rescored_fraction": rescored / float(N * ITERS * args.steps),
+        "plain_fp32": plain,
+        "tc_vs_plain": (value / plain["iters_per_s"]) if plain else None,
         "knn_plain": knn,
     }
     print(json.dumps(line), flush=True)
@@ -288,7 +311,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="fp32")
+    ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="bf16")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -555,7 +555,7 @@ int fuelg_kmeans_lloyd(const float* data, int64_t n, int32_t d, int32_t k, const
     stats->distance_evals = (int64_t)r.iters * n * k;
     stats->rescored = r.rescored;
     stats->iterations = r.iters;
-    stats->precision_used = precision;
+    stats->precision_used = r.precision_used;
     meter.fill(stats);
   }
   return ST_OK;

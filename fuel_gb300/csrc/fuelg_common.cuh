@@ -197,6 +197,86 @@ __device__ __forceinline__ void pair_dists(const float* __restrict__ q, const fl
   }
 }
 
+// Same arithmetic as pair_dists<KIND, ORDER, 1>, reading both rows with scalar
+// loads from any address (global memory, no alignment requirement).  Used to
+// re-score the few candidates a tensor-core screen cannot decide.
+template <int KIND, int ORDER>
+__device__ __forceinline__ float exact_dist_scalar(const float* __restrict__ q, const float* __restrict__ x, int d) {
+  const bool lane8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
+  const bool fma8 = (KIND == KIND_KNN && ORDER == ORDER_X86);
+  if (lane8) {
+    float acc[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) acc[l] = 0.0f;
+    const int sd = d & ~7;
+    for (int i = 0; i < sd; i += 8) {
+#pragma unroll
+      for (int l = 0; l < 8; l++) {
+        const float df = __fsub_rn(__ldg(q + i + l), __ldg(x + i + l));
+        acc[l] = fma8 ? __fmaf_rn(df, df, acc[l]) : __fadd_rn(sq_rn(df), acc[l]);
+      }
+    }
+    float s = acc[0];
+#pragma unroll
+    for (int l = 1; l < 8; l++) s = __fadd_rn(s, acc[l]);
+    for (int i = sd; i < d; i++) {
+      const float df = __fsub_rn(__ldg(q + i), __ldg(x + i));
+      s = fma8 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+    }
+    return s;
+  }
+  if (KIND == KIND_SQDIST) {  // x86 avx2::sqdist_f32
+    if (d < 4) {
+      float s = 0.0f;
+      for (int i = 0; i < d; i++) {
+        const float df = __fsub_rn(__ldg(q + i), __ldg(x + i));
+        s = __fadd_rn(s, sq_rn(df));
+      }
+      return s;
+    }
+    float a[4][8];
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+#pragma unroll
+      for (int l = 0; l < 8; l++) a[u][l] = 0.0f;
+    int i = 0;
+    for (; i + 32 <= d; i += 32) {
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int l = 0; l < 8; l++) {
+          const float df = __fsub_rn(__ldg(q + i + u * 8 + l), __ldg(x + i + u * 8 + l));
+          a[u][l] = __fmaf_rn(df, df, a[u][l]);
+        }
+    }
+    float c[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) c[l] = __fadd_rn(__fadd_rn(a[0][l], a[1][l]), __fadd_rn(a[2][l], a[3][l]));
+    for (; i + 8 <= d; i += 8) {
+#pragma unroll
+      for (int l = 0; l < 8; l++) {
+        const float df = __fsub_rn(__ldg(q + i + l), __ldg(x + i + l));
+        c[l] = __fmaf_rn(df, df, c[l]);
+      }
+    }
+    float s = __fadd_rn(__fadd_rn(__fadd_rn(c[0], c[4]), __fadd_rn(c[1], c[5])),
+                        __fadd_rn(__fadd_rn(c[2], c[6]), __fadd_rn(c[3], c[7])));
+    for (; i < d; i++) {
+      const float df = __fsub_rn(__ldg(q + i), __ldg(x + i));
+      s = __fmaf_rn(df, df, s);
+    }
+    return s;
+  }
+  // KIND_PAIRWISE: one chain; FMA chain for x86 with d >= 4
+  const bool fma_chain = (ORDER == ORDER_X86) && d >= 4;
+  float s = 0.0f;
+  for (int i = 0; i < d; i++) {
+    const float df = __fsub_rn(__ldg(q + i), __ldg(x + i));
+    s = fma_chain ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+  }
+  return s;
+}
+
 // Row stride (floats) for shared-memory tiles: 16-byte aligned rows whose
 // stride is an odd number of float4s, so eight lanes reading eight different
 // rows with 16-byte loads hit 32 distinct banks.

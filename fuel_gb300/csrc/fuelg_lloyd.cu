@@ -28,8 +28,14 @@
 
 namespace fuelg {
 
-int lloyd_assign_tc(const LloydParams& p, const float* centers, int32_t* labels, int32_t* changed_count,
-                    int64_t* rescored, int* dev_status, cudaStream_t stream);
+struct TcLloydState;
+TcLloydState* lloyd_tc_new();
+void lloyd_tc_delete(TcLloydState*);
+bool lloyd_tc_supported(int d, int k);
+int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream);
+int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* labels,
+                    int32_t* changed_count, int* dev_status, cudaStream_t stream);
+int lloyd_tc_rescored_total(TcLloydState* st, cudaStream_t stream, int64_t* out);
 
 namespace {
 
@@ -238,6 +244,21 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
     }
   } hf{h_changed};
 
+  // Tensor-core tier: BF16 (or hi+lo BF16) screen + exact re-score, for d >= 32 and k <= 256.
+  TcLloydState* tc = nullptr;
+  struct TcFree {
+    TcLloydState*& t;
+    ~TcFree() {
+      if (t) lloyd_tc_delete(t);
+    }
+  } tcf{tc};
+  r->precision_used = 0;
+  if (p.precision != 0 && lloyd_tc_supported(d, k)) {
+    tc = lloyd_tc_new();
+    FUELG_TRY(lloyd_tc_prepare(p, tc, stream));
+    r->precision_used = p.precision;
+  }
+
   cudaEvent_t ev0, ev1;
   FUELG_CUDA(cudaEventCreate(&ev0));
   FUELG_CUDA(cudaEventCreate(&ev1));
@@ -245,9 +266,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
 
   auto assign = [&](bool first) -> int {
     FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t) * 2, stream));
-    if (p.precision != 0 && !first) {
-      return lloyd_assign_tc(p, C, labels, changed.as<int32_t>(), &r->rescored, dev_status, stream);
-    }
+    if (tc) return lloyd_assign_tc(p, tc, C, first, labels, changed.as<int32_t>(), dev_status, stream);
     ExactScanParams sp;
     sp.A = p.X;
     sp.m = n;
@@ -330,6 +349,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   }
   r->iters = iters;
   FUELG_CUDA(cudaEventRecord(ev1, stream));
+  if (tc) FUELG_TRY(lloyd_tc_rescored_total(tc, stream, &r->rescored));
   inertia_partial_kernel<<<inert_blocks, 256, 0, stream>>>(p.X, n, d, inertia_centers, labels, inert_part.as<double>()); ::fuelg::note_launch();
   sum_partials_kernel<<<1, 32, 0, stream>>>(inert_part.as<double>(), inert_blocks, inert.as<double>()); ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());

@@ -103,3 +103,41 @@ def test_deterministic(gpu):
     assert np.array_equal(a.labels, b.labels)
     assert np.array_equal(a.centers.view(np.uint32), b.centers.view(np.uint32))
     assert a.inertia == b.inertia
+
+
+# ---------------------------------------------------------------------------
+# Tensor-core tiers: BF16 / split-BF16 screen + exact re-score must give the
+# same assignment as the exact path, iteration by iteration.
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("precision", ["bf16", "split_bf16"])
+@pytest.mark.parametrize("order", ["arm", "x86"])
+@pytest.mark.parametrize("d,k", [(32, 10), (64, 33), (100, 64), (784, 64), (128, 256), (40, 17)])
+def test_tc_tier_per_iteration_bit_exact(gpu, oracle, precision, order, d, k):
+    n = 3000 if d < 784 else 2000
+    X = mixture(n, d, k, d * 7 + k)
+    init = X[np.random.default_rng(2).choice(n, k, replace=False)]
+    for t in (1, 2, 4):
+        r = kmeans(X, k=k, variant="lloyd", max_iter=t, init=init, order=order, fixed_iters=True,
+                   precision=precision)
+        assert r.stats["precision_used"] == {"bf16": 1, "split_bf16": 2}[precision]
+        lab, _ = oracle.lloyd_assign(X, r.centers, initial=(t == 1), order=order, threads=threads())
+        assert np.array_equal(r.labels, lab), f"iteration {t}: {np.sum(r.labels != lab)} labels differ"
+
+
+@pytest.mark.parametrize("precision", ["bf16", "split_bf16"])
+def test_tc_tier_matches_exact_run(gpu, precision):
+    X, init = workloads.lloyd_sparse(n=9000)
+    a = kmeans(X, k=64, variant="lloyd", max_iter=12, init=init, fixed_iters=True)
+    b = kmeans(X, k=64, variant="lloyd", max_iter=12, init=init, fixed_iters=True, precision=precision)
+    assert np.array_equal(a.labels, b.labels)
+    assert np.array_equal(a.centers.view(np.uint32), b.centers.view(np.uint32))
+    assert a.inertia == b.inertia
+    # the hi+lo screen decides almost every point without re-scoring
+    if precision == "split_bf16":
+        assert b.stats["rescored"] < 0.2 * 9000 * 12
+
+
+def test_tc_tier_small_d_falls_back_to_exact(gpu):
+    X = mixture(500, 8, 4, 1)
+    r = kmeans(X, k=4, variant="lloyd", init="first", precision="bf16")
+    assert r.stats["precision_used"] == 0
