@@ -159,6 +159,7 @@ struct LloydResult {
   double inertia = 0.0;
   int64_t rescored = 0;       // points re-scored exactly (tensor-core tiers)
   int precision_used = 0;     // tier that actually ran
+  bool exact_sums = false;    // centroid sums exact (integer) rather than FP64
   double kernel_ms = 0.0;
 };
 int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_t stream);

@@ -33,20 +33,31 @@ TcLloydState* lloyd_tc_new();
 void lloyd_tc_delete(TcLloydState*);
 bool lloyd_tc_supported(int d, int k);
 int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream);
-int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* labels,
-                    int32_t* changed_count, int* dev_status, cudaStream_t stream);
+int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* lab_new,
+                    int* dev_status, cudaStream_t stream);
+struct ExactSums;
+ExactSums* exact_sums_new();
+void exact_sums_delete(ExactSums*);
+int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaStream_t stream);
+int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
+                    bool write_centers, float* centers, int32_t* changed, cudaStream_t stream);
 int lloyd_tc_rescored_total(TcLloydState* st, cudaStream_t stream, int64_t* out);
 
 namespace {
 
 constexpr int kChunk = 32;  // rows per FP64 partial-sum chunk
 
-__global__ void post_assign_kernel(const uint64_t* __restrict__ keys, int64_t n, int32_t* __restrict__ labels,
+__global__ void keys_to_labels_kernel(const uint64_t* __restrict__ keys, int64_t n, int32_t* __restrict__ lab) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) lab[i] = (int32_t)key_idx(keys[i]);
+}
+
+__global__ void post_assign_kernel(const int32_t* __restrict__ lab_new, int64_t n, int32_t* __restrict__ labels,
                                    int first, int32_t* __restrict__ changed) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int c = 0;
   if (i < n) {
-    const int32_t a = (int32_t)key_idx(keys[i]);
+    const int32_t a = lab_new[i];
     if (first || labels[i] != a) c = 1;
     labels[i] = a;
   }
@@ -189,6 +200,79 @@ int end_bit_for(int k) {
   return b;
 }
 
+// ---- FP64 fallback sums (data whose exponent range exceeds 128 bits) -----
+struct Fp64Sums {
+  int64_t n = 0;
+  int d = 0, k = 0, ebit = 0;
+  int64_t max_chunks = 0;
+  size_t sort_bytes = 0, scan_bytes = 0;
+  Scratch perm_in, perm, lab_sorted, counts, offs, nchunks, chunk_off, chunk_cluster, partial, tmp;
+};
+
+int fp64_sums_init(Fp64Sums* f, int64_t n, int d, int k, int32_t* labels, cudaStream_t stream) {
+  f->n = n;
+  f->d = d;
+  f->k = k;
+  f->ebit = end_bit_for(k);
+  f->max_chunks = n / kChunk + k + 1;
+  FUELG_TRY(f->perm_in.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(f->perm.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(f->lab_sorted.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(f->counts.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(f->offs.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(f->nchunks.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(f->chunk_off.alloc(sizeof(int32_t) * (k + 1), stream));
+  FUELG_TRY(f->chunk_cluster.alloc(sizeof(int32_t) * f->max_chunks, stream));
+  FUELG_TRY(f->partial.alloc(sizeof(double) * f->max_chunks * d, stream));
+  FUELG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, f->sort_bytes, labels, f->lab_sorted.as<int32_t>(),
+                                             f->perm_in.as<int32_t>(), f->perm.as<int32_t>(), (int)n, 0, f->ebit,
+                                             stream));
+  FUELG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, f->scan_bytes, f->counts.as<int32_t>(), f->offs.as<int32_t>(),
+                                           k + 1, stream));
+  FUELG_TRY(f->tmp.alloc(std::max(f->sort_bytes, f->scan_bytes), stream));
+  iota_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(f->perm_in.as<int32_t>(), n); ::fuelg::note_launch();
+  return ST_OK;
+}
+
+// centre_j = (f32)(FP64 sum of member rows in ascending point order / count)
+int fp64_sums_update(Fp64Sums* f, const float* X, const int32_t* labels, float* C, cudaStream_t stream) {
+  const int64_t n = f->n;
+  const int d = f->d, k = f->k;
+  FUELG_CUDA(cudaMemsetAsync(f->counts.p, 0, sizeof(int32_t) * (k + 1), stream));
+  if (k <= 8192) {
+    count_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, sizeof(int32_t) * k, stream>>>(
+        labels, n, k, f->counts.as<int32_t>()); ::fuelg::note_launch();
+  } else {
+    count_global_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, stream>>>(
+        labels, n, f->counts.as<int32_t>()); ::fuelg::note_launch();
+  }
+  size_t sb = f->sort_bytes;
+  FUELG_CUDA(cub::DeviceRadixSort::SortPairs(f->tmp.p, sb, labels, f->lab_sorted.as<int32_t>(),
+                                             f->perm_in.as<int32_t>(), f->perm.as<int32_t>(), (int)n, 0, f->ebit,
+                                             stream));
+  size_t scb = f->scan_bytes;
+  FUELG_CUDA(cub::DeviceScan::ExclusiveSum(f->tmp.p, scb, f->counts.as<int32_t>(), f->offs.as<int32_t>(), k + 1,
+                                           stream));
+  chunk_count_kernel<<<(k + 255) / 256, 256, 0, stream>>>(f->counts.as<int32_t>(), k, f->nchunks.as<int32_t>()); ::fuelg::note_launch();
+  FUELG_CUDA(cudaMemsetAsync(f->nchunks.as<int32_t>() + k, 0, sizeof(int32_t), stream));
+  scb = f->scan_bytes;
+  FUELG_CUDA(cub::DeviceScan::ExclusiveSum(f->tmp.p, scb, f->nchunks.as<int32_t>(), f->chunk_off.as<int32_t>(),
+                                           k + 1, stream));
+  chunk_table_kernel<<<k, 128, 0, stream>>>(f->chunk_off.as<int32_t>(), f->nchunks.as<int32_t>(), k,
+                                            f->chunk_cluster.as<int32_t>()); ::fuelg::note_launch();
+  const int ty = (d + 255) / 256;
+  dim3 g1((unsigned)f->max_chunks, ty);
+  chunk_sum_kernel<<<g1, 256, 0, stream>>>(X, d, f->perm.as<int32_t>(), f->offs.as<int32_t>(),
+                                           f->counts.as<int32_t>(), f->chunk_off.as<int32_t>(),
+                                           f->chunk_cluster.as<int32_t>(), f->chunk_off.as<int32_t>() + k,
+                                           f->partial.as<double>()); ::fuelg::note_launch();
+  dim3 g2(k, ty);
+  reduce_update_kernel<<<g2, 256, 0, stream>>>(f->partial.as<double>(), d, k, f->counts.as<int32_t>(),
+                                               f->chunk_off.as<int32_t>(), f->nchunks.as<int32_t>(), C); ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  return ST_OK;
+}
+
 }  // namespace
 
 int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_t stream) {
@@ -206,34 +290,14 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   int32_t* labels = r->labels;
   FUELG_CUDA(cudaMemcpyAsync(C, p.init, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
 
-  Scratch keys, changed, perm_in, perm, lab_sorted, counts, offs, nchunks, chunk_off, chunk_cluster, partial, tmp,
-      frob, cold, inert_part, inert;
-  const int64_t max_chunks = n / kChunk + k + 1;
-  FUELG_TRY(keys.alloc(sizeof(uint64_t) * n, stream));
+  Scratch keys, lab_new, changed, frob, cold, inert_part, inert;
+  FUELG_TRY(lab_new.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(changed.alloc(sizeof(int32_t) * 2, stream));
-  FUELG_TRY(perm_in.alloc(sizeof(int32_t) * n, stream));
-  FUELG_TRY(perm.alloc(sizeof(int32_t) * n, stream));
-  FUELG_TRY(lab_sorted.alloc(sizeof(int32_t) * n, stream));
-  FUELG_TRY(counts.alloc(sizeof(int32_t) * (k + 1), stream));
-  FUELG_TRY(offs.alloc(sizeof(int32_t) * (k + 1), stream));
-  FUELG_TRY(nchunks.alloc(sizeof(int32_t) * (k + 1), stream));
-  FUELG_TRY(chunk_off.alloc(sizeof(int32_t) * (k + 1), stream));
-  FUELG_TRY(chunk_cluster.alloc(sizeof(int32_t) * max_chunks, stream));
-  FUELG_TRY(partial.alloc(sizeof(double) * max_chunks * d, stream));
   FUELG_TRY(frob.alloc(sizeof(double) * 2, stream));
   if (p.tol > 0) FUELG_TRY(cold.alloc(sizeof(float) * k * d, stream));
   const int inert_blocks = 4 * 152;
   FUELG_TRY(inert_part.alloc(sizeof(double) * inert_blocks, stream));
   FUELG_TRY(inert.alloc(sizeof(double), stream));
-
-  size_t sort_bytes = 0, scan_bytes = 0;
-  const int ebit = end_bit_for(k);
-  FUELG_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, sort_bytes, labels, lab_sorted.as<int32_t>(),
-                                             perm_in.as<int32_t>(), perm.as<int32_t>(), (int)n, 0, ebit, stream));
-  FUELG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, scan_bytes, counts.as<int32_t>(), offs.as<int32_t>(), k + 1,
-                                           stream));
-  FUELG_TRY(tmp.alloc(std::max(sort_bytes, scan_bytes), stream));
-  iota_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(perm_in.as<int32_t>(), n); ::fuelg::note_launch();
 
   int32_t* h_changed = nullptr;
   FUELG_CUDA(cudaMallocHost(&h_changed, sizeof(int32_t)));
@@ -243,6 +307,18 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
       if (p) cudaFreeHost(p);
     }
   } hf{h_changed};
+
+  // Exact integer centroid sums (fuelg_sums.cu); FP64 sums when the data's
+  // exponent range does not fit 128 bits.
+  ExactSums* es = exact_sums_new();
+  struct EsFree {
+    ExactSums* e;
+    ~EsFree() { exact_sums_delete(e); }
+  } esf{es};
+  const bool exact = exact_sums_init(es, p.X, n, d, k, stream) == ST_OK;
+  r->exact_sums = exact;
+  Fp64Sums fs;
+  if (!exact) FUELG_TRY(fp64_sums_init(&fs, n, d, k, labels, stream));
 
   // Tensor-core tier: BF16 (or hi+lo BF16) screen + exact re-score, for d >= 32 and k <= 256.
   TcLloydState* tc = nullptr;
@@ -257,6 +333,8 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
     tc = lloyd_tc_new();
     FUELG_TRY(lloyd_tc_prepare(p, tc, stream));
     r->precision_used = p.precision;
+  } else {
+    FUELG_TRY(keys.alloc(sizeof(uint64_t) * n, stream));
   }
 
   cudaEvent_t ev0, ev1;
@@ -264,9 +342,9 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   FUELG_CUDA(cudaEventCreate(&ev1));
   FUELG_CUDA(cudaEventRecord(ev0, stream));
 
+  // nearest centre of every point -> lab_new
   auto assign = [&](bool first) -> int {
-    FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t) * 2, stream));
-    if (tc) return lloyd_assign_tc(p, tc, C, first, labels, changed.as<int32_t>(), dev_status, stream);
+    if (tc) return lloyd_assign_tc(p, tc, C, first, lab_new.as<int32_t>(), dev_status, stream);
     ExactScanParams sp;
     sp.A = p.X;
     sp.m = n;
@@ -278,53 +356,33 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
     sp.metric = METRIC_SQEUCLIDEAN;
     sp.kk = 1;
     FUELG_TRY(exact_topk(sp, keys.as<uint64_t>(), dev_status, stream));
-    post_assign_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(keys.as<uint64_t>(), n, labels, first ? 1 : 0,
-                                                                       changed.as<int32_t>()); ::fuelg::note_launch();
+    keys_to_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(keys.as<uint64_t>(), n,
+                                                                          lab_new.as<int32_t>()); ::fuelg::note_launch();
     FUELG_CUDA(cudaGetLastError());
     return ST_OK;
   };
-
-  auto update_centers = [&]() -> int {
-    FUELG_CUDA(cudaMemsetAsync(counts.p, 0, sizeof(int32_t) * (k + 1), stream));
-    if (k <= 8192) {
-      count_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, sizeof(int32_t) * k, stream>>>(
-          labels, n, k, counts.as<int32_t>()); ::fuelg::note_launch();
-    } else {
-      count_global_kernel<<<(unsigned)std::min<int64_t>((n + 255) / 256, 1024), 256, 0, stream>>>(
-          labels, n, counts.as<int32_t>()); ::fuelg::note_launch();
-    }
-    size_t sb = sort_bytes;
-    FUELG_CUDA(cub::DeviceRadixSort::SortPairs(tmp.p, sb, labels, lab_sorted.as<int32_t>(), perm_in.as<int32_t>(),
-                                               perm.as<int32_t>(), (int)n, 0, ebit, stream));
-    size_t scb = scan_bytes;
-    FUELG_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, scb, counts.as<int32_t>(), offs.as<int32_t>(), k + 1, stream));
-    chunk_count_kernel<<<(k + 255) / 256, 256, 0, stream>>>(counts.as<int32_t>(), k, nchunks.as<int32_t>()); ::fuelg::note_launch();
-    FUELG_CUDA(cudaMemsetAsync(nchunks.as<int32_t>() + k, 0, sizeof(int32_t), stream));
-    scb = scan_bytes;
-    FUELG_CUDA(
-        cub::DeviceScan::ExclusiveSum(tmp.p, scb, nchunks.as<int32_t>(), chunk_off.as<int32_t>(), k + 1, stream));
-    chunk_table_kernel<<<k, 128, 0, stream>>>(chunk_off.as<int32_t>(), nchunks.as<int32_t>(), k,
-                                              chunk_cluster.as<int32_t>()); ::fuelg::note_launch();
-    const int ty = (d + 255) / 256;
-    dim3 g1((unsigned)max_chunks, ty);
-    chunk_sum_kernel<<<g1, 256, 0, stream>>>(p.X, d, perm.as<int32_t>(), offs.as<int32_t>(), counts.as<int32_t>(),
-                                             chunk_off.as<int32_t>(), chunk_cluster.as<int32_t>(),
-                                             chunk_off.as<int32_t>() + k, partial.as<double>()); ::fuelg::note_launch();
+  // one pass: assign, commit labels, update sums, and (if another pass
+  // follows) the centres it will use
+  auto pass = [&](bool first, bool write_centers) -> int {
+    FUELG_TRY(assign(first));
+    if (p.tol > 0 && write_centers)
+      FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
+    if (exact)
+      return exact_sums_step(es, p.X, lab_new.as<int32_t>(), labels, first, write_centers, C, changed.as<int32_t>(),
+                             stream);
+    FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t), stream));
+    post_assign_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(lab_new.as<int32_t>(), n, labels,
+                                                                       first ? 1 : 0, changed.as<int32_t>()); ::fuelg::note_launch();
     FUELG_CUDA(cudaGetLastError());
-    if (p.tol > 0) FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
-    dim3 g2(k, ty);
-    reduce_update_kernel<<<g2, 256, 0, stream>>>(partial.as<double>(), d, k, counts.as<int32_t>(),
-                                                 chunk_off.as<int32_t>(), nchunks.as<int32_t>(), C); ::fuelg::note_launch();
-    FUELG_CUDA(cudaGetLastError());
+    if (write_centers) FUELG_TRY(fp64_sums_update(&fs, p.X, labels, C, stream));
     return ST_OK;
   };
 
   const float* inertia_centers = C;
-  FUELG_TRY(assign(true));
+  FUELG_TRY(pass(true, p.max_iter > 1));
   int iters = 1;
   while (iters < p.max_iter) {
     iters++;
-    FUELG_TRY(update_centers());
     if (p.tol > 0) {
       frob_kernel<<<1, 256, 0, stream>>>(cold.as<float>(), C, (int64_t)k * d, frob.as<double>()); ::fuelg::note_launch();
       double h2[2];
@@ -340,7 +398,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
         break;
       }
     }
-    FUELG_TRY(assign(false));
+    FUELG_TRY(pass(false, iters < p.max_iter));
     if (!p.fixed_iters) {
       FUELG_CUDA(cudaMemcpyAsync(h_changed, changed.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
       FUELG_CUDA(cudaStreamSynchronize(stream));

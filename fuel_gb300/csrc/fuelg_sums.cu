@@ -1,0 +1,367 @@
+// fuelg_sums.cu -- exact, order-independent centroid sums for Lloyd.
+//
+// fuel keeps f32 running sums updated by per-chunk f32 deltas
+// (src/cluster/kmeans/lloyd.rs:154-199), so its centres depend on the rayon
+// chunking.  Here every coordinate sum is kept EXACTLY as an integer: each f32
+// value x is an integer multiple of 2^e_lo, where e_lo is the weight of the
+// lowest set mantissa bit over all of X, so x = I(x) * 2^e_lo with |I(x)| <
+// 2^(e_hi - e_lo + 1).  A running sum is stored modulo 2^(32L) as L
+// uint64 limbs of 32-bit slices (two's complement), updated only for the
+// points whose label changed (+x into the new cluster, -x out of the old).
+// Integer addition is associative, so the slices may be accumulated with
+// atomics in any order and the result is bit-for-bit deterministic.  The
+// centre is then the correctly rounded (round-to-nearest-even) f32 of the
+// exact mean sum/count -- the value an exact-arithmetic Lloyd would produce.
+// Empty clusters keep their centre (lloyd.rs:138-146).
+#include <algorithm>
+#include <cmath>
+
+#include "fuelg_common.cuh"
+#include "fuelg_internal.h"
+
+namespace fuelg {
+
+namespace {
+
+constexpr int kRows = 32;  // rows per accumulation chunk
+
+__device__ __forceinline__ void f32_parts(float x, uint32_t& mant, int& lsb, int& msb, bool& zero, bool& bad) {
+  const uint32_t b = __float_as_uint(x);
+  const uint32_t eb = (b >> 23) & 0xffu;
+  const uint32_t m = b & 0x7fffffu;
+  zero = (b & 0x7fffffffu) == 0;
+  bad = eb == 0xffu;
+  if (eb == 0) {  // subnormal: m * 2^-149
+    mant = m;
+    lsb = m ? -149 + __ffs((int)m) - 1 : 0;
+    msb = m ? -149 + 31 - __clz((int)m) : 0;
+  } else {
+    mant = m | 0x800000u;
+    lsb = (int)eb - 150 + __ffs((int)mant) - 1;
+    msb = (int)eb - 127;
+  }
+}
+
+__global__ void exp_range_kernel(const float* __restrict__ X, int64_t count, int* __restrict__ out) {
+  int lo = 1 << 30, hi = -(1 << 30), bad = 0;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
+    uint32_t mant;
+    int l, h;
+    bool z, b;
+    f32_parts(X[e], mant, l, h, z, b);
+    if (b) bad = 1;
+    if (!z && !b) {
+      lo = min(lo, l);
+      hi = max(hi, h);
+    }
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, off));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, off));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, off);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[0], lo);
+    atomicMax(&out[1], hi);
+    if (bad) atomicOr(&out[2], 1);
+  }
+}
+
+// Two's complement of +-I(x) modulo 2^128 (callers use the low 32L bits).
+__device__ __forceinline__ unsigned __int128 fixed_of(float x, int e_lo, bool negate) {
+  uint32_t mant;
+  int l, h;
+  bool z, b;
+  f32_parts(x, mant, l, h, z, b);
+  if (z) return 0;
+  const uint32_t bits = __float_as_uint(x);
+  const int eb = (int)((bits >> 23) & 0xffu);
+  const int unit = (eb == 0 ? -149 : eb - 150);  // weight of mantissa bit 0
+  const int sh = unit - e_lo;
+  unsigned __int128 v = sh >= 0 ? ((unsigned __int128)mant << sh) : (unsigned __int128)(mant >> (-sh));
+  const bool neg = ((bits >> 31) != 0) != negate;
+  return neg ? (unsigned __int128)0 - v : v;
+}
+
+// Changed labels -> change list + per-cluster in/out histograms.  `first`: no
+// previous label (the initial assignment puts every point in).
+__global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first,
+                                      int32_t* __restrict__ labels, int32_t* __restrict__ chg_i,
+                                      int32_t* __restrict__ chg_old, int32_t* __restrict__ chg_new,
+                                      int32_t* __restrict__ nchg, int32_t* __restrict__ cin,
+                                      int32_t* __restrict__ cout) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  bool ch = false;
+  int32_t nw = 0, old = -1;
+  if (i < n) {
+    nw = lab_new[i];
+    old = first ? -1 : labels[i];
+    ch = nw != old;
+    if (ch) labels[i] = nw;
+  }
+  const unsigned mask = __ballot_sync(0xffffffffu, ch);
+  if (!mask) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(nchg, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (ch) {
+    const int pos = base + __popc(mask & ((1u << lane) - 1));
+    chg_i[pos] = (int32_t)i;
+    chg_old[pos] = old;
+    chg_new[pos] = nw;
+    atomicAdd(&cin[nw], 1);
+    if (old >= 0) atomicAdd(&cout[old], 1);
+  }
+}
+
+// Single CTA: bucket offsets and the chunk table (in-chunks of cluster 0..k-1,
+// then out-chunks), member counts, cursor reset.
+__global__ void bucket_plan_kernel(int k, int32_t* __restrict__ cin, int32_t* __restrict__ cout,
+                                   int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
+                                   int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts) {
+  __shared__ int32_t s_in, s_out, s_ch;
+  if (threadIdx.x == 0) s_in = s_out = s_ch = 0;
+  __syncthreads();
+  // sequential scans in cluster order by thread 0 over tiles; k is small
+  if (threadIdx.x == 0) {
+    int32_t a = 0, b = 0, c = 0;
+    for (int j = 0; j < k; j++) {
+      off_in[j] = a;
+      a += cin[j];
+      chunk_off[j] = c;
+      c += (cin[j] + kRows - 1) / kRows;
+    }
+    for (int j = 0; j < k; j++) {
+      off_out[j] = b;
+      b += cout[j];
+      chunk_off[k + j] = c;
+      c += (cout[j] + kRows - 1) / kRows;
+    }
+    chunk_off[2 * k] = c;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < k; j += blockDim.x) counts[j] += cin[j] - cout[j];
+}
+
+__global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
+                                      const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg,
+                                      const int32_t* __restrict__ off_in, const int32_t* __restrict__ off_out,
+                                      int32_t* __restrict__ cur_in, int32_t* __restrict__ cur_out,
+                                      int32_t* __restrict__ bucket_in, int32_t* __restrict__ bucket_out) {
+  const int cnt = *nchg;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x) {
+    const int32_t i = chg_i[e], o = chg_old[e], w = chg_new[e];
+    bucket_in[off_in[w] + atomicAdd(&cur_in[w], 1)] = i;
+    if (o >= 0) bucket_out[off_out[o] + atomicAdd(&cur_out[o], 1)] = i;
+  }
+}
+
+// One chunk of <= 32 rows of one cluster, signed; thread per coordinate.
+template <int L>
+__global__ void accumulate_kernel(const float* __restrict__ X, int d, int k, int e_lo,
+                                  const int32_t* __restrict__ chunk_off, const int32_t* __restrict__ cin,
+                                  const int32_t* __restrict__ cout, const int32_t* __restrict__ off_in,
+                                  const int32_t* __restrict__ off_out, const int32_t* __restrict__ bucket_in,
+                                  const int32_t* __restrict__ bucket_out, unsigned long long* __restrict__ limbs) {
+  const int c = blockIdx.x;
+  const int total = chunk_off[2 * k];
+  if (c >= total) return;
+  // locate (cluster, sign) of chunk c: binary search over chunk_off[0..2k]
+  int lo = 0, hi = 2 * k - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (chunk_off[mid] <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  const bool out = lo >= k;
+  const int j = out ? lo - k : lo;
+  const int r0 = (c - chunk_off[lo]) * kRows;
+  const int cnt = out ? cout[j] : cin[j];
+  const int rows = min(kRows, cnt - r0);
+  const int32_t* src = (out ? bucket_out + off_out[j] : bucket_in + off_in[j]) + r0;
+  __shared__ int32_t rid[kRows];
+  if (threadIdx.x < rows) rid[threadIdx.x] = src[threadIdx.x];
+  __syncthreads();
+  for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < d; t += gridDim.y * blockDim.x) {
+    unsigned long long acc[L];
+#pragma unroll
+    for (int l = 0; l < L; l++) acc[l] = 0;
+    for (int r = 0; r < rows; r++) {
+      const unsigned __int128 v = fixed_of(__ldg(X + (int64_t)rid[r] * d + t), e_lo, out);
+#pragma unroll
+      for (int l = 0; l < L; l++) acc[l] += (unsigned long long)((v >> (32 * l)) & 0xffffffffu);
+    }
+    unsigned long long* dst = limbs + ((int64_t)j * d + t) * L;
+#pragma unroll
+    for (int l = 0; l < L; l++)
+      if (acc[l]) atomicAdd(dst + l, acc[l]);  // integer: exact in any order
+  }
+}
+
+// Correctly rounded (RNE) f32 of A * 2^e / cnt for A > 0 (normal range).
+__device__ float rn_ratio_f32(unsigned __int128 A, unsigned long long cnt, int e) {
+  const int bitsA = A >> 64 ? 128 - __clzll((long long)(unsigned long long)(A >> 64))
+                            : 64 - __clzll((long long)(unsigned long long)A);
+  const int bitsC = 64 - __clzll((long long)cnt);
+  int sh = 0;
+  if (bitsA - bitsC < 27) sh = 27 - (bitsA - bitsC);
+  const unsigned __int128 A2 = A << sh;
+  const unsigned __int128 q = A2 / cnt;
+  const unsigned __int128 r = A2 - q * cnt;
+  const int p = q >> 64 ? 128 - __clzll((long long)(unsigned long long)(q >> 64))
+                        : 64 - __clzll((long long)(unsigned long long)q);
+  const int drop = p - 24;
+  unsigned long long mant = (unsigned long long)(q >> drop);
+  const unsigned __int128 rem = q & (((unsigned __int128)1 << drop) - 1);
+  const unsigned __int128 half = (unsigned __int128)1 << (drop - 1);
+  if (rem > half || (rem == half && (r != 0 || (mant & 1)))) mant += 1;
+  return ldexpf((float)mant, drop + e - sh);
+}
+
+// Canonicalise every coordinate's limbs and write the exact mean of non-empty
+// clusters as the correctly rounded f32 centre.
+template <int L>
+__global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, int d, int e_lo,
+                            const int32_t* __restrict__ counts, float* __restrict__ centers) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kd; e += (int64_t)gridDim.x * blockDim.x) {
+    unsigned long long* lp = limbs + e * L;
+    unsigned __int128 tot = 0;
+#pragma unroll
+    for (int l = 0; l < L; l++) tot += (unsigned __int128)lp[l] << (32 * l);
+    if (L < 4) tot &= (((unsigned __int128)1) << (32 * L)) - 1;
+#pragma unroll
+    for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
+    const int j = (int)(e / d);
+    const int cnt = counts[j];
+    if (cnt <= 0) continue;
+    const bool neg = (tot >> (32 * L - 1)) & 1;
+    unsigned __int128 mag = tot;
+    if (neg) {
+      mag = (L < 4 ? (((unsigned __int128)1) << (32 * L)) : (unsigned __int128)0) - tot;
+      if (L < 4) mag &= (((unsigned __int128)1) << (32 * L)) - 1;
+    }
+    float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, e_lo);
+    centers[e] = neg ? -v : v;
+  }
+}
+
+}  // namespace
+
+struct ExactSums {
+  int L = 0, e_lo = 0, k = 0, d = 0;
+  int64_t n = 0;
+  Scratch limbs, counts, chg_i, chg_old, chg_new, nchg, cin, cout, off_in, off_out, cur, chunk_off, bucket_in,
+      bucket_out, range;
+  int64_t max_chunks = 0;
+};
+
+ExactSums* exact_sums_new() { return new ExactSums(); }
+void exact_sums_delete(ExactSums* s) { delete s; }
+
+// Scan X for its exponent range; returns ST_ENOTSUP when the exact integer
+// form would need more than 128 bits (or X holds inf/NaN): callers fall back.
+int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaStream_t stream) {
+  s->n = n;
+  s->d = d;
+  s->k = k;
+  FUELG_TRY(s->range.alloc(sizeof(int) * 3, stream));
+  int init[3] = {1 << 30, -(1 << 30), 0};
+  FUELG_CUDA(cudaMemcpyAsync(s->range.p, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+  exp_range_kernel<<<4 * 152, 256, 0, stream>>>(X, n * (int64_t)d, s->range.as<int>()); ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  int h[3];
+  FUELG_CUDA(cudaMemcpyAsync(h, s->range.p, sizeof(h), cudaMemcpyDeviceToHost, stream));
+  FUELG_CUDA(cudaStreamSynchronize(stream));
+  if (h[2]) {
+    set_error("data holds inf or NaN");
+    return ST_ENOTSUP;
+  }
+  int e_lo = h[0], e_hi = h[1];
+  if (e_lo > e_hi) e_lo = e_hi = 0;  // all zeros
+  int logn = 0;
+  while ((1ll << logn) < n + 1) logn++;
+  const int bits = (e_hi - e_lo + 1) + logn + 1;
+  const int L = (bits + 31) / 32;
+  if (L > 4) {
+    set_error("exponent range of the data (%d bits) exceeds the exact 128-bit centroid sums", e_hi - e_lo + 1);
+    return ST_ENOTSUP;
+  }
+  s->L = L;
+  s->e_lo = e_lo;
+  FUELG_TRY(s->limbs.alloc(sizeof(unsigned long long) * (size_t)k * d * L, stream));
+  FUELG_CUDA(cudaMemsetAsync(s->limbs.p, 0, sizeof(unsigned long long) * (size_t)k * d * L, stream));
+  FUELG_TRY(s->counts.alloc(sizeof(int32_t) * k, stream));
+  FUELG_CUDA(cudaMemsetAsync(s->counts.p, 0, sizeof(int32_t) * k, stream));
+  FUELG_TRY(s->chg_i.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(s->chg_old.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(s->chg_new.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(s->nchg.alloc(sizeof(int32_t), stream));
+  FUELG_TRY(s->cin.alloc(sizeof(int32_t) * 4 * (size_t)k, stream));  // cin, cout, cur_in, cur_out
+  FUELG_TRY(s->off_in.alloc(sizeof(int32_t) * 2 * (size_t)k, stream));
+  FUELG_TRY(s->chunk_off.alloc(sizeof(int32_t) * (2 * (size_t)k + 1), stream));
+  FUELG_TRY(s->bucket_in.alloc(sizeof(int32_t) * n, stream));
+  FUELG_TRY(s->bucket_out.alloc(sizeof(int32_t) * n, stream));
+  s->max_chunks = 2 * (n / kRows) + 2 * (int64_t)k + 2;
+  return ST_OK;
+}
+
+int exact_sums_L(const ExactSums* s) { return s->L; }
+
+// Apply one assignment pass: commit lab_new into labels, record the changes,
+// update the exact sums and counts, and write the new centres.  *changed
+// (device) receives the number of changed labels.
+int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
+                    bool write_centers, float* centers, int32_t* changed, cudaStream_t stream) {
+  const int64_t n = s->n;
+  const int k = s->k, d = s->d;
+  int32_t* cin = s->cin.as<int32_t>();
+  int32_t* cout = cin + k;
+  int32_t* cur_in = cin + 2 * k;
+  int32_t* cur_out = cin + 3 * k;
+  int32_t* off_in = s->off_in.as<int32_t>();
+  int32_t* off_out = off_in + k;
+  FUELG_CUDA(cudaMemsetAsync(s->cin.p, 0, sizeof(int32_t) * 4 * (size_t)k, stream));
+  FUELG_CUDA(cudaMemsetAsync(s->nchg.p, 0, sizeof(int32_t), stream));
+  commit_changes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(
+      lab_new, n, first ? 1 : 0, labels, s->chg_i.as<int32_t>(), s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(),
+      s->nchg.as<int32_t>(), cin, cout); ::fuelg::note_launch();
+  bucket_plan_kernel<<<1, 256, 0, stream>>>(k, cin, cout, off_in, off_out, s->chunk_off.as<int32_t>(),
+                                            s->counts.as<int32_t>()); ::fuelg::note_launch();
+  bucket_scatter_kernel<<<2 * 152, 256, 0, stream>>>(s->chg_i.as<int32_t>(), s->chg_old.as<int32_t>(),
+                                                     s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), off_in, off_out,
+                                                     cur_in, cur_out, s->bucket_in.as<int32_t>(),
+                                                     s->bucket_out.as<int32_t>()); ::fuelg::note_launch();
+  const int ty = (d + 255) / 256;
+  dim3 g((unsigned)s->max_chunks, ty);
+  auto acc = [&](auto Lc) {
+    constexpr int LL = decltype(Lc)::value;
+    accumulate_kernel<LL><<<g, 256, 0, stream>>>(X, d, k, s->e_lo, s->chunk_off.as<int32_t>(), cin, cout, off_in,
+                                                 off_out, s->bucket_in.as<int32_t>(), s->bucket_out.as<int32_t>(),
+                                                 s->limbs.as<unsigned long long>()); ::fuelg::note_launch();
+  };
+  switch (s->L) {
+    case 1: acc(std::integral_constant<int, 1>()); break;
+    case 2: acc(std::integral_constant<int, 2>()); break;
+    case 3: acc(std::integral_constant<int, 3>()); break;
+    default: acc(std::integral_constant<int, 4>()); break;
+  }
+  FUELG_CUDA(cudaGetLastError());
+  if (write_centers) {
+    const int64_t kd = (int64_t)k * d;
+    const unsigned mg = (unsigned)std::min<int64_t>((kd + 255) / 256, 8 * 152);
+    switch (s->L) {
+      case 1: mean_kernel<1><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
+      case 2: mean_kernel<2><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
+      case 3: mean_kernel<3><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
+      default: mean_kernel<4><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
+    }
+    ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+  }
+  FUELG_CUDA(cudaMemcpyAsync(changed, s->nchg.p, sizeof(int32_t), cudaMemcpyDeviceToDevice, stream));
+  return ST_OK;
+}
+
+}  // namespace fuelg

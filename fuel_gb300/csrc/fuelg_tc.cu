@@ -413,38 +413,107 @@ __global__ void prep_rows_kernel(const float* __restrict__ X, int64_t rows, int6
   }
 }
 
-// Exact re-score of the undecided points: the candidate centres of each are
-// scored with the reference's own f32 operation order, first minimum wins.
+// Exact re-score of the undecided points: each candidate centre is scored
+// with the reference's own f32 operation order, first minimum wins.  One warp
+// per undecided point; the lanes mirror the reference's SIMD lanes:
+//   8-lane kinds (math::sqdist on non-x86, the linear-scan distance): 8 lanes
+//     per candidate, lane l owns accumulator l, 4 candidates at a time;
+//   avx2::sqdist_f32: 32 lanes per candidate, lane 8u+l owns accumulator u,l;
+//   pairwise chains (initial pass): one lane per candidate.
+template <int KIND, int ORDER>
+__device__ __forceinline__ float warp_candidate_dist(const float* __restrict__ x, const float* __restrict__ c, int d,
+                                                     int lane) {
+  constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
+  constexpr bool FMA8 = (KIND == KIND_KNN && ORDER == ORDER_X86);
+  if constexpr (LANE8) {
+    const int l = lane & 7, g0 = lane & ~7;
+    const int sd = d & ~7;
+    float acc = 0.0f;
+    for (int i = l; i < sd; i += 8) {
+      const float df = __fsub_rn(__ldg(x + i), __ldg(c + i));
+      acc = FMA8 ? __fmaf_rn(df, df, acc) : __fadd_rn(sq_rn(df), acc);
+    }
+    float s = __shfl_sync(0xffffffffu, acc, g0);
+#pragma unroll
+    for (int t = 1; t < 8; t++) s = __fadd_rn(s, __shfl_sync(0xffffffffu, acc, g0 + t));
+    for (int i = sd; i < d; i++) {
+      const float df = __fsub_rn(__ldg(x + i), __ldg(c + i));
+      s = FMA8 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+    }
+    return s;  // valid on every lane of the group
+  } else if constexpr (KIND == KIND_SQDIST) {  // x86 avx2::sqdist_f32, d >= 4
+    const int nb = d / 32;
+    float a = 0.0f;
+    for (int b = 0; b < nb; b++) {
+      const float df = __fsub_rn(__ldg(x + b * 32 + lane), __ldg(c + b * 32 + lane));
+      a = __fmaf_rn(df, df, a);
+    }
+    const int l = lane & 7;
+    const float a0 = __shfl_sync(0xffffffffu, a, l), a1 = __shfl_sync(0xffffffffu, a, l + 8);
+    const float a2 = __shfl_sync(0xffffffffu, a, l + 16), a3 = __shfl_sync(0xffffffffu, a, l + 24);
+    float cl = __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
+    int i = nb * 32;
+    for (; i + 8 <= d; i += 8) {
+      const float df = __fsub_rn(__ldg(x + i + l), __ldg(c + i + l));
+      cl = __fmaf_rn(df, df, cl);
+    }
+    float v[8];
+#pragma unroll
+    for (int t = 0; t < 8; t++) v[t] = __shfl_sync(0xffffffffu, cl, t);
+    float s = __fadd_rn(__fadd_rn(__fadd_rn(v[0], v[4]), __fadd_rn(v[1], v[5])),
+                        __fadd_rn(__fadd_rn(v[2], v[6]), __fadd_rn(v[3], v[7])));
+    for (; i < d; i++) {
+      const float df = __fsub_rn(__ldg(x + i), __ldg(c + i));
+      s = __fmaf_rn(df, df, s);
+    }
+    return s;
+  } else {
+    return exact_dist_scalar<KIND, ORDER>(x, c, d);  // one lane, one chain
+  }
+}
+
 template <int KIND, int ORDER>
 __global__ void rescore_kernel(const float* __restrict__ X, const float* __restrict__ C, int d, int mw,
                                const int32_t* __restrict__ ulist, const uint64_t* __restrict__ umask,
-                               const int32_t* __restrict__ ucount, int32_t* __restrict__ lab_new) {
+                               const int32_t* __restrict__ ucount, int32_t* __restrict__ lab_new,
+                               unsigned long long* __restrict__ tally) {
+  constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
+  constexpr int G = LANE8 ? 8 : (KIND == KIND_SQDIST ? 32 : 1);  // lanes per candidate
+  constexpr int PER = 32 / G;                                      // candidates per warp step
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int cnt = *ucount;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *tally += (unsigned long long)cnt;
   for (int64_t u = gw; u < cnt; u += nwarps) {
     const int64_t i = ulist[u];
     const float* x = X + i * d;
     uint64_t best = KEY_NONE;
-    int seen = 0;
-    for (int w = 0; w < mw; w++) {
-      uint64_t m = umask[u * mw + w];
-      while (m) {
+    // walk the candidate bits PER at a time; this lane's slot is lane / G
+    int w = 0;
+    uint64_t m = umask[u * mw];
+    const int slot = lane / G;
+    for (;;) {
+      int got = 0, j = 0;
+      while (got < PER) {
+        while (m == 0 && w + 1 < mw) m = umask[u * mw + (++w)];
+        if (m == 0) break;
         const int b = __ffsll((long long)m) - 1;
         m &= m - 1;
-        const int j = w * 64 + b;
-        if ((seen & 31) == lane) {
-          const float* c = C + (int64_t)j * d;
-          // lloyd.rs:166-168 calls sqdist(centre, point); the pairwise kernel of
-          // the initial pass takes (point, centre).  The squares are identical.
-          const float dist = KIND == KIND_PAIRWISE ? exact_dist_scalar<KIND, ORDER>(x, c, d)
-                                                   : exact_dist_scalar<KIND, ORDER>(c, x, d);
-          const uint64_t key = make_key(dist, (uint32_t)j);
-          best = key < best ? key : best;
-        }
-        seen++;
+        if (got == slot) j = w * 64 + b;
+        got++;
       }
+      if (got == 0) break;
+      const bool mine = slot < got;
+      if (!mine) j = 0;  // idle slots score centre 0 and discard it
+      // lloyd.rs:166-168 calls sqdist(centre, point); the initial pairwise
+      // kernel takes (point, centre).  The squares are identical either way.
+      const float dist = warp_candidate_dist<KIND, ORDER>(x, C + (int64_t)j * d, d, lane);
+      if (mine && (lane % G) == 0) {
+        const uint64_t key = make_key(dist, (uint32_t)j);
+        best = key < best ? key : best;
+      }
+      if (got < PER) break;
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -453,21 +522,6 @@ __global__ void rescore_kernel(const float* __restrict__ X, const float* __restr
     }
     if (lane == 0) lab_new[i] = (int32_t)key_idx(best);
   }
-}
-
-__global__ void commit_labels_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first,
-                                     int32_t* __restrict__ labels, int32_t* __restrict__ changed,
-                                     const int32_t* __restrict__ ucount, unsigned long long* __restrict__ rescored) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i == 0) *rescored += (unsigned long long)*ucount;
-  int c = 0;
-  if (i < n) {
-    const int32_t v = lab_new[i];
-    if (first || labels[i] != v) c = 1;
-    labels[i] = v;
-  }
-  c = __syncthreads_count(c);
-  if (threadIdx.x == 0 && c) atomicAdd(changed, c);
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -512,7 +566,7 @@ struct TcLloydState {
   bool split = false;
   int dp = 0, kp = 0, kc = 0, mw = 0, stages = 0;
   size_t smem = 0;
-  Scratch xhi, xlo, xnrm2, xnrm, chi, clo, cnrm2, cnrm, lab_new, ulist, umask, ucount, rescored_total;
+  Scratch xhi, xlo, xnrm2, xnrm, chi, clo, cnrm2, cnrm, ulist, umask, ucount, rescored_total;
   CUtensorMap tmA, tmAlo, tmB, tmBlo;
 };
 
@@ -545,7 +599,6 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   if (st->split) FUELG_TRY(st->clo.alloc(cb, stream));
   FUELG_TRY(st->cnrm2.alloc(sizeof(float) * st->kp, stream));
   FUELG_TRY(st->cnrm.alloc(sizeof(float) * st->kp, stream));
-  FUELG_TRY(st->lab_new.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(st->ulist.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(st->umask.alloc(sizeof(uint64_t) * n * st->mw, stream));
   FUELG_TRY(st->ucount.alloc(sizeof(int32_t), stream));
@@ -573,8 +626,8 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   return ST_OK;
 }
 
-int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* labels,
-                    int32_t* changed_count, int* dev_status, cudaStream_t stream) {
+int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* lab_new,
+                    int* dev_status, cudaStream_t stream) {
   const int64_t n = p.n;
   // centre copies and norms for this iteration (padded rows are zero)
   if (st->split)
@@ -597,7 +650,7 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
   a.xn = st->xnrm.as<float>();
   a.nc = st->cnrm2.as<float>();
   a.cn = st->cnrm.as<float>();
-  a.lab_new = st->lab_new.as<int32_t>();
+  a.lab_new = lab_new;
   a.ulist = st->ulist.as<int32_t>();
   a.umask = st->umask.as<uint64_t>();
   a.ucount = st->ucount.as<int32_t>();
@@ -639,21 +692,19 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
   if (kind == KIND_PAIRWISE) {
     if (p.order == ORDER_X86)
       rescore_kernel<KIND_PAIRWISE, ORDER_X86><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
-                                                                         a.ucount, a.lab_new);
+                                                                         a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>());
     else
       rescore_kernel<KIND_PAIRWISE, ORDER_ARM><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
-                                                                         a.ucount, a.lab_new); ::fuelg::note_launch();
+                                                                         a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
   } else {
     if (p.order == ORDER_X86)
       rescore_kernel<KIND_SQDIST, ORDER_X86><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
-                                                                       a.ucount, a.lab_new);
+                                                                       a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>());
     else
       rescore_kernel<KIND_SQDIST, ORDER_ARM><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
-                                                                       a.ucount, a.lab_new); ::fuelg::note_launch();
+                                                                       a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
   }
-  commit_labels_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(
-      a.lab_new, n, first ? 1 : 0, labels, changed_count, a.ucount, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
-  FUELG_CUDA(cudaGetLastError());
+FUELG_CUDA(cudaGetLastError());
   return ST_OK;
 }
 

@@ -294,3 +294,101 @@ def knn_with_ties(X, q, k: int, metric: str = "sqeuclidean", order: str | None =
     dd = np.empty(cap, np.float32)
     cnt = fn(_p(X), X.shape[0], X.shape[1], _p(q), k, METRICS[metric], ORDERS[order], cap, _p(idx), _p(dd))
     return idx[:cnt].copy(), dd[:cnt].copy()
+
+
+# --------------------------------------------------------------------------
+# Exact-mean Lloyd: fuel's assignment order, centres = correctly rounded f32
+# of the exact mean of each cluster's member rows.
+# --------------------------------------------------------------------------
+
+def rn_f32_ratio(S: int, cnt: int, e_lo: int) -> np.float32:
+    """Round-to-nearest-even f32 of S * 2**e_lo / cnt (S, cnt Python ints)."""
+    import math
+    if S == 0:
+        return np.float32(0.0)
+    neg = S < 0
+    A = -S if neg else S
+    sh = max(0, 27 - (A.bit_length() - cnt.bit_length()))
+    q, r = divmod(A << sh, cnt)
+    drop = q.bit_length() - 24
+    mant = q >> drop
+    rem = q & ((1 << drop) - 1)
+    half = 1 << (drop - 1)
+    if rem > half or (rem == half and (r != 0 or (mant & 1))):
+        mant += 1
+    v = np.float32(math.ldexp(float(mant), drop + e_lo - sh))
+    return -v if neg else v
+
+
+def fixed_point(X: np.ndarray):
+    """Exact integer form of f32 data: X == I * 2**e_lo.  Returns (I, e_lo)
+    with I int64 when the sums of up to len(X) rows fit, else Python ints."""
+    X = np.ascontiguousarray(X, np.float32)
+    bits = X.view(np.uint32).astype(np.int64)
+    eb = (bits >> 23) & 0xFF
+    mant = (bits & 0x7FFFFF) | np.where(eb != 0, 1 << 23, 0)
+    unit = np.where(eb == 0, -149, eb - 150)
+    nz = mant != 0
+    if not nz.any():
+        return np.zeros(X.shape, np.int64), 0
+    ctz = np.zeros_like(mant)
+    mm = np.where(nz, mant, 1)
+    while True:
+        odd = (mm & 1) == 1
+        if odd.all():
+            break
+        ctz += np.where(odd, 0, 1)
+        mm = np.where(odd, mm, mm >> 1)
+    # mant = mm * 2**ctz with mm odd, so X = mm * 2**(unit + ctz)
+    low = unit + ctz
+    e_lo = int(low[nz].min())
+    e_hi = int((unit[nz] + np.floor(np.log2(mant[nz])).astype(np.int64)).max())
+    sign = np.where((bits >> 31) & 1, -1, 1)
+    width = e_hi - e_lo + 1 + int(np.ceil(np.log2(X.shape[0] + 1))) + 1
+    if width <= 62:
+        I = np.where(nz, sign * (mm << (low - e_lo)), 0)
+        return I.astype(np.int64), e_lo
+    obj = np.empty(X.shape, dtype=object)
+    flat_m, flat_s, flat_l, flat_z = mm.ravel(), sign.ravel(), low.ravel(), nz.ravel()
+    out = obj.ravel()
+    for t in range(out.size):
+        out[t] = int(flat_s[t]) * (int(flat_m[t]) << int(flat_l[t] - e_lo)) if flat_z[t] else 0
+    return obj, e_lo
+
+
+def exact_means(I, e_lo, labels, k, prev):
+    C = np.array(prev, np.float32, copy=True)
+    for j in range(k):
+        rows = np.nonzero(labels == j)[0]
+        if len(rows) == 0:
+            continue
+        S = I[rows].sum(axis=0)
+        cnt = len(rows)
+        C[j] = [rn_f32_ratio(int(s), cnt, e_lo) for s in S]
+    return C
+
+
+def lloyd_exact(X, k: int, init, max_iter: int = 300, order: str | None = None, threads: int = 1,
+                fixed_iters: bool = False):
+    """Lloyd with fuel's assignment arithmetic (iteration 1: pairwise order;
+    later: math::sqdist order; first index wins ties) and exact-mean centres;
+    the loop and iteration count follow src/cluster/kmeans/lloyd.rs:118-202
+    (fixed_iters ignores the changed == 0 stop).  Returns (centres, labels,
+    iterations, fp64 inertia)."""
+    X = np.ascontiguousarray(X, np.float32)
+    C = np.ascontiguousarray(init, np.float32).copy()
+    I, e_lo = fixed_point(X)
+    labels, _ = lloyd_assign(X, C, initial=True, order=order, threads=threads)
+    if max_iter > 1:
+        C = exact_means(I, e_lo, labels, k, C)
+    it = 1
+    while it < max_iter:
+        it += 1
+        new, _ = lloyd_assign(X, C, initial=False, order=order, threads=threads)
+        changed = int((new != labels).sum())
+        labels = new
+        if it < max_iter:
+            C = exact_means(I, e_lo, labels, k, C)
+        if not fixed_iters and changed == 0:
+            break
+    return C, labels, it, lloyd_inertia_fp64(X, C, labels)

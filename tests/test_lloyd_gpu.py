@@ -3,9 +3,11 @@
 Per iteration (the primary bar): given the same centres, the GPU assignment is
 bit-identical to fuel's (iteration 1 in the vec_pairwise_sqdist order,
 later iterations in the math::sqdist order, strict '<' so the lowest index
-wins ties).  Whole runs: the GPU forms centre sums in FP64, so it is compared
-with the oracle's FP64-sums Lloyd (labels, iteration count, centres within
-1 ulp, inertia within 1e-7 relative) and with fuel's f32-sums Lloyd (labels).
+wins ties).  Whole runs: the GPU keeps exact integer centroid sums and sets
+every centre to the correctly rounded f32 of the exact mean, so it is compared
+bit-for-bit (labels, iteration count, centre bits) with the exact-mean Lloyd
+oracle, with inertia within 1e-7 relative of the FP64 value; fuel's own
+f32-sums Lloyd is checked to land on the same partition.
 """
 import numpy as np
 import pytest
@@ -41,30 +43,43 @@ def test_per_iteration_assignment_bit_exact(gpu, oracle, order, d, k):
 
 
 @pytest.mark.parametrize("order", ["arm", "x86"])
-def test_full_run_vs_fp64_oracle(gpu, oracle, order):
+def test_full_run_vs_exact_oracle(gpu, oracle, order):
     X = mixture(4000, 16, 12, 5)
     init = X[:12].copy()
     r = kmeans(X, k=12, variant="lloyd", max_iter=100, init=init, order=order)
-    c, lab, it, inert = oracle.lloyd(X, 12, init, max_iter=100, order=order, sums="fp64", threads=threads())
+    c, lab, it, inert = oracle.lloyd_exact(X, 12, init, max_iter=100, order=order, threads=threads())
     assert r.n_iter == it
     assert np.array_equal(r.labels, lab)
-    assert ulp_diff(r.centers, c) <= 1
+    assert np.array_equal(r.centers.view(np.uint32), c.view(np.uint32))
     assert abs(r.inertia - inert) <= 1e-7 * inert
     # fuel's own f32-sums trajectory lands on the same partition here
     c2, lab2, it2, _ = oracle.lloyd(X, 12, init, max_iter=100, order=order, threads=8)
     assert np.array_equal(r.labels, lab2)
 
 
-def test_lloyd_sparse_config_reduced(gpu, oracle):
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
+def test_lloyd_sparse_config_reduced(gpu, oracle, precision):
     """The k=64, d=784 sparse 0..255/255 workload at n=7,000, 10 iterations."""
     X, init = workloads.lloyd_sparse(n=7000)
-    r = kmeans(X, k=64, variant="lloyd", max_iter=10, init=init, fixed_iters=True)
-    c, lab, it, inert = oracle.lloyd(X, 64, init, max_iter=10, sums="fp64", threads=threads())
-    assert r.n_iter == 10
+    r = kmeans(X, k=64, variant="lloyd", max_iter=10, init=init, fixed_iters=True, precision=precision)
+    c, lab, it, inert = oracle.lloyd_exact(X, 64, init, max_iter=10, threads=threads(), fixed_iters=True)
+    assert r.n_iter == 10 == it
     assert np.array_equal(r.labels, lab)
-    assert ulp_diff(r.centers, c) <= 1
+    assert np.array_equal(r.centers.view(np.uint32), c.view(np.uint32))
     assert abs(r.inertia - inert) <= 1e-7 * inert
-    assert abs(r.inertia - oracle.lloyd_inertia_fp64(X, r.centers, r.labels)) <= 1e-9 * inert
+
+
+def test_wide_exponent_range_uses_fp64_sums(gpu, oracle):
+    """Data spanning more than 128 bits of exponent falls back to FP64 sums;
+    assignments stay bit-exact per iteration."""
+    X = mixture(1500, 6, 5, 3)
+    X[::7, 0] *= np.float32(1e-30)
+    X[::11, 1] *= np.float32(1e25)
+    init = X[np.random.default_rng(0).choice(1500, 5, replace=False)]
+    for t in (1, 2, 4):
+        r = kmeans(X, k=5, variant="lloyd", max_iter=t, init=init, fixed_iters=True)
+        lab, _ = oracle.lloyd_assign(X, r.centers, initial=(t == 1), threads=threads())
+        assert np.array_equal(r.labels, lab)
 
 
 def test_fixed_iters_and_stop_rule(gpu):
@@ -83,7 +98,7 @@ def test_edge_cases(gpu, oracle):
     # duplicate initial centre: centre 1 loses every tie and stays empty
     init = np.array([[1.0], [1.0], [10.0]], np.float32)
     r = kmeans(X, k=3, variant="lloyd", max_iter=5, init=init)
-    c, lab, it, _ = oracle.lloyd(X, 3, init, max_iter=5, sums="fp64")
+    c, lab, it, _ = oracle.lloyd_exact(X, 3, init, max_iter=5)
     assert np.array_equal(r.labels, lab) and r.n_iter == it
     assert r.centers[1, 0] == 1.0
     # k = 1 and k = n
