@@ -37,6 +37,12 @@ __device__ __forceinline__ uint32_t key_idx(uint64_t k) { return static_cast<uin
 
 __device__ __forceinline__ float sq_rn(float x) { return __fmul_rn(x, x); }
 
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while its predecessor drains; it must call
+// griddep_wait() before touching any memory the predecessor (or an earlier
+// kernel) reads or writes.  Without the launch attribute this is a no-op.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // Per-pair distances, NP point rows against one query row, all in shared
 // memory.  q: query row; xb: first of NP rows with stride xs (floats).  The

@@ -104,6 +104,28 @@ struct HotTimer {
 // The timer the current call installed for its hot kernel (or nullptr).
 HotTimer*& hot_timer();
 
+// Launch with programmatic stream serialisation (see griddep_wait()).
+template <typename... KArgs, typename... Args>
+int launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  note_launch();
+  cudaError_t e = cudaLaunchKernelEx(&cfg, kern, ((KArgs)args)...);
+  if (e != cudaSuccess) {
+    set_error("kernel launch failed: %s", cudaGetErrorString(e));
+    return ST_ECUDA;
+  }
+  return ST_OK;
+}
+
 // Host-mapped cancel word (pinned, device-visible); set by fuelg_cancel().
 int* cancel_word_device();
 bool cancel_requested();

@@ -161,12 +161,18 @@ __global__ void inertia_partial_kernel(const float* __restrict__ X, int64_t n, i
   }
 }
 
+// Fixed-shape tree reduction of the per-block partials (deterministic).
 __global__ void sum_partials_kernel(const double* __restrict__ partial, int nb, double* __restrict__ out) {
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    double s = 0.0;
-    for (int b = 0; b < nb; b++) s += partial[b];
-    *out = s;
+  __shared__ double red[1024];
+  double s = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) s += partial[b];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
   }
+  if (threadIdx.x == 0) *out = red[0];
 }
 
 // FP64 ||C_new - C_old||_F^2 and ||C_old||_F^2 for the tol>0 stop rule
@@ -329,7 +335,9 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
     }
   } tcf{tc};
   r->precision_used = 0;
-  if (p.precision != 0 && lloyd_tc_supported(d, k)) {
+  // TMA row coordinates are 32-bit: the tile-major copy needs n * ceil(d/64) < 2^31
+  const bool tc_fits = n * (int64_t)((d + 63) / 64) < (1ll << 31) - 4096;
+  if (p.precision != 0 && lloyd_tc_supported(d, k) && tc_fits) {
     tc = lloyd_tc_new();
     FUELG_TRY(lloyd_tc_prepare(p, tc, stream));
     r->precision_used = p.precision;
@@ -409,7 +417,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   FUELG_CUDA(cudaEventRecord(ev1, stream));
   if (tc) FUELG_TRY(lloyd_tc_rescored_total(tc, stream, &r->rescored));
   inertia_partial_kernel<<<inert_blocks, 256, 0, stream>>>(p.X, n, d, inertia_centers, labels, inert_part.as<double>()); ::fuelg::note_launch();
-  sum_partials_kernel<<<1, 32, 0, stream>>>(inert_part.as<double>(), inert_blocks, inert.as<double>()); ::fuelg::note_launch();
+  sum_partials_kernel<<<1, 1024, 0, stream>>>(inert_part.as<double>(), inert_blocks, inert.as<double>()); ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   double h_inert = 0.0;
   FUELG_CUDA(cudaMemcpyAsync(&h_inert, inert.p, sizeof(double), cudaMemcpyDeviceToHost, stream));

@@ -42,18 +42,34 @@ __device__ __forceinline__ void f32_parts(float x, uint32_t& mant, int& lsb, int
   }
 }
 
+__device__ __forceinline__ void range_acc(float x, int& lo, int& hi, int& bad) {
+  uint32_t mant;
+  int l, h;
+  bool z, b;
+  f32_parts(x, mant, l, h, z, b);
+  if (b) bad = 1;
+  if (!z && !b) {
+    lo = min(lo, l);
+    hi = max(hi, h);
+  }
+}
+
 __global__ void exp_range_kernel(const float* __restrict__ X, int64_t count, int* __restrict__ out) {
   int lo = 1 << 30, hi = -(1 << 30), bad = 0;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < count; e += (int64_t)gridDim.x * blockDim.x) {
-    uint32_t mant;
-    int l, h;
-    bool z, b;
-    f32_parts(X[e], mant, l, h, z, b);
-    if (b) bad = 1;
-    if (!z && !b) {
-      lo = min(lo, l);
-      hi = max(hi, h);
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  if ((reinterpret_cast<uintptr_t>(X) & 15) == 0) {
+    const int64_t c4 = count / 4;
+    const float4* X4 = reinterpret_cast<const float4*>(X);
+    for (int64_t e = tid; e < c4; e += nth) {
+      const float4 v = __ldg(X4 + e);
+      range_acc(v.x, lo, hi, bad);
+      range_acc(v.y, lo, hi, bad);
+      range_acc(v.z, lo, hi, bad);
+      range_acc(v.w, lo, hi, bad);
     }
+    for (int64_t e = c4 * 4 + tid; e < count; e += nth) range_acc(X[e], lo, hi, bad);
+  } else {
+    for (int64_t e = tid; e < count; e += nth) range_acc(X[e], lo, hi, bad);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -85,118 +101,212 @@ __device__ __forceinline__ unsigned __int128 fixed_of(float x, int e_lo, bool ne
 }
 
 // Changed labels -> change list + per-cluster in/out histograms.  `first`: no
-// previous label (the initial assignment puts every point in).
-__global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first,
+// previous label (the initial assignment puts every point in).  Histograms are
+// aggregated in shared memory per block when k fits (integer counts: exact).
+constexpr int kSmemK = 4096;
+
+__global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first, int k,
                                       int32_t* __restrict__ labels, int32_t* __restrict__ chg_i,
                                       int32_t* __restrict__ chg_old, int32_t* __restrict__ chg_new,
                                       int32_t* __restrict__ nchg, int32_t* __restrict__ cin,
                                       int32_t* __restrict__ cout) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int32_t h_in[kSmemK], h_out[kSmemK];
+  griddep_wait();
+  const bool local = k <= kSmemK;
+  if (local)
+    for (int j = threadIdx.x; j < k; j += blockDim.x) h_in[j] = h_out[j] = 0;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
-  bool ch = false;
-  int32_t nw = 0, old = -1;
-  if (i < n) {
-    nw = lab_new[i];
-    old = first ? -1 : labels[i];
-    ch = nw != old;
-    if (ch) labels[i] = nw;
+  for (int64_t base0 = (int64_t)blockIdx.x * blockDim.x; base0 < n; base0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = base0 + threadIdx.x;
+    bool ch = false;
+    int32_t nw = 0, old = -1;
+    if (i < n) {
+      nw = lab_new[i];
+      old = first ? -1 : labels[i];
+      ch = nw != old;
+      if (ch) labels[i] = nw;
+    }
+    const unsigned mask = __ballot_sync(0xffffffffu, ch);
+    if (mask) {
+      int base = 0;
+      if (lane == 0) base = atomicAdd(nchg, __popc(mask));
+      base = __shfl_sync(0xffffffffu, base, 0);
+      if (ch) {
+        const int pos = base + __popc(mask & ((1u << lane) - 1));
+        chg_i[pos] = (int32_t)i;
+        chg_old[pos] = old;
+        chg_new[pos] = nw;
+        if (local) {
+          atomicAdd(&h_in[nw], 1);
+          if (old >= 0) atomicAdd(&h_out[old], 1);
+        } else {
+          atomicAdd(&cin[nw], 1);
+          if (old >= 0) atomicAdd(&cout[old], 1);
+        }
+      }
+    }
   }
-  const unsigned mask = __ballot_sync(0xffffffffu, ch);
-  if (!mask) return;
-  int base = 0;
-  if (lane == 0) base = atomicAdd(nchg, __popc(mask));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (ch) {
-    const int pos = base + __popc(mask & ((1u << lane) - 1));
-    chg_i[pos] = (int32_t)i;
-    chg_old[pos] = old;
-    chg_new[pos] = nw;
-    atomicAdd(&cin[nw], 1);
-    if (old >= 0) atomicAdd(&cout[old], 1);
-  }
+  __syncthreads();
+  if (local)
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+      if (h_in[j]) atomicAdd(&cin[j], h_in[j]);
+      if (h_out[j]) atomicAdd(&cout[j], h_out[j]);
+    }
 }
 
-// Single CTA: bucket offsets and the chunk table (in-chunks of cluster 0..k-1,
-// then out-chunks), member counts, cursor reset.
-__global__ void bucket_plan_kernel(int k, int32_t* __restrict__ cin, int32_t* __restrict__ cout,
+// Single warp: bucket offsets and the chunk table (in-chunks of cluster
+// 0..k-1, then out-chunks), member counts, and chunk_info[c] = cluster of
+// chunk c (bit 31: an out-chunk).  Warp-shuffle scans over 32-entry tiles.
+__global__ void bucket_plan_kernel(int k, const int32_t* __restrict__ cin, const int32_t* __restrict__ cout,
                                    int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
-                                   int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts) {
-  __shared__ int32_t s_in, s_out, s_ch;
-  if (threadIdx.x == 0) s_in = s_out = s_ch = 0;
-  __syncthreads();
-  // sequential scans in cluster order by thread 0 over tiles; k is small
-  if (threadIdx.x == 0) {
-    int32_t a = 0, b = 0, c = 0;
-    for (int j = 0; j < k; j++) {
-      off_in[j] = a;
-      a += cin[j];
-      chunk_off[j] = c;
-      c += (cin[j] + kRows - 1) / kRows;
+                                   int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts,
+                                   int32_t* __restrict__ chunk_info) {
+  griddep_wait();
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x >= 32) return;
+  int32_t carry_c = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    const int32_t* cnt = pass == 0 ? cin : cout;
+    int32_t* off = pass == 0 ? off_in : off_out;
+    int32_t carry_m = 0;
+    for (int t0 = 0; t0 < k; t0 += 32) {
+      const int j = t0 + lane;
+      const int32_t c = j < k ? cnt[j] : 0;
+      const int32_t nc = (c + kRows - 1) / kRows;
+      int32_t a = c, b = nc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+        if (lane >= o) {
+          a += ua;
+          b += ub;
+        }
+      }
+      if (j < k) {
+        off[j] = carry_m + a - c;
+        const int32_t c0 = carry_c + b - nc;
+        chunk_off[pass * k + j] = c0;
+        for (int q = 0; q < nc; q++) chunk_info[c0 + q] = j | (pass << 31);
+        if (pass == 0) counts[j] += cin[j] - cout[j];
+      }
+      carry_m += __shfl_sync(0xffffffffu, a, 31);
+      carry_c += __shfl_sync(0xffffffffu, b, 31);
     }
-    for (int j = 0; j < k; j++) {
-      off_out[j] = b;
-      b += cout[j];
-      chunk_off[k + j] = c;
-      c += (cout[j] + kRows - 1) / kRows;
-    }
-    chunk_off[2 * k] = c;
   }
-  __syncthreads();
-  for (int j = threadIdx.x; j < k; j += blockDim.x) counts[j] += cin[j] - cout[j];
+  if (lane == 0) chunk_off[2 * k] = carry_c;
 }
 
 __global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
-                                      const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg,
+                                      const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg, int k,
                                       const int32_t* __restrict__ off_in, const int32_t* __restrict__ off_out,
                                       int32_t* __restrict__ cur_in, int32_t* __restrict__ cur_out,
                                       int32_t* __restrict__ bucket_in, int32_t* __restrict__ bucket_out) {
+  __shared__ int32_t c_in[kSmemK], c_out[kSmemK];
+  griddep_wait();
   const int cnt = *nchg;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x) {
-    const int32_t i = chg_i[e], o = chg_old[e], w = chg_new[e];
-    bucket_in[off_in[w] + atomicAdd(&cur_in[w], 1)] = i;
-    if (o >= 0) bucket_out[off_out[o] + atomicAdd(&cur_out[o], 1)] = i;
+  const bool local = k <= kSmemK;
+  for (int e0 = blockIdx.x * blockDim.x; e0 < cnt; e0 += gridDim.x * blockDim.x) {
+    const int e = e0 + threadIdx.x;
+    const bool v = e < cnt;
+    int32_t i = 0, o = -1, w = 0;
+    if (v) {
+      i = chg_i[e];
+      o = chg_old[e];
+      w = chg_new[e];
+    }
+    if (!local) {
+      if (v) {
+        bucket_in[off_in[w] + atomicAdd(&cur_in[w], 1)] = i;
+        if (o >= 0) bucket_out[off_out[o] + atomicAdd(&cur_out[o], 1)] = i;
+      }
+      continue;
+    }
+    // block-local ranks, one global reservation per (block, cluster)
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x) c_in[j] = c_out[j] = 0;
+    __syncthreads();
+    int r_in = 0, r_out = 0;
+    if (v) {
+      r_in = atomicAdd(&c_in[w], 1);
+      if (o >= 0) r_out = atomicAdd(&c_out[o], 1);
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+      c_in[j] = c_in[j] ? atomicAdd(&cur_in[j], c_in[j]) : 0;
+      c_out[j] = c_out[j] ? atomicAdd(&cur_out[j], c_out[j]) : 0;
+    }
+    __syncthreads();
+    if (v) {
+      bucket_in[off_in[w] + c_in[w] + r_in] = i;
+      if (o >= 0) bucket_out[off_out[o] + c_out[o] + r_out] = i;
+    }
   }
+}
+
+// 64-bit form of fixed_of for L <= 2 (|I(x)| < 2^63 by construction).
+__device__ __forceinline__ unsigned long long fixed_of64(float x, int e_lo, bool negate) {
+  const uint32_t bits = __float_as_uint(x);
+  const uint32_t eb = (bits >> 23) & 0xffu;
+  const uint32_t m = bits & 0x7fffffu;
+  if ((bits & 0x7fffffffu) == 0) return 0;
+  const uint32_t mant = eb ? (m | 0x800000u) : m;
+  const int sh = (eb == 0 ? -149 : (int)eb - 150) - e_lo;
+  const unsigned long long v = sh >= 0 ? ((unsigned long long)mant << sh) : (unsigned long long)(mant >> (-sh));
+  const bool neg = ((bits >> 31) != 0) != negate;
+  return neg ? 0ull - v : v;
 }
 
 // One chunk of <= 32 rows of one cluster, signed; thread per coordinate.
 template <int L>
-__global__ void accumulate_kernel(const float* __restrict__ X, int d, int k, int e_lo,
-                                  const int32_t* __restrict__ chunk_off, const int32_t* __restrict__ cin,
-                                  const int32_t* __restrict__ cout, const int32_t* __restrict__ off_in,
-                                  const int32_t* __restrict__ off_out, const int32_t* __restrict__ bucket_in,
-                                  const int32_t* __restrict__ bucket_out, unsigned long long* __restrict__ limbs) {
-  const int c = blockIdx.x;
+__global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict__ X, int d, int k, int e_lo,
+                                                         const int32_t* __restrict__ chunk_off,
+                                                         const int32_t* __restrict__ chunk_info,
+                                                         const int32_t* __restrict__ cin,
+                                                         const int32_t* __restrict__ cout,
+                                                         const int32_t* __restrict__ off_in,
+                                                         const int32_t* __restrict__ off_out,
+                                                         const int32_t* __restrict__ bucket_in,
+                                                         const int32_t* __restrict__ bucket_out,
+                                                         unsigned long long* __restrict__ limbs) {
+  griddep_wait();
   const int total = chunk_off[2 * k];
-  if (c >= total) return;
-  // locate (cluster, sign) of chunk c: binary search over chunk_off[0..2k]
-  int lo = 0, hi = 2 * k - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (chunk_off[mid] <= c) lo = mid;
-    else hi = mid - 1;
-  }
-  const bool out = lo >= k;
-  const int j = out ? lo - k : lo;
-  const int r0 = (c - chunk_off[lo]) * kRows;
-  const int cnt = out ? cout[j] : cin[j];
-  const int rows = min(kRows, cnt - r0);
-  const int32_t* src = (out ? bucket_out + off_out[j] : bucket_in + off_in[j]) + r0;
   __shared__ int32_t rid[kRows];
-  if (threadIdx.x < rows) rid[threadIdx.x] = src[threadIdx.x];
-  __syncthreads();
-  for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < d; t += gridDim.y * blockDim.x) {
-    unsigned long long acc[L];
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    const int32_t info = chunk_info[c];
+    const bool out = info < 0;
+    const int j = info & 0x7fffffff;
+    const int r0 = (c - chunk_off[(out ? k : 0) + j]) * kRows;
+    const int cnt = out ? cout[j] : cin[j];
+    const int rows = min(kRows, cnt - r0);
+    const int32_t* src = (out ? bucket_out + off_out[j] : bucket_in + off_in[j]) + r0;
+    __syncthreads();
+    if (threadIdx.x < kRows) rid[threadIdx.x] = threadIdx.x < rows ? src[threadIdx.x] : -1;
+    __syncthreads();
+    for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < d; t += gridDim.y * blockDim.x) {
+      float xv[kRows];
 #pragma unroll
-    for (int l = 0; l < L; l++) acc[l] = 0;
-    for (int r = 0; r < rows; r++) {
-      const unsigned __int128 v = fixed_of(__ldg(X + (int64_t)rid[r] * d + t), e_lo, out);
+      for (int q = 0; q < kRows; q++) xv[q] = rid[q] >= 0 ? __ldg(X + (int64_t)rid[q] * d + t) : 0.0f;
+      unsigned long long acc[L];
 #pragma unroll
-      for (int l = 0; l < L; l++) acc[l] += (unsigned long long)((v >> (32 * l)) & 0xffffffffu);
+      for (int l = 0; l < L; l++) acc[l] = 0;
+#pragma unroll
+      for (int q = 0; q < kRows; q++) {
+        if (L <= 2) {
+          const unsigned long long v = fixed_of64(xv[q], e_lo, out);
+          acc[0] += v & 0xffffffffull;
+          if (L == 2) acc[L == 2 ? 1 : 0] += v >> 32;
+        } else {
+          const unsigned __int128 v = fixed_of(xv[q], e_lo, out);
+#pragma unroll
+          for (int l = 0; l < L; l++) acc[l] += (unsigned long long)((v >> (32 * l)) & 0xffffffffu);
+        }
+      }
+      unsigned long long* dst = limbs + ((int64_t)j * d + t) * L;
+#pragma unroll
+      for (int l = 0; l < L; l++)
+        if (acc[l]) atomicAdd(dst + l, acc[l]);  // integer: exact in any order
     }
-    unsigned long long* dst = limbs + ((int64_t)j * d + t) * L;
-#pragma unroll
-    for (int l = 0; l < L; l++)
-      if (acc[l]) atomicAdd(dst + l, acc[l]);  // integer: exact in any order
   }
 }
 
@@ -224,7 +334,17 @@ __device__ float rn_ratio_f32(unsigned __int128 A, unsigned long long cnt, int e
 // clusters as the correctly rounded f32 centre.
 template <int L>
 __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, int d, int e_lo,
-                            const int32_t* __restrict__ counts, float* __restrict__ centers) {
+                            const int32_t* __restrict__ counts, float* __restrict__ centers, int write_centers,
+                            int32_t* __restrict__ nchg, int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
+                            int nzero) {
+  griddep_wait();
+  // hand the change count to the host and reset the per-pass counters
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *changed = *nchg;
+    *nchg = 0;
+  }
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nzero; e += (int64_t)gridDim.x * blockDim.x)
+    zero4k[e] = 0;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kd; e += (int64_t)gridDim.x * blockDim.x) {
     unsigned long long* lp = limbs + e * L;
     unsigned __int128 tot = 0;
@@ -235,7 +355,7 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
     for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
     const int j = (int)(e / d);
     const int cnt = counts[j];
-    if (cnt <= 0) continue;
+    if (cnt <= 0 || !write_centers) continue;
     const bool neg = (tot >> (32 * L - 1)) & 1;
     unsigned __int128 mag = tot;
     if (neg) {
@@ -252,8 +372,8 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
 struct ExactSums {
   int L = 0, e_lo = 0, k = 0, d = 0;
   int64_t n = 0;
-  Scratch limbs, counts, chg_i, chg_old, chg_new, nchg, cin, cout, off_in, off_out, cur, chunk_off, bucket_in,
-      bucket_out, range;
+  Scratch limbs, counts, chg_i, chg_old, chg_new, nchg, cin, cout, off_in, off_out, cur, chunk_off, chunk_info,
+      bucket_in, bucket_out, range;
   int64_t max_chunks = 0;
 };
 
@@ -269,7 +389,7 @@ int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaS
   FUELG_TRY(s->range.alloc(sizeof(int) * 3, stream));
   int init[3] = {1 << 30, -(1 << 30), 0};
   FUELG_CUDA(cudaMemcpyAsync(s->range.p, init, sizeof(init), cudaMemcpyHostToDevice, stream));
-  exp_range_kernel<<<4 * 152, 256, 0, stream>>>(X, n * (int64_t)d, s->range.as<int>()); ::fuelg::note_launch();
+  exp_range_kernel<<<8 * 152, 256, 0, stream>>>(X, n * (int64_t)d, s->range.as<int>()); ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   int h[3];
   FUELG_CUDA(cudaMemcpyAsync(h, s->range.p, sizeof(h), cudaMemcpyDeviceToHost, stream));
@@ -298,12 +418,15 @@ int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaS
   FUELG_TRY(s->chg_old.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(s->chg_new.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(s->nchg.alloc(sizeof(int32_t), stream));
+  FUELG_CUDA(cudaMemsetAsync(s->nchg.p, 0, sizeof(int32_t), stream));
   FUELG_TRY(s->cin.alloc(sizeof(int32_t) * 4 * (size_t)k, stream));  // cin, cout, cur_in, cur_out
+  FUELG_CUDA(cudaMemsetAsync(s->cin.p, 0, sizeof(int32_t) * 4 * (size_t)k, stream));
   FUELG_TRY(s->off_in.alloc(sizeof(int32_t) * 2 * (size_t)k, stream));
   FUELG_TRY(s->chunk_off.alloc(sizeof(int32_t) * (2 * (size_t)k + 1), stream));
   FUELG_TRY(s->bucket_in.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(s->bucket_out.alloc(sizeof(int32_t) * n, stream));
   s->max_chunks = 2 * (n / kRows) + 2 * (int64_t)k + 2;
+  FUELG_TRY(s->chunk_info.alloc(sizeof(int32_t) * s->max_chunks, stream));
   return ST_OK;
 }
 
@@ -322,45 +445,40 @@ int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_
   int32_t* cur_out = cin + 3 * k;
   int32_t* off_in = s->off_in.as<int32_t>();
   int32_t* off_out = off_in + k;
-  FUELG_CUDA(cudaMemsetAsync(s->cin.p, 0, sizeof(int32_t) * 4 * (size_t)k, stream));
-  FUELG_CUDA(cudaMemsetAsync(s->nchg.p, 0, sizeof(int32_t), stream));
-  commit_changes_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(
-      lab_new, n, first ? 1 : 0, labels, s->chg_i.as<int32_t>(), s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(),
-      s->nchg.as<int32_t>(), cin, cout); ::fuelg::note_launch();
-  bucket_plan_kernel<<<1, 256, 0, stream>>>(k, cin, cout, off_in, off_out, s->chunk_off.as<int32_t>(),
-                                            s->counts.as<int32_t>()); ::fuelg::note_launch();
-  bucket_scatter_kernel<<<2 * 152, 256, 0, stream>>>(s->chg_i.as<int32_t>(), s->chg_old.as<int32_t>(),
-                                                     s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), off_in, off_out,
-                                                     cur_in, cur_out, s->bucket_in.as<int32_t>(),
-                                                     s->bucket_out.as<int32_t>()); ::fuelg::note_launch();
+  // counters were zeroed at init and are reset by mean_kernel after every pass
+  FUELG_TRY(launch_pdl(commit_changes_kernel, dim3((unsigned)std::min<int64_t>((n + 255) / 256, 2 * 152)), dim3(256),
+                       0, stream, lab_new, n, first ? 1 : 0, k, labels, s->chg_i.as<int32_t>(),
+                       s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), cin, cout));
+  FUELG_TRY(launch_pdl(bucket_plan_kernel, dim3(1), dim3(32), 0, stream, k, (const int32_t*)cin,
+                       (const int32_t*)cout, off_in, off_out, s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(),
+                       s->chunk_info.as<int32_t>()));
+  FUELG_TRY(launch_pdl(bucket_scatter_kernel, dim3(2 * 152), dim3(256), 0, stream,
+                       (const int32_t*)s->chg_i.as<int32_t>(), (const int32_t*)s->chg_old.as<int32_t>(),
+                       (const int32_t*)s->chg_new.as<int32_t>(), (const int32_t*)s->nchg.as<int32_t>(), k,
+                       (const int32_t*)off_in, (const int32_t*)off_out, cur_in, cur_out, s->bucket_in.as<int32_t>(),
+                       s->bucket_out.as<int32_t>()));
   const int ty = (d + 255) / 256;
-  dim3 g((unsigned)s->max_chunks, ty);
-  auto acc = [&](auto Lc) {
+  dim3 g((unsigned)std::min<int64_t>(s->max_chunks, std::max(1, 8 * 152 / ty)), ty);
+  const int64_t kd = (int64_t)k * d;
+  const unsigned mg = (unsigned)std::min<int64_t>((kd + 255) / 256, 8 * 152);
+  auto run = [&](auto Lc) -> int {
     constexpr int LL = decltype(Lc)::value;
-    accumulate_kernel<LL><<<g, 256, 0, stream>>>(X, d, k, s->e_lo, s->chunk_off.as<int32_t>(), cin, cout, off_in,
-                                                 off_out, s->bucket_in.as<int32_t>(), s->bucket_out.as<int32_t>(),
-                                                 s->limbs.as<unsigned long long>()); ::fuelg::note_launch();
+    FUELG_TRY(launch_pdl(accumulate_kernel<LL>, g, dim3(256), 0, stream, X, d, k, s->e_lo,
+                         (const int32_t*)s->chunk_off.as<int32_t>(), (const int32_t*)s->chunk_info.as<int32_t>(),
+                         (const int32_t*)cin, (const int32_t*)cout, (const int32_t*)off_in, (const int32_t*)off_out,
+                         (const int32_t*)s->bucket_in.as<int32_t>(), (const int32_t*)s->bucket_out.as<int32_t>(),
+                         s->limbs.as<unsigned long long>()));
+    FUELG_TRY(launch_pdl(mean_kernel<LL>, dim3(mg), dim3(256), 0, stream, s->limbs.as<unsigned long long>(), kd, d,
+                         s->e_lo, (const int32_t*)s->counts.as<int32_t>(), centers, write_centers ? 1 : 0,
+                         s->nchg.as<int32_t>(), changed, cin, 4 * k));
+    return ST_OK;
   };
   switch (s->L) {
-    case 1: acc(std::integral_constant<int, 1>()); break;
-    case 2: acc(std::integral_constant<int, 2>()); break;
-    case 3: acc(std::integral_constant<int, 3>()); break;
-    default: acc(std::integral_constant<int, 4>()); break;
+    case 1: FUELG_TRY(run(std::integral_constant<int, 1>())); break;
+    case 2: FUELG_TRY(run(std::integral_constant<int, 2>())); break;
+    case 3: FUELG_TRY(run(std::integral_constant<int, 3>())); break;
+    default: FUELG_TRY(run(std::integral_constant<int, 4>())); break;
   }
-  FUELG_CUDA(cudaGetLastError());
-  if (write_centers) {
-    const int64_t kd = (int64_t)k * d;
-    const unsigned mg = (unsigned)std::min<int64_t>((kd + 255) / 256, 8 * 152);
-    switch (s->L) {
-      case 1: mean_kernel<1><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
-      case 2: mean_kernel<2><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
-      case 3: mean_kernel<3><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
-      default: mean_kernel<4><<<mg, 256, 0, stream>>>(s->limbs.as<unsigned long long>(), kd, d, s->e_lo, s->counts.as<int32_t>(), centers); break;
-    }
-    ::fuelg::note_launch();
-    FUELG_CUDA(cudaGetLastError());
-  }
-  FUELG_CUDA(cudaMemcpyAsync(changed, s->nchg.p, sizeof(int32_t), cudaMemcpyDeviceToDevice, stream));
   return ST_OK;
 }
 

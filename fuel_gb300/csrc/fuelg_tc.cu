@@ -31,6 +31,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 
 #include "fuelg_common.cuh"
 #include "fuelg_internal.h"
@@ -59,6 +60,10 @@ struct TcArgs {
   float alpha, beta, gamma;
   uint32_t idesc;
   uint32_t tmem_cols;
+  int a_tiled;  // A copies are tile-major (see prep_offset)
+  float s_scale;              // nonneg data: sum|x_i c_i| <= dot * s_scale
+  int sep_lo;                 // hi+lo: the hi.lo + lo.hi terms have their own accumulator
+  const int* neg_flag;        // != 0 when X holds a negative value
   int* status;
   const volatile int* cancel;
 };
@@ -110,6 +115,29 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, in
       "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
       : "memory");
 }
+// Same load with an L2 cache-policy hint (streamed point tiles: evict-first;
+// the small centre tiles every CTA re-reads: evict-last).
+__device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar,
+                                                 uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
+      "%3}], [%4], %5;" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+__device__ __forceinline__ uint64_t policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void prefetch_tmap(const CUtensorMap* tm) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm)) : "memory");
+}
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -149,7 +177,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 }
 
 template <bool SPLIT>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kTcThreads, 2)
     lloyd_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
                     const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo, TcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -184,10 +212,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int j = threadIdx.x; j < a.kp; j += blockDim.x) {
-    snc[j] = a.nc[j];
-    scn[j] = a.cn[j];
-  }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
                  "r"(a.tmem_cols)
@@ -198,9 +222,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_holder;
+  // the prologue above overlaps the predecessor; centres and norms come from it
+  griddep_wait();
+  for (int j = threadIdx.x; j < a.kp; j += blockDim.x) {
+    snc[j] = a.nc[j];
+    scn[j] = a.cn[j];
+  }
+  __syncthreads();
 
   if (warp == 0) {
     if (lane == 0) {
+      prefetch_tmap(&tmA);
+      prefetch_tmap(&tmB);
+      if (SPLIT) {
+        prefetch_tmap(&tmAlo);
+        prefetch_tmap(&tmBlo);
+      }
+      const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
       uint32_t stage = 0, phase = 0;
       uint32_t armed = 0, last_ph = 0;  // per-stage bit: armed at least once / parity of the last arm
       int tile_no = 0;
@@ -221,11 +259,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           mbar_expect_tx(&full[stage], stage_bytes);
           armed |= 1u << stage;
           last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
-          tma_load_2d(sA, &tmA, kc * BK, (int)(t * BM), &full[stage]);
-          tma_load_2d(sB, &tmB, kc * BK, 0, &full[stage]);
+          const int ax = a.a_tiled ? 0 : kc * BK;
+          const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
+          tma_load_2d_hint(sA, &tmA, ax, ay, &full[stage], pol_a);
+          tma_load_2d_hint(sB, &tmB, kc * BK, 0, &full[stage], pol_b);
           if (SPLIT) {
-            tma_load_2d(sB + b_bytes, &tmAlo, kc * BK, (int)(t * BM), &full[stage]);
-            tma_load_2d(sB + b_bytes + a_bytes, &tmBlo, kc * BK, 0, &full[stage]);
+            tma_load_2d_hint(sB + b_bytes, &tmAlo, ax, ay, &full[stage], pol_a);
+            tma_load_2d_hint(sB + b_bytes + a_bytes, &tmBlo, kc * BK, 0, &full[stage], pol_b);
           }
           if (++stage == (uint32_t)NS) {
             stage = 0;
@@ -253,7 +293,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           break;
         }
         tc_fence_after();
-        const uint32_t d_tmem = tmem_base + buf * (uint32_t)a.kp;
+        // split: hi.hi accumulates at [0, kp), the hi.lo + lo.hi terms at [kp, 2kp)
+        const uint32_t acc_cols = (SPLIT && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
+        const uint32_t d_tmem = tmem_base + buf * acc_cols;
+        const uint32_t d_lo = d_tmem + (a.sep_lo ? (uint32_t)a.kp : 0u);
         bool ok = true;
         for (int kc = 0; kc < a.kc; kc++) {
           if (!mbar_wait(&full[stage], phase, abort_flag)) {
@@ -274,8 +317,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (SPLIT) {
               const uint64_t adlo = smem_desc_sw128(smem_u32(sB + b_bytes));
               const uint64_t bdlo = smem_desc_sw128(smem_u32(sB + b_bytes + a_bytes));
-              umma_bf16(d_tmem, ad + 2 * kk, bdlo + 2 * kk, a.idesc, 1u);
-              umma_bf16(d_tmem, adlo + 2 * kk, bd + 2 * kk, a.idesc, 1u);
+              umma_bf16(d_lo, ad + 2 * kk, bdlo + 2 * kk, a.idesc, (a.sep_lo && (kc | kk) == 0) ? 0u : 1u);
+              umma_bf16(d_lo, adlo + 2 * kk, bd + 2 * kk, a.idesc, 1u);
             }
           }
           umma_commit(&empty[stage]);
@@ -309,13 +352,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       const bool valid = i < a.n;
       const float nxi = valid ? a.nx[i] : 0.0f;
       const float xni = valid ? a.xn[i] : 0.0f;
-      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + buf * (uint32_t)a.kp;
+      const uint32_t acc_cols = (SPLIT && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
+      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + buf * acc_cols;
+      const bool nonneg = *a.neg_flag == 0;
       // pass 1: screened argmin (first index wins ties)
-      float best = __int_as_float(0x7f800000);
+      float best = __int_as_float(0x7f800000), best_dot = 0.0f;
       int bj = 0;
       for (int c0 = 0; c0 < a.kp; c0 += 16) {
         float v[16];
         tmem_ld16(taddr + c0, v);
+        if (SPLIT && a.sep_lo) {
+          float w[16];
+          tmem_ld16(taddr + a.kp + c0, w);
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] += w[j];
+        }
 #pragma unroll
         for (int j = 0; j < 16; j++) {
           const int col = c0 + j;
@@ -324,24 +375,33 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (dt < best) {
               best = dt;
               bj = col;
+              best_dot = v[j];
             }
           }
         }
       }
-      const float eb = (a.alpha * xni * scn[bj] + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
+      // S_j bounds sum_i |x_i c_ij|: |x||c_j| in general, the (inflated) dot product for nonnegative data
+      const float sb = nonneg ? fmaxf(best_dot, 0.0f) * a.s_scale : xni * scn[bj];
+      const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
       const float hi = best + eb;
       // pass 2: every other centre whose lower bound reaches the best's upper bound
       uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
       for (int c0 = 0; c0 < a.kp; c0 += 16) {
         float v[16];
         tmem_ld16(taddr + c0, v);
+        if (SPLIT && a.sep_lo) {
+          float w[16];
+          tmem_ld16(taddr + a.kp + c0, w);
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] += w[j];
+        }
 #pragma unroll
         for (int j = 0; j < 16; j++) {
           const int col = c0 + j;
           if (col < a.k && col != bj) {
             const float dt = fmaf(-2.0f, v[j], nxi + snc[col]);
-            const float e = (a.alpha * xni * scn[col] + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) +
-                            a.gamma * fabsf(dt);
+            const float sj = nonneg ? fmaxf(v[j], 0.0f) * a.s_scale : xni * scn[col];
+            const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
             if (!(dt - e > hi)) {
               const uint64_t bit = 1ull << (col & 63);
               const int w = col >> 6;
@@ -387,30 +447,71 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 }
 
 // X (f32) -> BF16 hi (and lo = BF16(x - hi)) copies with rows padded to dp
-// (a multiple of 8, zero filled), plus ||x||^2 (FP64 sum rounded) and ||x||.
+// (a multiple of 8, zero filled), plus ||x||^2 and ||x||.  One warp per row,
+// four columns per lane per step; the squared norm is an FP32 sum of at most
+// 4*ceil(dp/128) terms per lane and a 5-level tree, so its relative error is
+// below (ceil(d/32) + 9) 2^-24 -- the beta term of the screen's error bound.
+// With tile_kc > 0 the copies are written tile-major -- [row tile of 128][K
+// chunk of 64][128 rows][64 columns] -- so that every TMA box the screen loads
+// is one contiguous 16 KB block of HBM; dp is then tile_kc * 64.
+__device__ __forceinline__ int64_t prep_offset(int64_t r, int c, int dp, int tile_kc) {
+  if (tile_kc == 0) return r * dp + c;
+  return (((r >> 7) * tile_kc + (c >> 6)) * 128 + (r & 127)) * 64 + (c & 63);
+}
+
 template <bool SPLIT>
 __global__ void prep_rows_kernel(const float* __restrict__ X, int64_t rows, int64_t valid_rows, int d, int dp,
-                                 __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                                 float* __restrict__ nrm2, float* __restrict__ nrm) {
+                                 int tile_kc, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                 float* __restrict__ nrm2, float* __restrict__ nrm, int* __restrict__ neg_flag,
+                                 int32_t* __restrict__ zero_word) {
+  griddep_wait();
+  if (zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *zero_word = 0;
+  bool anyneg = false;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const bool vec = ((d & 3) == 0) && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
   for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < rows; r += (int64_t)gridDim.x * nw) {
-    double s = 0.0;
+    float acc = 0.0f;
     const bool v = r < valid_rows;
-    for (int c = lane; c < dp; c += 32) {
-      const float x = (v && c < d) ? X[r * d + c] : 0.0f;
-      const __nv_bfloat16 h = __float2bfloat16_rn(x);
-      hi[r * dp + c] = h;
-      if (SPLIT) lo[r * dp + c] = __float2bfloat16_rn(x - __bfloat162float(h));
-      s = fma((double)x, (double)x, s);
+    const float* xr = X + r * d;
+    for (int c0 = 4 * lane; c0 < dp; c0 += 128) {
+      float x4[4];
+      if (v && vec && c0 + 3 < d) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(xr + c0));
+        x4[0] = t.x, x4[1] = t.y, x4[2] = t.z, x4[3] = t.w;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 4; q++) x4[q] = (v && c0 + q < d) ? __ldg(xr + c0 + q) : 0.0f;
+      }
+      __nv_bfloat162 h01 = __floats2bfloat162_rn(x4[0], x4[1]);
+      __nv_bfloat162 h23 = __floats2bfloat162_rn(x4[2], x4[3]);
+      uint2 hpack;
+      hpack.x = *reinterpret_cast<uint32_t*>(&h01);
+      hpack.y = *reinterpret_cast<uint32_t*>(&h23);
+      const int64_t off = prep_offset(r, c0, dp, tile_kc);
+      *reinterpret_cast<uint2*>(hi + off) = hpack;
+      if (SPLIT) {
+        const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+        __nv_bfloat162 l01 = __floats2bfloat162_rn(x4[0] - f01.x, x4[1] - f01.y);
+        __nv_bfloat162 l23 = __floats2bfloat162_rn(x4[2] - f23.x, x4[3] - f23.y);
+        uint2 lpack;
+        lpack.x = *reinterpret_cast<uint32_t*>(&l01);
+        lpack.y = *reinterpret_cast<uint32_t*>(&l23);
+        *reinterpret_cast<uint2*>(lo + off) = lpack;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; q++) {
+        acc = fmaf(x4[q], x4[q], acc);
+        anyneg |= x4[q] < 0.0f;
+      }
     }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
     if (lane == 0) {
-      const float f = __double2float_rn(s);
-      nrm2[r] = f;
-      nrm[r] = __double2float_rn(sqrt(s));
+      nrm2[r] = acc;
+      nrm[r] = sqrtf(acc);
     }
   }
+  if (neg_flag != nullptr && __any_sync(0xffffffffu, anyneg) && (threadIdx.x & 31) == 0) atomicOr(neg_flag, 1);
 }
 
 // Exact re-score of the undecided points: each candidate centre is scored
@@ -429,23 +530,25 @@ __device__ __forceinline__ float warp_candidate_dist(const float* __restrict__ x
     const int l = lane & 7, g0 = lane & ~7;
     const int sd = d & ~7;
     float acc = 0.0f;
+#pragma unroll 8
     for (int i = l; i < sd; i += 8) {
-      const float df = __fsub_rn(__ldg(x + i), __ldg(c + i));
+      const float df = __fsub_rn(x[i], c[i]);
       acc = FMA8 ? __fmaf_rn(df, df, acc) : __fadd_rn(sq_rn(df), acc);
     }
     float s = __shfl_sync(0xffffffffu, acc, g0);
 #pragma unroll
     for (int t = 1; t < 8; t++) s = __fadd_rn(s, __shfl_sync(0xffffffffu, acc, g0 + t));
     for (int i = sd; i < d; i++) {
-      const float df = __fsub_rn(__ldg(x + i), __ldg(c + i));
+      const float df = __fsub_rn(x[i], c[i]);
       s = FMA8 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
     }
     return s;  // valid on every lane of the group
   } else if constexpr (KIND == KIND_SQDIST) {  // x86 avx2::sqdist_f32, d >= 4
     const int nb = d / 32;
     float a = 0.0f;
+#pragma unroll 8
     for (int b = 0; b < nb; b++) {
-      const float df = __fsub_rn(__ldg(x + b * 32 + lane), __ldg(c + b * 32 + lane));
+      const float df = __fsub_rn(x[b * 32 + lane], c[b * 32 + lane]);
       a = __fmaf_rn(df, df, a);
     }
     const int l = lane & 7;
@@ -454,7 +557,7 @@ __device__ __forceinline__ float warp_candidate_dist(const float* __restrict__ x
     float cl = __fadd_rn(__fadd_rn(a0, a1), __fadd_rn(a2, a3));
     int i = nb * 32;
     for (; i + 8 <= d; i += 8) {
-      const float df = __fsub_rn(__ldg(x + i + l), __ldg(c + i + l));
+      const float df = __fsub_rn(x[i + l], c[i + l]);
       cl = __fmaf_rn(df, df, cl);
     }
     float v[8];
@@ -463,7 +566,7 @@ __device__ __forceinline__ float warp_candidate_dist(const float* __restrict__ x
     float s = __fadd_rn(__fadd_rn(__fadd_rn(v[0], v[4]), __fadd_rn(v[1], v[5])),
                         __fadd_rn(__fadd_rn(v[2], v[6]), __fadd_rn(v[3], v[7])));
     for (; i < d; i++) {
-      const float df = __fsub_rn(__ldg(x + i), __ldg(c + i));
+      const float df = __fsub_rn(x[i], c[i]);
       s = __fmaf_rn(df, df, s);
     }
     return s;
@@ -524,6 +627,84 @@ __global__ void rescore_kernel(const float* __restrict__ X, const float* __restr
   }
 }
 
+// Same re-score with the point row and the current candidate rows staged in
+// shared memory by all 32 lanes (coalesced 16-byte loads, one round trip),
+// then the sequential per-lane accumulations read shared memory.  4 warps per
+// block; used for d <= 1024.
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restrict__ X, const float* __restrict__ C,
+                                                           int d, int ds, int mw, const int32_t* __restrict__ ulist,
+                                                           const uint64_t* __restrict__ umask,
+                                                           const int32_t* __restrict__ ucount,
+                                                           int32_t* __restrict__ lab_new,
+                                                           unsigned long long* __restrict__ tally) {
+  constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
+  constexpr int G = LANE8 ? 8 : 32;
+  constexpr int PER = 32 / G;
+  extern __shared__ __align__(16) float rs_smem[];
+  griddep_wait();
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  float* xs = rs_smem + (size_t)wib * (PER + 1) * ds;
+  float* cs = xs + ds;
+  const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int cnt = *ucount;
+  if (blockIdx.x == 0 && threadIdx.x == 0) *tally += (unsigned long long)cnt;
+  const bool v4 = (d & 3) == 0;
+  for (int64_t u = gw; u < cnt; u += nwarps) {
+    const int64_t i = ulist[u];
+    const float* x = X + i * d;
+    __syncwarp();
+    if (v4)
+      for (int e = lane; e < d / 4; e += 32) reinterpret_cast<float4*>(xs)[e] = __ldg(reinterpret_cast<const float4*>(x) + e);
+    else
+      for (int e = lane; e < d; e += 32) xs[e] = __ldg(x + e);
+    uint64_t best = KEY_NONE;
+    int w = 0;
+    uint64_t m = umask[u * mw];
+    const int slot = lane / G;
+    for (;;) {
+      int got = 0, j = 0;
+      int js[PER];
+      while (got < PER) {
+        while (m == 0 && w + 1 < mw) m = umask[u * mw + (++w)];
+        if (m == 0) break;
+        const int b = __ffsll((long long)m) - 1;
+        m &= m - 1;
+        js[got] = w * 64 + b;
+        if (got == slot) j = js[got];
+        got++;
+      }
+      if (got == 0) break;
+      __syncwarp();
+      for (int t = 0; t < got; t++) {
+        const float* c = C + (int64_t)js[t] * d;
+        float* dst = cs + (size_t)t * ds;
+        if (v4)
+          for (int e = lane; e < d / 4; e += 32)
+            reinterpret_cast<float4*>(dst)[e] = __ldg(reinterpret_cast<const float4*>(c) + e);
+        else
+          for (int e = lane; e < d; e += 32) dst[e] = __ldg(c + e);
+      }
+      __syncwarp();
+      const bool mine = slot < got;
+      if (!mine) j = 0;
+      const float dist = warp_candidate_dist<KIND, ORDER>(xs, cs + (size_t)(mine ? slot : 0) * ds, d, lane);
+      if (mine && (lane % G) == 0) {
+        const uint64_t key = make_key(dist, (uint32_t)j);
+        best = key < best ? key : best;
+      }
+      if (got < PER) break;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const uint64_t o = __shfl_xor_sync(0xffffffffu, best, off);
+      best = o < best ? o : best;
+    }
+    if (lane == 0) lab_new[i] = (int32_t)key_idx(best);
+  }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
   if (!fn) {
@@ -565,8 +746,11 @@ int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int dp, int box_row
 struct TcLloydState {
   bool split = false;
   int dp = 0, kp = 0, kc = 0, mw = 0, stages = 0;
+  int64_t arows = 0;  // rows of the tile-major A copies (whole tiles)
+  int ctas_per_sm = 1;
+  bool sep_lo = false;
   size_t smem = 0;
-  Scratch xhi, xlo, xnrm2, xnrm, chi, clo, cnrm2, cnrm, ulist, umask, ucount, rescored_total;
+  Scratch xhi, xlo, xnrm2, xnrm, chi, clo, cnrm2, cnrm, ulist, umask, ucount, rescored_total, negf;
   CUtensorMap tmA, tmAlo, tmB, tmBlo;
 };
 
@@ -581,19 +765,34 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   st->mw = (st->kp + 63) / 64;
   const size_t a_bytes = BM * BK * 2, b_bytes = (size_t)st->kp * BK * 2;
   const size_t stage_bytes = (st->split ? 2 : 1) * (a_bytes + b_bytes);
-  int stages = (int)((200 * 1024) / stage_bytes);
+  // Tunables (defaults measured on GB300): FUELG_TC_STAGES pipeline depth,
+  // FUELG_TC_CTAS_PER_SM resident CTAs per SM (shared memory is divided).
+  int per_sm = 2;
+  if (const char* e = getenv("FUELG_TC_CTAS_PER_SM")) per_sm = std::max(1, std::min(2, atoi(e)));
+  const size_t budget = per_sm == 1 ? 200 * 1024 : 100 * 1024;
+  int stages = (int)(budget / stage_bytes);
+  if (const char* e = getenv("FUELG_TC_STAGES")) stages = atoi(e);
   stages = std::max(2, std::min(8, stages));
+  {
+    uint32_t cols = 32;
+    st->sep_lo = st->split && st->kp <= 128;
+    while (cols < (uint32_t)((st->sep_lo ? 4 : 2) * st->kp)) cols <<= 1;
+    if (cols * per_sm > 512) per_sm = 1;
+    if (per_sm == 1 && getenv("FUELG_TC_STAGES") == nullptr) stages = std::max(2, std::min(8, (int)((200 * 1024) / stage_bytes)));
+  }
+  st->ctas_per_sm = per_sm;
   st->stages = stages;
   st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 8 * st->kp;
   if (st->smem > 227 * 1024) {
     set_error("tensor-core Lloyd tile does not fit shared memory (k=%d)", p.k);
     return ST_ENOTSUP;
   }
-  const size_t xb = (size_t)n * st->dp * 2;
+  st->arows = ((n + BM - 1) / BM) * BM;
+  const size_t xb = (size_t)st->arows * st->kc * BK * 2;
   FUELG_TRY(st->xhi.alloc(xb, stream));
   if (st->split) FUELG_TRY(st->xlo.alloc(xb, stream));
-  FUELG_TRY(st->xnrm2.alloc(sizeof(float) * n, stream));
-  FUELG_TRY(st->xnrm.alloc(sizeof(float) * n, stream));
+  FUELG_TRY(st->xnrm2.alloc(sizeof(float) * st->arows, stream));
+  FUELG_TRY(st->xnrm.alloc(sizeof(float) * st->arows, stream));
   const size_t cb = (size_t)st->kp * st->dp * 2;
   FUELG_TRY(st->chi.alloc(cb, stream));
   if (st->split) FUELG_TRY(st->clo.alloc(cb, stream));
@@ -602,20 +801,27 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   FUELG_TRY(st->ulist.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(st->umask.alloc(sizeof(uint64_t) * n * st->mw, stream));
   FUELG_TRY(st->ucount.alloc(sizeof(int32_t), stream));
+  FUELG_TRY(st->negf.alloc(sizeof(int), stream));
+  FUELG_CUDA(cudaMemsetAsync(st->negf.p, 0, sizeof(int), stream));
   FUELG_TRY(st->rescored_total.alloc(sizeof(unsigned long long), stream));
   FUELG_CUDA(cudaMemsetAsync(st->rescored_total.p, 0, sizeof(unsigned long long), stream));
   if (st->split)
-    prep_rows_kernel<true><<<4 * 152, 256, 0, stream>>>(p.X, n, n, p.d, st->dp, st->xhi.as<__nv_bfloat16>(),
+    prep_rows_kernel<true><<<8 * 152, 256, 0, stream>>>(p.X, st->arows, n, p.d, st->kc * BK, st->kc,
+                                                         st->xhi.as<__nv_bfloat16>(),
                                                          st->xlo.as<__nv_bfloat16>(), st->xnrm2.as<float>(),
-                                                         st->xnrm.as<float>());
+                                                         st->xnrm.as<float>(), st->negf.as<int>(), nullptr);
   else
-    prep_rows_kernel<false><<<4 * 152, 256, 0, stream>>>(p.X, n, n, p.d, st->dp, st->xhi.as<__nv_bfloat16>(),
-                                                          nullptr, st->xnrm2.as<float>(), st->xnrm.as<float>()); ::fuelg::note_launch();
+    prep_rows_kernel<false><<<8 * 152, 256, 0, stream>>>(p.X, st->arows, n, p.d, st->kc * BK, st->kc,
+                                                          st->xhi.as<__nv_bfloat16>(),
+                                                          nullptr, st->xnrm2.as<float>(), st->xnrm.as<float>(), st->negf.as<int>(),
+                                                          nullptr);
+  ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
-  FUELG_TRY(make_map(&st->tmA, st->xhi.p, n, st->dp, BM));
+  // A: tile-major [arows * kc, 64] -- each box is one contiguous 16 KB block
+  FUELG_TRY(make_map(&st->tmA, st->xhi.p, st->arows * st->kc, BK, BM));
   FUELG_TRY(make_map(&st->tmB, st->chi.p, st->kp, st->dp, st->kp));
   if (st->split) {
-    FUELG_TRY(make_map(&st->tmAlo, st->xlo.p, n, st->dp, BM));
+    FUELG_TRY(make_map(&st->tmAlo, st->xlo.p, st->arows * st->kc, BK, BM));
     FUELG_TRY(make_map(&st->tmBlo, st->clo.p, st->kp, st->dp, st->kp));
   } else {
     st->tmAlo = st->tmA;
@@ -629,16 +835,18 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
 int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* lab_new,
                     int* dev_status, cudaStream_t stream) {
   const int64_t n = p.n;
-  // centre copies and norms for this iteration (padded rows are zero)
+  // centre copies and norms for this iteration (padded rows are zero); block 0
+  // also clears the undecided-point counter for this pass
   if (st->split)
-    prep_rows_kernel<true><<<(st->kp + 7) / 8, 256, 0, stream>>>(centers, st->kp, p.k, p.d, st->dp,
-                                                                 st->chi.as<__nv_bfloat16>(), st->clo.as<__nv_bfloat16>(),
-                                                                 st->cnrm2.as<float>(), st->cnrm.as<float>());
+    FUELG_TRY(launch_pdl(prep_rows_kernel<true>, dim3((st->kp + 7) / 8), dim3(256), 0, stream, centers,
+                         (int64_t)st->kp, (int64_t)p.k, p.d, st->dp, 0, st->chi.as<__nv_bfloat16>(),
+                         st->clo.as<__nv_bfloat16>(), st->cnrm2.as<float>(), st->cnrm.as<float>(), (int*)nullptr,
+                         st->ucount.as<int32_t>()));
   else
-    prep_rows_kernel<false><<<(st->kp + 7) / 8, 256, 0, stream>>>(centers, st->kp, p.k, p.d, st->dp,
-                                                                  st->chi.as<__nv_bfloat16>(), nullptr,
-                                                                  st->cnrm2.as<float>(), st->cnrm.as<float>()); ::fuelg::note_launch();
-  FUELG_CUDA(cudaMemsetAsync(st->ucount.p, 0, sizeof(int32_t), stream));
+    FUELG_TRY(launch_pdl(prep_rows_kernel<false>, dim3((st->kp + 7) / 8), dim3(256), 0, stream, centers,
+                         (int64_t)st->kp, (int64_t)p.k, p.d, st->dp, 0, st->chi.as<__nv_bfloat16>(),
+                         (__nv_bfloat16*)nullptr, st->cnrm2.as<float>(), st->cnrm.as<float>(), (int*)nullptr,
+                         st->ucount.as<int32_t>()));
   TcArgs a{};
   a.n = n;
   a.d = p.d;
@@ -655,39 +863,55 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
   a.umask = st->umask.as<uint64_t>();
   a.ucount = st->ucount.as<int32_t>();
   a.mw = st->mw;
-  // Error-bound constants (see the file comment): operand rounding u = 2^-8
-  // per BF16 value (2^-16 residual for hi+lo), FP32 accumulation of KP
-  // (3*KP for hi+lo) products bounded by KP * 2^-23 of sum|x_i c_i| <= |x||c|,
-  // epilogue roundings within 2^-21 (|x|^2 + |c|^2), and fuel's own f32 sum of
-  // d squares within (d + 4) 2^-24 of the distance.
+  // Error-bound constants.  Operand rounding: u = 2^-8 per BF16 value, so a
+  // BF16 product is within (2u + u^2)|x_i c_i|; hi+lo leaves x_lo c_lo and the
+  // residuals, within 3.01 * 2^-16 |x_i c_i|.  FP32 accumulation of KP terms in
+  // the tensor core: within KP * 2^-23 of their absolute sum (allowing
+  // truncation); with hi+lo the hi.hi terms and the (2^-8 smaller) hi.lo +
+  // lo.hi terms use separate accumulators.  Both scale with
+  // S = sum_i |x_i c_i| <= |x||c| (for nonnegative data S = x.c itself).  The
+  // distance takes 2 x.c.  Norms and epilogue roundings stay within beta
+  // (|x|^2 + |c|^2); fuel's own f32 sum of d squares within (d + 4) 2^-24 of
+  // the distance (gamma).
   const double KP = (double)st->kc * BK;
-  const double u8 = std::ldexp(1.0, -8), u23 = std::ldexp(1.0, -23);
-  const double prod = st->split ? 3.1 * std::ldexp(1.0, -16) : (2 * u8 + u8 * u8);
-  const double acc = (st->split ? 3.0 : 1.0) * KP * u23 * (1.0 + 2 * u8);
-  a.alpha = (float)(2.0 * (prod + acc) * 1.01);
-  a.beta = (float)std::ldexp(1.0, -21);
+  const double u8 = std::ldexp(1.0, -8), u23 = std::ldexp(1.0, -23), u24 = std::ldexp(1.0, -24);
+  double rel;
+  if (st->split && st->sep_lo)
+    rel = 3.01 * std::ldexp(1.0, -16) + KP * u23 * (1.0 + 2 * u8) + 2.0 * KP * u23 * 2.01 * u8 + u24;
+  else if (st->split)
+    rel = 3.01 * std::ldexp(1.0, -16) + 3.0 * KP * u23 * (1.0 + 2 * u8);
+  else
+    rel = (2 * u8 + u8 * u8) + KP * u23 * (1.0 + 2 * u8);
+  a.alpha = (float)(2.0 * rel * 1.01);
+  a.s_scale = (float)(1.0 / (1.0 - 1.01 * rel) * (1.0 + std::ldexp(1.0, -20)));
+  a.neg_flag = st->negf.as<int>();
+  a.beta = (float)(((p.d + 31) / 32 + 9) * std::ldexp(1.0, -24) * 1.01);
   a.gamma = (float)((p.d + 4) * std::ldexp(1.0, -24) * 1.01);
   // instruction descriptor: D=F32, A=B=BF16, K-major both, N=kp, M=128
+  a.a_tiled = 1;
   a.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(st->kp >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
   uint32_t cols = 32;
-  while (cols < (uint32_t)(2 * st->kp)) cols <<= 1;
+  while (cols < (uint32_t)((st->sep_lo ? 4 : 2) * st->kp)) cols <<= 1;
   a.tmem_cols = cols;
+  a.sep_lo = st->sep_lo ? 1 : 0;
   a.status = dev_status;
   a.cancel = cancel_word_device();
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t ntiles = (n + BM - 1) / BM;
-  const int grid = (int)std::min<int64_t>(ntiles, sms);
+  const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * st->ctas_per_sm);
   HotTimer* ht = hot_timer();
   if (ht) ht->begin(stream);
   if (st->split)
-    lloyd_tc_kernel<true><<<grid, kTcThreads, st->smem, stream>>>(st->tmA, st->tmAlo, st->tmB, st->tmBlo, a);
+    FUELG_TRY(launch_pdl(lloyd_tc_kernel<true>, dim3(grid), dim3(kTcThreads), st->smem, stream, st->tmA, st->tmAlo,
+                         st->tmB, st->tmBlo, a));
   else
-    lloyd_tc_kernel<false><<<grid, kTcThreads, st->smem, stream>>>(st->tmA, st->tmAlo, st->tmB, st->tmBlo, a); ::fuelg::note_launch();
+    FUELG_TRY(launch_pdl(lloyd_tc_kernel<false>, dim3(grid), dim3(kTcThreads), st->smem, stream, st->tmA,
+                         st->tmAlo, st->tmB, st->tmBlo, a));
   if (ht) ht->end(stream);
   FUELG_CUDA(cudaGetLastError());
-  const int rgrid = 4 * sms;
+  const int rgrid = 8 * sms;
   const int kind = first ? KIND_PAIRWISE : KIND_SQDIST;
   if (kind == KIND_PAIRWISE) {
     if (p.order == ORDER_X86)
@@ -697,12 +921,34 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
       rescore_kernel<KIND_PAIRWISE, ORDER_ARM><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
                                                                          a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
   } else {
-    if (p.order == ORDER_X86)
+    // staged row stride: 16-byte aligned and == 8 (mod 32) floats, so the four
+    // 8-lane groups of a warp read four different bank groups
+    int ds = (p.d + 3) & ~3;
+    while (ds % 32 != 8) ds += 4;
+    if (p.d <= 1024) {
+      const int per = p.order == ORDER_X86 ? 1 : 4;
+      const size_t sm = (size_t)4 * (per + 1) * ds * sizeof(float);
+      const int g2 = 4 * sms;
+      if (p.order == ORDER_X86) {
+        auto kfn = rescore_smem_kernel<KIND_SQDIST, ORDER_X86>;
+        FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FUELG_TRY(launch_pdl(kfn, dim3(g2), dim3(128), sm, stream, p.X, centers, p.d, ds, st->mw,
+                             (const int32_t*)a.ulist, (const uint64_t*)a.umask, (const int32_t*)a.ucount, a.lab_new,
+                             st->rescored_total.as<unsigned long long>()));
+      } else {
+        auto kfn = rescore_smem_kernel<KIND_SQDIST, ORDER_ARM>;
+        FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        FUELG_TRY(launch_pdl(kfn, dim3(g2), dim3(128), sm, stream, p.X, centers, p.d, ds, st->mw,
+                             (const int32_t*)a.ulist, (const uint64_t*)a.umask, (const int32_t*)a.ucount, a.lab_new,
+                             st->rescored_total.as<unsigned long long>()));
+      }
+    } else if (p.order == ORDER_X86) {
       rescore_kernel<KIND_SQDIST, ORDER_X86><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
-                                                                       a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>());
-    else
+                                                                       a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
+    } else {
       rescore_kernel<KIND_SQDIST, ORDER_ARM><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
                                                                        a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
+    }
   }
 FUELG_CUDA(cudaGetLastError());
   return ST_OK;
