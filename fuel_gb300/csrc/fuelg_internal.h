@@ -157,6 +157,11 @@ int exact_topk(const ExactScanParams& p, uint64_t* out_keys, int* dev_status, cu
 int finalize_knn(const uint64_t* keys, int64_t m, int kk, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
                  cudaStream_t stream);
 
+// Top-k + finalize with every temporary inside the caller-provided scratch
+// region (no allocation; queries are batched to fit; no cancellation).
+int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
+                         void* scratch, size_t scratch_bytes, cudaStream_t stream);
+
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
                 float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream);

@@ -405,6 +405,142 @@ int finalize_knn(const uint64_t* keys, int64_t m, int kk, int k, int exclude_mod
 }
 
 // ---------------------------------------------------------------------------
+// The same scan + merge + finalize, driven entirely from a caller-provided
+// scratch region (no allocation, no cancel word).  Queries are processed in
+// batches sized to the region.  Used by the allocation-free C entry point.
+// ---------------------------------------------------------------------------
+namespace {
+
+__global__ void finalize_offset_kernel(const uint64_t* __restrict__ keys, int64_t m, int64_t q0, int kk, int k,
+                                       int mode, int64_t* __restrict__ out_idx, float* __restrict__ out_dist) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= m) return;
+  const int64_t qi = q0 + r;  // query index in the whole call (exclude-self compares against it)
+  const uint64_t* c = keys + r * kk;
+  int64_t* oi = out_idx + qi * k;
+  float* od = out_dist + qi * k;
+  int w = 0;
+  if (mode == 0) {
+    for (; w < k && w < kk; w++) {
+      const uint64_t key = c[w];
+      if (key == KEY_NONE) break;
+      oi[w] = key_idx(key);
+      od[w] = key_dist(key);
+    }
+  } else {
+    const uint64_t kth = (mode == 1 && k >= 1) ? c[k - 1] : KEY_NONE;
+    for (int j = 0; j < kk && w < k; j++) {
+      const uint64_t key = c[j];
+      if (key == KEY_NONE) break;
+      if ((int64_t)key_idx(key) == qi) continue;
+      if (mode == 1 && j >= k && !(kth != KEY_NONE && key_dist(key) == key_dist(kth))) break;
+      oi[w] = key_idx(key);
+      od[w] = key_dist(key);
+      w++;
+    }
+  }
+  for (; w < k; w++) {
+    oi[w] = -1;
+    od[w] = __int_as_float(0x7f800000);
+  }
+}
+
+}  // namespace
+
+int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
+                         void* scratch, size_t scratch_bytes, cudaStream_t stream) {
+  if (p.m == 0 || k == 0) return ST_OK;
+  const size_t head = 256;  // device status word
+  if (scratch_bytes <= head) {
+    set_error("scratch region too small");
+    return ST_ENOTSUP;
+  }
+  int* dev_status = static_cast<int*>(scratch);
+  uint8_t* base = static_cast<uint8_t*>(scratch) + head;
+  const size_t avail = scratch_bytes - head;
+  FUELG_CUDA(cudaMemsetAsync(dev_status, 0, sizeof(int), stream));
+  if (p.n == 0) {
+    const int64_t qb = std::max<int64_t>(1, (int64_t)(avail / ((size_t)p.kk * 8)));
+    for (int64_t b0 = 0; b0 < p.m; b0 += qb) {
+      const int64_t mcur = std::min<int64_t>(qb, p.m - b0);
+      FUELG_CUDA(cudaMemsetAsync(base, 0xff, (size_t)mcur * p.kk * 8, stream));
+      finalize_offset_kernel<<<(unsigned)((mcur + 127) / 128), 128, 0, stream>>>(
+          reinterpret_cast<uint64_t*>(base), mcur, b0, p.kk, k, exclude_mode, out_idx, out_dist); ::fuelg::note_launch();
+    }
+    FUELG_CUDA(cudaGetLastError());
+    return ST_OK;
+  }
+  if (p.n >= 0xffffffffll) {
+    set_error("index too large: n=%lld (limit 2^32-2)", (long long)p.n);
+    return ST_ENOTSUP;
+  }
+  const bool kk1 = p.kk == 1;
+  Plan pl;
+  FUELG_TRY(make_plan(p, kk1, scan_np(p.kind, p.order), &pl));
+  // per query: split lists (or best keys) + the merged keys
+  auto per_query = [&](int S) { return (kk1 ? (size_t)S * 8 : (size_t)S * 2 * p.kk * 8) + (size_t)p.kk * 8; };
+  while (pl.S_grid > 1 && per_query(pl.S_grid * pl.ws) * pl.qpb > avail) {
+    pl.S_grid = std::max(1, pl.S_grid / 2);
+    int64_t split_len = (p.n + pl.S_grid - 1) / pl.S_grid;
+    split_len = ((split_len + pl.pt - 1) / pl.pt) * pl.pt;
+    pl.split_len = split_len;
+    pl.S_grid = (int)std::max<int64_t>(1, (p.n + split_len - 1) / split_len);
+  }
+  const int S = pl.S_grid * pl.ws;
+  const size_t pq = per_query(S);
+  if (pq * pl.qpb > avail) {
+    set_error("k=%d needs %zu bytes of scratch per %d queries; the static region holds %zu", k, pq * pl.qpb,
+              pl.qpb, avail);
+    return ST_ENOTSUP;
+  }
+  int64_t mb = (int64_t)(avail / pq);
+  mb = std::max<int64_t>(pl.qpb, (mb / pl.qpb) * pl.qpb);
+  mb = std::min<int64_t>(mb, p.m);
+  uint64_t* lists = reinterpret_cast<uint64_t*>(base);
+  uint64_t* keys = lists + (pq / 8 - p.kk) * (size_t)mb;
+  for (int64_t b0 = 0; b0 < p.m; b0 += mb) {
+    const int64_t mcur = std::min<int64_t>(mb, p.m - b0);
+    ScanArgs a{};
+    a.A = p.A + b0 * p.d;
+    a.m = mcur;
+    a.B = p.B;
+    a.n = p.n;
+    a.d = p.d;
+    a.kk = p.kk;
+    a.metric = p.metric;
+    a.split_len = pl.split_len;
+    a.ws = pl.ws;
+    a.qpb = pl.qpb;
+    a.pt = pl.pt;
+    a.qs = pl.qs;
+    a.xs = pl.xs;
+    a.lists = kk1 ? nullptr : lists;
+    a.best = kk1 ? lists : nullptr;
+    a.status = dev_status;
+    a.cancel = nullptr;
+    a.a_vec4 = vec4_ok(a.A, a.d);
+    a.b_vec4 = vec4_ok(a.B, a.d);
+    const int64_t qblocks = (mcur + pl.qpb - 1) / pl.qpb;
+    int st;
+    if (p.order == ORDER_X86) st = dispatch_np<KIND_KNN, ORDER_X86>(a, pl, qblocks, kk1, stream);
+    else st = dispatch_np<KIND_KNN, ORDER_ARM>(a, pl, qblocks, kk1, stream);
+    if (st != ST_OK) return st;
+    if (kk1) {
+      min_splits_kernel<<<(unsigned)((mcur + 255) / 256), 256, 0, stream>>>(lists, mcur, S, keys); ::fuelg::note_launch();
+    } else if (S == 1) {
+      const int64_t tot = mcur * p.kk;
+      copy_lists_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, stream>>>(lists, mcur, p.kk, keys); ::fuelg::note_launch();
+    } else {
+      merge_splits_kernel<<<(unsigned)((mcur * 32 + 255) / 256), 256, 0, stream>>>(lists, mcur, S, p.kk, keys); ::fuelg::note_launch();
+    }
+    finalize_offset_kernel<<<(unsigned)((mcur + 127) / 128), 128, 0, stream>>>(keys, mcur, b0, p.kk, k, exclude_mode,
+                                                                             out_idx, out_dist); ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+  }
+  return ST_OK;
+}
+
+// ---------------------------------------------------------------------------
 // Range search (linear_scan_range, src/api/search.rs:154-166): two passes of
 // the same scan -- count, then fill at scanned offsets -- then a segmented
 // sort of the (distance, index) keys of every query.

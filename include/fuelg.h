@@ -120,6 +120,28 @@ int fuelg_kmeans_lloyd(const float *data, int64_t n, int32_t d, int32_t k, const
                        float *out_centers, int64_t *out_labels, int32_t *out_iters, double *out_inertia,
                        fuelg_stats *stats);
 
+/* Allocation-free exact kNN.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory -- code recording a CUDA graph
+ * (cudaMalloc is not allowed during capture), hosts whose GPU memory belongs to
+ * another allocator or is budgeted up front, and embedded callers that must
+ * not grow their footprint after start-up.  Same results as fuelg_knn on a
+ * linear index built from `data` with the same metric and order.
+ *  - data [n, d], queries [m, d], out_idx / out_dist [m, k] must be device
+ *    (or managed / mapped) memory: host buffers are rejected with
+ *    FUELG_EINVAL, since staging them would need an allocation.
+ *  - every temporary lives in one static 32 MiB device array of the library,
+ *    held by each GPU that loads it until the process exits; queries are
+ *    processed in batches that fit it; k <= 4095.
+ *  - the first call on a device resolves that array's address; make it before
+ *    any stream capture.
+ *  - all calls share the array and leave their contents in it, so calls that
+ *    overlap on the GPU (different streams, host threads) race: serialise them.
+ *  - work is ordered on `stream` (a cudaStream_t, NULL = legacy default); the
+ *    call returns after that stream has finished it; no cancellation. */
+int fuelg_knn_noalloc(const float *data, int64_t n, int32_t d, const float *queries, int64_t m, int32_t k,
+                      int32_t metric, int32_t order, int32_t exclude_mode, int64_t *out_idx, float *out_dist,
+                      void *stream);
+
 /* Cooperative cancellation (src/api/mod.rs:29 SHUTDOWN_REQUESTED): running
  * kernels poll a host-mapped word and stop; the call returns
  * FUELG_ECANCELLED.  Each call clears the word when it starts, as
