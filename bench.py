@@ -7,9 +7,17 @@ stand-in for MNIST), init = 64 seeded distinct rows, 100 fixed iterations.
 The input matrix (219.5 MB) is larger than the 129 MB L2, so no explicit L2
 flush is needed between steps.
 
+Beside it (same JSON line): the plain kNN self-join (n=20,000, d=16, k=10)
+and the tensor-core kNN self-join (n=1,000,000, d=128, k=100, integer data)
+with its plain FP32 CUDA-core rate on a query subset.
+
 Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun (N>1) each rank runs an independent replica ("replicas only";
 the path is a single-device engine) and rank 0 prints one JSON line.
+
+python bench.py --profile lloyd|knn_tc|knn_plain [--steps K] [--warmup W]
+runs one workload alone (no CPU baseline, no side legs) for profiler
+captures; --knn-queries sets the query count of the kNN workloads there.
 """
 from __future__ import annotations
 
@@ -30,6 +38,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "k-means Lloyd iters/s & kNN queries/s: TC+refine vs plain FP32, 1 GB300; p99"
 N, D, K, ITERS = 70_000, 784, 64, 100
+REF_SAMPLE_ITERS = 10    # Lloyd iterations per reference-arm step (about 1 s of CPU work)
+CPU_SAMPLE_ITERS = 100   # iterations of the CPU baseline leg (one full step, about 10 s)
+KNN_N, KNN_D, KNN_K = 1_000_000, 128, 100
+KNN_PLAIN_QUERIES = 20_000  # plain FP32 tier on a query subset (about 0.6 s)
 
 
 def peaks():
@@ -101,11 +113,12 @@ def dist_env():
 
 def cpu_lloyd_sample(X, init, iters, threads):
     """fuel's CPU Lloyd (restated, f32 running sums, host summation order) on
-    the full matrix for a bounded number of iterations; returns seconds."""
+    the full matrix for at most `iters` iterations; returns (seconds,
+    iterations run).  fuel counts the initial assignment as iteration 1."""
     from oracle import oracle
     t0 = time.perf_counter()
-    oracle.lloyd(X, K, init, max_iter=iters, order=oracle.host_order(), threads=threads)
-    return time.perf_counter() - t0
+    _, _, it, _ = oracle.lloyd(X, K, init, max_iter=iters, order=oracle.host_order(), threads=threads)
+    return time.perf_counter() - t0, it
 
 
 def run_reference(args):
@@ -117,12 +130,13 @@ def run_reference(args):
     oracle.build()
     X, init = workloads.lloyd_sparse(N, D, K)
     threads = os.cpu_count() or 1
-    sample_iters = 3
+    sample_iters = REF_SAMPLE_ITERS
     for _ in range(args.warmup):
         cpu_lloyd_sample(X, init, sample_iters, threads)
-    times = [cpu_lloyd_sample(X, init, sample_iters, threads) for _ in range(args.steps)]
-    tot = sum(times)
-    value = sample_iters * len(times) / tot
+    runs = [cpu_lloyd_sample(X, init, sample_iters, threads) for _ in range(args.steps)]
+    tot = sum(t for t, _ in runs)
+    value = sum(it for _, it in runs) / tot
+    times = runs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
@@ -245,11 +259,14 @@ def run_ours(args):
     # kNN plain self-join (n=20,000, d=16, k=10) queries/s, device-resident, plain FP32
     knn = knn_plain_rate(lib, _lib, torch, args)
 
+    # tensor-core kNN self-join next to its plain FP32 tier
+    knn_tc = knn_tc_rate(lib, _lib, torch, args)
+
     # CPU baseline: restated fuel CPU Lloyd on the host cores, bounded sample
     threads = os.cpu_count() or 1
-    sample_iters = 2
-    cpu_t = cpu_lloyd_sample(X, init, sample_iters, threads)
-    cpu_value = sample_iters / cpu_t
+    sample_iters = CPU_SAMPLE_ITERS
+    cpu_t, cpu_it = cpu_lloyd_sample(X, init, sample_iters, threads)
+    cpu_value = cpu_it / cpu_t
 
     line = {
         "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
@@ -267,7 +284,8 @@ def run_ours(args):
                      "avg_launch_ms": avg_launch_ms, "peak_source": "measured" if "_fallback" not in pk else
                      "fallback"},
         "cpu_baseline": {"value": cpu_value, "unit": "iters/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample_iters} iterations of the full n={N} matrix, restated fuel CPU Lloyd"},
+                         "sample": f"{cpu_it} iterations of the full n={N} matrix (one call, max_iter="
+                                   f"{sample_iters}), restated fuel CPU Lloyd, {cpu_t:.1f} s"},
         "clocks": clk.summary(),
         "inertia": inertia,
         "precision_used": {0: "fp32", 1: "bf16", 2: "split_bf16"}[prec_used],
@@ -275,6 +293,7 @@ def run_ours(args):
         "plain_fp32": plain,
         "tc_vs_plain": (value / plain["iters_per_s"]) if plain else None,
         "knn_plain": knn,
+        "knn_tc": knn_tc,
     }
     print(json.dumps(line), flush=True)
 
@@ -305,15 +324,99 @@ def knn_plain_rate(lib, _lib, torch, args):
         lib.fuelg_index_destroy(h)
 
 
+def knn_tc_rate(lib, _lib, torch, args, m_tc=None, plain=True, reps=1, n_index=KNN_N):
+    """Exact kNN self-join n=1e6, d=128, k=100 (integer data): tensor-core tier
+    over m_tc queries (default all n), plain FP32 tier over a query subset;
+    device-resident queries and outputs; distance evaluations = m * n."""
+    from fuel_gb300 import workloads
+    X = workloads.knn_geometric(n_index, KNN_D)
+    n, d, k = n_index, KNN_D, KNN_K
+    m_tc = n if m_tc is None else m_tc
+    h = ctypes.c_void_p()
+    _lib.check(lib.fuelg_index_create(_lib.ptr(X), n, d, 0, _lib.ORDER[_lib.default_order()], ctypes.byref(h)))
+    try:
+        Qd = torch.from_numpy(X[:m_tc]).cuda()
+        oi = torch.empty((m_tc, k), dtype=torch.int64, device="cuda")
+        od = torch.empty((m_tc, k), dtype=torch.float32, device="cuda")
+
+        def call(m, prec):
+            st = _lib.Stats()
+            _lib.check(lib.fuelg_knn(h, _lib.ptr(Qd), m, k, 1, prec, _lib.ptr(oi), _lib.ptr(od), ctypes.byref(st)))
+            return st
+
+        call(min(m_tc, 4096), 1)
+        sts = [call(m_tc, 1) for _ in range(reps)]
+        t = sum(s.device_ms for s in sts) / len(sts)
+        hot = sum(s.hot_kernel_ms for s in sts) / max(1, sum(s.hot_kernel_launches for s in sts))
+        out = {"workload": f"knn self-join n={n} d={d} k={k} sqeuclidean, integer geometric(0.1) data",
+               "queries": m_tc, "queries_per_s": m_tc / (t / 1e3), "ms_per_call": t,
+               "distance_evals_per_s": m_tc * float(n) / (t / 1e3), "hot_kernel_ms": hot,
+               "hot_kernel_launches": sts[-1].hot_kernel_launches, "rescored": sts[-1].rescored,
+               "precision_used": {0: "fp32", 1: "bf16", 2: "split_bf16"}[sts[-1].precision_used],
+               "kernel_launches": sts[-1].kernel_launches}
+        # tensor pipe: 2*m*n*dp flops in the screen kernel
+        dp = ((d + 63) // 64) * 64
+        out["screen_tflops"] = 2.0 * m_tc * n * dp / (hot * sts[-1].hot_kernel_launches / 1e3) / 1e12
+        if plain:
+            mp = min(KNN_PLAIN_QUERIES, m_tc)
+            call(min(mp, 2048), 0)
+            st = call(mp, 0)
+            pr = mp * float(n) / (st.device_ms / 1e3)
+            out["plain_fp32"] = {"queries": mp, "ms_per_call": st.device_ms, "distance_evals_per_s": pr}
+            out["tc_vs_plain"] = out["distance_evals_per_s"] / pr
+        return out
+    finally:
+        lib.fuelg_index_destroy(h)
+
+
+def run_profile(args):
+    """One workload alone, for profiler captures."""
+    import torch
+    from fuel_gb300 import _lib, build, workloads
+    build.build()
+    lib = _lib.load()
+    if args.profile == "lloyd":
+        X, init = workloads.lloyd_sparse(N, D, K)
+        Xd = torch.from_numpy(X).cuda()
+        Cd = torch.from_numpy(init).cuda()
+        oc = torch.empty((K, D), dtype=torch.float32, device="cuda")
+        ol = torch.empty((N,), dtype=torch.int64, device="cuda")
+        ms = []
+        for i in range(args.warmup + args.steps):
+            st = _lib.Stats()
+            it = ctypes.c_int32()
+            inert = ctypes.c_double()
+            _lib.check(lib.fuelg_kmeans_lloyd(_lib.ptr(Xd), N, D, K, _lib.ptr(Cd), args.iters, 0.0,
+                                              _lib.PRECISION[args.precision], _lib.ORDER[_lib.default_order()],
+                                              _lib.LLOYD_FIXED_ITERS, _lib.ptr(oc), _lib.ptr(ol), ctypes.byref(it),
+                                              ctypes.byref(inert), ctypes.byref(st)))
+            if i >= args.warmup:
+                ms.append(st.device_ms)
+        print(json.dumps({"profile": "lloyd", "iters": args.iters, "ms_per_call": sum(ms) / max(1, len(ms))}))
+    elif args.profile == "knn_tc":
+        r = knn_tc_rate(lib, _lib, torch, args, m_tc=args.knn_queries, plain=False, reps=max(1, args.steps),
+                        n_index=args.knn_n)
+        print(json.dumps({"profile": "knn_tc", **r}))
+    else:
+        args.steps = max(1, args.steps)
+        print(json.dumps({"profile": "knn_plain", **knn_plain_rate(lib, _lib, torch, args)}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="bf16")
+    ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="split_bf16")
+    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain"], default=None)
+    ap.add_argument("--iters", type=int, default=ITERS, help="Lloyd iterations per call (--profile lloyd)")
+    ap.add_argument("--knn-queries", type=int, default=20_000, help="query count (--profile knn_tc)")
+    ap.add_argument("--knn-n", type=int, default=KNN_N, help="index rows (--profile knn_tc)")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

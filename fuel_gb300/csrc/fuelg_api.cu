@@ -374,8 +374,16 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   p.order = ix->order;
   p.metric = ix->metric;
   p.kk = kk;
-  // Tensor-core tiers are served by the exact path until the screen lands.
-  FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
+  int used = FUELG_PREC_FP32;
+  int64_t rescored = 0;
+  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk) && ix->n > 0) {
+    int exact = 0;
+    FUELG_TRY(knn_tc_topk(p.A, m, ix->X, ix->n, ix->d, kk, ix->order, ix->metric, keys.as<uint64_t>(),
+                          dstat.as<int>(), s, &rescored, &exact));
+    used = FUELG_PREC_BF16;
+  } else {
+    FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
+  }
   FUELG_TRY(finalize_knn(keys.as<uint64_t>(), m, kk, k, exclude_mode, static_cast<int64_t*>(oi.dptr),
                          static_cast<float*>(od.dptr), s));
   int64_t d2h = 0;
@@ -388,7 +396,8 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
     stats->h2d_bytes = q.h2d;
     stats->d2h_bytes = d2h;
     stats->distance_evals = m * ix->n;
-    stats->precision_used = FUELG_PREC_FP32;
+    stats->precision_used = used;
+    stats->rescored = rescored;
     meter.fill(stats);
   }
   return ST_OK;

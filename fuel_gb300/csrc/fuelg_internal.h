@@ -162,6 +162,12 @@ int finalize_knn(const uint64_t* keys, int64_t m, int kk, int k, int exclude_mod
 int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
                          void* scratch, size_t scratch_bytes, cudaStream_t stream);
 
+// Tensor-core kNN (fuelg_knn_tc.cu): top-kk keys per query [m, kk] via a BF16
+// tcgen05 screen; exact for integer data, otherwise re-scored and proven.
+bool knn_tc_supported(int d, int kk);
+int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d, int kk, int order, int metric,
+                uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out);
+
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
                 float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream);

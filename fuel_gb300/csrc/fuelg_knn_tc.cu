@@ -1,0 +1,649 @@
+// fuelg_knn_tc.cu -- tensor-core (tcgen05 / TMEM / TMA) linear-scan kNN.
+//
+// Each CTA owns 128 query rows: their BF16 copy stays resident in shared
+// memory while the index streams through in 256-row tiles.  One thread issues
+// tcgen05.mma (M=128, N=256, K=16, BF16 operands, FP32 accumulators in TMEM,
+// two accumulators alternating); four epilogue warps read their query's 256
+// dot products with tcgen05.ld, form D~ = |q|^2 + |x|^2 - 2 q.x and keep the
+// query's kk2 best (D~, index) keys with the same threshold-filter + sorted
+// list scheme as the exact scan.
+//
+// Exact mode: when every value of the index and the queries is an integer of
+// magnitude <= 256 and 2 d V^2 < 2^24, every BF16 product, every FP32 partial
+// sum and D~ itself are exact integers below 2^24 -- D~ then IS fuel's f32
+// distance (src/distance/squared_euclidean.rs sums the same exact integers),
+// whatever the summation order, and the screen keys are final.
+// Otherwise the kk2 = kk + margin best screened keys are re-scored with the
+// reference's f32 operation order and kept only when a rigorous bound proves
+// every unscreened point is strictly worse than the kk-th re-scored key; the
+// queries that fail the proof are re-run through the exact scan.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fuelg_common.cuh"
+#include "fuelg_internal.h"
+#include "fuelg_tc_common.cuh"
+
+namespace fuelg {
+
+using namespace tcx;
+
+namespace {
+
+constexpr int QM = 128;        // queries per CTA (UMMA M)
+constexpr int XN = 256;        // index rows per tile (UMMA N)
+constexpr int kEpi = 128;      // epilogue threads
+constexpr int kThreadsKT = 192;
+constexpr int kCBk = 32;       // candidate buffer entries per epilogue thread
+
+struct KnnTcArgs {
+  int64_t m, n;
+  int kc;        // K chunks of 64
+  int kk2;       // keys kept per query
+  int exact;     // D~ is exact (integer data)
+  int stages;
+  const float* qn2;  // |q|^2 per query row
+  const float* xn2;  // |x|^2 per index row (padded rows: 0)
+  uint64_t* lists;   // [m][2*kk2]
+  uint64_t* out_keys;  // [m][kk2]
+  uint32_t idesc;
+  int* status;
+  const volatile int* cancel;
+};
+
+__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
+  const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
+  const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
+  return ((uint64_t)hi << 32) | lo;
+}
+__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
+  const uint32_t lo = __shfl_xor_sync(0xffffffffu, (uint32_t)v, m);
+  const uint32_t hi = __shfl_xor_sync(0xffffffffu, (uint32_t)(v >> 32), m);
+  return ((uint64_t)hi << 32) | lo;
+}
+
+// Warp-cooperative merge of one query's buffered candidates (cnt <= 32
+// unsorted keys in shared memory at stride kEpi) into its sorted kk-list
+// cur[0..kk) -> nxt[0..kk).  The buffer is bitonic-sorted across the lanes;
+// every output slot is written exactly once: a list key L[i] lands at
+// i + #{buffer < L[i]}, a buffer key B[t] at t + #{list < B[t]} (keys are
+// unique: the index is in the low half), and slots >= kk are dropped.
+// Returns the new kk-th key on every lane.
+__device__ __noinline__ uint64_t warp_merge(const uint64_t* __restrict__ sbuf, int cnt,
+                                            const uint64_t* __restrict__ cur, uint64_t* __restrict__ nxt, int kk,
+                                            int lane) {
+  uint64_t b = lane < cnt ? sbuf[lane * kEpi] : KEY_NONE;
+#pragma unroll
+  for (int k2 = 2; k2 <= 32; k2 <<= 1) {
+#pragma unroll
+    for (int j = k2 >> 1; j > 0; j >>= 1) {
+      const uint64_t o = shfl_xor64(b, j);
+      const bool up = (lane & k2) == 0 || k2 == 32;
+      const bool lower = (lane & j) == 0;
+      b = (lower == up) ? (o < b ? o : b) : (o > b ? o : b);
+    }
+  }
+  uint64_t tv = KEY_NONE;
+  int has = 0;
+  if (b != KEY_NONE) {
+    int lo = 0, hi = kk;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (cur[mid] < b) lo = mid + 1;
+      else hi = mid;
+    }
+    const int slot = lane + lo;
+    if (slot < kk) {
+      nxt[slot] = b;
+      if (slot == kk - 1) {
+        tv = b;
+        has = 1;
+      }
+    }
+  }
+#pragma unroll 2
+  for (int i0 = 0; i0 < kk; i0 += 32) {
+    const int i = i0 + lane;
+    const uint64_t v = i < kk ? cur[i] : KEY_NONE;
+    int pos = 0;
+#pragma unroll
+    for (int st = 16; st >= 1; st >>= 1)
+      if (shfl64(b, pos + st - 1) < v) pos += st;
+    if (shfl64(b, pos) < v) pos++;
+    const int slot = i + pos;
+    if (i < kk && slot < kk) {
+      nxt[slot] = v;
+      if (slot == kk - 1) {
+        tv = v;
+        has = 1;
+      }
+    }
+  }
+  const unsigned bm = __ballot_sync(0xffffffffu, has);
+  return shfl64(tv, __ffs(bm) - 1);
+}
+
+__global__ void __launch_bounds__(kThreadsKT, 1)
+    knn_tc_kernel(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmX, KnnTcArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_chunk = QM * BK * 2;  // 16 KB
+  const uint32_t b_bytes = XN * BK * 2;  // 32 KB per stage
+  const int NS = a.stages;
+  uint8_t* sA = base;
+  uint8_t* sB = base + (size_t)a.kc * a_chunk;
+  uint64_t* full = reinterpret_cast<uint64_t*>(sB + (size_t)NS * b_bytes);
+  uint64_t* empty = full + NS;
+  uint64_t* accf = empty + NS;
+  uint64_t* acce = accf + 2;
+  uint64_t* afull = acce + 2;
+  uint64_t* fin = afull + 1;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+  uint64_t* cbuf = reinterpret_cast<uint64_t*>(tmem_holder + 4);  // [kCBk][kEpi]
+  float* xnsm = reinterpret_cast<float*>(cbuf + (size_t)kCBk * kEpi);  // [2][XN] index norms
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t q0 = (int64_t)blockIdx.x * QM;
+  const int64_t ntiles = (a.n + XN - 1) / XN;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], kEpi);
+    }
+    mbar_init(afull, 1);
+    mbar_init(fin, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                 "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_holder;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      prefetch_tmap(&tmQ);
+      prefetch_tmap(&tmX);
+      const uint64_t pol_q = policy_evict_first(), pol_x = policy_evict_last();
+      // the query tile, once
+      mbar_expect_tx(afull, (uint32_t)a.kc * a_chunk);
+      for (int kc = 0; kc < a.kc; kc++) tma_load_2d_hint(sA + (size_t)kc * a_chunk, &tmQ, kc * BK, (int)q0, afull, pol_q);
+      uint32_t stage = 0, phase = 0, armed = 0, last_ph = 0;
+      for (int64_t t = 0; t < ntiles && !*abort_flag; t++) {
+        if ((t & 63) == 63 && a.cancel != nullptr && *a.cancel) {
+          atomicOr(a.status, DEV_CANCELLED);
+          *abort_flag = 1;
+          break;
+        }
+        for (int kc = 0; kc < a.kc; kc++) {
+          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+            if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+            *abort_flag = 1;
+            break;
+          }
+          mbar_expect_tx(&full[stage], b_bytes);
+          armed |= 1u << stage;
+          last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
+          tma_load_2d_hint(sB + (size_t)stage * b_bytes, &tmX, kc * BK, (int)(t * XN), &full[stage], pol_x);
+          if (++stage == (uint32_t)NS) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      volatile int never = 0;
+      if (!mbar_wait(afull, 0, &never)) atomicOr(a.status, DEV_TIMEOUT);
+      for (int s2 = 0; s2 < NS; s2++)
+        if (armed & (1u << s2))
+          if (!mbar_wait(&full[s2], (last_ph >> s2) & 1u, &never)) atomicOr(a.status, DEV_TIMEOUT);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      bool ok = mbar_wait(afull, 0, abort_flag);
+      if (!ok) {
+        if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+        *abort_flag = 1;
+      }
+      tc_fence_after();
+      uint32_t stage = 0, phase = 0;
+      for (int64_t t = 0; ok && t < ntiles && !*abort_flag; t++) {
+        const uint32_t buf = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
+        if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag)) {
+          if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d_tmem = tmem_base + buf * XN;
+        for (int kc = 0; kc < a.kc; kc++) {
+          if (!mbar_wait(&full[stage], phase, abort_flag)) {
+            if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+            *abort_flag = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint64_t ad = smem_desc_sw128(smem_u32(sA + (size_t)kc * a_chunk));
+          const uint64_t bd = smem_desc_sw128(smem_u32(sB + (size_t)stage * b_bytes));
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; kk++)
+            umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (kc | kk) != 0 ? 1u : 0u);
+          umma_commit(&empty[stage]);
+          if (++stage == (uint32_t)NS) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        umma_commit(&accf[buf]);
+      }
+      umma_commit(fin);
+      volatile int never = 0;
+      if (!mbar_wait(fin, 0, &never)) atomicOr(a.status, DEV_TIMEOUT);
+    }
+  } else {
+    const int g = warp & 3;
+    const int row = g * 32 + lane;  // TMEM lane = query row of the tile
+    const int et = threadIdx.x - 64;  // epilogue thread id 0..127
+    const int64_t qi = q0 + row;
+    const bool valid = qi < a.m;
+    const float nq = valid ? a.qn2[qi] : 0.0f;
+    uint64_t* list = a.lists + (valid ? qi : 0) * 2ull * a.kk2;
+    if (valid)
+      for (int o = 0; o < a.kk2; o++) list[o] = KEY_NONE;
+    uint64_t* buf = cbuf + et;
+    uint64_t tau = KEY_NONE;
+    float tau_d = __int_as_float(0x7f800000);
+    int cnt = 0, half = 0;
+    // Lanes whose buffer passed `lim` entries merge, one query at a time, with
+    // the whole warp.
+    auto flush = [&](int lim) {
+      unsigned need = __ballot_sync(0xffffffffu, cnt > lim);
+      if (!need) return;
+      __syncwarp();
+      while (need) {
+        const int src = __ffs(need) - 1;
+        need &= need - 1;
+        const int scnt = __shfl_sync(0xffffffffu, cnt, src);
+        const int shalf = __shfl_sync(0xffffffffu, half, src);
+        uint64_t* lb = a.lists + (q0 + g * 32 + src) * 2ull * a.kk2;
+        const uint64_t nt = warp_merge(cbuf + (et - lane + src), scnt, lb + (size_t)shalf * a.kk2,
+                                       lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
+        if (lane == src) {
+          tau = nt;
+          tau_d = nt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(nt);
+          half ^= 1;
+          cnt = 0;
+        }
+        __syncwarp();
+      }
+    };
+    for (int64_t t = 0; t < ntiles; t++) {
+      const uint32_t b = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
+      const int64_t p0 = t * XN;
+      // this tile's index norms into shared memory (double-buffered by tile parity)
+      float* nsm = xnsm + b * XN;
+      nsm[et] = __ldg(a.xn2 + p0 + et);
+      nsm[et + kEpi] = __ldg(a.xn2 + p0 + et + kEpi);
+      // the wait outcome is combined over the 128 epilogue threads (which also
+      // publishes the norms), so all of them leave the loop on the same tile
+      bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag);
+      if (!ok) {
+        if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+        *abort_flag = 1;
+      }
+      if (named_bar_or(1, kEpi, !ok)) break;
+      tc_fence_after();
+      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN;
+      const bool live = valid && p0 < a.n;
+      for (int c0 = 0; c0 < XN; c0 += 64) {
+        uint32_t r[4][16];
+#pragma unroll
+        for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+        tmem_ld_wait();
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+          if (live) {
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+              const int c = c0 + 16 * h + j;
+              const int64_t p = p0 + c;
+              float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nq + nsm[c]);
+              if (!a.exact) dt = fmaxf(dt, 0.0f);
+              if (dt <= tau_d && p < a.n) {
+                const uint64_t key = make_key(dt, (uint32_t)p);
+                if (key < tau) {
+                  buf[cnt * kEpi] = key;
+                  cnt++;
+                }
+              }
+            }
+          }
+          flush(kCBk - 16);
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acce[b]);
+    }
+    flush(0);
+    // results out, one query at a time per warp (coalesced)
+    for (int src = 0; src < 32; src++) {
+      const int64_t qs = q0 + g * 32 + src;
+      if (qs >= a.m) break;
+      const int shalf = __shfl_sync(0xffffffffu, half, src);
+      const uint64_t* from = a.lists + qs * 2ull * a.kk2 + (size_t)shalf * a.kk2;
+      uint64_t* to = a.out_keys + qs * a.kk2;
+      for (int o = lane; o < a.kk2; o += 32) to[o] = from[o];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512) : "memory");
+  }
+}
+
+// Rows -> BF16 copy padded to dp columns and rows_pad rows (zeros), |row|^2 in
+// FP32, plus an integer-data census: flags[0] |= non-integer or |v| > 256,
+// flags[1] = max |v| (as float bits; non-negative so integer order works).
+__global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64_t rows_pad, int d, int dp,
+                                __nv_bfloat16* __restrict__ out, float* __restrict__ n2, int* __restrict__ flags) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  int bad = 0;
+  float vmax = 0.0f;
+  for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < rows_pad; r += (int64_t)gridDim.x * nw) {
+    float acc = 0.0f;
+    for (int c = lane; c < dp; c += 32) {
+      const float x = (r < rows && c < d) ? __ldg(X + r * d + c) : 0.0f;
+      out[r * dp + c] = __float2bfloat16_rn(x);
+      acc = fmaf(x, x, acc);
+      if (x != rintf(x) || fabsf(x) > 256.0f) bad = 1;
+      vmax = fmaxf(vmax, fabsf(x));
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) n2[r] = acc;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    bad |= __shfl_xor_sync(0xffffffffu, bad, off);
+    vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, off));
+  }
+  if (lane == 0) {
+    if (bad) atomicOr(&flags[0], 1);
+    atomicMax(&flags[1], __float_as_int(vmax));
+  }
+}
+
+// Re-score the kk2 screened candidates of every query with the reference's
+// own f32 order (8-lane groups = fuel's SIMD lanes, 4 candidates per warp
+// step), sort them by (distance, index) in the metric's domain, and prove that
+// no unscreened point can displace the kk-th: every unscreened point has
+// D~ >= D~_last, so its reference distance is >= D~_last - E_max.  Queries that
+// fail the proof are flagged for the exact scan.
+template <int ORDER>
+__global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __restrict__ X, int d, int64_t m,
+                                   int kk, int kk2, int metric, const uint64_t* __restrict__ keys_in,
+                                   uint64_t* __restrict__ keys_out, const float* __restrict__ qn2, float xmax_norm,
+                                   float xmax_n2, float alpha, float beta, float gamma,
+                                   int32_t* __restrict__ redo, int32_t* __restrict__ nredo) {
+  extern __shared__ __align__(16) float qsm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int64_t qi = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (qi >= m) return;
+  float* qs = qsm + (size_t)wib * (d + 4);
+  for (int e = lane; e < d; e += 32) qs[e] = __ldg(Q + qi * d + e);
+  __syncwarp();
+  const uint64_t* kin = keys_in + qi * kk2;
+  uint64_t* kout = keys_out + qi * kk2;
+  // exact keys of the candidates, written in place of the screened ones
+  const int l = lane & 7, grp = lane >> 3;
+  float last_screen = 0.0f;
+  for (int c0 = 0; c0 < kk2; c0 += 4) {
+    const int c = c0 + grp;
+    const uint64_t sk = c < kk2 ? kin[c] : KEY_NONE;
+    const bool real = sk != KEY_NONE;
+    const uint32_t idx = real ? key_idx(sk) : 0u;
+    const float* x = X + (int64_t)idx * d;
+    const int sd = d & ~7;
+    float acc = 0.0f;
+    for (int i = l; i < sd; i += 8) {
+      const float df = __fsub_rn(qs[i], __ldg(x + i));
+      acc = ORDER == ORDER_X86 ? __fmaf_rn(df, df, acc) : __fadd_rn(sq_rn(df), acc);
+    }
+    float s = __shfl_sync(0xffffffffu, acc, lane & ~7);
+#pragma unroll
+    for (int t = 1; t < 8; t++) s = __fadd_rn(s, __shfl_sync(0xffffffffu, acc, (lane & ~7) + t));
+    for (int i = sd; i < d; i++) {
+      const float df = __fsub_rn(qs[i], __ldg(x + i));
+      s = ORDER == ORDER_X86 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+    }
+    if (metric == METRIC_EUCLIDEAN) s = __fsqrt_rn(s);
+    if (l == 0 && c < kk2) kout[c] = real ? make_key(s, idx) : KEY_NONE;
+    if (real) last_screen = fmaxf(last_screen, key_dist(sk));
+  }
+  // the largest screened distance kept (candidates are sorted by screened key)
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) last_screen = fmaxf(last_screen, __shfl_xor_sync(0xffffffffu, last_screen, off));
+  __syncwarp();
+  // sort the kk2 exact keys (small: insertion sort by lane 0)
+  if (lane == 0) {
+    for (int a1 = 1; a1 < kk2; a1++) {
+      const uint64_t v = kout[a1];
+      int b = a1 - 1;
+      while (b >= 0 && kout[b] > v) {
+        kout[b + 1] = kout[b];
+        b--;
+      }
+      kout[b + 1] = v;
+    }
+    // proof: only needed when every slot was filled (otherwise every point was kept)
+    const bool full_list = kin[kk2 - 1] != KEY_NONE;
+    if (full_list) {
+      const float nq = qn2[qi];
+      const float qn = sqrtf(nq);
+      const float e = (alpha * qn * xmax_norm + beta * (nq + xmax_n2)) * (1.0f + gamma) + gamma * last_screen;
+      const float lower = last_screen - e;  // every unscreened point's reference squared distance is >= this
+      const uint64_t kth = kout[kk - 1];
+      bool ok;
+      if (metric == METRIC_EUCLIDEAN) ok = kth != KEY_NONE && lower > 0.0f && key_dist(kth) < __fsqrt_rd(lower);
+      else ok = kth != KEY_NONE && key_dist(kth) < lower;
+      if (!ok) redo[atomicAdd(nredo, 1)] = (int32_t)qi;
+    }
+  }
+}
+
+__global__ void gather_rows_kernel(const float* __restrict__ Q, int d, const int32_t* __restrict__ rows,
+                                   const int32_t* __restrict__ nrows, float* __restrict__ out) {
+  const int cnt = *nrows;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < (int64_t)cnt * d;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = e / d, c = e - r * d;
+    out[e] = Q[(int64_t)rows[r] * d + c];
+  }
+}
+
+__global__ void scatter_keys_kernel(const uint64_t* __restrict__ src, int kk, int kk2,
+                                    const int32_t* __restrict__ rows, int cnt, uint64_t* __restrict__ dst) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (int64_t)cnt * kk2) return;
+  const int64_t r = e / kk2, j = e - r * kk2;
+  dst[(int64_t)rows[r] * kk2 + j] = j < kk ? src[r * kk + j] : KEY_NONE;
+}
+
+}  // namespace
+
+bool knn_tc_supported(int d, int kk) { return d >= 32 && d <= 256 && kk <= 1024; }
+
+// Top-kk keys of every query via the tensor-core screen.  out_keys: [m, kk]
+// (device).  X32/Q32: the f32 rows (for the exact re-score).
+int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d, int kk, int order, int metric,
+                uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out) {
+  const int dp = ((d + BK - 1) / BK) * BK;
+  const int kc = dp / BK;
+  const int64_t mpad = ((m + QM - 1) / QM) * QM;
+  const int64_t npad = ((n + XN - 1) / XN) * XN;
+  Scratch qb, xb, qn2, xn2, flags;
+  FUELG_TRY(qb.alloc((size_t)mpad * dp * 2, stream));
+  FUELG_TRY(xb.alloc((size_t)npad * dp * 2, stream));
+  FUELG_TRY(qn2.alloc(sizeof(float) * mpad, stream));
+  FUELG_TRY(xn2.alloc(sizeof(float) * npad, stream));
+  FUELG_TRY(flags.alloc(sizeof(int) * 4, stream));
+  FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 4, stream));
+  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.as<__nv_bfloat16>(), qn2.as<float>(),
+                                               flags.as<int>()); ::fuelg::note_launch();
+  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, n, npad, d, dp, xb.as<__nv_bfloat16>(), xn2.as<float>(),
+                                               flags.as<int>() + 2); ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  int hf[4];
+  FUELG_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, stream));
+  FUELG_CUDA(cudaStreamSynchronize(stream));
+  float vmax;
+  {
+    int mx = std::max(hf[1], hf[3]);
+    memcpy(&vmax, &mx, sizeof(float));
+  }
+  const bool integer = hf[0] == 0 && hf[2] == 0;
+  const bool exact = integer && 2.0 * dp * (double)vmax * vmax < 16777216.0;
+  *exact_out = exact ? 1 : 0;
+  // screened keys kept per query: exact sqeuclidean needs none extra
+  const int margin = (exact && metric == METRIC_SQEUCLIDEAN) ? 0 : std::max(8, kk / 8);
+  const int kk2 = kk + margin;
+
+  CUtensorMap tmQ, tmX;
+  FUELG_TRY(make_map_bf16(&tmQ, qb.p, mpad, dp, QM));
+  FUELG_TRY(make_map_bf16(&tmX, xb.p, npad, dp, XN));
+  const size_t a_bytes = (size_t)kc * QM * BK * 2, b_bytes = (size_t)XN * BK * 2;
+  const size_t fixed = 1024 + a_bytes + 8 * 32 + 16 + (size_t)kCBk * kEpi * 8 + 2 * XN * sizeof(float);
+  int stages = (int)((220 * 1024 - fixed) / b_bytes);
+  stages = std::max(2, std::min(4, stages));
+  const size_t smem = fixed + stages * b_bytes;
+  if (smem > 227 * 1024) {
+    set_error("tensor-core kNN tile does not fit shared memory (d=%d)", d);
+    return ST_ENOTSUP;
+  }
+  // Bound scratch: batches of queries whose lists take at most ~1 GiB.
+  const size_t per_query = (size_t)kk2 * 8 * 3;  // two list halves + kept keys
+  int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
+  mb = std::min<int64_t>(mb, mpad);
+  Scratch lists, kept, kept2, redo, nredo;
+  FUELG_TRY(lists.alloc((size_t)mb * 2 * kk2 * 8, stream));
+  FUELG_TRY(kept.alloc((size_t)mb * kk2 * 8, stream));
+  if (margin) {
+    FUELG_TRY(kept2.alloc((size_t)mb * kk2 * 8, stream));
+    FUELG_TRY(redo.alloc(sizeof(int32_t) * mb, stream));
+    FUELG_TRY(nredo.alloc(sizeof(int32_t), stream));
+  }
+  auto kern = knn_tc_kernel;
+  FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // integer data aside, keep the error-bound constants of the Lloyd screen
+  const double u8 = std::ldexp(1.0, -8), u23 = std::ldexp(1.0, -23), u24 = std::ldexp(1.0, -24);
+  const double rel = (2 * u8 + u8 * u8) + dp * u23 * (1.0 + 2 * u8);
+  // exact integer data: the screen and fuel's own f32 sum are both exact
+  const float alpha = exact ? 0.0f : (float)(2.0 * rel * 1.01);
+  const float beta = exact ? 0.0f : (float)(((d + 31) / 32 + 9) * u24 * 1.01 + u24);
+  const float gamma = exact ? 0.0f : (float)((d + 4) * u24 * 1.01);
+  // max |x| and |x|^2 over the index, for the proof
+  float xmax_n2 = 0.0f;
+  {
+    std::vector<float> h((size_t)npad);
+    FUELG_CUDA(cudaMemcpyAsync(h.data(), xn2.p, sizeof(float) * npad, cudaMemcpyDeviceToHost, stream));
+    FUELG_CUDA(cudaStreamSynchronize(stream));
+    for (float v : h) xmax_n2 = std::max(xmax_n2, v);
+  }
+  const float xmax_norm = sqrtf(xmax_n2) * (1.0f + 1e-6f);
+  int64_t total_redo = 0;
+  HotTimer* ht = hot_timer();
+  for (int64_t b0 = 0; b0 < m; b0 += mb) {
+    const int64_t mcur = std::min<int64_t>(mb, m - b0);
+    KnnTcArgs a{};
+    a.m = mcur;
+    a.n = n;
+    a.kc = kc;
+    a.kk2 = kk2;
+    a.exact = exact ? 1 : 0;
+    a.stages = stages;
+    a.qn2 = qn2.as<float>() + b0;
+    a.xn2 = xn2.as<float>();
+    a.lists = lists.as<uint64_t>();
+    a.out_keys = kept.as<uint64_t>();
+    a.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(XN >> 3) << 17) | ((uint32_t)(QM >> 4) << 24);
+    a.status = dev_status;
+    a.cancel = cancel_word_device();
+    // the query map addresses rows b0.. through the y coordinate
+    CUtensorMap tmQb;
+    FUELG_TRY(make_map_bf16(&tmQb, qb.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
+    const unsigned grid = (unsigned)((mcur + QM - 1) / QM);
+    if (ht) ht->begin(stream);
+    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, tmX, a); ::fuelg::note_launch();
+    if (ht) ht->end(stream);
+    FUELG_CUDA(cudaGetLastError());
+    uint64_t* dst = out_keys + b0 * kk;
+    if (margin == 0) {
+      FUELG_CUDA(cudaMemcpyAsync(dst, kept.p, (size_t)mcur * kk * 8, cudaMemcpyDeviceToDevice, stream));
+      continue;
+    }
+    FUELG_CUDA(cudaMemsetAsync(nredo.p, 0, sizeof(int32_t), stream));
+    const size_t rsm = (size_t)8 * (d + 4) * sizeof(float);
+    const unsigned rg = (unsigned)((mcur * 32 + 255) / 256);
+    if (order == ORDER_X86)
+      knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2, metric,
+                                                              kept.as<uint64_t>(), kept2.as<uint64_t>(),
+                                                              qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
+                                                              gamma, redo.as<int32_t>(), nredo.as<int32_t>());
+    else
+      knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2, metric,
+                                                              kept.as<uint64_t>(), kept2.as<uint64_t>(),
+                                                              qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
+                                                              gamma, redo.as<int32_t>(), nredo.as<int32_t>());
+    ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+    // first kk exact keys of every query
+    FUELG_CUDA(cudaMemcpy2DAsync(dst, (size_t)kk * 8, kept2.p, (size_t)kk2 * 8, (size_t)kk * 8, (size_t)mcur,
+                                 cudaMemcpyDeviceToDevice, stream));
+    int h_redo = 0;
+    FUELG_CUDA(cudaMemcpyAsync(&h_redo, nredo.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+    FUELG_CUDA(cudaStreamSynchronize(stream));
+    if (h_redo > 0) {
+      // queries the proof could not certify: exact scan
+      Scratch qre, kre;
+      FUELG_TRY(qre.alloc(sizeof(float) * (size_t)h_redo * d, stream));
+      FUELG_TRY(kre.alloc(sizeof(uint64_t) * (size_t)h_redo * kk, stream));
+      gather_rows_kernel<<<4 * 152, 256, 0, stream>>>(Q32 + b0 * d, d, redo.as<int32_t>(), nredo.as<int32_t>(),
+                                                      qre.as<float>()); ::fuelg::note_launch();
+      ExactScanParams sp;
+      sp.A = qre.as<float>();
+      sp.m = h_redo;
+      sp.B = X32;
+      sp.n = n;
+      sp.d = d;
+      sp.kind = KIND_KNN;
+      sp.order = order;
+      sp.metric = metric;
+      sp.kk = kk;
+      FUELG_TRY(exact_topk(sp, kre.as<uint64_t>(), dev_status, stream));
+      scatter_keys_kernel<<<(unsigned)(((int64_t)h_redo * kk + 255) / 256), 256, 0, stream>>>(
+          kre.as<uint64_t>(), kk, kk, redo.as<int32_t>(), h_redo, dst); ::fuelg::note_launch();
+      FUELG_CUDA(cudaGetLastError());
+      total_redo += h_redo;
+    }
+  }
+  if (rescored) *rescored = margin ? m * (int64_t)kk2 + total_redo * n : 0;
+  return ST_OK;
+}
+
+}  // namespace fuelg

@@ -35,15 +35,16 @@
 
 #include "fuelg_common.cuh"
 #include "fuelg_internal.h"
+#include "fuelg_tc_common.cuh"
 
 namespace fuelg {
+
+using namespace tcx;
 
 namespace {
 
 constexpr int BM = 128;  // points per tile (UMMA M)
-constexpr int BK = 64;   // BF16 elements per K chunk = one 128-byte swizzle row
 constexpr int kTcThreads = 192;
-constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s: far beyond any legitimate wait
 
 struct TcArgs {
   int64_t n;
@@ -67,114 +68,6 @@ struct TcArgs {
   int* status;
   const volatile int* cancel;
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: false when the barrier did not complete within kWaitNs or the
-// CTA is aborting.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
-  if (mbar_try_wait(bar, parity)) return true;
-  const uint64_t t0 = globaltimer();
-  for (uint32_t it = 1;; ++it) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255) == 0) {
-      if (*abort_flag) return false;
-      if (globaltimer() - t0 > kWaitNs) return false;
-    }
-  }
-}
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
-      : "memory");
-}
-// Same load with an L2 cache-policy hint (streamed point tiles: evict-first;
-// the small centre tiles every CTA re-reads: evict-last).
-__device__ __forceinline__ void tma_load_2d_hint(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar,
-                                                 uint64_t policy) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1, {%2, "
-      "%3}], [%4], %5;" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
-      : "memory");
-}
-__device__ __forceinline__ uint64_t policy_evict_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t policy_evict_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ void prefetch_tmap(const CUtensorMap* tm) {
-  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tm)) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
-// groups 1024 bytes apart (SBO), descriptor version 1, base 1024-aligned.
-__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
-  uint64_t desc = 0;
-  desc |= (uint64_t)((saddr & 0x3FFFF) >> 4);
-  desc |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
-  desc |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
-  desc |= (uint64_t)1 << 46;             // version
-  desc |= (uint64_t)2 << 61;             // SWIZZLE_128B
-  return desc;
-}
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                          uint32_t accumulate) {
-  asm volatile(
-      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
-          d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate));
-}
-__device__ __forceinline__ void umma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
-}
 
 template <bool SPLIT>
 __global__ void __launch_bounds__(kTcThreads, 2)
@@ -705,40 +598,6 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
   }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-            cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
-  return fn;
-}
-
-int make_map(CUtensorMap* tm, const void* ptr, int64_t rows, int dp, int box_rows) {
-  auto fn = encode_fn();
-  if (!fn) {
-    set_error("cuTensorMapEncodeTiled is unavailable from the driver");
-    return ST_ECUDA;
-  }
-  cuuint64_t dims[2] = {(cuuint64_t)dp, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)dp * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(tm, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) {
-    set_error("cuTensorMapEncodeTiled failed (%d) for rows=%lld dp=%d box_rows=%d", (int)r, (long long)rows, dp,
-              box_rows);
-    return ST_ECUDA;
-  }
-  return ST_OK;
-}
-
 }  // namespace
 
 // Per-call state of the tensor-core Lloyd tier: the BF16 copy of X is made
@@ -818,11 +677,11 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   // A: tile-major [arows * kc, 64] -- each box is one contiguous 16 KB block
-  FUELG_TRY(make_map(&st->tmA, st->xhi.p, st->arows * st->kc, BK, BM));
-  FUELG_TRY(make_map(&st->tmB, st->chi.p, st->kp, st->dp, st->kp));
+  FUELG_TRY(tcx::make_map_bf16(&st->tmA, st->xhi.p, st->arows * st->kc, BK, BM));
+  FUELG_TRY(tcx::make_map_bf16(&st->tmB, st->chi.p, st->kp, st->dp, st->kp));
   if (st->split) {
-    FUELG_TRY(make_map(&st->tmAlo, st->xlo.p, st->arows * st->kc, BK, BM));
-    FUELG_TRY(make_map(&st->tmBlo, st->clo.p, st->kp, st->dp, st->kp));
+    FUELG_TRY(tcx::make_map_bf16(&st->tmAlo, st->xlo.p, st->arows * st->kc, BK, BM));
+    FUELG_TRY(tcx::make_map_bf16(&st->tmBlo, st->clo.p, st->kp, st->dp, st->kp));
   } else {
     st->tmAlo = st->tmA;
     st->tmBlo = st->tmB;

@@ -163,3 +163,52 @@ def test_cancel_from_another_thread(gpu):
     # the next call starts with a cleared cancel word and succeeds
     i, d = ix.knn(X[:10], 3, exclude_self=False)
     assert (i[:, 0] == np.arange(10)).all()
+
+
+# ---------------------------------------------------------------------------
+# Tensor-core tier (tcgen05 BF16 screen): same bar -- bit-exact vs the oracle.
+# Integer data below 2^24 takes the exact path (no re-score); other data is
+# re-scored in the reference order and proven; failures fall back to the scan.
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("d", [32, 64, 100, 128, 256])
+@pytest.mark.parametrize("order", ["arm", "x86"])
+@pytest.mark.parametrize("metric", ["sqeuclidean", "euclidean"])
+def test_knn_tc_general_data(gpu, oracle, d, order, metric):
+    rng = np.random.default_rng(d + 7)
+    X = rng.normal(size=(3000, d)).astype(np.float32)
+    Q = rng.normal(size=(300, d)).astype(np.float32)
+    for k in (1, 10, 64):
+        g = gpu_knn(X, Q, k, metric=metric, order=order, precision="bf16")
+        c = oracle.knn(X, Q, k, metric=metric, order=order, threads=threads())
+        assert_same(g, c)
+
+
+@pytest.mark.parametrize("mode", ["none", "linear", "kplus1"])
+@pytest.mark.parametrize("metric", ["sqeuclidean", "euclidean"])
+def test_knn_tc_integer_ties(gpu, oracle, mode, metric):
+    X = workloads.knn_geometric(n=4000, d=128)
+    for k in (1, 10, 100):
+        g = gpu_knn(X, X, k, metric=metric, mode=mode, precision="bf16")
+        c = oracle.knn(X, X, k, metric=metric, exclude=mode, threads=threads())
+        assert_same(g, c)
+
+
+def test_knn_tc_geometric_config_reduced(gpu, oracle):
+    """n=50,000 integer geometric rows (d=128), k=100, 2,000 query rows."""
+    X = workloads.knn_geometric(n=50_000)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="bf16")
+    g = ix.knn(X[:2000], 100, exclude_self=False)
+    assert ix.last_stats["precision_used"] == 1
+    c = oracle.knn(X, X[:2000], 100, threads=threads())
+    assert_same(g, c)
+
+
+def test_knn_tc_small_shapes(gpu, oracle):
+    rng = np.random.default_rng(5)
+    for n, m, d in ((1, 1, 32), (5, 3, 40), (257, 129, 33), (300, 1, 64)):
+        X = rng.normal(size=(n, d)).astype(np.float32)
+        Q = rng.normal(size=(m, d)).astype(np.float32)
+        for k in (1, 3, 8):
+            g = gpu_knn(X, Q, k, precision="bf16")
+            c = oracle.knn(X, Q, k)
+            assert_same(g, c)
