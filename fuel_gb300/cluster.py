@@ -114,3 +114,24 @@ def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, ini
     res = KMeansResult(centers, labels, int(iters.value), float(inertia.value), None)
     res.stats = st.as_dict()
     return res
+
+
+def lloyd_assign(data, centers, *, initial=False, order=None):
+    """One Lloyd assignment pass on the GPU: (labels int64[n], best float32[n]).
+
+    Nearest centre per point with fuel's arithmetic (``initial=True``: the
+    initial pass, src/cluster/kmeans/lloyd.rs:12-112; otherwise the
+    iteration loop's math::sqdist, lloyd.rs:140-158), first index on ties.
+    This is the local step of ``fuel_gb300.shard.sharded_lloyd``.
+    """
+    X = np.ascontiguousarray(data, np.float32)
+    C = np.ascontiguousarray(centers, np.float32)
+    if X.ndim != 2 or C.ndim != 2 or X.shape[1] != C.shape[1]:
+        raise ValueError("data [n, d] and centers [k, d] must share d")
+    n, d = X.shape
+    labels = np.empty(n, np.int64)
+    best = np.empty(n, np.float32)
+    _lib.check(_lib.load().fuelg_lloyd_assign(_lib.ptr(X), n, d, _lib.ptr(C), C.shape[0], int(bool(initial)),
+                                              _lib.ORDER[order or _lib.default_order()], _lib.ptr(labels),
+                                              _lib.ptr(best), None))
+    return labels, best

@@ -570,5 +570,70 @@ int fuelg_kmeans_lloyd(const float* data, int64_t n, int32_t d, int32_t k, const
   return ST_OK;
 }
 
+int fuelg_lloyd_assign(const float* data, int64_t n, int32_t d, const float* centers, int32_t k, int32_t initial,
+                       int32_t order, int64_t* out_labels, float* out_best, fuelg_stats* stats) {
+  if (n <= 0 || d <= 0 || k <= 0 || !data || !centers || !out_labels) {
+    set_error("invalid lloyd_assign arguments n=%lld d=%d k=%d", (long long)n, d, k);
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  FUELG_TRY(begin_call());
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaStream_t s;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  CallMeter meter;
+  Timer tm(s);
+  InBuf X, C;
+  FUELG_TRY(X.init(data, (size_t)n * d * sizeof(float), s));
+  FUELG_TRY(C.init(centers, (size_t)k * d * sizeof(float), s));
+  OutBuf ol, ob;
+  FUELG_TRY(ol.init(out_labels, (size_t)n * sizeof(int64_t), s));
+  Scratch best_tmp, keys, dstat;
+  float* best = nullptr;
+  if (out_best) {
+    FUELG_TRY(ob.init(out_best, (size_t)n * sizeof(float), s));
+    best = static_cast<float*>(ob.dptr);
+  } else {
+    FUELG_TRY(best_tmp.alloc(sizeof(float) * n, s));
+    best = best_tmp.as<float>();
+  }
+  FUELG_TRY(keys.alloc(sizeof(uint64_t) * n, s));
+  FUELG_TRY(dstat.alloc(sizeof(int), s));
+  FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
+  ExactScanParams p;
+  p.A = static_cast<const float*>(X.dptr);
+  p.m = n;
+  p.B = static_cast<const float*>(C.dptr);
+  p.n = k;
+  p.d = d;
+  p.kind = initial ? KIND_PAIRWISE : KIND_SQDIST;
+  p.order = order;
+  p.metric = METRIC_SQEUCLIDEAN;
+  p.kk = 1;
+  FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
+  FUELG_TRY(finalize_knn(keys.as<uint64_t>(), n, 1, 1, FUELG_EXCLUDE_NONE, static_cast<int64_t*>(ol.dptr), best, s));
+  int64_t d2h = 0;
+  FUELG_TRY(ol.flush(s, &d2h));
+  if (out_best) FUELG_TRY(ob.flush(s, &d2h));
+  const double ms = tm.stop();
+  FUELG_TRY(read_dev_status(dstat.as<int>(), s));
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = X.h2d + C.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = n * (int64_t)k;
+    stats->iterations = 1;
+    meter.fill(stats);
+  }
+  return ST_OK;
+}
+
 }  // extern "C"
 

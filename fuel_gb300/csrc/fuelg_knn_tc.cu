@@ -33,9 +33,11 @@ namespace {
 
 constexpr int QM = 128;        // queries per CTA (UMMA M)
 constexpr int XN = 256;        // index rows per tile (UMMA N)
-constexpr int kEpi = 128;      // epilogue threads
-constexpr int kThreadsKT = 192;
-constexpr int kCBk = 32;       // candidate buffer entries per epilogue thread
+constexpr int kEpiWarps = 8;   // epilogue warps: 4 TMEM lane quarters x 2 column halves
+constexpr int kEpi = 32 * kEpiWarps;
+constexpr int kThreadsKT = 64 + kEpi;
+constexpr int kHalfN = XN / 2;  // columns of a tile per epilogue warp
+constexpr int kApp = 256;      // appended candidates per query between compactions
 
 struct KnnTcArgs {
   int64_t m, n;
@@ -45,7 +47,8 @@ struct KnnTcArgs {
   int stages;
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
-  uint64_t* lists;   // [m][2*kk2]
+  float xmax_n2;     // max |x|^2 over the index (filter slack)
+  uint64_t* lists;   // [m][2][2*kk2 + kApp]: per column half, two sorted prefix halves + append log
   uint64_t* out_keys;  // [m][kk2]
   uint32_t idesc;
   int* status;
@@ -57,71 +60,80 @@ __device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
   const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
   return ((uint64_t)hi << 32) | lo;
 }
-__device__ __forceinline__ uint64_t shfl_xor64(uint64_t v, int m) {
-  const uint32_t lo = __shfl_xor_sync(0xffffffffu, (uint32_t)v, m);
-  const uint32_t hi = __shfl_xor_sync(0xffffffffu, (uint32_t)(v >> 32), m);
-  return ((uint64_t)hi << 32) | lo;
+
+// First index in sorted smem keys[0, len) whose key is >= x (= #keys < x).
+__device__ __forceinline__ int lower_bound_smem(const uint64_t* keys, int len, uint64_t x) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (keys[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
 }
 
-// Warp-cooperative merge of one query's buffered candidates (cnt <= 32
-// unsorted keys in shared memory at stride kEpi) into its sorted kk-list
-// cur[0..kk) -> nxt[0..kk).  The buffer is bitonic-sorted across the lanes;
-// every output slot is written exactly once: a list key L[i] lands at
-// i + #{buffer < L[i]}, a buffer key B[t] at t + #{list < B[t]} (keys are
-// unique: the index is in the low half), and slots >= kk are dropped.
-// Returns the new kk-th key on every lane.
-__device__ __noinline__ uint64_t warp_merge(const uint64_t* __restrict__ sbuf, int cnt,
-                                            const uint64_t* __restrict__ cur, uint64_t* __restrict__ nxt, int kk,
-                                            int lane) {
-  uint64_t b = lane < cnt ? sbuf[lane * kEpi] : KEY_NONE;
-#pragma unroll
-  for (int k2 = 2; k2 <= 32; k2 <<= 1) {
-#pragma unroll
+// Warp-cooperative compaction of one query's candidates: the na (<= kApp)
+// unsorted keys of its append log are bitonic-sorted in shared memory
+// (padded to a power of two >= 32) and merged with its sorted prefix of plen
+// keys; the kk smallest go to the other prefix half.  Output slots: a prefix
+// key P[i] lands at i + #{appended < P[i]}, an appended key A[e] at
+// e + #{prefix < A[e]} (keys are unique: the index is in the low half), so
+// every slot below min(kk, plen + na) is written once.  stage: this warp's
+// shared-memory staging area of kApp + kk keys.  The code is loops, not
+// unrolled networks, so it stays small in the instruction cache.  Returns the
+// new kk-th key (KEY_NONE while fewer than kk are held) on every lane.
+__device__ __noinline__ uint64_t warp_compact(const uint64_t* __restrict__ app, int na,
+                                              const uint64_t* __restrict__ cur, int plen, uint64_t* __restrict__ nxt,
+                                              int kk, uint64_t* __restrict__ stage, int lane) {
+  int P = 32;
+  while (P < na) P <<= 1;
+  uint64_t* sp = stage + kApp;
+#pragma unroll 4
+  for (int e = lane; e < P; e += 32) stage[e] = e < na ? app[e] : KEY_NONE;
+#pragma unroll 4
+  for (int i = lane; i < plen; i += 32) sp[i] = cur[i];
+  __syncwarp();
+  for (int k2 = 2; k2 <= P; k2 <<= 1) {
     for (int j = k2 >> 1; j > 0; j >>= 1) {
-      const uint64_t o = shfl_xor64(b, j);
-      const bool up = (lane & k2) == 0 || k2 == 32;
-      const bool lower = (lane & j) == 0;
-      b = (lower == up) ? (o < b ? o : b) : (o > b ? o : b);
+      for (int q = lane; q < (P >> 1); q += 32) {
+        const int e = ((q & ~(j - 1)) << 1) | (q & (j - 1));  // q with a 0 inserted at bit log2(j)
+        const uint64_t x = stage[e], y = stage[e | j];
+        const bool up = (e & k2) == 0;
+        if (up ? (x > y) : (x < y)) {
+          stage[e] = y;
+          stage[e | j] = x;
+        }
+      }
+      __syncwarp();
     }
   }
   uint64_t tv = KEY_NONE;
   int has = 0;
-  if (b != KEY_NONE) {
-    int lo = 0, hi = kk;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (cur[mid] < b) lo = mid + 1;
-      else hi = mid;
-    }
-    const int slot = lane + lo;
-    if (slot < kk) {
-      nxt[slot] = b;
-      if (slot == kk - 1) {
-        tv = b;
+  for (int e = lane; e < na; e += 32) {
+    const uint64_t x = stage[e];
+    const int pos = e + lower_bound_smem(sp, plen, x);
+    if (pos < kk) {
+      nxt[pos] = x;
+      if (pos == kk - 1) {
+        tv = x;
         has = 1;
       }
     }
   }
-#pragma unroll 2
-  for (int i0 = 0; i0 < kk; i0 += 32) {
-    const int i = i0 + lane;
-    const uint64_t v = i < kk ? cur[i] : KEY_NONE;
-    int pos = 0;
-#pragma unroll
-    for (int st = 16; st >= 1; st >>= 1)
-      if (shfl64(b, pos + st - 1) < v) pos += st;
-    if (shfl64(b, pos) < v) pos++;
-    const int slot = i + pos;
-    if (i < kk && slot < kk) {
-      nxt[slot] = v;
-      if (slot == kk - 1) {
-        tv = v;
+  for (int i = lane; i < plen; i += 32) {
+    const uint64_t x = sp[i];
+    const int pos = i + lower_bound_smem(stage, na, x);
+    if (pos < kk) {
+      nxt[pos] = x;
+      if (pos == kk - 1) {
+        tv = x;
         has = 1;
       }
     }
   }
   const unsigned bm = __ballot_sync(0xffffffffu, has);
-  return shfl64(tv, __ffs(bm) - 1);
+  __syncwarp();
+  return bm ? shfl64(tv, __ffs(bm) - 1) : KEY_NONE;
 }
 
 __global__ void __launch_bounds__(kThreadsKT, 1)
@@ -141,8 +153,11 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
   uint64_t* fin = afull + 1;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
-  uint64_t* cbuf = reinterpret_cast<uint64_t*>(tmem_holder + 4);  // [kCBk][kEpi]
-  float* xnsm = reinterpret_cast<float*>(cbuf + (size_t)kCBk * kEpi);  // [2][XN] index norms
+  float* xnsm = reinterpret_cast<float*>(tmem_holder + 4);  // [kEpiWarps][2][kHalfN] index norms
+  uint64_t* tau_sh = reinterpret_cast<uint64_t*>(xnsm + kEpiWarps * 2 * kHalfN);  // [2][QM] running k-th keys
+  int* fin_sh = reinterpret_cast<int*>(tau_sh + 2 * QM);  // [QM][2] final (half, plen) of column half 1
+  uint32_t* scratch_all = reinterpret_cast<uint32_t*>(fin_sh + 2 * QM);  // [kEpi][16] slow-path dots
+  uint64_t* stage_all = reinterpret_cast<uint64_t*>(scratch_all + kEpi * 16);  // [kEpiWarps][kApp + kk2] staging
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = (int64_t)blockIdx.x * QM;
@@ -162,6 +177,7 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
+  if (threadIdx.x < 2 * QM) tau_sh[threadIdx.x] = KEY_NONE;
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
                  "r"(512)
@@ -255,98 +271,176 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
       if (!mbar_wait(fin, 0, &never)) atomicOr(a.status, DEV_TIMEOUT);
     }
   } else {
+    // Epilogue: warp w handles query rows 32*(w%4).. (its TMEM lane quarter)
+    // and column half hc of every tile; each (query, half) keeps its own
+    // sorted top-kk2 prefix + append log, and filters with the smaller of its
+    // own and the other half's running kk2-th key (a key at or above either
+    // cannot be among the query's kk2 smallest).
     const int g = warp & 3;
+    const int hc = (warp - 2) >> 2;
+    const int ew = warp - 2;
     const int row = g * 32 + lane;  // TMEM lane = query row of the tile
-    const int et = threadIdx.x - 64;  // epilogue thread id 0..127
     const int64_t qi = q0 + row;
     const bool valid = qi < a.m;
     const float nq = valid ? a.qn2[qi] : 0.0f;
-    uint64_t* list = a.lists + (valid ? qi : 0) * 2ull * a.kk2;
-    if (valid)
-      for (int o = 0; o < a.kk2; o++) list[o] = KEY_NONE;
-    uint64_t* buf = cbuf + et;
-    uint64_t tau = KEY_NONE;
+    const size_t hstride = 2ull * a.kk2 + kApp;
+    const size_t qstride = 2 * hstride;
+    uint64_t* mine = a.lists + (valid ? qi : 0) * qstride + hc * hstride;
+    uint64_t* app = mine + 2ull * a.kk2;  // this (query, half)'s append log
+    uint64_t* stage = stage_all + (size_t)ew * (kApp + a.kk2);
+    uint32_t* scr = scratch_all + (threadIdx.x - 64) * 16;
+    float* nsm_w = xnsm + ew * 2 * kHalfN;
+    volatile uint64_t* tau_other = tau_sh + (hc ^ 1) * QM + row;
+    volatile uint64_t* tau_mine = tau_sh + hc * QM + row;
+    uint64_t tau = KEY_NONE;   // own kk2-th key
+    uint64_t tflt = KEY_NONE;  // filter key: min(own, other half's)
     float tau_d = __int_as_float(0x7f800000);
-    int cnt = 0, half = 0;
-    // Lanes whose buffer passed `lim` entries merge, one query at a time, with
-    // the whole warp.
+    int na = 0, half = 0, plen = 0;
+    auto set_filter = [&](uint64_t other) {
+      tflt = other < tau ? other : tau;
+      tau_d = tflt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(tflt);
+    };
+    // Screen filter in the shifted domain: a column can enter only if
+    // |x|^2 - 2 q.x <= tau - |q|^2 (+ slack covering the rounding of both
+    // forms when the data are not exact integers); the exact screened value
+    // is formed only for the rare columns that pass.
+    auto threshold = [&]() -> float {
+      if (!valid) return -__int_as_float(0x7f800000);
+      if (tflt == KEY_NONE) return __int_as_float(0x7f800000);
+      const float th = tau_d - nq;
+      return a.exact ? th : th + (nq + a.xmax_n2 + tau_d) * 3.814697265625e-06f;  // 2^-18
+    };
+    // Lanes whose append log passed `lim` entries compact, one query at a
+    // time, with the whole warp.
     auto flush = [&](int lim) {
-      unsigned need = __ballot_sync(0xffffffffu, cnt > lim);
+      unsigned need = __ballot_sync(0xffffffffu, na > lim);
       if (!need) return;
       __syncwarp();
       while (need) {
         const int src = __ffs(need) - 1;
         need &= need - 1;
-        const int scnt = __shfl_sync(0xffffffffu, cnt, src);
+        const int sna = __shfl_sync(0xffffffffu, na, src);
         const int shalf = __shfl_sync(0xffffffffu, half, src);
-        uint64_t* lb = a.lists + (q0 + g * 32 + src) * 2ull * a.kk2;
-        const uint64_t nt = warp_merge(cbuf + (et - lane + src), scnt, lb + (size_t)shalf * a.kk2,
-                                       lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
+        const int splen = __shfl_sync(0xffffffffu, plen, src);
+        uint64_t* lb = a.lists + (q0 + g * 32 + src) * qstride + hc * hstride;
+        const uint64_t nt = warp_compact(lb + 2ull * a.kk2, sna, lb + (size_t)shalf * a.kk2, splen,
+                                         lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, stage, lane);
         if (lane == src) {
           tau = nt;
-          tau_d = nt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(nt);
           half ^= 1;
-          cnt = 0;
+          plen = min(a.kk2, plen + na);
+          na = 0;
+          *tau_mine = tau;
         }
-        __syncwarp();
       }
     };
+    float thr = threshold();
+    // norms of this warp's 128 columns: 4 per lane, fetched one tile ahead
+    float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + hc * kHalfN) + lane);
     for (int64_t t = 0; t < ntiles; t++) {
       const uint32_t b = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
-      const int64_t p0 = t * XN;
-      // this tile's index norms into shared memory (double-buffered by tile parity)
-      float* nsm = xnsm + b * XN;
-      nsm[et] = __ldg(a.xn2 + p0 + et);
-      nsm[et + kEpi] = __ldg(a.xn2 + p0 + et + kEpi);
-      // the wait outcome is combined over the 128 epilogue threads (which also
-      // publishes the norms), so all of them leave the loop on the same tile
+      const int64_t p0 = t * XN + hc * kHalfN;
+      float* nsm = nsm_w + b * kHalfN;
+      reinterpret_cast<float4*>(nsm)[lane] = pn;
+      if (t + 1 < ntiles) pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + p0 + XN) + lane);
+      // the other half's progress tightens the filter
+      {
+        const uint64_t o = *tau_other;
+        if (o < tflt) {
+          set_filter(o);
+          thr = threshold();
+        }
+      }
       bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag);
       if (!ok) {
         if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
         *abort_flag = 1;
       }
-      if (named_bar_or(1, kEpi, !ok)) break;
+      if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
+      __syncwarp();
       tc_fence_after();
-      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN;
-      const bool live = valid && p0 < a.n;
-      for (int c0 = 0; c0 < XN; c0 += 64) {
+      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN + hc * kHalfN;
+#pragma unroll 1
+      for (int c0 = 0; c0 < kHalfN; c0 += 64) {
         uint32_t r[4][16];
 #pragma unroll
         for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
         tmem_ld_wait();
 #pragma unroll
         for (int h = 0; h < 4; h++) {
-          if (live) {
+          const float4* n4 = reinterpret_cast<const float4*>(nsm + c0 + 16 * h);
+          float f[16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
+          for (int v = 0; v < 4; v++) {
+            const float4 q4 = n4[v];
+            f[4 * v] = fmaf(-2.0f, __uint_as_float(r[h][4 * v]), q4.x);
+            f[4 * v + 1] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 1]), q4.y);
+            f[4 * v + 2] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z);
+            f[4 * v + 3] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w);
+          }
+          float mn = f[0];
+#pragma unroll
+          for (int j = 1; j < 16; j++) mn = fminf(mn, f[j]);
+          if (mn <= thr) {
+            // the few passing columns: through shared memory, one loop trip each
+            uint4* s4 = reinterpret_cast<uint4*>(scr);
+#pragma unroll
+            for (int v = 0; v < 4; v++) s4[v] = make_uint4(r[h][4 * v], r[h][4 * v + 1], r[h][4 * v + 2], r[h][4 * v + 3]);
+            unsigned mask = 0;
+#pragma unroll
+            for (int j = 0; j < 16; j++) mask |= (f[j] <= thr ? 1u : 0u) << j;
+            while (mask) {
+              const int j = __ffs(mask) - 1;
+              mask &= mask - 1;
               const int c = c0 + 16 * h + j;
               const int64_t p = p0 + c;
-              float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nq + nsm[c]);
+              float dt = fmaf(-2.0f, __uint_as_float(scr[j]), nq + nsm[c]);
               if (!a.exact) dt = fmaxf(dt, 0.0f);
               if (dt <= tau_d && p < a.n) {
                 const uint64_t key = make_key(dt, (uint32_t)p);
-                if (key < tau) {
-                  buf[cnt * kEpi] = key;
-                  cnt++;
-                }
+                if (key < tflt) app[na++] = key;
               }
             }
           }
-          flush(kCBk - 16);
+          if (__any_sync(0xffffffffu, na > kApp - 16)) {
+            flush(kApp - 16);
+            set_filter(*tau_other);
+            thr = threshold();
+          }
         }
       }
       tc_fence_before();
       mbar_arrive(&acce[b]);
     }
     flush(0);
-    // results out, one query at a time per warp (coalesced)
-    for (int src = 0; src < 32; src++) {
-      const int64_t qs = q0 + g * 32 + src;
-      if (qs >= a.m) break;
-      const int shalf = __shfl_sync(0xffffffffu, half, src);
-      const uint64_t* from = a.lists + qs * 2ull * a.kk2 + (size_t)shalf * a.kk2;
-      uint64_t* to = a.out_keys + qs * a.kk2;
-      for (int o = lane; o < a.kk2; o += 32) to[o] = from[o];
+    // column half 1 publishes its final (prefix half, length); half 0 merges
+    // it into its own prefix, 256 keys per compaction, and writes the result
+    if (hc == 1) {
+      fin_sh[2 * row] = half;
+      fin_sh[2 * row + 1] = plen;
+    }
+    asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
+    if (hc == 0) {
+      for (int src = 0; src < 32; src++) {
+        const int64_t qs = q0 + g * 32 + src;
+        if (qs >= a.m) break;
+        const int orow = g * 32 + src;
+        const int ohalf = fin_sh[2 * orow], oplen = fin_sh[2 * orow + 1];
+        const uint64_t* other = a.lists + qs * qstride + hstride + (size_t)ohalf * a.kk2;
+        uint64_t* lb = a.lists + qs * qstride;
+        int shalf = __shfl_sync(0xffffffffu, half, src);
+        int splen = __shfl_sync(0xffffffffu, plen, src);
+        for (int o0 = 0; o0 < oplen; o0 += kApp) {
+          const int cnt = min(kApp, oplen - o0);
+          warp_compact(other + o0, cnt, lb + (size_t)shalf * a.kk2, splen, lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2,
+                       stage, lane);
+          shalf ^= 1;
+          splen = min(a.kk2, splen + cnt);
+        }
+        const uint64_t* from = lb + (size_t)shalf * a.kk2;
+        uint64_t* to = a.out_keys + qs * a.kk2;
+        for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
+      }
     }
   }
   tc_fence_before();
@@ -487,7 +581,22 @@ __global__ void scatter_keys_kernel(const uint64_t* __restrict__ src, int kk, in
 
 }  // namespace
 
-bool knn_tc_supported(int d, int kk) { return d >= 32 && d <= 256 && kk <= 1024; }
+namespace {
+// Shared memory of knn_tc_kernel without the B stages.
+size_t knn_tc_fixed_smem(int d, int kk2) {
+  const int dp = ((d + BK - 1) / BK) * BK;
+  const size_t a_bytes = (size_t)(dp / BK) * QM * BK * 2;
+  return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * kHalfN * sizeof(float) + 2 * QM * 8 +
+         2 * QM * sizeof(int) + (size_t)kEpi * 16 * 4 + (size_t)kEpiWarps * (kApp + kk2) * 8;
+}
+int knn_tc_margin(int kk, bool exact_sq) { return exact_sq ? 0 : std::max(8, kk / 8); }
+}  // namespace
+
+bool knn_tc_supported(int d, int kk) {
+  if (d < 32 || d > 256 || kk < 1 || kk > 1024) return false;
+  // two B stages must fit beside the resident query tile and staging
+  return knn_tc_fixed_smem(d, kk + knn_tc_margin(kk, false)) + 2 * (size_t)XN * BK * 2 <= 227 * 1024;
+}
 
 // Top-kk keys of every query via the tensor-core screen.  out_keys: [m, kk]
 // (device).  X32/Q32: the f32 rows (for the exact re-score).
@@ -521,14 +630,14 @@ int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d,
   const bool exact = integer && 2.0 * dp * (double)vmax * vmax < 16777216.0;
   *exact_out = exact ? 1 : 0;
   // screened keys kept per query: exact sqeuclidean needs none extra
-  const int margin = (exact && metric == METRIC_SQEUCLIDEAN) ? 0 : std::max(8, kk / 8);
+  const int margin = knn_tc_margin(kk, exact && metric == METRIC_SQEUCLIDEAN);
   const int kk2 = kk + margin;
 
   CUtensorMap tmQ, tmX;
   FUELG_TRY(make_map_bf16(&tmQ, qb.p, mpad, dp, QM));
   FUELG_TRY(make_map_bf16(&tmX, xb.p, npad, dp, XN));
-  const size_t a_bytes = (size_t)kc * QM * BK * 2, b_bytes = (size_t)XN * BK * 2;
-  const size_t fixed = 1024 + a_bytes + 8 * 32 + 16 + (size_t)kCBk * kEpi * 8 + 2 * XN * sizeof(float);
+  const size_t b_bytes = (size_t)XN * BK * 2;
+  const size_t fixed = knn_tc_fixed_smem(d, kk2);
   int stages = (int)((220 * 1024 - fixed) / b_bytes);
   stages = std::max(2, std::min(4, stages));
   const size_t smem = fixed + stages * b_bytes;
@@ -537,11 +646,11 @@ int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d,
     return ST_ENOTSUP;
   }
   // Bound scratch: batches of queries whose lists take at most ~1 GiB.
-  const size_t per_query = (size_t)kk2 * 8 * 3;  // two list halves + kept keys
+  const size_t per_query = ((size_t)kk2 * 5 + 2 * kApp) * 8;  // 2 x (two prefix halves + log) + kept keys
   int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
   mb = std::min<int64_t>(mb, mpad);
   Scratch lists, kept, kept2, redo, nredo;
-  FUELG_TRY(lists.alloc((size_t)mb * 2 * kk2 * 8, stream));
+  FUELG_TRY(lists.alloc((size_t)mb * 2 * (2 * kk2 + kApp) * 8, stream));
   FUELG_TRY(kept.alloc((size_t)mb * kk2 * 8, stream));
   if (margin) {
     FUELG_TRY(kept2.alloc((size_t)mb * kk2 * 8, stream));
@@ -579,6 +688,7 @@ int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d,
     a.stages = stages;
     a.qn2 = qn2.as<float>() + b0;
     a.xn2 = xn2.as<float>();
+    a.xmax_n2 = xmax_n2;
     a.lists = lists.as<uint64_t>();
     a.out_keys = kept.as<uint64_t>();
     a.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(XN >> 3) << 17) | ((uint32_t)(QM >> 4) << 24);

@@ -112,13 +112,26 @@ int fuelg_range_free(fuelg_range_result *res);
 /* Lloyd k-means with fixed initial centres.  Replaces lloyd_f32
  * (python/kmeans.rs:188-218, 355) -> cluster::kmeans::lloyd
  * (src/cluster/kmeans/lloyd.rs:118-202) with InitMethod::Fixed
- * (python/kmeans.rs:111-130).  Centre sums/means are formed in FP64 and
- * inertia is the FP64 sum of squared distances of the final pass.
+ * (python/kmeans.rs:111-130).  Centre sums are exact integer sums (every
+ * f32 coordinate is an integer multiple of a common power of two; FP64 sums
+ * when the exponent range is too wide), means are rounded to nearest f32,
+ * and inertia is the FP64 sum of squared distances of the final pass.
  * out_centers [k, d] f32, out_labels [n] int64. */
 int fuelg_kmeans_lloyd(const float *data, int64_t n, int32_t d, int32_t k, const float *init_centers,
                        int32_t max_iter, double tol, int32_t precision, int32_t order, int32_t flags,
                        float *out_centers, int64_t *out_labels, int32_t *out_iters, double *out_inertia,
                        fuelg_stats *stats);
+
+/* One Lloyd assignment pass against fixed centres: for every point the
+ * nearest centre, the first index winning ties (strict < over centres in
+ * order).  initial != 0 uses the initial pass's arithmetic
+ * (lloyd_initial_assignment, src/cluster/kmeans/lloyd.rs:12-112, through
+ * vec_pairwise_sqdist), initial == 0 that of the iteration loop
+ * (lloyd.rs:140-158, math::sqdist).  It is the per-shard compute of a
+ * sharded Lloyd (points split across devices, exact sums all-reduced).
+ * out_labels [n] int64; out_best [n] f32 squared distance (may be NULL). */
+int fuelg_lloyd_assign(const float *data, int64_t n, int32_t d, const float *centers, int32_t k, int32_t initial,
+                       int32_t order, int64_t *out_labels, float *out_best, fuelg_stats *stats);
 
 /* Allocation-free exact kNN.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory -- code recording a CUDA graph

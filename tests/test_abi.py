@@ -72,5 +72,6 @@ def test_argument_validation_before_any_device_work(lib):
     assert lib.fuelg_index_create(None, 0, 3, 7, 0, ctypes.byref(h)) == _lib.EINVAL
     assert lib.fuelg_knn(None, None, 0, 1, 0, 0, None, None, None) == _lib.EINVAL
     assert lib.fuelg_kmeans_lloyd(None, 0, 1, 1, None, 1, 0.0, 0, 0, 0, None, None, None, None, None) == _lib.EINVAL
+    assert lib.fuelg_lloyd_assign(None, 0, 1, None, 1, 0, 0, None, None, None) == _lib.EINVAL
     assert lib.fuelg_range_free(None) == _lib.OK
     assert lib.fuelg_index_destroy(None) == _lib.OK

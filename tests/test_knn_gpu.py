@@ -212,3 +212,19 @@ def test_knn_tc_small_shapes(gpu, oracle):
             g = gpu_knn(X, Q, k, precision="bf16")
             c = oracle.knn(X, Q, k)
             assert_same(g, c)
+
+
+@pytest.mark.parametrize("k", [255, 256, 257, 600, 1024])
+def test_knn_tc_large_k(gpu, oracle, k):
+    """k around and above the 256-entry append log, up to the tensor-core
+    tier's limit: many compactions whose prefix exceeds the log."""
+    rng = np.random.default_rng(k)
+    X = rng.normal(size=(6000, 48)).astype(np.float32)
+    Q = rng.normal(size=(150, 48)).astype(np.float32)
+    g = gpu_knn(X, Q, k, precision="bf16")
+    c = oracle.knn(X, Q, k, threads=threads())
+    assert_same(g, c)
+    Xi = workloads.knn_geometric(n=3000, d=64)
+    g = gpu_knn(Xi, Xi, k, mode="linear", precision="bf16")
+    c = oracle.knn(Xi, Xi, k, exclude="linear", threads=threads())
+    assert_same(g, c)

@@ -156,3 +156,38 @@ def test_tc_tier_small_d_falls_back_to_exact(gpu):
     X = mixture(500, 8, 4, 1)
     r = kmeans(X, k=4, variant="lloyd", init="first", precision="bf16")
     assert r.stats["precision_used"] == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("initial", [True, False])
+@pytest.mark.parametrize("n,d,k", [(1000, 3, 7), (3000, 40, 17), (513, 784, 64)])
+def test_lloyd_assign_entry_point(oracle, gpu, initial, n, d, k):
+    """fuelg_lloyd_assign: labels bit-exact and best distances bit-exact vs the
+    oracle's assignment pass, in both the initial and the loop arithmetic."""
+    from fuel_gb300 import lloyd_assign
+    rng = np.random.default_rng(n + d + k)
+    X = rng.normal(size=(n, d)).astype(np.float32)
+    C = X[rng.choice(n, k, replace=False)].copy()
+    C[1] = C[0]  # duplicate centre: the first index must win
+    for order in ("arm", "x86"):
+        lab, best = lloyd_assign(X, C, initial=initial, order=order)
+        rl, rb = oracle.lloyd_assign(X, C, initial=initial, order=order)
+        np.testing.assert_array_equal(lab, rl)
+        np.testing.assert_array_equal(best.view(np.uint32), np.asarray(rb, np.float32).view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_sharded_lloyd_with_engine_assign(oracle, gpu):
+    """The sharded exchange driven by the GPU assignment reproduces the exact
+    single-process Lloyd bit for bit (one process, world size 1)."""
+    from fuel_gb300 import lloyd_assign, shard
+    rng = np.random.default_rng(4)
+    X = (rng.normal(size=(4000, 33)) + rng.integers(0, 4, size=(4000, 1)) * 3).astype(np.float32)
+    init = X[rng.choice(4000, 9, replace=False)].copy()
+    assign = lambda A, C, initial: lloyd_assign(A, C, initial=initial)[0]  # noqa: E731
+    C, lab, it, _, inert = shard.sharded_lloyd(X, 9, init, assign, max_iter=20)
+    rc, rl, rit, rinert = oracle.lloyd_exact(X, 9, init, max_iter=20)
+    np.testing.assert_array_equal(C.view(np.uint32), rc.view(np.uint32))
+    np.testing.assert_array_equal(lab, rl)
+    assert it == rit
+    assert abs(inert - rinert) <= 1e-9 * abs(rinert)
