@@ -76,6 +76,7 @@ struct fuelg_index {
   int32_t metric = 0;
   int32_t order = 0;
   float* X = nullptr;  // device copy [n, d]
+  TcIndex* tc = nullptr;  // tensor-core form, built on the first tensor-core call
   cudaStream_t stream = nullptr;
   std::mutex mu;  // calls on one handle are serialised
 };
@@ -306,6 +307,9 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
 
 int fuelg_index_destroy(fuelg_index* ix) {
   if (!ix) return ST_OK;
+  cudaSetDevice(ix->device);
+  if (ix->stream) cudaStreamSynchronize(ix->stream);
+  knn_tc_index_free(ix->tc);
   if (ix->X) cudaFree(ix->X);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;
@@ -378,8 +382,9 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   int64_t rescored = 0;
   if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk) && ix->n > 0) {
     int exact = 0;
-    FUELG_TRY(knn_tc_topk(p.A, m, ix->X, ix->n, ix->d, kk, ix->order, ix->metric, keys.as<uint64_t>(),
-                          dstat.as<int>(), s, &rescored, &exact));
+    if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
+    FUELG_TRY(knn_tc_topk(ix->tc, p.A, m, ix->X, kk, ix->order, ix->metric, keys.as<uint64_t>(), dstat.as<int>(), s,
+                          &rescored, &exact));
     used = FUELG_PREC_BF16;
   } else {
     FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));

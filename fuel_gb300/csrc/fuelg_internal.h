@@ -165,7 +165,12 @@ int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int6
 // Tensor-core kNN (fuelg_knn_tc.cu): top-kk keys per query [m, kk] via a BF16
 // tcgen05 screen; exact for integer data, otherwise re-scored and proven.
 bool knn_tc_supported(int d, int kk);
-int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d, int kk, int order, int metric,
+// Resident tensor-core form of an index: BF16 copy padded to whole tiles, FP32
+// norms, integer census and the index-side bounds; built once per handle.
+struct TcIndex;
+int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, TcIndex** out);
+void knn_tc_index_free(TcIndex* t);
+int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
                 uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out);
 
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.

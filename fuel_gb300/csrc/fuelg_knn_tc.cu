@@ -48,92 +48,156 @@ struct KnnTcArgs {
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
   float xmax_n2;     // max |x|^2 over the index (filter slack)
-  uint64_t* lists;   // [m][2][2*kk2 + kApp]: per column half, two sorted prefix halves + append log
+  uint64_t* lists;   // [m][2][2*kk2 + kApp]: per column half, two kept-key buffers + append log
   uint64_t* out_keys;  // [m][kk2]
   uint32_t idesc;
   int* status;
   const volatile int* cancel;
 };
 
-__device__ __forceinline__ uint64_t shfl64(uint64_t v, int src) {
-  const uint32_t lo = __shfl_sync(0xffffffffu, (uint32_t)v, src);
-  const uint32_t hi = __shfl_sync(0xffffffffu, (uint32_t)(v >> 32), src);
-  return ((uint64_t)hi << 32) | lo;
+
+constexpr int kSel = 8;  // keys per lane in a selection (appended or prefix): 256 per warp
+
+// Number of held keys below t over the warp.
+__device__ __forceinline__ int warp_count_hi_below(const uint32_t (&hi)[2 * kSel], uint32_t t) {
+  int c = 0;
+#pragma unroll
+  for (int i = 0; i < 2 * kSel; i++) c += hi[i] < t ? 1 : 0;
+  return __reduce_add_sync(0xffffffffu, c);
 }
 
-// First index in sorted smem keys[0, len) whose key is >= x (= #keys < x).
-__device__ __forceinline__ int lower_bound_smem(const uint64_t* keys, int len, uint64_t x) {
-  int lo = 0, hi = len;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (keys[mid] < x) lo = mid + 1;
-    else hi = mid;
+// Warp-cooperative selection for one (query, column half): the union of its
+// na (<= 256) appended keys and its plen (<= kk <= 256) kept keys is reduced
+// to its kk smallest, written unsorted to nxt[0, min(kk, na + plen)).  The
+// kk-th smallest key is found by a bitwise binary search over the
+// distance word (32 steps, counting with a warp reduction) and, only when
+// several keys share that distance, over the index word; keys are unique.
+// No shared memory, no sort.  Returns the kk-th smallest key, or KEY_NONE
+// while fewer than kk are held, on every lane.
+__device__ __noinline__ uint64_t warp_select(const uint64_t* __restrict__ app, int na,
+                                             const uint64_t* __restrict__ cur, int plen, uint64_t* __restrict__ nxt,
+                                             int kk, int lane) {
+  uint64_t key[2 * kSel];
+#pragma unroll
+  for (int i = 0; i < kSel; i++) {
+    const int e = lane + 32 * i;
+    key[i] = e < na ? app[e] : KEY_NONE;
+    key[kSel + i] = e < plen ? cur[e] : KEY_NONE;
   }
-  return lo;
+  uint32_t hi[2 * kSel];
+#pragma unroll
+  for (int i = 0; i < 2 * kSel; i++) hi[i] = (uint32_t)(key[i] >> 32);
+  const int total = na + plen;
+  uint64_t kth = KEY_NONE;
+  uint32_t H = 0xffffffffu, Lo = 0xffffffffu;  // keep keys <= (H, Lo)
+  if (total >= kk) {
+    H = 0;
+    for (int b = 31; b >= 0; b--) {
+      const uint32_t t = H | (1u << b);
+      if (warp_count_hi_below(hi, t) < kk) H = t;
+    }
+    // keys below H: fewer than kk; keys with hi == H: the rest is taken from them
+    const int below = warp_count_hi_below(hi, H);
+    int eq = 0;
+    uint32_t lo_max = 0;
+#pragma unroll
+    for (int i = 0; i < 2 * kSel; i++)
+      if (hi[i] == H) {
+        eq++;
+        lo_max = max(lo_max, (uint32_t)key[i]);
+      }
+    eq = __reduce_add_sync(0xffffffffu, eq);
+    const int need = kk - below;
+    if (eq == need) {
+      Lo = __reduce_max_sync(0xffffffffu, lo_max);
+    } else {
+      Lo = 0;
+      for (int b = 31; b >= 0; b--) {
+        const uint32_t t = Lo | (1u << b);
+        int c = 0;
+#pragma unroll
+        for (int i = 0; i < 2 * kSel; i++) c += (hi[i] == H && (uint32_t)key[i] < t) ? 1 : 0;
+        if (__reduce_add_sync(0xffffffffu, c) < need) Lo = t;
+      }
+    }
+    kth = ((uint64_t)H << 32) | Lo;
+  }
+  // compact the kept keys: lane offsets by a warp scan of per-lane counts
+  int mine = 0;
+#pragma unroll
+  for (int i = 0; i < 2 * kSel; i++) mine += (key[i] != KEY_NONE && key[i] <= kth) ? 1 : 0;
+  int incl = mine;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  int pos = incl - mine;
+#pragma unroll
+  for (int i = 0; i < 2 * kSel; i++)
+    if (key[i] != KEY_NONE && key[i] <= kth) nxt[pos++] = key[i];
+  __syncwarp();
+  return total >= kk ? kth : KEY_NONE;
 }
 
-// Warp-cooperative compaction of one query's candidates: the na (<= kApp)
-// unsorted keys of its append log are bitonic-sorted in shared memory
-// (padded to a power of two >= 32) and merged with its sorted prefix of plen
-// keys; the kk smallest go to the other prefix half.  Output slots: a prefix
-// key P[i] lands at i + #{appended < P[i]}, an appended key A[e] at
-// e + #{prefix < A[e]} (keys are unique: the index is in the low half), so
-// every slot below min(kk, plen + na) is written once.  stage: this warp's
-// shared-memory staging area of kApp + kk keys.  The code is loops, not
-// unrolled networks, so it stays small in the instruction cache.  Returns the
-// new kk-th key (KEY_NONE while fewer than kk are held) on every lane.
-__device__ __noinline__ uint64_t warp_compact(const uint64_t* __restrict__ app, int na,
-                                              const uint64_t* __restrict__ cur, int plen, uint64_t* __restrict__ nxt,
-                                              int kk, uint64_t* __restrict__ stage, int lane) {
-  int P = 32;
-  while (P < na) P <<= 1;
-  uint64_t* sp = stage + kApp;
-#pragma unroll 4
-  for (int e = lane; e < P; e += 32) stage[e] = e < na ? app[e] : KEY_NONE;
-#pragma unroll 4
-  for (int i = lane; i < plen; i += 32) sp[i] = cur[i];
-  __syncwarp();
-  for (int k2 = 2; k2 <= P; k2 <<= 1) {
+// 16-way register select without local memory: v[j] for a runtime j.
+__device__ __forceinline__ float sel16(const float (&v)[16], int j) {
+  float l1[8], l2[4], l3[2];
+#pragma unroll
+  for (int i = 0; i < 8; i++) l1[i] = (j & 1) ? v[2 * i + 1] : v[2 * i];
+#pragma unroll
+  for (int i = 0; i < 4; i++) l2[i] = (j & 2) ? l1[2 * i + 1] : l1[2 * i];
+#pragma unroll
+  for (int i = 0; i < 2; i++) l3[i] = (j & 4) ? l2[2 * i + 1] : l2[2 * i];
+  return (j & 8) ? l3[1] : l3[0];
+}
+
+// Sort each row of kk2 (<= 256) keys ascending: one warp per row, 8 keys
+// per lane (element e = lane * 8 + r), bitonic network in registers.
+__global__ void __launch_bounds__(256) sort_rows_kernel(uint64_t* __restrict__ keys, int64_t rows, int kk2) {
+  const int lane = threadIdx.x & 31;
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= rows) return;
+  uint64_t* kr = keys + row * kk2;
+  uint64_t v[8];
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int e = lane * 8 + r;
+    v[r] = e < kk2 ? kr[e] : KEY_NONE;
+  }
+#pragma unroll
+  for (int k2 = 2; k2 <= 256; k2 <<= 1) {
+#pragma unroll
     for (int j = k2 >> 1; j > 0; j >>= 1) {
-      for (int q = lane; q < (P >> 1); q += 32) {
-        const int e = ((q & ~(j - 1)) << 1) | (q & (j - 1));  // q with a 0 inserted at bit log2(j)
-        const uint64_t x = stage[e], y = stage[e | j];
-        const bool up = (e & k2) == 0;
-        if (up ? (x > y) : (x < y)) {
-          stage[e] = y;
-          stage[e | j] = x;
+      if (j >= 8) {
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          const uint64_t o = ((uint64_t)__shfl_xor_sync(0xffffffffu, (uint32_t)(v[r] >> 32), j >> 3) << 32) |
+                             __shfl_xor_sync(0xffffffffu, (uint32_t)v[r], j >> 3);
+          const int e = lane * 8 + r;
+          const bool up = (e & k2) == 0;
+          const bool lower = (e & j) == 0;
+          v[r] = (lower == up) ? (o < v[r] ? o : v[r]) : (o > v[r] ? o : v[r]);
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 8; r++) {
+          if (r & j) continue;
+          const int e = lane * 8 + r;
+          const bool up = (e & k2) == 0;
+          const uint64_t x = v[r], y = v[r ^ j];
+          const bool sw = up ? (x > y) : (x < y);
+          v[r] = sw ? y : x;
+          v[r ^ j] = sw ? x : y;
         }
       }
-      __syncwarp();
     }
   }
-  uint64_t tv = KEY_NONE;
-  int has = 0;
-  for (int e = lane; e < na; e += 32) {
-    const uint64_t x = stage[e];
-    const int pos = e + lower_bound_smem(sp, plen, x);
-    if (pos < kk) {
-      nxt[pos] = x;
-      if (pos == kk - 1) {
-        tv = x;
-        has = 1;
-      }
-    }
+#pragma unroll
+  for (int r = 0; r < 8; r++) {
+    const int e = lane * 8 + r;
+    if (e < kk2) kr[e] = v[r];
   }
-  for (int i = lane; i < plen; i += 32) {
-    const uint64_t x = sp[i];
-    const int pos = i + lower_bound_smem(stage, na, x);
-    if (pos < kk) {
-      nxt[pos] = x;
-      if (pos == kk - 1) {
-        tv = x;
-        has = 1;
-      }
-    }
-  }
-  const unsigned bm = __ballot_sync(0xffffffffu, has);
-  __syncwarp();
-  return bm ? shfl64(tv, __ffs(bm) - 1) : KEY_NONE;
 }
 
 __global__ void __launch_bounds__(kThreadsKT, 1)
@@ -156,8 +220,6 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
   float* xnsm = reinterpret_cast<float*>(tmem_holder + 4);  // [kEpiWarps][2][kHalfN] index norms
   uint64_t* tau_sh = reinterpret_cast<uint64_t*>(xnsm + kEpiWarps * 2 * kHalfN);  // [2][QM] running k-th keys
   int* fin_sh = reinterpret_cast<int*>(tau_sh + 2 * QM);  // [QM][2] final (half, plen) of column half 1
-  uint32_t* scratch_all = reinterpret_cast<uint32_t*>(fin_sh + 2 * QM);  // [kEpi][16] slow-path dots
-  uint64_t* stage_all = reinterpret_cast<uint64_t*>(scratch_all + kEpi * 16);  // [kEpiWarps][kApp + kk2] staging
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = (int64_t)blockIdx.x * QM;
@@ -287,8 +349,6 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
     const size_t qstride = 2 * hstride;
     uint64_t* mine = a.lists + (valid ? qi : 0) * qstride + hc * hstride;
     uint64_t* app = mine + 2ull * a.kk2;  // this (query, half)'s append log
-    uint64_t* stage = stage_all + (size_t)ew * (kApp + a.kk2);
-    uint32_t* scr = scratch_all + (threadIdx.x - 64) * 16;
     float* nsm_w = xnsm + ew * 2 * kHalfN;
     volatile uint64_t* tau_other = tau_sh + (hc ^ 1) * QM + row;
     volatile uint64_t* tau_mine = tau_sh + hc * QM + row;
@@ -310,8 +370,8 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
       const float th = tau_d - nq;
       return a.exact ? th : th + (nq + a.xmax_n2 + tau_d) * 3.814697265625e-06f;  // 2^-18
     };
-    // Lanes whose append log passed `lim` entries compact, one query at a
-    // time, with the whole warp.
+    // Lanes whose append log passed `lim` entries are reduced to their kk2
+    // smallest keys, one query at a time, by the whole warp.
     auto flush = [&](int lim) {
       unsigned need = __ballot_sync(0xffffffffu, na > lim);
       if (!need) return;
@@ -323,8 +383,8 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
         const int shalf = __shfl_sync(0xffffffffu, half, src);
         const int splen = __shfl_sync(0xffffffffu, plen, src);
         uint64_t* lb = a.lists + (q0 + g * 32 + src) * qstride + hc * hstride;
-        const uint64_t nt = warp_compact(lb + 2ull * a.kk2, sna, lb + (size_t)shalf * a.kk2, splen,
-                                         lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, stage, lane);
+        const uint64_t nt = warp_select(lb + 2ull * a.kk2, sna, lb + (size_t)shalf * a.kk2, splen,
+                                        lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
         if (lane == src) {
           tau = nt;
           half ^= 1;
@@ -382,19 +442,16 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
 #pragma unroll
           for (int j = 1; j < 16; j++) mn = fminf(mn, f[j]);
           if (mn <= thr) {
-            // the few passing columns: through shared memory, one loop trip each
-            uint4* s4 = reinterpret_cast<uint4*>(scr);
-#pragma unroll
-            for (int v = 0; v < 4; v++) s4[v] = make_uint4(r[h][4 * v], r[h][4 * v + 1], r[h][4 * v + 2], r[h][4 * v + 3]);
+            // the few passing columns, one loop trip each; the screened
+            // distance is D~ = |q|^2 + (|x|^2 - 2 q.x) in f32
             unsigned mask = 0;
 #pragma unroll
             for (int j = 0; j < 16; j++) mask |= (f[j] <= thr ? 1u : 0u) << j;
             while (mask) {
               const int j = __ffs(mask) - 1;
               mask &= mask - 1;
-              const int c = c0 + 16 * h + j;
-              const int64_t p = p0 + c;
-              float dt = fmaf(-2.0f, __uint_as_float(scr[j]), nq + nsm[c]);
+              const int64_t p = p0 + c0 + 16 * h + j;
+              float dt = nq + sel16(f, j);
               if (!a.exact) dt = fmaxf(dt, 0.0f);
               if (dt <= tau_d && p < a.n) {
                 const uint64_t key = make_key(dt, (uint32_t)p);
@@ -413,8 +470,8 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
       mbar_arrive(&acce[b]);
     }
     flush(0);
-    // column half 1 publishes its final (prefix half, length); half 0 merges
-    // it into its own prefix, 256 keys per compaction, and writes the result
+    // column half 1 publishes its final (kept half, count); half 0 selects
+    // the kk2 smallest of both and writes them (unsorted; sorted afterwards)
     if (hc == 1) {
       fin_sh[2 * row] = half;
       fin_sh[2 * row + 1] = plen;
@@ -430,12 +487,10 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
         uint64_t* lb = a.lists + qs * qstride;
         int shalf = __shfl_sync(0xffffffffu, half, src);
         int splen = __shfl_sync(0xffffffffu, plen, src);
-        for (int o0 = 0; o0 < oplen; o0 += kApp) {
-          const int cnt = min(kApp, oplen - o0);
-          warp_compact(other + o0, cnt, lb + (size_t)shalf * a.kk2, splen, lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2,
-                       stage, lane);
+        if (oplen > 0) {
+          warp_select(other, oplen, lb + (size_t)shalf * a.kk2, splen, lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
           shalf ^= 1;
-          splen = min(a.kk2, splen + cnt);
+          splen = min(a.kk2, splen + oplen);
         }
         const uint64_t* from = lb + (size_t)shalf * a.kk2;
         uint64_t* to = a.out_keys + qs * a.kk2;
@@ -583,61 +638,105 @@ __global__ void scatter_keys_kernel(const uint64_t* __restrict__ src, int kk, in
 
 namespace {
 // Shared memory of knn_tc_kernel without the B stages.
-size_t knn_tc_fixed_smem(int d, int kk2) {
+size_t knn_tc_fixed_smem(int d) {
   const int dp = ((d + BK - 1) / BK) * BK;
   const size_t a_bytes = (size_t)(dp / BK) * QM * BK * 2;
   return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * kHalfN * sizeof(float) + 2 * QM * 8 +
-         2 * QM * sizeof(int) + (size_t)kEpi * 16 * 4 + (size_t)kEpiWarps * (kApp + kk2) * 8;
+         2 * QM * sizeof(int);
 }
 int knn_tc_margin(int kk, bool exact_sq) { return exact_sq ? 0 : std::max(8, kk / 8); }
 }  // namespace
 
 bool knn_tc_supported(int d, int kk) {
-  if (d < 32 || d > 256 || kk < 1 || kk > 1024) return false;
-  // two B stages must fit beside the resident query tile and staging
-  return knn_tc_fixed_smem(d, kk + knn_tc_margin(kk, false)) + 2 * (size_t)XN * BK * 2 <= 227 * 1024;
+  if (d < 32 || d > 256 || kk < 1) return false;
+  // kept keys per (query, column half) are selected 8 per lane by one warp
+  if (kk + knn_tc_margin(kk, false) > 32 * kSel) return false;
+  return knn_tc_fixed_smem(d) + 2 * (size_t)XN * BK * 2 <= 227 * 1024;
 }
 
 // Top-kk keys of every query via the tensor-core screen.  out_keys: [m, kk]
 // (device).  X32/Q32: the f32 rows (for the exact re-score).
-int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d, int kk, int order, int metric,
+struct TcIndex {
+  int64_t n = 0, npad = 0;
+  int d = 0, dp = 0;
+  __nv_bfloat16* xb = nullptr;  // [npad, dp] BF16, zero padded
+  float* xn2 = nullptr;         // [npad] FP32 |x|^2 (padded rows 0)
+  bool integer = false;         // every value an integer with |v| <= 256
+  float vmax = 0.0f;            // max |v|
+  float xmax_n2 = 0.0f;         // max |x|^2
+  CUtensorMap tmX;
+};
+
+void knn_tc_index_free(TcIndex* t) {
+  if (!t) return;
+  if (t->xb) cudaFree(t->xb);
+  if (t->xn2) cudaFree(t->xn2);
+  delete t;
+}
+
+int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, TcIndex** out) {
+  *out = nullptr;
+  TcIndex* t = new TcIndex();
+  struct Guard {
+    TcIndex*& t;
+    ~Guard() { knn_tc_index_free(t); }
+  } guard{t};
+  t->n = n;
+  t->d = d;
+  t->dp = ((d + BK - 1) / BK) * BK;
+  t->npad = ((n + XN - 1) / XN) * XN;
+  FUELG_CUDA(cudaMalloc(&t->xb, (size_t)t->npad * t->dp * 2));
+  FUELG_CUDA(cudaMalloc(&t->xn2, sizeof(float) * t->npad));
+  Scratch flags;
+  FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
+  FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 2, stream));
+  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, n, t->npad, d, t->dp, t->xb, t->xn2, flags.as<int>());
+  ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  int hf[2];
+  FUELG_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, stream));
+  std::vector<float> h((size_t)t->npad);
+  FUELG_CUDA(cudaMemcpyAsync(h.data(), t->xn2, sizeof(float) * t->npad, cudaMemcpyDeviceToHost, stream));
+  FUELG_CUDA(cudaStreamSynchronize(stream));
+  t->integer = hf[0] == 0;
+  memcpy(&t->vmax, &hf[1], sizeof(float));
+  for (float v : h) t->xmax_n2 = std::max(t->xmax_n2, v);
+  FUELG_TRY(make_map_bf16(&t->tmX, t->xb, t->npad, t->dp, XN));
+  *out = t;
+  t = nullptr;  // owned by the caller now
+  return ST_OK;
+}
+
+int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
                 uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out) {
-  const int dp = ((d + BK - 1) / BK) * BK;
+  const int64_t n = ti->n;
+  const int d = ti->d;
+  const int dp = ti->dp;
   const int kc = dp / BK;
   const int64_t mpad = ((m + QM - 1) / QM) * QM;
-  const int64_t npad = ((n + XN - 1) / XN) * XN;
-  Scratch qb, xb, qn2, xn2, flags;
+  Scratch qb, qn2, flags;
   FUELG_TRY(qb.alloc((size_t)mpad * dp * 2, stream));
-  FUELG_TRY(xb.alloc((size_t)npad * dp * 2, stream));
   FUELG_TRY(qn2.alloc(sizeof(float) * mpad, stream));
-  FUELG_TRY(xn2.alloc(sizeof(float) * npad, stream));
-  FUELG_TRY(flags.alloc(sizeof(int) * 4, stream));
-  FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 4, stream));
+  FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
+  FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 2, stream));
   knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.as<__nv_bfloat16>(), qn2.as<float>(),
                                                flags.as<int>()); ::fuelg::note_launch();
-  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, n, npad, d, dp, xb.as<__nv_bfloat16>(), xn2.as<float>(),
-                                               flags.as<int>() + 2); ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
-  int hf[4];
+  int hf[2];
   FUELG_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, stream));
   FUELG_CUDA(cudaStreamSynchronize(stream));
-  float vmax;
-  {
-    int mx = std::max(hf[1], hf[3]);
-    memcpy(&vmax, &mx, sizeof(float));
-  }
-  const bool integer = hf[0] == 0 && hf[2] == 0;
+  float qmax;
+  memcpy(&qmax, &hf[1], sizeof(float));
+  const float vmax = std::max(qmax, ti->vmax);
+  const bool integer = hf[0] == 0 && ti->integer;
   const bool exact = integer && 2.0 * dp * (double)vmax * vmax < 16777216.0;
   *exact_out = exact ? 1 : 0;
   // screened keys kept per query: exact sqeuclidean needs none extra
   const int margin = knn_tc_margin(kk, exact && metric == METRIC_SQEUCLIDEAN);
   const int kk2 = kk + margin;
 
-  CUtensorMap tmQ, tmX;
-  FUELG_TRY(make_map_bf16(&tmQ, qb.p, mpad, dp, QM));
-  FUELG_TRY(make_map_bf16(&tmX, xb.p, npad, dp, XN));
   const size_t b_bytes = (size_t)XN * BK * 2;
-  const size_t fixed = knn_tc_fixed_smem(d, kk2);
+  const size_t fixed = knn_tc_fixed_smem(d);
   int stages = (int)((220 * 1024 - fixed) / b_bytes);
   stages = std::max(2, std::min(4, stages));
   const size_t smem = fixed + stages * b_bytes;
@@ -664,16 +763,11 @@ int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d,
   const double rel = (2 * u8 + u8 * u8) + dp * u23 * (1.0 + 2 * u8);
   // exact integer data: the screen and fuel's own f32 sum are both exact
   const float alpha = exact ? 0.0f : (float)(2.0 * rel * 1.01);
-  const float beta = exact ? 0.0f : (float)(((d + 31) / 32 + 9) * u24 * 1.01 + u24);
+  // (+3 u: the screened value is rounded as fl(|q|^2 + fl(|x|^2 - 2 q.x)))
+  const float beta = exact ? 0.0f : (float)(((d + 31) / 32 + 9) * u24 * 1.01 + 4 * u24);
   const float gamma = exact ? 0.0f : (float)((d + 4) * u24 * 1.01);
-  // max |x| and |x|^2 over the index, for the proof
-  float xmax_n2 = 0.0f;
-  {
-    std::vector<float> h((size_t)npad);
-    FUELG_CUDA(cudaMemcpyAsync(h.data(), xn2.p, sizeof(float) * npad, cudaMemcpyDeviceToHost, stream));
-    FUELG_CUDA(cudaStreamSynchronize(stream));
-    for (float v : h) xmax_n2 = std::max(xmax_n2, v);
-  }
+  // max |x|^2 over the index, for the proof
+  const float xmax_n2 = ti->xmax_n2;
   const float xmax_norm = sqrtf(xmax_n2) * (1.0f + 1e-6f);
   int64_t total_redo = 0;
   HotTimer* ht = hot_timer();
@@ -687,7 +781,7 @@ int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d,
     a.exact = exact ? 1 : 0;
     a.stages = stages;
     a.qn2 = qn2.as<float>() + b0;
-    a.xn2 = xn2.as<float>();
+    a.xn2 = ti->xn2;
     a.xmax_n2 = xmax_n2;
     a.lists = lists.as<uint64_t>();
     a.out_keys = kept.as<uint64_t>();
@@ -699,10 +793,14 @@ int knn_tc_topk(const float* Q32, int64_t m, const float* X32, int64_t n, int d,
     FUELG_TRY(make_map_bf16(&tmQb, qb.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
     const unsigned grid = (unsigned)((mcur + QM - 1) / QM);
     if (ht) ht->begin(stream);
-    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, tmX, a); ::fuelg::note_launch();
+    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, ti->tmX, a); ::fuelg::note_launch();
     if (ht) ht->end(stream);
     FUELG_CUDA(cudaGetLastError());
     uint64_t* dst = out_keys + b0 * kk;
+    // each query's kept keys in (distance, index) order
+    sort_rows_kernel<<<(unsigned)((mcur * 32 + 255) / 256), 256, 0, stream>>>(kept.as<uint64_t>(), mcur, kk2);
+    ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
     if (margin == 0) {
       FUELG_CUDA(cudaMemcpyAsync(dst, kept.p, (size_t)mcur * kk * 8, cudaMemcpyDeviceToDevice, stream));
       continue;

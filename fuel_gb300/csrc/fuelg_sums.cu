@@ -350,7 +350,7 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
     unsigned __int128 tot = 0;
 #pragma unroll
     for (int l = 0; l < L; l++) tot += (unsigned __int128)lp[l] << (32 * l);
-    if (L < 4) tot &= (((unsigned __int128)1) << (32 * L)) - 1;
+    if constexpr (L < 4) tot &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
 #pragma unroll
     for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
     const int j = (int)(e / d);
@@ -359,8 +359,12 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
     const bool neg = (tot >> (32 * L - 1)) & 1;
     unsigned __int128 mag = tot;
     if (neg) {
-      mag = (L < 4 ? (((unsigned __int128)1) << (32 * L)) : (unsigned __int128)0) - tot;
-      if (L < 4) mag &= (((unsigned __int128)1) << (32 * L)) - 1;
+      if constexpr (L < 4) {
+        mag = (((unsigned __int128)1) << (32 * (L % 4))) - tot;
+        mag &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
+      } else {
+        mag = (unsigned __int128)0 - tot;
+      }
     }
     float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, e_lo);
     centers[e] = neg ? -v : v;
