@@ -32,11 +32,12 @@ using namespace tcx;
 namespace {
 
 constexpr int QM = 128;        // queries per CTA (UMMA M)
-constexpr int XN = 256;        // index rows per tile (UMMA N)
-constexpr int kEpiWarps = 8;   // epilogue warps: 4 TMEM lane quarters x 2 column halves
+constexpr int XN = 128;        // index rows per tile (UMMA N)
+constexpr int kEpiWarps = 4;   // epilogue warps: one per TMEM lane quarter
 constexpr int kEpi = 32 * kEpiWarps;
 constexpr int kThreadsKT = 64 + kEpi;
-constexpr int kHalfN = XN / 2;  // columns of a tile per epilogue warp
+constexpr int kCtasPerSm = 2;  // 2 x (2 TMEM buffers of XN columns) = all 512 columns
+constexpr int kSmemPerCta = 112 * 1024;
 constexpr int kApp = 256;      // appended candidates per query between compactions
 
 struct KnnTcArgs {
@@ -48,7 +49,7 @@ struct KnnTcArgs {
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
   float xmax_n2;     // max |x|^2 over the index (filter slack)
-  uint64_t* lists;   // [m][2][2*kk2 + kApp]: per column half, two kept-key buffers + append log
+  uint64_t* lists;   // [m][2*kk2 + kApp]: two kept-key buffers + append log
   uint64_t* out_keys;  // [m][kk2]
   uint32_t idesc;
   int* status;
@@ -66,7 +67,7 @@ __device__ __forceinline__ int warp_count_hi_below(const uint32_t (&hi)[2 * kSel
   return __reduce_add_sync(0xffffffffu, c);
 }
 
-// Warp-cooperative selection for one (query, column half): the union of its
+// Warp-cooperative selection for one query: the union of its
 // na (<= 256) appended keys and its plen (<= kk <= 256) kept keys is reduced
 // to its kk smallest, written unsorted to nxt[0, min(kk, na + plen)).  The
 // kk-th smallest key is found by a bitwise binary search over the
@@ -200,12 +201,12 @@ __global__ void __launch_bounds__(256) sort_rows_kernel(uint64_t* __restrict__ k
   }
 }
 
-__global__ void __launch_bounds__(kThreadsKT, 1)
+__global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     knn_tc_kernel(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmX, KnnTcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const uint32_t a_chunk = QM * BK * 2;  // 16 KB
-  const uint32_t b_bytes = XN * BK * 2;  // 32 KB per stage
+  const uint32_t b_bytes = XN * BK * 2;  // 16 KB per stage
   const int NS = a.stages;
   uint8_t* sA = base;
   uint8_t* sB = base + (size_t)a.kc * a_chunk;
@@ -217,9 +218,7 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
   uint64_t* fin = afull + 1;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
-  float* xnsm = reinterpret_cast<float*>(tmem_holder + 4);  // [kEpiWarps][2][kHalfN] index norms
-  uint64_t* tau_sh = reinterpret_cast<uint64_t*>(xnsm + kEpiWarps * 2 * kHalfN);  // [2][QM] running k-th keys
-  int* fin_sh = reinterpret_cast<int*>(tau_sh + 2 * QM);  // [QM][2] final (half, plen) of column half 1
+  float* xnsm = reinterpret_cast<float*>(tmem_holder + 4);  // [kEpiWarps][2][XN] index norms
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = (int64_t)blockIdx.x * QM;
@@ -239,10 +238,9 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (threadIdx.x < 2 * QM) tau_sh[threadIdx.x] = KEY_NONE;
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                 "r"(512)
+                 "r"(2 * XN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -334,39 +332,27 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
     }
   } else {
     // Epilogue: warp w handles query rows 32*(w%4).. (its TMEM lane quarter)
-    // and column half hc of every tile; each (query, half) keeps its own
-    // sorted top-kk2 prefix + append log, and filters with the smaller of its
-    // own and the other half's running kk2-th key (a key at or above either
-    // cannot be among the query's kk2 smallest).
+    // over every column; each query keeps its kk2 smallest keys (unsorted)
+    // plus an append log of candidates below its running kk2-th key.
     const int g = warp & 3;
-    const int hc = (warp - 2) >> 2;
     const int ew = warp - 2;
     const int row = g * 32 + lane;  // TMEM lane = query row of the tile
     const int64_t qi = q0 + row;
     const bool valid = qi < a.m;
     const float nq = valid ? a.qn2[qi] : 0.0f;
-    const size_t hstride = 2ull * a.kk2 + kApp;
-    const size_t qstride = 2 * hstride;
-    uint64_t* mine = a.lists + (valid ? qi : 0) * qstride + hc * hstride;
-    uint64_t* app = mine + 2ull * a.kk2;  // this (query, half)'s append log
-    float* nsm_w = xnsm + ew * 2 * kHalfN;
-    volatile uint64_t* tau_other = tau_sh + (hc ^ 1) * QM + row;
-    volatile uint64_t* tau_mine = tau_sh + hc * QM + row;
-    uint64_t tau = KEY_NONE;   // own kk2-th key
-    uint64_t tflt = KEY_NONE;  // filter key: min(own, other half's)
+    const size_t qstride = 2ull * a.kk2 + kApp;
+    uint64_t* app = a.lists + (valid ? qi : 0) * qstride + 2ull * a.kk2;  // this query's append log
+    float* nsm_w = xnsm + ew * 2 * XN;
+    uint64_t tau = KEY_NONE;  // kk2-th key held
     float tau_d = __int_as_float(0x7f800000);
     int na = 0, half = 0, plen = 0;
-    auto set_filter = [&](uint64_t other) {
-      tflt = other < tau ? other : tau;
-      tau_d = tflt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(tflt);
-    };
     // Screen filter in the shifted domain: a column can enter only if
     // |x|^2 - 2 q.x <= tau - |q|^2 (+ slack covering the rounding of both
-    // forms when the data are not exact integers); the exact screened value
-    // is formed only for the rare columns that pass.
+    // forms when the data are not exact integers); the screened distance is
+    // formed only for the rare columns that pass.
     auto threshold = [&]() -> float {
       if (!valid) return -__int_as_float(0x7f800000);
-      if (tflt == KEY_NONE) return __int_as_float(0x7f800000);
+      if (tau == KEY_NONE) return __int_as_float(0x7f800000);
       const float th = tau_d - nq;
       return a.exact ? th : th + (nq + a.xmax_n2 + tau_d) * 3.814697265625e-06f;  // 2^-18
     };
@@ -382,35 +368,27 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
         const int sna = __shfl_sync(0xffffffffu, na, src);
         const int shalf = __shfl_sync(0xffffffffu, half, src);
         const int splen = __shfl_sync(0xffffffffu, plen, src);
-        uint64_t* lb = a.lists + (q0 + g * 32 + src) * qstride + hc * hstride;
+        uint64_t* lb = a.lists + (q0 + g * 32 + src) * qstride;
         const uint64_t nt = warp_select(lb + 2ull * a.kk2, sna, lb + (size_t)shalf * a.kk2, splen,
                                         lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
         if (lane == src) {
           tau = nt;
+          tau_d = nt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(nt);
           half ^= 1;
           plen = min(a.kk2, plen + na);
           na = 0;
-          *tau_mine = tau;
         }
       }
     };
     float thr = threshold();
-    // norms of this warp's 128 columns: 4 per lane, fetched one tile ahead
-    float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + hc * kHalfN) + lane);
+    // norms of the tile's XN columns: 4 per lane, fetched one tile ahead
+    float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2) + lane);
     for (int64_t t = 0; t < ntiles; t++) {
       const uint32_t b = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
-      const int64_t p0 = t * XN + hc * kHalfN;
-      float* nsm = nsm_w + b * kHalfN;
+      const int64_t p0 = t * XN;
+      float* nsm = nsm_w + b * XN;
       reinterpret_cast<float4*>(nsm)[lane] = pn;
       if (t + 1 < ntiles) pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + p0 + XN) + lane);
-      // the other half's progress tightens the filter
-      {
-        const uint64_t o = *tau_other;
-        if (o < tflt) {
-          set_filter(o);
-          thr = threshold();
-        }
-      }
       bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag);
       if (!ok) {
         if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
@@ -419,9 +397,9 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
       if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
       __syncwarp();
       tc_fence_after();
-      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN + hc * kHalfN;
+      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN;
 #pragma unroll 1
-      for (int c0 = 0; c0 < kHalfN; c0 += 64) {
+      for (int c0 = 0; c0 < XN; c0 += 64) {
         uint32_t r[4][16];
 #pragma unroll
         for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
@@ -455,13 +433,12 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
               if (!a.exact) dt = fmaxf(dt, 0.0f);
               if (dt <= tau_d && p < a.n) {
                 const uint64_t key = make_key(dt, (uint32_t)p);
-                if (key < tflt) app[na++] = key;
+                if (key < tau) app[na++] = key;
               }
             }
           }
           if (__any_sync(0xffffffffu, na > kApp - 16)) {
             flush(kApp - 16);
-            set_filter(*tau_other);
             thr = threshold();
           }
         }
@@ -470,39 +447,23 @@ __global__ void __launch_bounds__(kThreadsKT, 1)
       mbar_arrive(&acce[b]);
     }
     flush(0);
-    // column half 1 publishes its final (kept half, count); half 0 selects
-    // the kk2 smallest of both and writes them (unsorted; sorted afterwards)
-    if (hc == 1) {
-      fin_sh[2 * row] = half;
-      fin_sh[2 * row + 1] = plen;
-    }
-    asm volatile("bar.sync 1, %0;" ::"n"(kEpi) : "memory");
-    if (hc == 0) {
-      for (int src = 0; src < 32; src++) {
-        const int64_t qs = q0 + g * 32 + src;
-        if (qs >= a.m) break;
-        const int orow = g * 32 + src;
-        const int ohalf = fin_sh[2 * orow], oplen = fin_sh[2 * orow + 1];
-        const uint64_t* other = a.lists + qs * qstride + hstride + (size_t)ohalf * a.kk2;
-        uint64_t* lb = a.lists + qs * qstride;
-        int shalf = __shfl_sync(0xffffffffu, half, src);
-        int splen = __shfl_sync(0xffffffffu, plen, src);
-        if (oplen > 0) {
-          warp_select(other, oplen, lb + (size_t)shalf * a.kk2, splen, lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
-          shalf ^= 1;
-          splen = min(a.kk2, splen + oplen);
-        }
-        const uint64_t* from = lb + (size_t)shalf * a.kk2;
-        uint64_t* to = a.out_keys + qs * a.kk2;
-        for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
-      }
+    // kept keys out (unsorted; sorted afterwards), one query at a time per
+    // warp (coalesced); slots past the held count are KEY_NONE
+    for (int src = 0; src < 32; src++) {
+      const int64_t qs = q0 + g * 32 + src;
+      if (qs >= a.m) break;
+      const int shalf = __shfl_sync(0xffffffffu, half, src);
+      const int splen = __shfl_sync(0xffffffffu, plen, src);
+      const uint64_t* from = a.lists + qs * qstride + (size_t)shalf * a.kk2;
+      uint64_t* to = a.out_keys + qs * a.kk2;
+      for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
     }
   }
   tc_fence_before();
   __syncthreads();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(512) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(2 * XN) : "memory");
   }
 }
 
@@ -641,17 +602,16 @@ namespace {
 size_t knn_tc_fixed_smem(int d) {
   const int dp = ((d + BK - 1) / BK) * BK;
   const size_t a_bytes = (size_t)(dp / BK) * QM * BK * 2;
-  return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * kHalfN * sizeof(float) + 2 * QM * 8 +
-         2 * QM * sizeof(int);
+  return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * XN * sizeof(float);
 }
 int knn_tc_margin(int kk, bool exact_sq) { return exact_sq ? 0 : std::max(8, kk / 8); }
 }  // namespace
 
 bool knn_tc_supported(int d, int kk) {
   if (d < 32 || d > 256 || kk < 1) return false;
-  // kept keys per (query, column half) are selected 8 per lane by one warp
+  // kept keys per query are selected 8 per lane by one warp
   if (kk + knn_tc_margin(kk, false) > 32 * kSel) return false;
-  return knn_tc_fixed_smem(d) + 2 * (size_t)XN * BK * 2 <= 227 * 1024;
+  return knn_tc_fixed_smem(d) + 2 * (size_t)XN * BK * 2 <= kSmemPerCta;
 }
 
 // Top-kk keys of every query via the tensor-core screen.  out_keys: [m, kk]
@@ -737,19 +697,19 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
 
   const size_t b_bytes = (size_t)XN * BK * 2;
   const size_t fixed = knn_tc_fixed_smem(d);
-  int stages = (int)((220 * 1024 - fixed) / b_bytes);
-  stages = std::max(2, std::min(4, stages));
+  int stages = (int)((kSmemPerCta - fixed) / b_bytes);
+  stages = std::max(2, std::min(6, stages));
   const size_t smem = fixed + stages * b_bytes;
-  if (smem > 227 * 1024) {
+  if (smem > kSmemPerCta) {
     set_error("tensor-core kNN tile does not fit shared memory (d=%d)", d);
     return ST_ENOTSUP;
   }
   // Bound scratch: batches of queries whose lists take at most ~1 GiB.
-  const size_t per_query = ((size_t)kk2 * 5 + 2 * kApp) * 8;  // 2 x (two prefix halves + log) + kept keys
+  const size_t per_query = ((size_t)kk2 * 3 + kApp) * 8;  // two kept-key buffers + log + kept keys
   int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
   mb = std::min<int64_t>(mb, mpad);
   Scratch lists, kept, kept2, redo, nredo;
-  FUELG_TRY(lists.alloc((size_t)mb * 2 * (2 * kk2 + kApp) * 8, stream));
+  FUELG_TRY(lists.alloc((size_t)mb * (2 * kk2 + kApp) * 8, stream));
   FUELG_TRY(kept.alloc((size_t)mb * kk2 * 8, stream));
   if (margin) {
     FUELG_TRY(kept2.alloc((size_t)mb * kk2 * 8, stream));
