@@ -15,7 +15,7 @@ Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun (N>1) each rank runs an independent replica ("replicas only";
 the path is a single-device engine) and rank 0 prints one JSON line.
 
-python bench.py --profile lloyd|knn_tc|knn_plain [--steps K] [--warmup W]
+python bench.py --profile lloyd|knn_tc|knn_plain|serving [--steps K] [--warmup W]
 runs one workload alone (no CPU baseline, no side legs) for profiler
 captures; --knn-queries sets the query count of the kNN workloads there.
 """
@@ -42,6 +42,8 @@ REF_SAMPLE_ITERS = 10    # Lloyd iterations per reference-arm step (about 1 s of
 CPU_SAMPLE_ITERS = 100   # iterations of the CPU baseline leg (one full step, about 10 s)
 KNN_N, KNN_D, KNN_K = 1_000_000, 128, 100
 KNN_PLAIN_QUERIES = 20_000  # plain FP32 tier on a query subset (about 0.6 s)
+SERVE_N, SERVE_D, SERVE_RATE = 2_000_000, 96, 2000.0  # resident index rows, dims, requests/s
+SERVE_SECONDS_TC, SERVE_SECONDS_PLAIN = 2.0, 0.05      # seconds of Poisson arrivals per tier
 
 
 def peaks():
@@ -262,6 +264,9 @@ def run_ours(args):
     # tensor-core kNN self-join next to its plain FP32 tier
     knn_tc = knn_tc_rate(lib, _lib, torch, args)
 
+    # kNN serving (continuous batching): p50 / p99 latency and queries/s
+    serving = serving_rates() if not args.no_serving else None
+
     # CPU baseline: restated fuel CPU Lloyd on the host cores, bounded sample
     threads = os.cpu_count() or 1
     sample_iters = CPU_SAMPLE_ITERS
@@ -294,6 +299,7 @@ def run_ours(args):
         "tc_vs_plain": (value / plain["iters_per_s"]) if plain else None,
         "knn_plain": knn,
         "knn_tc": knn_tc,
+        "knn_serving": serving,
     }
     print(json.dumps(line), flush=True)
 
@@ -369,6 +375,62 @@ def knn_tc_rate(lib, _lib, torch, args, m_tc=None, plain=True, reps=1, n_index=K
         lib.fuelg_index_destroy(h)
 
 
+def serving_run(precision, seconds, X=None, seed=1):
+    """kNN serving: resident index n=2,000,000, d=96 (unit-norm rows);
+    Poisson arrivals (2,000 requests/s) of query batches of log-uniform size
+    in [1, 4096] with k drawn from {1, 10, 100}, submitted in real time to the
+    continuous-batching server; latency = submit to completion."""
+    import threading
+    from fuel_gb300 import SearchIndex, workloads
+    from fuel_gb300.serving import Server
+    X = workloads.unit_normal_rows(SERVE_N, SERVE_D, seed=0) if X is None else X
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision=precision)
+    rng = np.random.default_rng(seed)
+    pool = workloads.unit_normal_rows(1 << 16, SERVE_D, seed=2)
+    reqs, t = [], 0.0
+    while True:
+        t += rng.exponential(1.0 / SERVE_RATE)
+        if t > seconds:
+            break
+        m = int(np.exp(rng.uniform(0.0, np.log(4096.0))))
+        o = int(rng.integers(0, pool.shape[0] - m))
+        reqs.append((t, pool[o:o + m], int(rng.choice([1, 10, 100]))))
+    with Server(ix, precision=precision, max_batch_queries=16384, budget_bytes=8 << 30, workers=3) as sv:
+        sv.submit(pool[:256], 10).result()  # warm-up (tensor-core form, streams)
+        handles = []
+        t0 = time.perf_counter()
+
+        def feed():
+            for ta, Q, k in reqs:
+                dt = t0 + ta - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                handles.append(sv.submit(Q, k))
+
+        th = threading.Thread(target=feed)
+        th.start()
+        th.join()
+        for h in handles:
+            h.result()
+        wall = time.perf_counter() - t0
+        st = sv.stats()
+    lat = np.array([h.latency_ms for h in handles])
+    q = sum(Q.shape[0] for _, Q, _ in reqs)
+    return {"precision": precision, "requests": len(reqs), "queries": q, "arrival_seconds": seconds,
+            "offered_queries_per_s": q / seconds, "queries_per_s": q / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "batches": st["batches"] - 1,
+            "max_batch_requests": st["max_batch_requests"], "device_ms": st["device_ms"]}
+
+
+def serving_rates():
+    from fuel_gb300 import workloads
+    X = workloads.unit_normal_rows(SERVE_N, SERVE_D, seed=0)
+    tc = serving_run("bf16", SERVE_SECONDS_TC, X)
+    plain = serving_run("fp32", SERVE_SECONDS_PLAIN, X)
+    return {"workload": f"knn serving n={SERVE_N} d={SERVE_D} unit-norm rows, Poisson {SERVE_RATE:.0f} req/s, "
+                        "batch log-U[1,4096], k in {1,10,100}", "tc": tc, "plain_fp32": plain}
+
+
 def run_profile(args):
     """One workload alone, for profiler captures."""
     import torch
@@ -397,6 +459,8 @@ def run_profile(args):
         r = knn_tc_rate(lib, _lib, torch, args, m_tc=args.knn_queries, plain=False, reps=max(1, args.steps),
                         n_index=args.knn_n)
         print(json.dumps({"profile": "knn_tc", **r}))
+    elif args.profile == "serving":
+        print(json.dumps({"profile": "serving", **serving_rates()}))
     else:
         args.steps = max(1, args.steps)
         print(json.dumps({"profile": "knn_plain", **knn_plain_rate(lib, _lib, torch, args)}))
@@ -409,10 +473,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="split_bf16")
-    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain"], default=None)
+    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain", "serving"], default=None)
     ap.add_argument("--iters", type=int, default=ITERS, help="Lloyd iterations per call (--profile lloyd)")
     ap.add_argument("--knn-queries", type=int, default=20_000, help="query count (--profile knn_tc)")
     ap.add_argument("--knn-n", type=int, default=KNN_N, help="index rows (--profile knn_tc)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -61,6 +61,12 @@ SIGNATURES = {
     "fuelg_kmeans_lloyd": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _i32, _dbl, _i32, _i32, _i32, _vp, _vp,
                                           ctypes.POINTER(_i32), ctypes.POINTER(_dbl), ctypes.POINTER(Stats)]),
     "fuelg_lloyd_assign": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
+    "fuelg_server_create": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, ctypes.POINTER(_vp)]),
+    "fuelg_server_submit": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, ctypes.POINTER(_i64)]),
+    "fuelg_server_wait": (ctypes.c_int, [_vp, _i64, _i32, ctypes.POINTER(_dbl)]),
+    "fuelg_server_stats": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64), ctypes.POINTER(_i64),
+                                          ctypes.POINTER(_i64), ctypes.POINTER(_dbl)]),
+    "fuelg_server_destroy": (ctypes.c_int, [_vp]),
     "fuelg_knn_noalloc": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32, _i32, _vp, _vp, _vp]),
     "fuelg_cancel": (ctypes.c_int, []),
     "fuelg_reset_cancel": (ctypes.c_int, []),
@@ -111,6 +117,8 @@ def check(rc: int):
         raise KeyboardInterrupt(msg)
     if rc == ENOTSUP:
         raise NotImplementedError(msg)
+    if rc == ENOMEM:
+        raise MemoryError(msg)
     raise RuntimeError(f"fuelg error {rc}: {msg}")
 
 

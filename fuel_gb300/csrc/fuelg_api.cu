@@ -305,6 +305,27 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
   return ST_OK;
 }
 
+}  // extern "C"
+
+namespace fuelg {
+int index_view_get(fuelg_index* ix, bool want_tc, IndexView* out) {
+  std::lock_guard<std::mutex> lk(ix->mu);
+  cudaSetDevice(ix->device);
+  if (want_tc && !ix->tc && ix->n > 0 && knn_tc_supported(ix->d, 1))
+    FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, ix->stream, &ix->tc));
+  out->device = ix->device;
+  out->n = ix->n;
+  out->d = ix->d;
+  out->metric = ix->metric;
+  out->order = ix->order;
+  out->X = ix->X;
+  out->tc = ix->tc;
+  return ST_OK;
+}
+}  // namespace fuelg
+
+extern "C" {
+
 int fuelg_index_destroy(fuelg_index* ix) {
   if (!ix) return ST_OK;
   cudaSetDevice(ix->device);

@@ -173,6 +173,22 @@ void knn_tc_index_free(TcIndex* t);
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
                 uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out);
 
+// Read-only view of an index handle for concurrent users (the serving loop);
+// with want_tc the tensor-core form is built first when the shape allows it.
+struct IndexView {
+  int device = 0;
+  int64_t n = 0;
+  int d = 0;
+  int metric = 0;
+  int order = 0;
+  const float* X = nullptr;
+  const TcIndex* tc = nullptr;
+};
+}  // namespace fuelg
+struct fuelg_index;
+namespace fuelg {
+int index_view_get(fuelg_index* ix, bool want_tc, IndexView* out);
+
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
                 float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream);

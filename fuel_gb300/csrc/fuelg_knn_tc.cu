@@ -49,8 +49,8 @@ struct KnnTcArgs {
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
   float xmax_n2;     // max |x|^2 over the index (filter slack)
-  uint64_t* lists;   // [m][2*kk2 + kApp]: two kept-key buffers + append log
-  uint64_t* out_keys;  // [m][kk2]
+  uint64_t* lists;   // [S][m][2*kk2 + kApp]: two kept-key buffers + append log per index split
+  uint64_t* out_keys;  // [S][m][kk2]
   uint32_t idesc;
   int* status;
   const volatile int* cancel;
@@ -201,6 +201,45 @@ __global__ void __launch_bounds__(256) sort_rows_kernel(uint64_t* __restrict__ k
   }
 }
 
+constexpr int kMaxSplits = 128;
+
+// One warp per query: k-way merge of the S (<= kMaxSplits) sorted split
+// lists in[s][q][0, kk2) into out[q][0, kk2); lane l owns lists l, l+32, ...
+__global__ void __launch_bounds__(256) merge_tc_splits_kernel(const uint64_t* __restrict__ in, int64_t m, int S,
+                                                              int kk2, uint64_t* __restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= m) return;
+  int pos[kMaxSplits / 32];
+  uint64_t head[kMaxSplits / 32];
+#pragma unroll
+  for (int t = 0; t < kMaxSplits / 32; t++) {
+    const int sp = lane + 32 * t;
+    pos[t] = 0;
+    head[t] = sp < S ? in[((size_t)sp * m + q) * kk2] : KEY_NONE;
+  }
+  for (int j = 0; j < kk2; j++) {
+    uint64_t mn = head[0];
+#pragma unroll
+    for (int t = 1; t < kMaxSplits / 32; t++) mn = head[t] < mn ? head[t] : mn;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const uint64_t v = ((uint64_t)__shfl_xor_sync(0xffffffffu, (uint32_t)(mn >> 32), o) << 32) |
+                         __shfl_xor_sync(0xffffffffu, (uint32_t)mn, o);
+      mn = v < mn ? v : mn;
+    }
+    if (lane == 0) out[(size_t)q * kk2 + j] = mn;
+    if (mn == KEY_NONE) continue;
+#pragma unroll
+    for (int t = 0; t < kMaxSplits / 32; t++)
+      if (head[t] == mn) {  // keys are unique: one list advances
+        const int sp = lane + 32 * t;
+        pos[t]++;
+        head[t] = pos[t] < kk2 ? in[((size_t)sp * m + q) * kk2 + pos[t]] : KEY_NONE;
+      }
+  }
+}
+
 __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     knn_tc_kernel(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmX, KnnTcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
@@ -222,7 +261,12 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t q0 = (int64_t)blockIdx.x * QM;
-  const int64_t ntiles = (a.n + XN - 1) / XN;
+  // index split blockIdx.y of gridDim.y: tiles [tb, tb + ntiles)
+  const int64_t ntiles_all = (a.n + XN - 1) / XN;
+  const int64_t tb = ntiles_all * blockIdx.y / gridDim.y;
+  const int64_t ntiles = ntiles_all * (blockIdx.y + 1) / gridDim.y - tb;
+  uint64_t* const lists_sp = a.lists + (size_t)blockIdx.y * a.m * (2ull * a.kk2 + kApp);
+  uint64_t* const out_sp = a.out_keys + (size_t)blockIdx.y * a.m * a.kk2;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; s++) {
@@ -273,7 +317,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           mbar_expect_tx(&full[stage], b_bytes);
           armed |= 1u << stage;
           last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
-          tma_load_2d_hint(sB + (size_t)stage * b_bytes, &tmX, kc * BK, (int)(t * XN), &full[stage], pol_x);
+          tma_load_2d_hint(sB + (size_t)stage * b_bytes, &tmX, kc * BK, (int)((tb + t) * XN), &full[stage], pol_x);
           if (++stage == (uint32_t)NS) {
             stage = 0;
             phase ^= 1;
@@ -341,7 +385,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     const bool valid = qi < a.m;
     const float nq = valid ? a.qn2[qi] : 0.0f;
     const size_t qstride = 2ull * a.kk2 + kApp;
-    uint64_t* app = a.lists + (valid ? qi : 0) * qstride + 2ull * a.kk2;  // this query's append log
+    uint64_t* app = lists_sp + (valid ? qi : 0) * qstride + 2ull * a.kk2;  // this query's append log
     float* nsm_w = xnsm + ew * 2 * XN;
     uint64_t tau = KEY_NONE;  // kk2-th key held
     float tau_d = __int_as_float(0x7f800000);
@@ -368,7 +412,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
         const int sna = __shfl_sync(0xffffffffu, na, src);
         const int shalf = __shfl_sync(0xffffffffu, half, src);
         const int splen = __shfl_sync(0xffffffffu, plen, src);
-        uint64_t* lb = a.lists + (q0 + g * 32 + src) * qstride;
+        uint64_t* lb = lists_sp + (q0 + g * 32 + src) * qstride;
         const uint64_t nt = warp_select(lb + 2ull * a.kk2, sna, lb + (size_t)shalf * a.kk2, splen,
                                         lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
         if (lane == src) {
@@ -382,10 +426,10 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     };
     float thr = threshold();
     // norms of the tile's XN columns: 4 per lane, fetched one tile ahead
-    float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2) + lane);
+    float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + tb * XN) + lane);
     for (int64_t t = 0; t < ntiles; t++) {
       const uint32_t b = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
-      const int64_t p0 = t * XN;
+      const int64_t p0 = (tb + t) * XN;
       float* nsm = nsm_w + b * XN;
       reinterpret_cast<float4*>(nsm)[lane] = pn;
       if (t + 1 < ntiles) pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + p0 + XN) + lane);
@@ -454,8 +498,8 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
       if (qs >= a.m) break;
       const int shalf = __shfl_sync(0xffffffffu, half, src);
       const int splen = __shfl_sync(0xffffffffu, plen, src);
-      const uint64_t* from = a.lists + qs * qstride + (size_t)shalf * a.kk2;
-      uint64_t* to = a.out_keys + qs * a.kk2;
+      const uint64_t* from = lists_sp + qs * qstride + (size_t)shalf * a.kk2;
+      uint64_t* to = out_sp + qs * a.kk2;
       for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
     }
   }
@@ -704,13 +748,24 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     set_error("tensor-core kNN tile does not fit shared memory (d=%d)", d);
     return ST_ENOTSUP;
   }
+  // Index splits: when the query blocks cannot fill the GPU's CTA slots,
+  // each block's scan is split over S index ranges (>= 16 tiles each) whose
+  // sorted kept lists are merged afterwards.
+  const int64_t ntiles_all = (n + XN - 1) / XN;
+  const int64_t slots = 152 * kCtasPerSm;
+  const int64_t qblocks = (m + QM - 1) / QM;
+  int S = 1;
+  if (qblocks < slots)
+    S = (int)std::max<int64_t>(1, std::min<int64_t>({slots / qblocks, ntiles_all / 16, (int64_t)kMaxSplits}));
   // Bound scratch: batches of queries whose lists take at most ~1 GiB.
-  const size_t per_query = ((size_t)kk2 * 3 + kApp) * 8;  // two kept-key buffers + log + kept keys
+  const size_t per_query = ((size_t)S * (kk2 * 3 + kApp) + kk2 * 2) * 8;  // per split: lists + kept; merged
   int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
   mb = std::min<int64_t>(mb, mpad);
-  Scratch lists, kept, kept2, redo, nredo;
-  FUELG_TRY(lists.alloc((size_t)mb * (2 * kk2 + kApp) * 8, stream));
-  FUELG_TRY(kept.alloc((size_t)mb * kk2 * 8, stream));
+  Scratch lists, kept_sp, kept_m, kept2, redo, nredo;
+  FUELG_TRY(lists.alloc((size_t)S * mb * (2 * kk2 + kApp) * 8, stream));
+  FUELG_TRY(kept_sp.alloc((size_t)S * mb * kk2 * 8, stream));
+  if (S > 1) FUELG_TRY(kept_m.alloc((size_t)mb * kk2 * 8, stream));
+  uint64_t* kept = S > 1 ? kept_m.as<uint64_t>() : kept_sp.as<uint64_t>();
   if (margin) {
     FUELG_TRY(kept2.alloc((size_t)mb * kk2 * 8, stream));
     FUELG_TRY(redo.alloc(sizeof(int32_t) * mb, stream));
@@ -744,25 +799,31 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.xn2 = ti->xn2;
     a.xmax_n2 = xmax_n2;
     a.lists = lists.as<uint64_t>();
-    a.out_keys = kept.as<uint64_t>();
+    a.out_keys = kept_sp.as<uint64_t>();
     a.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(XN >> 3) << 17) | ((uint32_t)(QM >> 4) << 24);
     a.status = dev_status;
     a.cancel = cancel_word_device();
     // the query map addresses rows b0.. through the y coordinate
     CUtensorMap tmQb;
     FUELG_TRY(make_map_bf16(&tmQb, qb.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
-    const unsigned grid = (unsigned)((mcur + QM - 1) / QM);
+    const dim3 grid((unsigned)((mcur + QM - 1) / QM), (unsigned)S);
     if (ht) ht->begin(stream);
     kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, ti->tmX, a); ::fuelg::note_launch();
     if (ht) ht->end(stream);
     FUELG_CUDA(cudaGetLastError());
     uint64_t* dst = out_keys + b0 * kk;
     // each query's kept keys in (distance, index) order
-    sort_rows_kernel<<<(unsigned)((mcur * 32 + 255) / 256), 256, 0, stream>>>(kept.as<uint64_t>(), mcur, kk2);
+    sort_rows_kernel<<<(unsigned)((S * mcur * 32 + 255) / 256), 256, 0, stream>>>(kept_sp.as<uint64_t>(),
+                                                                                   S * mcur, kk2);
     ::fuelg::note_launch();
+    if (S > 1) {
+      merge_tc_splits_kernel<<<(unsigned)((mcur * 32 + 255) / 256), 256, 0, stream>>>(kept_sp.as<uint64_t>(), mcur, S,
+                                                                                      kk2, kept);
+      ::fuelg::note_launch();
+    }
     FUELG_CUDA(cudaGetLastError());
     if (margin == 0) {
-      FUELG_CUDA(cudaMemcpyAsync(dst, kept.p, (size_t)mcur * kk * 8, cudaMemcpyDeviceToDevice, stream));
+      FUELG_CUDA(cudaMemcpyAsync(dst, kept, (size_t)mcur * kk * 8, cudaMemcpyDeviceToDevice, stream));
       continue;
     }
     FUELG_CUDA(cudaMemsetAsync(nredo.p, 0, sizeof(int32_t), stream));
@@ -770,12 +831,12 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     const unsigned rg = (unsigned)((mcur * 32 + 255) / 256);
     if (order == ORDER_X86)
       knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2, metric,
-                                                              kept.as<uint64_t>(), kept2.as<uint64_t>(),
+                                                              kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
                                                               gamma, redo.as<int32_t>(), nredo.as<int32_t>());
     else
       knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2, metric,
-                                                              kept.as<uint64_t>(), kept2.as<uint64_t>(),
+                                                              kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
                                                               gamma, redo.as<int32_t>(), nredo.as<int32_t>());
     ::fuelg::note_launch();

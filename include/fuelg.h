@@ -133,6 +133,35 @@ int fuelg_kmeans_lloyd(const float *data, int64_t n, int32_t d, int32_t k, const
 int fuelg_lloyd_assign(const float *data, int64_t n, int32_t d, const float *centers, int32_t k, int32_t initial,
                        int32_t order, int64_t *out_labels, float *out_best, fuelg_stats *stats);
 
+/* kNN serving with continuous batching over a resident index.  No
+ * counterpart in the reference (fuel answers one call at a time); it serves
+ * streams of independent query batches.  `workers` threads each own a CUDA
+ * stream; a free worker takes every queued request that fits
+ * max_batch_queries rows and the device-memory budget (budget_bytes, charged
+ * per request while its batch runs) and runs them as one batch, so requests
+ * that arrive while others are on the GPU are admitted as memory frees up and
+ * their device work overlaps.  Each request gets exactly what fuelg_knn
+ * (exclude_mode FUELG_EXCLUDE_NONE, same precision tier) returns for its rows.
+ * The index must outlive the server and must not be used by other calls while
+ * the server runs. */
+typedef struct fuelg_server fuelg_server;
+int fuelg_server_create(fuelg_index *ix, int32_t precision, int64_t max_batch_queries, int64_t budget_bytes,
+                        int32_t workers, fuelg_server **out);
+/* Queues m query rows (copied before returning); out_idx [m, k] / out_dist
+ * [m, k] are host memory written when the request completes (keep them alive
+ * until fuelg_server_wait returns).  Fails with FUELG_ENOMEM when the request
+ * alone exceeds the budget. */
+int fuelg_server_submit(fuelg_server *s, const float *queries, int64_t m, int32_t k, int64_t *out_idx,
+                        float *out_dist, int64_t *request_id);
+/* Blocks until the request finished (timeout_ms < 0: no limit; on expiry
+ * FUELG_ETIMEOUT and the request stays pending); returns its status and the
+ * submit-to-completion latency.  Each id can be waited for once. */
+int fuelg_server_wait(fuelg_server *s, int64_t request_id, int32_t timeout_ms, double *latency_ms);
+int fuelg_server_stats(fuelg_server *s, int64_t *batches, int64_t *queries, int64_t *max_batch_rows,
+                       int64_t *max_batch_requests, double *device_ms);
+/* Finishes every queued request, then stops the workers. */
+int fuelg_server_destroy(fuelg_server *s);
+
 /* Allocation-free exact kNN.  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory -- code recording a CUDA graph
  * (cudaMalloc is not allowed during capture), hosts whose GPU memory belongs to
