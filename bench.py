@@ -425,7 +425,7 @@ def serving_run(precision, seconds, X=None, seed=1):
 def serving_rates():
     from fuel_gb300 import workloads
     X = workloads.unit_normal_rows(SERVE_N, SERVE_D, seed=0)
-    tc = serving_run("bf16", SERVE_SECONDS_TC, X)
+    tc = serving_run("split_bf16", SERVE_SECONDS_TC, X)
     plain = serving_run("fp32", SERVE_SECONDS_PLAIN, X)
     return {"workload": f"knn serving n={SERVE_N} d={SERVE_D} unit-norm rows, Poisson {SERVE_RATE:.0f} req/s, "
                         "batch log-U[1,4096], k in {1,10,100}", "tc": tc, "plain_fp32": plain}

@@ -6,6 +6,6 @@ search and Lloyd k-means hot path.
 sm_103a CUDA behind the C ABI of include/fuelg.h).
 """
 from .search import SearchIndex, knn_search, range_search  # noqa: F401
-from .cluster import KMeansResult, kmeans, lloyd_assign  # noqa: F401
+from .cluster import KMeansResult, kmeans, kmeans_batched, lloyd_assign  # noqa: F401
 
 __version__ = "0.1.0"

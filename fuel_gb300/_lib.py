@@ -40,6 +40,13 @@ class Stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class KMeansProblem(ctypes.Structure):
+    """fuelg_kmeans_problem (include/fuelg.h)."""
+    _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_int64), ("d", ctypes.c_int32), ("k", ctypes.c_int32),
+                ("init", ctypes.c_void_p), ("out_centers", ctypes.c_void_p), ("out_labels", ctypes.c_void_p),
+                ("out_iters", ctypes.c_int32), ("status", ctypes.c_int32), ("out_inertia", ctypes.c_double)]
+
+
 _lib = None
 
 # name -> (restype, argtypes); kept in step with include/fuelg.h
@@ -61,6 +68,7 @@ SIGNATURES = {
     "fuelg_kmeans_lloyd": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _i32, _dbl, _i32, _i32, _i32, _vp, _vp,
                                           ctypes.POINTER(_i32), ctypes.POINTER(_dbl), ctypes.POINTER(Stats)]),
     "fuelg_lloyd_assign": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
+    "fuelg_kmeans_batched": (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32, ctypes.POINTER(Stats)]),
     "fuelg_server_create": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, ctypes.POINTER(_vp)]),
     "fuelg_server_submit": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, ctypes.POINTER(_i64)]),
     "fuelg_server_wait": (ctypes.c_int, [_vp, _i64, _i32, ctypes.POINTER(_dbl)]),

@@ -135,3 +135,44 @@ def lloyd_assign(data, centers, *, initial=False, order=None):
                                               _lib.ORDER[order or _lib.default_order()], _lib.ptr(labels),
                                               _lib.ptr(best), None))
     return labels, best
+
+
+def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False):
+    """Many independent Lloyd k-means problems in one engine call.
+
+    ``problems``: iterable of ``(data float32[n, d], init float32[k, d])``.
+    Returns a list of ``KMeansResult`` -- each exactly what
+    ``kmeans(data, k=k, variant="lloyd", init=init, max_iter=max_iter,
+    fixed_iters=fixed_iters)`` returns for that problem.  All problems'
+    points are assigned by one persistent kernel per iteration and the
+    middle iterations run as one replayed CUDA graph.
+    """
+    order = order or _lib.default_order()
+    keep, descs, outs = [], [], []
+    for data, init in problems:
+        X = np.ascontiguousarray(data, np.float32)
+        C0 = np.ascontiguousarray(init, np.float32)
+        if X.ndim != 2 or C0.ndim != 2 or X.shape[1] != C0.shape[1]:
+            raise ValueError("each problem needs data [n, d] and init [k, d]")
+        n, d = X.shape
+        k = C0.shape[0]
+        centers = np.empty((k, d), np.float32)
+        labels = np.empty(n, np.int64)
+        keep += [X, C0, centers, labels]
+        descs.append(_lib.KMeansProblem(X.ctypes.data, n, d, k, C0.ctypes.data, centers.ctypes.data,
+                                        labels.ctypes.data, 0, 0, 0.0))
+        outs.append((centers, labels))
+    arr = (_lib.KMeansProblem * len(descs))(*descs)
+    st = _lib.Stats()
+    _lib.check(_lib.load().fuelg_kmeans_batched(ctypes.cast(arr, ctypes.c_void_p), len(descs), max(1, int(max_iter)),
+                                                _lib.ORDER[order], _lib.LLOYD_FIXED_ITERS if fixed_iters else 0,
+                                                ctypes.byref(st)))
+    res = []
+    for desc, (centers, labels) in zip(arr, outs):
+        if desc.status != _lib.OK:
+            raise NotImplementedError("a problem's data cannot be summed exactly (non-finite values or an exponent "
+                                      "range beyond 128 bits)")
+        r = KMeansResult(centers, labels, int(desc.out_iters), float(desc.out_inertia), None)
+        res.append(r)
+    kmeans_batched.last_stats = st.as_dict()
+    return res

@@ -308,11 +308,12 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
 }  // extern "C"
 
 namespace fuelg {
-int index_view_get(fuelg_index* ix, bool want_tc, IndexView* out) {
+int index_view_get(fuelg_index* ix, bool want_tc, bool want_split, IndexView* out) {
   std::lock_guard<std::mutex> lk(ix->mu);
   cudaSetDevice(ix->device);
-  if (want_tc && !ix->tc && ix->n > 0 && knn_tc_supported(ix->d, 1))
+  if (want_tc && !ix->tc && ix->n > 0 && knn_tc_supported(ix->d, 1, 0))
     FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, ix->stream, &ix->tc));
+  if (want_split && ix->tc && knn_tc_supported(ix->d, 1, 1)) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, ix->stream));
   out->device = ix->device;
   out->n = ix->n;
   out->d = ix->d;
@@ -401,12 +402,14 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   p.kk = kk;
   int used = FUELG_PREC_FP32;
   int64_t rescored = 0;
-  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk) && ix->n > 0) {
+  const int split = precision == FUELG_PREC_SPLIT_BF16 ? 1 : 0;
+  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk, split) && ix->n > 0) {
     int exact = 0;
     if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
-    FUELG_TRY(knn_tc_topk(ix->tc, p.A, m, ix->X, kk, ix->order, ix->metric, keys.as<uint64_t>(), dstat.as<int>(), s,
-                          &rescored, &exact));
-    used = FUELG_PREC_BF16;
+    if (split) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, s));
+    FUELG_TRY(knn_tc_topk(ix->tc, p.A, m, ix->X, kk, ix->order, ix->metric, split, keys.as<uint64_t>(),
+                          dstat.as<int>(), s, &rescored, &exact));
+    used = (split && !exact) ? FUELG_PREC_SPLIT_BF16 : FUELG_PREC_BF16;
   } else {
     FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
   }

@@ -1,0 +1,657 @@
+// fuelg_batched.cu -- many independent Lloyd k-means problems in one pass
+// per iteration.
+//
+// Every problem keeps fuel's Lloyd semantics exactly as fuelg_kmeans_lloyd
+// does (src/cluster/kmeans/lloyd.rs:12-202 with fixed initial centres): the
+// initial assignment in the vec_pairwise_sqdist order, later passes in the
+// math::sqdist order, strict < over centres (first index wins), empty
+// clusters keep their centre, centres = correctly rounded f32 of the exact
+// mean (integer sums at the problem's scale 2^e_lo, 32-bit slices in 64-bit
+// counters, order independent), iteration counting with the initial pass as
+// iteration 1 and the changed == 0 stop.  Results are bit-identical to one
+// fuelg_kmeans_lloyd call per problem.
+//
+// Layout: all problems' points are packed row-major one after another; work
+// items are 256-row slices of one problem, handed to persistent CTAs in
+// contiguous ranges so a CTA reloads a problem's centres into shared memory
+// only when its range crosses into the next problem.  One kernel per
+// iteration assigns every point of every problem and, for points whose label
+// changed, adds +x / -x to the cluster sums: per CTA in shared memory when a
+// problem's k*d*L counters fit (many points per counter: few global atomics),
+// straight to global counters otherwise.  A second kernel turns the sums into
+// centres.  The middle iterations are one CUDA graph replayed.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <vector>
+
+#include "../../include/fuelg.h"
+#include "fuelg_common.cuh"
+#include "fuelg_exact.cuh"
+#include "fuelg_internal.h"
+
+namespace fuelg {
+namespace {
+
+constexpr int kItemRows = 256;       // rows per work item = threads per CTA
+constexpr int kCentreCap = 16384;    // centre floats staged in shared memory (64 KB)
+constexpr int kAggCap = 2048;        // per-CTA sum counters in shared memory (16 KB)
+
+struct BProb {
+  int64_t x_off;     // float offset of the problem's rows
+  int64_t n;
+  int64_t lab_off;   // label offset
+  int64_t c_off;     // centre float offset (k * d)
+  int64_t limb_off;  // counter offset (k * d * L)
+  int32_t cnt_off;   // count offset (k)
+  int32_t d, k, L, e_lo;
+  int32_t item_begin;  // first work item
+  int32_t active;      // 0: skipped (bad data)
+};
+
+template <int D>
+struct Dim {
+  static constexpr int value = D;
+};
+
+// Exponent range of one problem's data: items of 64K values.
+__global__ void batched_range_kernel(const float* __restrict__ X, const int64_t* __restrict__ off,
+                                     const int32_t* __restrict__ blk_begin, int P, int* __restrict__ out) {
+  int lo_b = 0, hi_b = P;  // problem of this block
+  while (hi_b - lo_b > 1) {
+    const int mid = (lo_b + hi_b) >> 1;
+    if (blk_begin[mid] <= (int)blockIdx.x) lo_b = mid;
+    else hi_b = mid;
+  }
+  const int p = lo_b;
+  const int64_t b0 = off[p], b1 = off[p + 1];
+  const int64_t s0 = b0 + (int64_t)(blockIdx.x - blk_begin[p]) * 65536;
+  const int64_t s1 = min(s0 + 65536, b1);
+  int lo = 1 << 30, hi = -(1 << 30), bad = 0;
+  for (int64_t e = s0 + threadIdx.x; e < s1; e += blockDim.x) {
+    uint32_t mant;
+    int l, h;
+    bool z, b;
+    f32_parts(X[e], mant, l, h, z, b);
+    if (b) bad = 1;
+    if (!z && !b) {
+      lo = min(lo, l);
+      hi = max(hi, h);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[3 * p], lo);
+    atomicMax(&out[3 * p + 1], hi);
+    if (bad) atomicOr(&out[3 * p + 2], 1);
+  }
+}
+
+// Adds the exact slices of +-x (coordinate `dim` of a point) to cluster c.
+__device__ __forceinline__ void add_coord(unsigned long long* __restrict__ dst, float x, int e_lo, int L, bool neg) {
+  const unsigned __int128 v = fixed_of(x, e_lo, neg);
+  for (int l = 0; l < L; l++) {
+    const unsigned long long sl = (unsigned long long)((v >> (32 * l)) & 0xffffffffu);
+    if (sl) atomicAdd(dst + l, sl);
+  }
+}
+
+// One iteration over all problems: assignment + sum updates of changed points.
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(kItemRows) batched_assign_kernel(
+    const BProb* __restrict__ probs, int P, int items_total, const float* __restrict__ X,
+    const float* __restrict__ C, int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs,
+    int32_t* __restrict__ counts, int32_t* __restrict__ pchg, int first) {
+  extern __shared__ __align__(16) unsigned char smem_b[];
+  float* cs = reinterpret_cast<float*>(smem_b);                                           // [kCentreCap]
+  unsigned long long* agg = reinterpret_cast<unsigned long long*>(cs + kCentreCap);      // [kAggCap]
+  int* aggc = reinterpret_cast<int*>(agg + kAggCap);                                      // [256]
+  __shared__ int s_chg;
+  const int64_t it0 = (int64_t)items_total * blockIdx.x / gridDim.x;
+  const int64_t it1 = (int64_t)items_total * (blockIdx.x + 1) / gridDim.x;
+  int p = -1;
+  BProb pr{};
+  bool staged = false, use_agg = false;
+  // flush this CTA's partial sums / counts / change count of problem p
+  auto flush = [&]() {
+    __syncthreads();
+    if (p < 0 || !pr.active) return;
+    if (threadIdx.x == 0 && s_chg) atomicAdd(&pchg[p], s_chg);
+    if (use_agg) {
+      for (int e = threadIdx.x; e < pr.k * pr.d * pr.L; e += blockDim.x)
+        if (agg[e]) atomicAdd(limbs + pr.limb_off + e, agg[e]);
+      for (int e = threadIdx.x; e < pr.k; e += blockDim.x)
+        if (aggc[e]) atomicAdd(&counts[pr.cnt_off + e], aggc[e]);
+    }
+  };
+  for (int64_t item = it0; item < it1; item++) {
+    if (p < 0 || (p + 1 < P && item >= probs[p + 1].item_begin)) {
+      // next problem: flush the previous one, stage this one's centres
+      flush();
+      int lo = 0, hi = P;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (probs[mid].item_begin <= item) lo = mid;
+        else hi = mid;
+      }
+      __syncthreads();
+      p = lo;
+      pr = probs[p];
+      staged = pr.k * pr.d <= kCentreCap;
+      use_agg = pr.k * pr.d * pr.L <= kAggCap && pr.k <= 256;
+      if (pr.active) {
+        if (staged)
+          for (int e = threadIdx.x; e < pr.k * pr.d; e += blockDim.x) cs[e] = C[pr.c_off + e];
+        if (use_agg) {
+          for (int e = threadIdx.x; e < pr.k * pr.d * pr.L; e += blockDim.x) agg[e] = 0;
+          for (int e = threadIdx.x; e < pr.k; e += blockDim.x) aggc[e] = 0;
+        }
+      }
+      if (threadIdx.x == 0) s_chg = 0;
+      __syncthreads();
+    }
+    if (!pr.active) continue;
+    const int64_t i = (item - pr.item_begin) * kItemRows + threadIdx.x;
+    const bool live = i < pr.n;
+    int best = -1;
+    const float* xr = X + pr.x_off + (live ? i : 0) * pr.d;
+    const float* cbase = staged ? cs : C + pr.c_off;
+    if (live) {
+      float bd = 0.0f;
+      auto scan = [&](auto dimc) {
+        constexpr int DD = decltype(dimc)::value;
+        float xv[DD];
+#pragma unroll
+        for (int t = 0; t < DD; t++) xv[t] = __ldg(xr + t);
+        for (int c = 0; c < pr.k; c++) {
+          const float* cc = cbase + c * DD;
+          const float dv = exact_dist_fn<KIND, ORDER, DD>([&](int t) { return xv[t]; }, [&](int t) { return cc[t]; });
+          if (best < 0 || dv < bd) {
+            bd = dv;
+            best = c;
+          }
+        }
+      };
+      switch (pr.d) {
+        case 2: scan(Dim<2>{}); break;
+        case 8: scan(Dim<8>{}); break;
+        case 32: scan(Dim<32>{}); break;
+        case 64: scan(Dim<64>{}); break;
+        default:
+          for (int c = 0; c < pr.k; c++) {
+            const float dv = exact_dist_scalar<KIND, ORDER>(xr, C + pr.c_off + (int64_t)c * pr.d, pr.d);
+            if (best < 0 || dv < bd) {
+              bd = dv;
+              best = c;
+            }
+          }
+      }
+    }
+    const int old = live ? (first ? -1 : labels[pr.lab_off + i]) : -1;
+    if (live && best != old) {
+      labels[pr.lab_off + i] = best;
+      if (!first) atomicAdd(&s_chg, 1);
+      unsigned long long* base = use_agg ? agg : limbs + pr.limb_off;
+      if (use_agg) {
+        atomicAdd(&aggc[best], 1);
+        if (old >= 0) atomicAdd(&aggc[old], -1);
+      } else {
+        atomicAdd(&counts[pr.cnt_off + best], 1);
+        if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
+      }
+      for (int t = 0; t < pr.d; t++) {
+        const float xv = __ldg(xr + t);
+        add_coord(base + ((int64_t)best * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
+        if (old >= 0) add_coord(base + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+      }
+    }
+  }
+  flush();
+}
+
+// Centres from the sums: canonicalise each coordinate's counters (carry
+// propagation modulo 2^(32L)) and round the exact mean; empty clusters keep
+// their centre.  Also records per-problem convergence: conv[p] = the first
+// iteration (counting the initial pass as 1) with no changed label.
+__global__ void batched_mean_kernel(const BProb* __restrict__ probs, int P, const int64_t* __restrict__ kd_begin,
+                                    int64_t kd_total, unsigned long long* __restrict__ limbs,
+                                    const int32_t* __restrict__ counts, float* __restrict__ C, int write_centers) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kd_total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int lo = 0, hi = P;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (kd_begin[mid] <= e) lo = mid;
+      else hi = mid;
+    }
+    while (lo + 1 < P && kd_begin[lo + 1] <= e) lo++;
+    const BProb& pr = probs[lo];
+    if (!pr.active) continue;
+    const int64_t local = e - kd_begin[lo];
+    const int L = pr.L;
+    unsigned long long* lp = limbs + pr.limb_off + local * L;
+    unsigned __int128 tot = 0;
+    for (int l = 0; l < L; l++) tot += (unsigned __int128)lp[l] << (32 * l);
+    if (L < 4) tot &= (((unsigned __int128)1) << (32 * (L & 3))) - 1;
+    for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
+    const int j = (int)(local / pr.d);
+    const int cnt = counts[pr.cnt_off + j];
+    if (cnt <= 0 || !write_centers) continue;
+    const bool neg = (tot >> (32 * L - 1)) & 1;
+    unsigned __int128 mag = tot;
+    if (neg) {
+      if (L < 4) {
+        mag = (((unsigned __int128)1) << (32 * (L & 3))) - tot;
+        mag &= (((unsigned __int128)1) << (32 * (L & 3))) - 1;
+      } else {
+        mag = (unsigned __int128)0 - tot;
+      }
+    }
+    const float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, pr.e_lo);
+    C[pr.c_off + local] = neg ? -v : v;
+  }
+}
+
+// After each pass: record the iteration and convergence, reset the change
+// counters.  iter[0] counts passes (the initial one is 1).
+__global__ void batched_step_kernel(int P, int32_t* __restrict__ pchg, int32_t* __restrict__ conv,
+                                    int32_t* __restrict__ last_chg, int32_t* __restrict__ iter) {
+  const int it = iter[0] + 1;
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    const int c = pchg[p];
+    last_chg[p] = c;
+    if (it > 1 && c == 0 && conv[p] == 0) conv[p] = it;
+    pchg[p] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) iter[0] = it;
+}
+
+// FP64 sum of squared distances to the final centres, per problem.
+__global__ void batched_inertia_kernel(const BProb* __restrict__ probs, int P, int items_total,
+                                       const float* __restrict__ X, const float* __restrict__ C,
+                                       const int32_t* __restrict__ labels, double* __restrict__ inertia) {
+  for (int64_t item = blockIdx.x; item < items_total; item += gridDim.x) {
+    int lo = 0, hi = P;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (probs[mid].item_begin <= item) lo = mid;
+      else hi = mid;
+    }
+    while (lo + 1 < P && probs[lo + 1].item_begin <= item) lo++;
+    const BProb& pr = probs[lo];
+    const int64_t i = (item - pr.item_begin) * kItemRows + threadIdx.x;
+    double s = 0.0;
+    if (pr.active && i < pr.n) {
+      const float* x = X + pr.x_off + i * pr.d;
+      const float* c = C + pr.c_off + (int64_t)labels[pr.lab_off + i] * pr.d;
+      for (int t = 0; t < pr.d; t++) {
+        const double df = (double)x[t] - (double)c[t];
+        s += df * df;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(&inertia[lo], s);
+  }
+}
+
+struct DevBuf {
+  void* p = nullptr;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int alloc(size_t b) {
+    if (cudaMalloc(&p, b ? b : 16) != cudaSuccess) {
+      cudaGetLastError();
+      p = nullptr;
+      set_error("device allocation of %zu bytes failed", b);
+      return ST_ENOMEM;
+    }
+    return ST_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+// Launch shapes chosen per problem mix by timing the candidates once (the
+// first middle iteration of the first call with that mix), cached per
+// process.  Key: the sorted multiset of (d, k bucket) of the problems.
+struct Tuned {
+  int blocks_per_sm = 0;
+};
+std::mutex g_tune_mu;
+std::map<std::vector<int>, Tuned> g_tuned;
+
+}  // namespace
+}  // namespace fuelg
+
+using namespace fuelg;
+
+extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, int32_t max_iter, int32_t order,
+                                    int32_t flags, fuelg_stats* stats) {
+  if (count < 0 || (count > 0 && !probs) || max_iter < 1) {
+    set_error("invalid batched kmeans arguments count=%d max_iter=%d", count, max_iter);
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  for (int p = 0; p < count; p++) {
+    const fuelg_kmeans_problem& q = probs[p];
+    if (q.n < 1 || q.d < 1 || q.k < 1 || !q.data || !q.init || !q.out_centers || !q.out_labels) {
+      set_error("invalid problem %d (n=%lld d=%d k=%d)", p, (long long)q.n, q.d, q.k);
+      return ST_EINVAL;
+    }
+    if (q.n >= (1ll << 31) || (int64_t)q.k * q.d > (1ll << 28)) {
+      set_error("problem %d too large for the batched engine", p);
+      return ST_ENOTSUP;
+    }
+  }
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (count == 0) return ST_OK;
+  cudaStream_t s;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct SG {
+    cudaStream_t s;
+    ~SG() { cudaStreamDestroy(s); }
+  } sg{s};
+  const int64_t launches0 = launch_count();
+  cudaEvent_t ev0, ev1, evh0, evh1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  cudaEventCreate(&evh0);
+  cudaEventCreate(&evh1);
+  struct EG {
+    cudaEvent_t a, b, c, d;
+    ~EG() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      cudaEventDestroy(c);
+      cudaEventDestroy(d);
+    }
+  } eg{ev0, ev1, evh0, evh1};
+  cudaEventRecord(ev0, s);
+
+  // layout
+  const int P = count;
+  std::vector<BProb> hp(P);
+  std::vector<int64_t> xoff(P + 1, 0), kdb(P + 1, 0);
+  std::vector<int32_t> rblk(P + 1, 0);
+  int64_t xs = 0, cs = 0, ls = 0, ks = 0, kd = 0;
+  int64_t items = 0;
+  int64_t rb = 0;
+  for (int p = 0; p < P; p++) {
+    const fuelg_kmeans_problem& q = probs[p];
+    hp[p].x_off = xs;
+    hp[p].n = q.n;
+    hp[p].lab_off = ls;
+    hp[p].c_off = cs;
+    hp[p].cnt_off = (int32_t)ks;
+    hp[p].d = q.d;
+    hp[p].k = q.k;
+    hp[p].item_begin = (int32_t)items;
+    xoff[p] = xs;
+    kdb[p] = kd;
+    rblk[p] = (int32_t)rb;
+    xs += q.n * q.d;
+    cs += (int64_t)q.k * q.d;
+    ls += q.n;
+    ks += q.k;
+    kd += (int64_t)q.k * q.d;
+    items += (q.n + kItemRows - 1) / kItemRows;
+    rb += (q.n * q.d + 65535) / 65536;
+  }
+  xoff[P] = xs;
+  kdb[P] = kd;
+  rblk[P] = (int32_t)rb;
+  if (items >= (1ll << 31)) {
+    set_error("batch too large");
+    return ST_ENOTSUP;
+  }
+  DevBuf dX, dC, dLab, dCnt, dOff, dRb, dRange, dProbs, dKdb, dPchg, dConv, dLast, dIter, dInert, dLimbs;
+  FUELG_TRY(dX.alloc(sizeof(float) * xs));
+  FUELG_TRY(dC.alloc(sizeof(float) * cs));
+  FUELG_TRY(dLab.alloc(sizeof(int32_t) * ls));
+  FUELG_TRY(dCnt.alloc(sizeof(int32_t) * ks));
+  FUELG_TRY(dOff.alloc(sizeof(int64_t) * (P + 1)));
+  FUELG_TRY(dRb.alloc(sizeof(int32_t) * (P + 1)));
+  FUELG_TRY(dRange.alloc(sizeof(int) * 3 * P));
+  for (int p = 0; p < P; p++) {
+    FUELG_CUDA(cudaMemcpyAsync(dX.as<float>() + hp[p].x_off, probs[p].data, sizeof(float) * probs[p].n * probs[p].d,
+                               cudaMemcpyDefault, s));
+    FUELG_CUDA(cudaMemcpyAsync(dC.as<float>() + hp[p].c_off, probs[p].init, sizeof(float) * probs[p].k * probs[p].d,
+                               cudaMemcpyDefault, s));
+  }
+  FUELG_CUDA(cudaMemcpyAsync(dOff.p, xoff.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+  FUELG_CUDA(cudaMemcpyAsync(dRb.p, rblk.data(), sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice, s));
+  {
+    std::vector<int> init(3 * P);
+    for (int p = 0; p < P; p++) {
+      init[3 * p] = 1 << 30;
+      init[3 * p + 1] = -(1 << 30);
+      init[3 * p + 2] = 0;
+    }
+    FUELG_CUDA(cudaMemcpyAsync(dRange.p, init.data(), sizeof(int) * 3 * P, cudaMemcpyHostToDevice, s));
+    FUELG_CUDA(cudaStreamSynchronize(s));  // `init` leaves scope
+  }
+  if (rb > 0) {
+    batched_range_kernel<<<(unsigned)rb, 256, 0, s>>>(dX.as<float>(), dOff.as<int64_t>(), dRb.as<int32_t>(), P,
+                                                      dRange.as<int>());
+    note_launch();
+    FUELG_CUDA(cudaGetLastError());
+  }
+  std::vector<int> hr(3 * P);
+  FUELG_CUDA(cudaMemcpyAsync(hr.data(), dRange.p, sizeof(int) * 3 * P, cudaMemcpyDeviceToHost, s));
+  FUELG_CUDA(cudaStreamSynchronize(s));
+  int64_t limbs_total = 0;
+  for (int p = 0; p < P; p++) {
+    int e_lo = hr[3 * p], e_hi = hr[3 * p + 1];
+    if (e_lo > e_hi) e_lo = e_hi = 0;  // all zeros
+    int logn = 0;
+    while ((1ll << logn) <= hp[p].n) logn++;
+    const int bits = (e_hi - e_lo + 1) + logn + 1;
+    const int L = (bits + 31) / 32;
+    hp[p].active = (hr[3 * p + 2] == 0 && L <= 4) ? 1 : 0;
+    hp[p].L = std::max(1, std::min(4, L));
+    hp[p].e_lo = e_lo;
+    hp[p].limb_off = limbs_total;
+    limbs_total += (int64_t)hp[p].k * hp[p].d * hp[p].L;
+  }
+  FUELG_TRY(dLimbs.alloc(sizeof(unsigned long long) * limbs_total));
+  FUELG_TRY(dProbs.alloc(sizeof(BProb) * P));
+  FUELG_TRY(dKdb.alloc(sizeof(int64_t) * (P + 1)));
+  FUELG_TRY(dPchg.alloc(sizeof(int32_t) * P));
+  FUELG_TRY(dConv.alloc(sizeof(int32_t) * P));
+  FUELG_TRY(dLast.alloc(sizeof(int32_t) * P));
+  FUELG_TRY(dIter.alloc(sizeof(int32_t)));
+  FUELG_TRY(dInert.alloc(sizeof(double) * P));
+  FUELG_CUDA(cudaMemcpyAsync(dProbs.p, hp.data(), sizeof(BProb) * P, cudaMemcpyHostToDevice, s));
+  FUELG_CUDA(cudaMemcpyAsync(dKdb.p, kdb.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
+  FUELG_CUDA(cudaMemsetAsync(dLimbs.p, 0, sizeof(unsigned long long) * limbs_total, s));
+  FUELG_CUDA(cudaMemsetAsync(dCnt.p, 0, sizeof(int32_t) * ks, s));
+  FUELG_CUDA(cudaMemsetAsync(dPchg.p, 0, sizeof(int32_t) * P, s));
+  FUELG_CUDA(cudaMemsetAsync(dConv.p, 0, sizeof(int32_t) * P, s));
+  FUELG_CUDA(cudaMemsetAsync(dIter.p, 0, sizeof(int32_t), s));
+  FUELG_CUDA(cudaMemsetAsync(dInert.p, 0, sizeof(double) * P, s));
+
+  const size_t smem = sizeof(float) * kCentreCap + sizeof(unsigned long long) * kAggCap + sizeof(int) * 256;
+  auto k_init = order == FUELG_ORDER_X86 ? batched_assign_kernel<KIND_PAIRWISE, ORDER_X86>
+                                         : batched_assign_kernel<KIND_PAIRWISE, ORDER_ARM>;
+  auto k_iter = order == FUELG_ORDER_X86 ? batched_assign_kernel<KIND_SQDIST, ORDER_X86>
+                                         : batched_assign_kernel<KIND_SQDIST, ORDER_ARM>;
+  FUELG_CUDA(cudaFuncSetAttribute(k_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FUELG_CUDA(cudaFuncSetAttribute(k_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int sms = 152;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  }
+  // tuned launch shape for this mix of (d, k) buckets
+  std::vector<int> key;
+  for (int p = 0; p < P; p++) key.push_back(hp[p].d * 16 + std::min(15, (int)std::log2((double)hp[p].k)));
+  std::sort(key.begin(), key.end());
+  int bps = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) bps = it->second.blocks_per_sm;
+  }
+  auto grid_for = [&](int b) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)sms * b)); };
+  const unsigned mean_grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((kd + 255) / 256, (int64_t)sms * 8));
+  const int fixed = (flags & FUELG_LLOYD_FIXED_ITERS) ? 1 : 0;
+  (void)fixed;  // every pass runs; the reported count follows the changed == 0 stop unless fixed
+
+  auto pass = [&](bool first, bool write, unsigned grid) -> int {
+    if (first)
+      k_init<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
+                                           dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
+                                           dPchg.as<int32_t>(), 1);
+    else
+      k_iter<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
+                                           dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
+                                           dPchg.as<int32_t>(), 0);
+    note_launch();
+    if (write || true) {
+      batched_mean_kernel<<<mean_grid, 256, 0, s>>>(dProbs.as<BProb>(), P, dKdb.as<int64_t>(), kd,
+                                                    dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
+                                                    dC.as<float>(), write ? 1 : 0);
+      note_launch();
+    }
+    batched_step_kernel<<<1, 512, 0, s>>>(P, dPchg.as<int32_t>(), dConv.as<int32_t>(), dLast.as<int32_t>(),
+                                          dIter.as<int32_t>());
+    note_launch();
+    FUELG_CUDA(cudaGetLastError());
+    return ST_OK;
+  };
+  cudaEventRecord(evh0, s);
+  // iteration 1: initial assignment (pairwise order), every point enters
+  FUELG_TRY(pass(true, max_iter > 1, grid_for(bps ? bps : 3)));
+  int done = 1;
+  // autotune: time the candidate shapes on the first middle iterations
+  if (!bps && max_iter > 2) {
+    float best_ms = 1e30f;
+    int best_b = 3;
+    for (int b : {2, 3, 4}) {
+      if (done >= max_iter - 1) break;
+      cudaEvent_t t0, t1;
+      cudaEventCreate(&t0);
+      cudaEventCreate(&t1);
+      cudaEventRecord(t0, s);
+      FUELG_TRY(pass(false, true, grid_for(b)));
+      cudaEventRecord(t1, s);
+      FUELG_CUDA(cudaEventSynchronize(t1));
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, t0, t1);
+      cudaEventDestroy(t0);
+      cudaEventDestroy(t1);
+      done++;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best_b = b;
+      }
+    }
+    bps = best_b;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key].blocks_per_sm = bps;
+  }
+  if (!bps) bps = 3;
+  // middle iterations: one captured graph, replayed
+  const int middle = std::max(0, max_iter - 1 - done);
+  if (middle > 0) {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    FUELG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = launch_count();
+    const int rc = pass(false, true, grid_for(bps));
+    cudaError_t ce = cudaStreamEndCapture(s, &graph);
+    if (rc != ST_OK) return rc;
+    if (ce != cudaSuccess) {
+      set_error("graph capture failed: %s", cudaGetErrorString(ce));
+      return ST_ECUDA;
+    }
+    const int64_t per_pass = launch_count() - l0;
+    note_launch((int)(-per_pass));  // counted per replay below
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) {
+      set_error("graph instantiate failed: %s", cudaGetErrorString(ce));
+      return ST_ECUDA;
+    }
+    for (int i = 0; i < middle; i++) {
+      ce = cudaGraphLaunch(exec, s);
+      if (ce != cudaSuccess) break;
+      note_launch((int)per_pass);
+    }
+    cudaGraphExecDestroy(exec);
+    FUELG_CUDA(ce);
+    done += middle;
+  }
+  // last iteration: assignment, no centre update
+  if (done < max_iter) {
+    FUELG_TRY(pass(false, false, grid_for(bps)));
+    done++;
+  }
+  cudaEventRecord(evh1, s);
+  {
+    const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)sms * 8));
+    batched_inertia_kernel<<<ig, kItemRows, 0, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(),
+                                                    dC.as<float>(), dLab.as<int32_t>(), dInert.as<double>());
+    note_launch();
+    FUELG_CUDA(cudaGetLastError());
+  }
+  // results
+  std::vector<int32_t> conv(P), lab32;
+  std::vector<double> inert(P);
+  FUELG_CUDA(cudaMemcpyAsync(conv.data(), dConv.p, sizeof(int32_t) * P, cudaMemcpyDeviceToHost, s));
+  FUELG_CUDA(cudaMemcpyAsync(inert.data(), dInert.p, sizeof(double) * P, cudaMemcpyDeviceToHost, s));
+  lab32.resize(ls);
+  FUELG_CUDA(cudaMemcpyAsync(lab32.data(), dLab.p, sizeof(int32_t) * ls, cudaMemcpyDeviceToHost, s));
+  for (int p = 0; p < P; p++)
+    FUELG_CUDA(cudaMemcpyAsync(probs[p].out_centers, dC.as<float>() + hp[p].c_off,
+                               sizeof(float) * probs[p].k * probs[p].d, cudaMemcpyDefault, s));
+  cudaEventRecord(ev1, s);
+  FUELG_CUDA(cudaStreamSynchronize(s));
+  int64_t d2h = (int64_t)sizeof(int32_t) * ls + (int64_t)sizeof(float) * cs;
+  for (int p = 0; p < P; p++) {
+    fuelg_kmeans_problem& q = probs[p];
+    if (!hp[p].active) {
+      q.status = ST_ENOTSUP;
+      q.out_iters = 0;
+      q.out_inertia = 0.0;
+      continue;
+    }
+    for (int64_t i = 0; i < q.n; i++) q.out_labels[i] = lab32[hp[p].lab_off + i];
+    const int it = (!(flags & FUELG_LLOYD_FIXED_ITERS) && conv[p] > 0) ? conv[p] : max_iter;
+    q.out_iters = it;
+    q.out_inertia = inert[p];
+    q.status = ST_OK;
+  }
+  if (stats) {
+    float ms = 0.0f, hms = 0.0f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    cudaEventElapsedTime(&hms, evh0, evh1);
+    stats->device_ms = ms;
+    stats->hot_kernel_ms = hms;
+    stats->hot_kernel_launches = max_iter;
+    stats->h2d_bytes = (int64_t)sizeof(float) * (xs + cs);
+    stats->d2h_bytes = d2h;
+    int64_t evals = 0;
+    for (int p = 0; p < P; p++) evals += hp[p].n * hp[p].k;
+    stats->distance_evals = evals * max_iter;
+    stats->iterations = max_iter;
+    stats->kernel_launches = (int32_t)(launch_count() - launches0);
+  }
+  return ST_OK;
+}

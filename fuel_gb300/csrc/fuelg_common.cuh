@@ -283,6 +283,94 @@ __device__ __forceinline__ float exact_dist_scalar(const float* __restrict__ q, 
   return s;
 }
 
+// exact_dist_scalar's arithmetic for a compile-time d, with the two operands
+// given as element accessors q(i) / x(i) (registers, shared or global memory).
+// The operation sequence is the same, so the result is bit-identical.
+template <int KIND, int ORDER, int D, class QF, class XF>
+__device__ __forceinline__ float exact_dist_fn(QF q, XF x) {
+  constexpr bool lane8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
+  constexpr bool fma8 = (KIND == KIND_KNN && ORDER == ORDER_X86);
+  if constexpr (lane8) {
+    float acc[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) acc[l] = 0.0f;
+    constexpr int sd = D & ~7;
+#pragma unroll
+    for (int i = 0; i < sd; i += 8) {
+#pragma unroll
+      for (int l = 0; l < 8; l++) {
+        const float df = __fsub_rn(q(i + l), x(i + l));
+        acc[l] = fma8 ? __fmaf_rn(df, df, acc[l]) : __fadd_rn(sq_rn(df), acc[l]);
+      }
+    }
+    float s = acc[0];
+#pragma unroll
+    for (int l = 1; l < 8; l++) s = __fadd_rn(s, acc[l]);
+#pragma unroll
+    for (int i = sd; i < D; i++) {
+      const float df = __fsub_rn(q(i), x(i));
+      s = fma8 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+    }
+    return s;
+  } else if constexpr (KIND == KIND_SQDIST) {  // x86 avx2::sqdist_f32
+    if constexpr (D < 4) {
+      float s = 0.0f;
+#pragma unroll
+      for (int i = 0; i < D; i++) {
+        const float df = __fsub_rn(q(i), x(i));
+        s = __fadd_rn(s, sq_rn(df));
+      }
+      return s;
+    } else {
+      float a[4][8];
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+#pragma unroll
+        for (int l = 0; l < 8; l++) a[u][l] = 0.0f;
+      constexpr int d32 = D & ~31;
+#pragma unroll
+      for (int i = 0; i < d32; i += 32) {
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+#pragma unroll
+          for (int l = 0; l < 8; l++) {
+            const float df = __fsub_rn(q(i + u * 8 + l), x(i + u * 8 + l));
+            a[u][l] = __fmaf_rn(df, df, a[u][l]);
+          }
+      }
+      float c[8];
+#pragma unroll
+      for (int l = 0; l < 8; l++) c[l] = __fadd_rn(__fadd_rn(a[0][l], a[1][l]), __fadd_rn(a[2][l], a[3][l]));
+      constexpr int d8 = d32 + ((D - d32) & ~7);
+#pragma unroll
+      for (int i = d32; i < d8; i += 8) {
+#pragma unroll
+        for (int l = 0; l < 8; l++) {
+          const float df = __fsub_rn(q(i + l), x(i + l));
+          c[l] = __fmaf_rn(df, df, c[l]);
+        }
+      }
+      float s = __fadd_rn(__fadd_rn(__fadd_rn(c[0], c[4]), __fadd_rn(c[1], c[5])),
+                          __fadd_rn(__fadd_rn(c[2], c[6]), __fadd_rn(c[3], c[7])));
+#pragma unroll
+      for (int i = d8; i < D; i++) {
+        const float df = __fsub_rn(q(i), x(i));
+        s = __fmaf_rn(df, df, s);
+      }
+      return s;
+    }
+  } else {  // KIND_PAIRWISE: one chain; FMA chain for x86 with d >= 4
+    constexpr bool fma_chain = (ORDER == ORDER_X86) && D >= 4;
+    float s = 0.0f;
+#pragma unroll
+    for (int i = 0; i < D; i++) {
+      const float df = __fsub_rn(q(i), x(i));
+      s = fma_chain ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+    }
+    return s;
+  }
+}
+
 // Row stride (floats) for shared-memory tiles: 16-byte aligned rows whose
 // stride is an odd number of float4s, so eight lanes reading eight different
 // rows with 16-byte loads hit 32 distinct banks.

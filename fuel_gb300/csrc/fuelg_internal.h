@@ -164,14 +164,18 @@ int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int6
 
 // Tensor-core kNN (fuelg_knn_tc.cu): top-kk keys per query [m, kk] via a BF16
 // tcgen05 screen; exact for integer data, otherwise re-scored and proven.
-bool knn_tc_supported(int d, int kk);
+bool knn_tc_supported(int d, int kk, int split);
 // Resident tensor-core form of an index: BF16 copy padded to whole tiles, FP32
 // norms, integer census and the index-side bounds; built once per handle.
 struct TcIndex;
 int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, TcIndex** out);
 void knn_tc_index_free(TcIndex* t);
+int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream);
+// split: hi + lo BF16 operands (accuracy ~2^-16 instead of 2^-8); ignored for
+// integer data whose BF16 screen is exact.
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
-                uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out);
+                int split, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
+                int* exact_out);
 
 // Read-only view of an index handle for concurrent users (the serving loop);
 // with want_tc the tensor-core form is built first when the shape allows it.
@@ -187,7 +191,7 @@ struct IndexView {
 }  // namespace fuelg
 struct fuelg_index;
 namespace fuelg {
-int index_view_get(fuelg_index* ix, bool want_tc, IndexView* out);
+int index_view_get(fuelg_index* ix, bool want_tc, bool want_split, IndexView* out);
 
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,

@@ -45,6 +45,7 @@ struct KnnTcArgs {
   int kc;        // K chunks of 64
   int kk2;       // keys kept per query
   int exact;     // D~ is exact (integer data)
+  int split;     // hi + lo BF16 operands (three products)
   int stages;
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
@@ -241,14 +242,17 @@ __global__ void __launch_bounds__(256) merge_tc_splits_kernel(const uint64_t* __
 }
 
 __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
-    knn_tc_kernel(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmX, KnnTcArgs a) {
+    knn_tc_kernel(const __grid_constant__ CUtensorMap tmQ, const __grid_constant__ CUtensorMap tmX,
+                  const __grid_constant__ CUtensorMap tmQlo, const __grid_constant__ CUtensorMap tmXlo, KnnTcArgs a) {
   extern __shared__ __align__(1024) uint8_t smem_raw[];
   uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const uint32_t a_chunk = QM * BK * 2;  // 16 KB
   const uint32_t b_bytes = XN * BK * 2;  // 16 KB per stage
   const int NS = a.stages;
   uint8_t* sA = base;
-  uint8_t* sB = base + (size_t)a.kc * a_chunk;
+  // A: the query tile (hi chunks, then lo chunks in split mode), resident
+  uint8_t* sB = base + (size_t)(a.split ? 2 : 1) * a.kc * a_chunk;
+  const int nb = a.split ? 2 * a.kc : a.kc;  // B chunks per tile: x_hi (then x_lo)
   uint64_t* full = reinterpret_cast<uint64_t*>(sB + (size_t)NS * b_bytes);
   uint64_t* empty = full + NS;
   uint64_t* accf = empty + NS;
@@ -299,8 +303,11 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
       prefetch_tmap(&tmX);
       const uint64_t pol_q = policy_evict_first(), pol_x = policy_evict_last();
       // the query tile, once
-      mbar_expect_tx(afull, (uint32_t)a.kc * a_chunk);
+      mbar_expect_tx(afull, (uint32_t)(a.split ? 2 : 1) * a.kc * a_chunk);
       for (int kc = 0; kc < a.kc; kc++) tma_load_2d_hint(sA + (size_t)kc * a_chunk, &tmQ, kc * BK, (int)q0, afull, pol_q);
+      if (a.split)
+        for (int kc = 0; kc < a.kc; kc++)
+          tma_load_2d_hint(sA + (size_t)(a.kc + kc) * a_chunk, &tmQlo, kc * BK, (int)q0, afull, pol_q);
       uint32_t stage = 0, phase = 0, armed = 0, last_ph = 0;
       for (int64_t t = 0; t < ntiles && !*abort_flag; t++) {
         if ((t & 63) == 63 && a.cancel != nullptr && *a.cancel) {
@@ -308,7 +315,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           *abort_flag = 1;
           break;
         }
-        for (int kc = 0; kc < a.kc; kc++) {
+        for (int j = 0; j < nb; j++) {
           if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
             if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
             *abort_flag = 1;
@@ -317,7 +324,8 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           mbar_expect_tx(&full[stage], b_bytes);
           armed |= 1u << stage;
           last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
-          tma_load_2d_hint(sB + (size_t)stage * b_bytes, &tmX, kc * BK, (int)((tb + t) * XN), &full[stage], pol_x);
+          tma_load_2d_hint(sB + (size_t)stage * b_bytes, j < a.kc ? &tmX : &tmXlo, (j % a.kc) * BK,
+                           (int)((tb + t) * XN), &full[stage], pol_x);
           if (++stage == (uint32_t)NS) {
             stage = 0;
             phase ^= 1;
@@ -348,7 +356,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
         }
         tc_fence_after();
         const uint32_t d_tmem = tmem_base + buf * XN;
-        for (int kc = 0; kc < a.kc; kc++) {
+        for (int j = 0; j < nb; j++) {
           if (!mbar_wait(&full[stage], phase, abort_flag)) {
             if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
             *abort_flag = 1;
@@ -356,11 +364,18 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
             break;
           }
           tc_fence_after();
+          // B = x_hi[kc]: q_hi . x_hi (+ q_lo . x_hi); B = x_lo[kc]: q_hi . x_lo
+          const int kc = j % a.kc;
           const uint64_t ad = smem_desc_sw128(smem_u32(sA + (size_t)kc * a_chunk));
           const uint64_t bd = smem_desc_sw128(smem_u32(sB + (size_t)stage * b_bytes));
 #pragma unroll
           for (int kk = 0; kk < BK / 16; kk++)
-            umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (kc | kk) != 0 ? 1u : 0u);
+            umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (j | kk) != 0 ? 1u : 0u);
+          if (a.split && j < a.kc) {
+            const uint64_t al = smem_desc_sw128(smem_u32(sA + (size_t)(a.kc + kc) * a_chunk));
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; kk++) umma_bf16(d_tmem, al + 2 * kk, bd + 2 * kk, a.idesc, 1u);
+          }
           umma_commit(&empty[stage]);
           if (++stage == (uint32_t)NS) {
             stage = 0;
@@ -515,7 +530,8 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
 // FP32, plus an integer-data census: flags[0] |= non-integer or |v| > 256,
 // flags[1] = max |v| (as float bits; non-negative so integer order works).
 __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64_t rows_pad, int d, int dp,
-                                __nv_bfloat16* __restrict__ out, float* __restrict__ n2, int* __restrict__ flags) {
+                                __nv_bfloat16* __restrict__ out, __nv_bfloat16* __restrict__ out_lo,
+                                float* __restrict__ n2, int* __restrict__ flags) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   int bad = 0;
   float vmax = 0.0f;
@@ -523,7 +539,9 @@ __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64
     float acc = 0.0f;
     for (int c = lane; c < dp; c += 32) {
       const float x = (r < rows && c < d) ? __ldg(X + r * d + c) : 0.0f;
-      out[r * dp + c] = __float2bfloat16_rn(x);
+      const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+      out[r * dp + c] = hi;
+      if (out_lo) out_lo[r * dp + c] = __float2bfloat16_rn(x - __bfloat162float(hi));
       acc = fmaf(x, x, acc);
       if (x != rintf(x) || fabsf(x) > 256.0f) bad = 1;
       vmax = fmaxf(vmax, fabsf(x));
@@ -643,19 +661,19 @@ __global__ void scatter_keys_kernel(const uint64_t* __restrict__ src, int kk, in
 
 namespace {
 // Shared memory of knn_tc_kernel without the B stages.
-size_t knn_tc_fixed_smem(int d) {
+size_t knn_tc_fixed_smem(int d, int split) {
   const int dp = ((d + BK - 1) / BK) * BK;
-  const size_t a_bytes = (size_t)(dp / BK) * QM * BK * 2;
+  const size_t a_bytes = (size_t)(split ? 2 : 1) * (dp / BK) * QM * BK * 2;
   return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * XN * sizeof(float);
 }
 int knn_tc_margin(int kk, bool exact_sq) { return exact_sq ? 0 : std::max(8, kk / 8); }
 }  // namespace
 
-bool knn_tc_supported(int d, int kk) {
+bool knn_tc_supported(int d, int kk, int split) {
   if (d < 32 || d > 256 || kk < 1) return false;
   // kept keys per query are selected 8 per lane by one warp
   if (kk + knn_tc_margin(kk, false) > 32 * kSel) return false;
-  return knn_tc_fixed_smem(d) + 2 * (size_t)XN * BK * 2 <= kSmemPerCta;
+  return knn_tc_fixed_smem(d, split) + 2 * (size_t)XN * BK * 2 <= kSmemPerCta;
 }
 
 // Top-kk keys of every query via the tensor-core screen.  out_keys: [m, kk]
@@ -664,17 +682,19 @@ struct TcIndex {
   int64_t n = 0, npad = 0;
   int d = 0, dp = 0;
   __nv_bfloat16* xb = nullptr;  // [npad, dp] BF16, zero padded
+  __nv_bfloat16* xlo = nullptr; // [npad, dp] BF16 of x - xb (split tier; built on first use)
   float* xn2 = nullptr;         // [npad] FP32 |x|^2 (padded rows 0)
   bool integer = false;         // every value an integer with |v| <= 256
   float vmax = 0.0f;            // max |v|
   float xmax_n2 = 0.0f;         // max |x|^2
-  CUtensorMap tmX;
+  CUtensorMap tmX, tmXlo;
 };
 
 void knn_tc_index_free(TcIndex* t) {
   if (!t) return;
   if (t->xb) cudaFree(t->xb);
   if (t->xn2) cudaFree(t->xn2);
+  if (t->xlo) cudaFree(t->xlo);
   delete t;
 }
 
@@ -694,7 +714,7 @@ int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, 
   Scratch flags;
   FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
   FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 2, stream));
-  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, n, t->npad, d, t->dp, t->xb, t->xn2, flags.as<int>());
+  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, n, t->npad, d, t->dp, t->xb, nullptr, t->xn2, flags.as<int>());
   ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   int hf[2];
@@ -711,19 +731,43 @@ int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, 
   return ST_OK;
 }
 
+// Adds the BF16 residual copy x - BF16(x) of the index (split tier), once.
+int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream) {
+  if (t->xlo) return ST_OK;
+  FUELG_CUDA(cudaMalloc(&t->xlo, (size_t)t->npad * t->dp * 2));
+  Scratch hi, n2, flags;
+  FUELG_TRY(hi.alloc((size_t)t->npad * t->dp * 2, stream));
+  FUELG_TRY(n2.alloc(sizeof(float) * t->npad, stream));
+  FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
+  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, t->n, t->npad, t->d, t->dp, hi.as<__nv_bfloat16>(), t->xlo,
+                                               n2.as<float>(), flags.as<int>());
+  ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  FUELG_TRY(make_map_bf16(&t->tmXlo, t->xlo, t->npad, t->dp, XN));
+  FUELG_CUDA(cudaStreamSynchronize(stream));
+  return ST_OK;
+}
+
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
-                uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored, int* exact_out) {
+                int split, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
+                int* exact_out) {
   const int64_t n = ti->n;
   const int d = ti->d;
   const int dp = ti->dp;
   const int kc = dp / BK;
   const int64_t mpad = ((m + QM - 1) / QM) * QM;
-  Scratch qb, qn2, flags;
+  if (split && !ti->xlo) {
+    set_error("split-BF16 kNN needs the index residual copy");
+    return ST_ENOTSUP;
+  }
+  Scratch qb, qlo, qn2, flags;
   FUELG_TRY(qb.alloc((size_t)mpad * dp * 2, stream));
+  if (split) FUELG_TRY(qlo.alloc((size_t)mpad * dp * 2, stream));
   FUELG_TRY(qn2.alloc(sizeof(float) * mpad, stream));
   FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
   FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 2, stream));
-  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.as<__nv_bfloat16>(), qn2.as<float>(),
+  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.as<__nv_bfloat16>(),
+                                               split ? qlo.as<__nv_bfloat16>() : nullptr, qn2.as<float>(),
                                                flags.as<int>()); ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   int hf[2];
@@ -735,12 +779,13 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   const bool integer = hf[0] == 0 && ti->integer;
   const bool exact = integer && 2.0 * dp * (double)vmax * vmax < 16777216.0;
   *exact_out = exact ? 1 : 0;
+  if (exact) split = 0;  // integer data: the plain BF16 screen is already exact
   // screened keys kept per query: exact sqeuclidean needs none extra
   const int margin = knn_tc_margin(kk, exact && metric == METRIC_SQEUCLIDEAN);
   const int kk2 = kk + margin;
 
   const size_t b_bytes = (size_t)XN * BK * 2;
-  const size_t fixed = knn_tc_fixed_smem(d);
+  const size_t fixed = knn_tc_fixed_smem(d, split);
   int stages = (int)((kSmemPerCta - fixed) / b_bytes);
   stages = std::max(2, std::min(6, stages));
   const size_t smem = fixed + stages * b_bytes;
@@ -775,7 +820,10 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // integer data aside, keep the error-bound constants of the Lloyd screen
   const double u8 = std::ldexp(1.0, -8), u23 = std::ldexp(1.0, -23), u24 = std::ldexp(1.0, -24);
-  const double rel = (2 * u8 + u8 * u8) + dp * u23 * (1.0 + 2 * u8);
+  // operand rounding (2u + u^2 per BF16 product; 3.01 * 2^-16 with hi + lo)
+  // plus FP32 accumulation in the tensor core over dp (3 dp) products
+  const double rel = split ? 3.01 * std::ldexp(1.0, -16) + 3.0 * dp * u23 * (1.0 + 2 * u8)
+                           : (2 * u8 + u8 * u8) + dp * u23 * (1.0 + 2 * u8);
   // exact integer data: the screen and fuel's own f32 sum are both exact
   const float alpha = exact ? 0.0f : (float)(2.0 * rel * 1.01);
   // (+3 u: the screened value is rounded as fl(|q|^2 + fl(|x|^2 - 2 q.x)))
@@ -794,6 +842,7 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.kc = kc;
     a.kk2 = kk2;
     a.exact = exact ? 1 : 0;
+    a.split = split;
     a.stages = stages;
     a.qn2 = qn2.as<float>() + b0;
     a.xn2 = ti->xn2;
@@ -804,11 +853,14 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.status = dev_status;
     a.cancel = cancel_word_device();
     // the query map addresses rows b0.. through the y coordinate
-    CUtensorMap tmQb;
+    CUtensorMap tmQb, tmQl;
     FUELG_TRY(make_map_bf16(&tmQb, qb.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
+    if (split) FUELG_TRY(make_map_bf16(&tmQl, qlo.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
+    else tmQl = tmQb;
     const dim3 grid((unsigned)((mcur + QM - 1) / QM), (unsigned)S);
     if (ht) ht->begin(stream);
-    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, ti->tmX, a); ::fuelg::note_launch();
+    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, ti->tmX, tmQl, split ? ti->tmXlo : ti->tmX, a);
+    ::fuelg::note_launch();
     if (ht) ht->end(stream);
     FUELG_CUDA(cudaGetLastError());
     uint64_t* dst = out_keys + b0 * kk;

@@ -101,10 +101,11 @@ int run_batch(fuelg_server* sv, std::vector<Request*>& batch, cudaStream_t s, fl
   FUELG_TRY(dstat.alloc(sizeof(int), s));
   FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
   FUELG_CUDA(cudaMemcpyAsync(q.p, pin_q, sizeof(float) * m * ix.d, cudaMemcpyHostToDevice, s));
-  if (sv->precision != FUELG_PREC_FP32 && ix.tc && knn_tc_supported(ix.d, kmax)) {
+  const int split = sv->precision == FUELG_PREC_SPLIT_BF16 ? 1 : 0;
+  if (sv->precision != FUELG_PREC_FP32 && ix.tc && knn_tc_supported(ix.d, kmax, split)) {
     int64_t rescored = 0;
     int exact = 0;
-    FUELG_TRY(knn_tc_topk(ix.tc, q.as<float>(), m, ix.X, kmax, ix.order, ix.metric, keys.as<uint64_t>(),
+    FUELG_TRY(knn_tc_topk(ix.tc, q.as<float>(), m, ix.X, kmax, ix.order, ix.metric, split, keys.as<uint64_t>(),
                           dstat.as<int>(), s, &rescored, &exact));
   } else {
     ExactScanParams p;
@@ -242,7 +243,7 @@ int fuelg_server_create(fuelg_index* ix, int32_t precision, int64_t max_batch_qu
     return ST_EINVAL;
   }
   IndexView v;
-  FUELG_TRY(index_view_get(ix, precision != FUELG_PREC_FP32, &v));
+  FUELG_TRY(index_view_get(ix, precision != FUELG_PREC_FP32, precision == FUELG_PREC_SPLIT_BF16, &v));
   fuelg_server* sv = new fuelg_server();
   sv->view = v;
   sv->precision = precision;

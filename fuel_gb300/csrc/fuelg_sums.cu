@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "fuelg_common.cuh"
+#include "fuelg_exact.cuh"
 #include "fuelg_internal.h"
 
 namespace fuelg {
@@ -24,23 +25,6 @@ namespace fuelg {
 namespace {
 
 constexpr int kRows = 32;  // rows per accumulation chunk
-
-__device__ __forceinline__ void f32_parts(float x, uint32_t& mant, int& lsb, int& msb, bool& zero, bool& bad) {
-  const uint32_t b = __float_as_uint(x);
-  const uint32_t eb = (b >> 23) & 0xffu;
-  const uint32_t m = b & 0x7fffffu;
-  zero = (b & 0x7fffffffu) == 0;
-  bad = eb == 0xffu;
-  if (eb == 0) {  // subnormal: m * 2^-149
-    mant = m;
-    lsb = m ? -149 + __ffs((int)m) - 1 : 0;
-    msb = m ? -149 + 31 - __clz((int)m) : 0;
-  } else {
-    mant = m | 0x800000u;
-    lsb = (int)eb - 150 + __ffs((int)mant) - 1;
-    msb = (int)eb - 127;
-  }
-}
 
 __device__ __forceinline__ void range_acc(float x, int& lo, int& hi, int& bad) {
   uint32_t mant;
@@ -82,22 +66,6 @@ __global__ void exp_range_kernel(const float* __restrict__ X, int64_t count, int
     atomicMax(&out[1], hi);
     if (bad) atomicOr(&out[2], 1);
   }
-}
-
-// Two's complement of +-I(x) modulo 2^128 (callers use the low 32L bits).
-__device__ __forceinline__ unsigned __int128 fixed_of(float x, int e_lo, bool negate) {
-  uint32_t mant;
-  int l, h;
-  bool z, b;
-  f32_parts(x, mant, l, h, z, b);
-  if (z) return 0;
-  const uint32_t bits = __float_as_uint(x);
-  const int eb = (int)((bits >> 23) & 0xffu);
-  const int unit = (eb == 0 ? -149 : eb - 150);  // weight of mantissa bit 0
-  const int sh = unit - e_lo;
-  unsigned __int128 v = sh >= 0 ? ((unsigned __int128)mant << sh) : (unsigned __int128)(mant >> (-sh));
-  const bool neg = ((bits >> 31) != 0) != negate;
-  return neg ? (unsigned __int128)0 - v : v;
 }
 
 // Changed labels -> change list + per-cluster in/out histograms.  `first`: no
@@ -308,26 +276,6 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
         if (acc[l]) atomicAdd(dst + l, acc[l]);  // integer: exact in any order
     }
   }
-}
-
-// Correctly rounded (RNE) f32 of A * 2^e / cnt for A > 0 (normal range).
-__device__ float rn_ratio_f32(unsigned __int128 A, unsigned long long cnt, int e) {
-  const int bitsA = A >> 64 ? 128 - __clzll((long long)(unsigned long long)(A >> 64))
-                            : 64 - __clzll((long long)(unsigned long long)A);
-  const int bitsC = 64 - __clzll((long long)cnt);
-  int sh = 0;
-  if (bitsA - bitsC < 27) sh = 27 - (bitsA - bitsC);
-  const unsigned __int128 A2 = A << sh;
-  const unsigned __int128 q = A2 / cnt;
-  const unsigned __int128 r = A2 - q * cnt;
-  const int p = q >> 64 ? 128 - __clzll((long long)(unsigned long long)(q >> 64))
-                        : 64 - __clzll((long long)(unsigned long long)q);
-  const int drop = p - 24;
-  unsigned long long mant = (unsigned long long)(q >> drop);
-  const unsigned __int128 rem = q & (((unsigned __int128)1 << drop) - 1);
-  const unsigned __int128 half = (unsigned __int128)1 << (drop - 1);
-  if (rem > half || (rem == half && (r != 0 || (mant & 1)))) mant += 1;
-  return ldexpf((float)mant, drop + e - sh);
 }
 
 // Canonicalise every coordinate's limbs and write the exact mean of non-empty

@@ -64,3 +64,16 @@ def batched_kmeans_problems(count: int = 512, seed: int = 0, n_range=(1000, 2000
         k = int(np.exp(rng.uniform(np.log(k_range[0]), np.log(k_range[1]))))
         out.append((n, d, min(k, n), int(rng.integers(0, 2**31 - 1))))
     return out
+
+
+def batched_kmeans_data(desc):
+    """One problem of the batched workload: a Gaussian mixture with k centres
+    uniform in [-10, 10]^d and sd 1 (equal weights), float32; init = the
+    first k rows of a seeded permutation.  Returns (X [n, d], init [k, d])."""
+    n, d, k, seed = desc
+    rng = np.random.default_rng(seed)
+    centres = rng.uniform(-10.0, 10.0, size=(k, d))
+    comp = rng.integers(0, k, size=n)
+    X = (centres[comp] + rng.standard_normal((n, d))).astype(np.float32)
+    init = X[rng.permutation(n)[:k]].copy()
+    return np.ascontiguousarray(X), np.ascontiguousarray(init)

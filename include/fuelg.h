@@ -133,6 +133,31 @@ int fuelg_kmeans_lloyd(const float *data, int64_t n, int32_t d, int32_t k, const
 int fuelg_lloyd_assign(const float *data, int64_t n, int32_t d, const float *centers, int32_t k, int32_t initial,
                        int32_t order, int64_t *out_labels, float *out_best, fuelg_stats *stats);
 
+/* Many independent Lloyd k-means problems in one call.  No single
+ * counterpart in the reference (fuel runs one lloyd() at a time,
+ * src/cluster/kmeans/lloyd.rs:118-202); each problem gets exactly what
+ * fuelg_kmeans_lloyd (same order, same flags) returns for it: all problems'
+ * points are assigned by one persistent kernel per iteration over a work
+ * queue of 256-row items, sums of changed points are kept exactly, and the
+ * middle iterations run as one replayed CUDA graph.  Inputs are host or
+ * device arrays; per-problem results and status are written into the
+ * descriptors (status FUELG_ENOTSUP: data whose exponent range exceeds the
+ * exact 128-bit sums, or non-finite values). */
+typedef struct {
+  const float *data;   /* [n, d] */
+  int64_t n;
+  int32_t d;
+  int32_t k;
+  const float *init;   /* [k, d] initial centres */
+  float *out_centers;  /* [k, d] */
+  int64_t *out_labels; /* [n] */
+  int32_t out_iters;
+  int32_t status;
+  double out_inertia;
+} fuelg_kmeans_problem;
+int fuelg_kmeans_batched(fuelg_kmeans_problem *problems, int32_t count, int32_t max_iter, int32_t order,
+                         int32_t flags, fuelg_stats *stats);
+
 /* kNN serving with continuous batching over a resident index.  No
  * counterpart in the reference (fuel answers one call at a time); it serves
  * streams of independent query batches.  `workers` threads each own a CUDA

@@ -231,3 +231,33 @@ def test_knn_tc_large_k(gpu, oracle, k):
     g = gpu_knn(Xi, Xi, k, mode="linear", precision="bf16")
     c = oracle.knn(Xi, Xi, k, exclude="linear", threads=threads())
     assert_same(g, c)
+
+
+@pytest.mark.parametrize("d", [32, 64, 96, 128])
+@pytest.mark.parametrize("metric", ["sqeuclidean", "euclidean"])
+def test_knn_tc_split_general_data(gpu, oracle, d, metric):
+    """Split-BF16 (hi + lo) screen: bit-exact like every tier."""
+    rng = np.random.default_rng(d + 101)
+    X = rng.normal(size=(4000, d)).astype(np.float32)
+    Q = rng.normal(size=(257, d)).astype(np.float32)
+    ix = SearchIndex(X, distance=metric, tree="linear", precision="split_bf16")
+    for k in (1, 10, 100):
+        g = ix.knn(Q, k, exclude_self=False)
+        assert ix.last_stats["precision_used"] == 2
+        assert_same(g, oracle.knn(X, Q, k, metric=metric, threads=threads()))
+
+
+def test_knn_tc_split_unit_rows_certified(gpu, oracle):
+    """Unit-norm rows (d=96, the serving data): the split screen's error bound
+    is small enough that nearly every query is certified without the exact
+    rescan; results bit-exact."""
+    X = workloads.unit_normal_rows(60000, 96, seed=0)
+    Q = workloads.unit_normal_rows(300, 96, seed=5)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="split_bf16")
+    g = ix.knn(Q, 100, exclude_self=False)
+    st = ix.last_stats
+    assert st["precision_used"] == 2
+    kk2 = 100 + 12
+    redo = (st["rescored"] - 300 * kk2) / X.shape[0]
+    assert redo <= 0.02 * 300, f"{redo} of 300 queries needed the exact rescan"
+    assert_same(g, oracle.knn(X, Q, 100, threads=threads()))
