@@ -15,7 +15,7 @@ Run: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 Under torchrun (N>1) each rank runs an independent replica ("replicas only";
 the path is a single-device engine) and rank 0 prints one JSON line.
 
-python bench.py --profile lloyd|knn_tc|knn_plain|serving [--steps K] [--warmup W]
+python bench.py --profile lloyd|knn_tc|knn_plain|serving|batched [--steps K] [--warmup W]
 runs one workload alone (no CPU baseline, no side legs) for profiler
 captures; --knn-queries sets the query count of the kNN workloads there.
 """
@@ -42,6 +42,7 @@ REF_SAMPLE_ITERS = 10    # Lloyd iterations per reference-arm step (about 1 s of
 CPU_SAMPLE_ITERS = 100   # iterations of the CPU baseline leg (one full step, about 10 s)
 KNN_N, KNN_D, KNN_K = 1_000_000, 128, 100
 KNN_PLAIN_QUERIES = 20_000  # plain FP32 tier on a query subset (about 0.6 s)
+BATCH_PROBLEMS, BATCH_ITERS = 512, 20  # batched k-means: problems, fixed iterations
 SERVE_N, SERVE_D, SERVE_RATE = 2_000_000, 96, 2000.0  # resident index rows, dims, requests/s
 SERVE_SECONDS_TC, SERVE_SECONDS_PLAIN = 2.0, 0.05      # seconds of Poisson arrivals per tier
 
@@ -67,7 +68,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -255,6 +256,9 @@ def run_ours(args):
         alg_bytes = N * D * 4 + K * D * 4 + N * 8
         hot_name = "scan_topk_kernel (exact FP32 Lloyd assignment)"
     avg_launch_ms = hot_ms / max(1, hot_n)
+    # DRAM bytes (read + write) per launch of the split-BF16 screen on this
+    # workload, from an ncu capture of the same kernel: 233.8 MB + 3.2 MB
+    traffic = 237.0e6 if prec_used == 2 else None
     achieved = alg_bytes / (avg_launch_ms / 1e3) / 1e9
     hbm_peak = pk.get("hbm_gbs", 6800.0)
 
@@ -266,6 +270,9 @@ def run_ours(args):
 
     # kNN serving (continuous batching): p50 / p99 latency and queries/s
     serving = serving_rates() if not args.no_serving else None
+
+    # batched k-means (one call) vs one plain call per problem
+    batched = batched_rate() if not args.no_batched else None
 
     # CPU baseline: restated fuel CPU Lloyd on the host cores, bounded sample
     threads = os.cpu_count() or 1
@@ -284,7 +291,7 @@ def run_ours(args):
         "e2e": {"value": e2e_value, "unit": "iters/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": traffic,
                      "kernel": hot_name, "alg_bytes_per_launch": alg_bytes,
                      "avg_launch_ms": avg_launch_ms, "peak_source": "measured" if "_fallback" not in pk else
                      "fallback"},
@@ -300,6 +307,7 @@ def run_ours(args):
         "knn_plain": knn,
         "knn_tc": knn_tc,
         "knn_serving": serving,
+        "kmeans_batched": batched,
     }
     print(json.dumps(line), flush=True)
 
@@ -363,6 +371,11 @@ def knn_tc_rate(lib, _lib, torch, args, m_tc=None, plain=True, reps=1, n_index=K
         # tensor pipe: 2*m*n*dp flops in the screen kernel
         dp = ((d + 63) // 64) * 64
         out["screen_tflops"] = 2.0 * m_tc * n * dp / (hot * sts[-1].hot_kernel_launches / 1e3) / 1e12
+        pk = peaks()
+        tp = pk.get("bf16_tflops_sustained", 1700.0)  # the screen runs for tenths of a second
+        out["roofline"] = {"bound": "tensor", "achieved": out["screen_tflops"], "peak": tp, "unit": "TFLOP/s",
+                           "frac": out["screen_tflops"] / tp, "kernel": "knn_tc_kernel",
+                           "peak_source": "measured" if "_fallback" not in pk else "fallback"}
         if plain:
             mp = min(KNN_PLAIN_QUERIES, m_tc)
             call(min(mp, 2048), 0)
@@ -373,6 +386,36 @@ def knn_tc_rate(lib, _lib, torch, args, m_tc=None, plain=True, reps=1, n_index=K
         return out
     finally:
         lib.fuelg_index_destroy(h)
+
+
+def batched_rate(reps=1):
+    """Batched k-means: 512 Gaussian-mixture problems (n log-uniform in
+    [1e3, 2e5], d in {2, 8, 32, 64}, k log-uniform in [4, 256]), 20 fixed
+    Lloyd iterations, all in one engine call, against one plain FP32
+    fuelg_kmeans_lloyd call per problem.  Unit: problem-iterations/s."""
+    from fuel_gb300 import kmeans, kmeans_batched, workloads
+    descs = workloads.batched_kmeans_problems(count=BATCH_PROBLEMS, seed=0)
+    probs = [workloads.batched_kmeans_data(t) for t in descs]
+    kmeans_batched(probs[:8], max_iter=3, fixed_iters=True)  # warm-up
+    kmeans_batched(probs, max_iter=BATCH_ITERS, fixed_iters=True)  # launch-shape tuning for this mix
+    ms = []
+    for _ in range(reps):
+        kmeans_batched(probs, max_iter=BATCH_ITERS, fixed_iters=True)
+        ms.append(kmeans_batched.last_stats["device_ms"])
+    t = sum(ms) / len(ms)
+    hot = kmeans_batched.last_stats["hot_kernel_ms"]
+    plain_ms = 0.0
+    for X, init in probs:
+        r = kmeans(X, k=init.shape[0], variant="lloyd", init=init, max_iter=BATCH_ITERS, fixed_iters=True,
+                   precision="fp32")
+        plain_ms += r.stats["device_ms"]
+    pi = BATCH_PROBLEMS * BATCH_ITERS
+    return {"workload": f"batched k-means {BATCH_PROBLEMS} problems n~logU[1e3,2e5] d in {{2,8,32,64}} "
+                        f"k~logU[4,256], {BATCH_ITERS} fixed iterations",
+            "points": int(sum(d[0] for d in descs)), "ms_per_call": t, "iteration_loop_ms": hot,
+            "problem_iters_per_s": pi / (t / 1e3), "plain_per_problem_ms": plain_ms,
+            "plain_problem_iters_per_s": pi / (plain_ms / 1e3), "batched_vs_plain": plain_ms / t,
+            "kernel_launches": kmeans_batched.last_stats["kernel_launches"]}
 
 
 def serving_run(precision, seconds, X=None, seed=1):
@@ -461,6 +504,8 @@ def run_profile(args):
         print(json.dumps({"profile": "knn_tc", **r}))
     elif args.profile == "serving":
         print(json.dumps({"profile": "serving", **serving_rates()}))
+    elif args.profile == "batched":
+        print(json.dumps({"profile": "batched", **batched_rate()}))
     else:
         args.steps = max(1, args.steps)
         print(json.dumps({"profile": "knn_plain", **knn_plain_rate(lib, _lib, torch, args)}))
@@ -469,15 +514,16 @@ def run_profile(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="split_bf16")
-    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain", "serving"], default=None)
+    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain", "serving", "batched"], default=None)
     ap.add_argument("--iters", type=int, default=ITERS, help="Lloyd iterations per call (--profile lloyd)")
     ap.add_argument("--knn-queries", type=int, default=20_000, help="query count (--profile knn_tc)")
     ap.add_argument("--knn-n", type=int, default=KNN_N, help="index rows (--profile knn_tc)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched k-means leg")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
