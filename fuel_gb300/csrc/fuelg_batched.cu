@@ -49,7 +49,25 @@ struct BProb {
   int32_t d, k, L, e_lo;
   int32_t item_begin;  // first work item
   int32_t active;      // 0: skipped (bad data)
+  int64_t cost_begin;  // cumulative work before this problem's first item
+  int64_t item_cost;   // work of one item (~ k * d)
 };
+
+// First work item whose work offset is >= c (work offsets: the problem's
+// cost_begin + j * item_cost for its item j), so CTAs can take contiguous item
+// ranges of equal work instead of equal item counts.
+__device__ __forceinline__ int64_t item_at_cost(const BProb* __restrict__ probs, int P, int items_total, int64_t c) {
+  int lo = 0, hi = P;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (probs[mid].cost_begin <= c) lo = mid;
+    else hi = mid;
+  }
+  const BProb& pr = probs[lo];
+  const int64_t items = (lo + 1 < P ? probs[lo + 1].item_begin : items_total) - pr.item_begin;
+  const int64_t j = (c - pr.cost_begin + pr.item_cost - 1) / pr.item_cost;
+  return j >= items ? pr.item_begin + items : pr.item_begin + j;
+}
 
 template <int D>
 struct Dim {
@@ -108,14 +126,17 @@ template <int KIND, int ORDER>
 __global__ void __launch_bounds__(kItemRows) batched_assign_kernel(
     const BProb* __restrict__ probs, int P, int items_total, const float* __restrict__ X,
     const float* __restrict__ C, int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs,
-    int32_t* __restrict__ counts, int32_t* __restrict__ pchg, int first) {
+    int32_t* __restrict__ counts, int32_t* __restrict__ pchg, int first, int64_t work_total) {
   extern __shared__ __align__(16) unsigned char smem_b[];
   float* cs = reinterpret_cast<float*>(smem_b);                                           // [kCentreCap]
   unsigned long long* agg = reinterpret_cast<unsigned long long*>(cs + kCentreCap);      // [kAggCap]
   int* aggc = reinterpret_cast<int*>(agg + kAggCap);                                      // [256]
   __shared__ int s_chg;
-  const int64_t it0 = (int64_t)items_total * blockIdx.x / gridDim.x;
-  const int64_t it1 = (int64_t)items_total * (blockIdx.x + 1) / gridDim.x;
+  const int64_t it0 = item_at_cost(probs, P, items_total, (int64_t)((__int128)work_total * blockIdx.x / gridDim.x));
+  const int64_t it1 =
+      blockIdx.x + 1 == gridDim.x ? items_total
+                                  : item_at_cost(probs, P, items_total,
+                                                 (int64_t)((__int128)work_total * (blockIdx.x + 1) / gridDim.x));
   int p = -1;
   BProb pr{};
   bool staged = false, use_agg = false;
@@ -172,7 +193,19 @@ __global__ void __launch_bounds__(kItemRows) batched_assign_kernel(
         for (int t = 0; t < DD; t++) xv[t] = __ldg(xr + t);
         for (int c = 0; c < pr.k; c++) {
           const float* cc = cbase + c * DD;
-          const float dv = exact_dist_fn<KIND, ORDER, DD>([&](int t) { return xv[t]; }, [&](int t) { return cc[t]; });
+          // centre values by 16-byte (8-byte for d = 2) loads, one per 4 (2) values
+          auto cv = [&](int t) -> float {
+            if constexpr (DD % 4 == 0) {
+              const float4 v = reinterpret_cast<const float4*>(cc)[t >> 2];
+              return (t & 3) == 0 ? v.x : (t & 3) == 1 ? v.y : (t & 3) == 2 ? v.z : v.w;
+            } else if constexpr (DD % 2 == 0) {
+              const float2 v = reinterpret_cast<const float2*>(cc)[t >> 1];
+              return (t & 1) == 0 ? v.x : v.y;
+            } else {
+              return cc[t];
+            }
+          };
+          const float dv = exact_dist_fn<KIND, ORDER, DD>([&](int t) { return xv[t]; }, cv);
           if (best < 0 || dv < bd) {
             bd = dv;
             best = c;
@@ -390,6 +423,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   std::vector<int32_t> rblk(P + 1, 0);
   int64_t xs = 0, cs = 0, ls = 0, ks = 0, kd = 0;
   int64_t items = 0;
+  int64_t work = 0;
   int64_t rb = 0;
   for (int p = 0; p < P; p++) {
     const fuelg_kmeans_problem& q = probs[p];
@@ -401,6 +435,9 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     hp[p].d = q.d;
     hp[p].k = q.k;
     hp[p].item_begin = (int32_t)items;
+    hp[p].cost_begin = work;
+    hp[p].item_cost = (int64_t)q.k * q.d + 64;  // distance work + per-row overhead
+    work += hp[p].item_cost * ((q.n + kItemRows - 1) / kItemRows);
     xoff[p] = xs;
     kdb[p] = kd;
     rblk[p] = (int32_t)rb;
@@ -517,11 +554,11 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     if (first)
       k_init<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
                                            dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                           dPchg.as<int32_t>(), 1);
+                                           dPchg.as<int32_t>(), 1, work);
     else
       k_iter<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
                                            dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                           dPchg.as<int32_t>(), 0);
+                                           dPchg.as<int32_t>(), 0, work);
     note_launch();
     if (write || true) {
       batched_mean_kernel<<<mean_grid, 256, 0, s>>>(dProbs.as<BProb>(), P, dKdb.as<int64_t>(), kd,
