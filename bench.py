@@ -388,13 +388,13 @@ def knn_tc_rate(lib, _lib, torch, args, m_tc=None, plain=True, reps=1, n_index=K
         lib.fuelg_index_destroy(h)
 
 
-def batched_rate(reps=1):
+def batched_rate(reps=1, count=BATCH_PROBLEMS, plain=True):
     """Batched k-means: 512 Gaussian-mixture problems (n log-uniform in
     [1e3, 2e5], d in {2, 8, 32, 64}, k log-uniform in [4, 256]), 20 fixed
     Lloyd iterations, all in one engine call, against one plain FP32
     fuelg_kmeans_lloyd call per problem.  Unit: problem-iterations/s."""
     from fuel_gb300 import kmeans, kmeans_batched, workloads
-    descs = workloads.batched_kmeans_problems(count=BATCH_PROBLEMS, seed=0)
+    descs = workloads.batched_kmeans_problems(count=count, seed=0)
     probs = [workloads.batched_kmeans_data(t) for t in descs]
     kmeans_batched(probs[:8], max_iter=3, fixed_iters=True)  # warm-up
     kmeans_batched(probs, max_iter=BATCH_ITERS, fixed_iters=True)  # launch-shape tuning for this mix
@@ -405,12 +405,13 @@ def batched_rate(reps=1):
     t = sum(ms) / len(ms)
     hot = kmeans_batched.last_stats["hot_kernel_ms"]
     plain_ms = 0.0
-    for X, init in probs:
+    for X, init in (probs if plain else []):
         r = kmeans(X, k=init.shape[0], variant="lloyd", init=init, max_iter=BATCH_ITERS, fixed_iters=True,
                    precision="fp32")
         plain_ms += r.stats["device_ms"]
-    pi = BATCH_PROBLEMS * BATCH_ITERS
-    return {"workload": f"batched k-means {BATCH_PROBLEMS} problems n~logU[1e3,2e5] d in {{2,8,32,64}} "
+    pi = count * BATCH_ITERS
+    plain_ms = plain_ms or float("nan")
+    return {"workload": f"batched k-means {count} problems n~logU[1e3,2e5] d in {{2,8,32,64}} "
                         f"k~logU[4,256], {BATCH_ITERS} fixed iterations",
             "points": int(sum(d[0] for d in descs)), "ms_per_call": t, "iteration_loop_ms": hot,
             "problem_iters_per_s": pi / (t / 1e3), "plain_per_problem_ms": plain_ms,
@@ -505,7 +506,7 @@ def run_profile(args):
     elif args.profile == "serving":
         print(json.dumps({"profile": "serving", **serving_rates()}))
     elif args.profile == "batched":
-        print(json.dumps({"profile": "batched", **batched_rate()}))
+        print(json.dumps({"profile": "batched", **batched_rate(count=args.batched_problems, plain=False)}))
     else:
         args.steps = max(1, args.steps)
         print(json.dumps({"profile": "knn_plain", **knn_plain_rate(lib, _lib, torch, args)}))
@@ -524,6 +525,7 @@ def main():
     ap.add_argument("--knn-n", type=int, default=KNN_N, help="index rows (--profile knn_tc)")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched k-means leg")
+    ap.add_argument("--batched-problems", type=int, default=BATCH_PROBLEMS, help="problems (--profile batched)")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)

@@ -386,6 +386,43 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
     return ST_OK;
   };
 
+  // Middle passes (another pass follows) replay one captured CUDA graph of a
+  // pass from the fourth iteration on; the first ones run as plain launches so
+  // the screen kernel's launches are timed individually.
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphFree {
+    cudaGraphExec_t& g;
+    ~GraphFree() {
+      if (g) cudaGraphExecDestroy(g);
+    }
+  } gf{gexec};
+  int64_t graph_launches = 0;
+  auto graph_pass = [&]() -> int {
+    if (!gexec) {
+      HotTimer* saved = hot_timer();
+      hot_timer() = nullptr;
+      cudaGraph_t g = nullptr;
+      FUELG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
+      const int64_t l0 = launch_count();
+      const int rc = pass(false, true);
+      const cudaError_t ce = cudaStreamEndCapture(stream, &g);
+      hot_timer() = saved;
+      graph_launches = launch_count() - l0;
+      note_launch((int)-graph_launches);  // counted per replay
+      if (rc != ST_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      FUELG_CUDA(ce);
+      const cudaError_t ie = cudaGraphInstantiate(&gexec, g, 0);
+      cudaGraphDestroy(g);
+      FUELG_CUDA(ie);
+    }
+    FUELG_CUDA(cudaGraphLaunch(gexec, stream));
+    note_launch((int)graph_launches);
+    return ST_OK;
+  };
+
   const float* inertia_centers = C;
   FUELG_TRY(pass(true, p.max_iter > 1));
   int iters = 1;
@@ -406,7 +443,8 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
         break;
       }
     }
-    FUELG_TRY(pass(false, iters < p.max_iter));
+    if (iters >= 4 && iters < p.max_iter) FUELG_TRY(graph_pass());
+    else FUELG_TRY(pass(false, iters < p.max_iter));
     if (!p.fixed_iters) {
       FUELG_CUDA(cudaMemcpyAsync(h_changed, changed.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
       FUELG_CUDA(cudaStreamSynchronize(stream));
