@@ -68,7 +68,7 @@ SIGNATURES = {
     "fuelg_kmeans_lloyd": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _i32, _dbl, _i32, _i32, _i32, _vp, _vp,
                                           ctypes.POINTER(_i32), ctypes.POINTER(_dbl), ctypes.POINTER(Stats)]),
     "fuelg_lloyd_assign": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
-    "fuelg_kmeans_batched": (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32, ctypes.POINTER(Stats)]),
+    "fuelg_kmeans_batched": (ctypes.c_int, [_vp, _i32, _i32, _i32, _i32, _i32, ctypes.POINTER(Stats)]),
     "fuelg_server_create": (ctypes.c_int, [_vp, _i32, _i64, _i64, _i32, ctypes.POINTER(_vp)]),
     "fuelg_server_submit": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, ctypes.POINTER(_i64)]),
     "fuelg_server_wait": (ctypes.c_int, [_vp, _i64, _i32, ctypes.POINTER(_dbl)]),

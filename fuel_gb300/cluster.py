@@ -137,7 +137,7 @@ def lloyd_assign(data, centers, *, initial=False, order=None):
     return labels, best
 
 
-def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False):
+def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False, precision="split_bf16"):
     """Many independent Lloyd k-means problems in one engine call.
 
     ``problems``: iterable of ``(data float32[n, d], init float32[k, d])``.
@@ -145,7 +145,9 @@ def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False):
     ``kmeans(data, k=k, variant="lloyd", init=init, max_iter=max_iter,
     fixed_iters=fixed_iters)`` returns for that problem.  All problems'
     points are assigned by one persistent kernel per iteration and the
-    middle iterations run as one replayed CUDA graph.
+    middle iterations run as one replayed CUDA graph.  ``precision``
+    other than "fp32" screens problems with 32 <= d <= 64 and k <= 256 on
+    the tensor cores (exact re-score where undecided; same results).
     """
     order = order or _lib.default_order()
     keep, descs, outs = [], [], []
@@ -165,8 +167,8 @@ def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False):
     arr = (_lib.KMeansProblem * len(descs))(*descs)
     st = _lib.Stats()
     _lib.check(_lib.load().fuelg_kmeans_batched(ctypes.cast(arr, ctypes.c_void_p), len(descs), max(1, int(max_iter)),
-                                                _lib.ORDER[order], _lib.LLOYD_FIXED_ITERS if fixed_iters else 0,
-                                                ctypes.byref(st)))
+                                                _lib.ORDER[order], _lib.PRECISION[precision],
+                                                _lib.LLOYD_FIXED_ITERS if fixed_iters else 0, ctypes.byref(st)))
     res = []
     for desc, (centers, labels) in zip(arr, outs):
         if desc.status != _lib.OK:

@@ -31,6 +31,7 @@
 #include "fuelg_common.cuh"
 #include "fuelg_exact.cuh"
 #include "fuelg_internal.h"
+#include "fuelg_tc_common.cuh"
 
 namespace fuelg {
 namespace {
@@ -51,6 +52,8 @@ struct BProb {
   int32_t active;      // 0: skipped (bad data)
   int64_t cost_begin;  // cumulative work before this problem's first item
   int64_t item_cost;   // work of one item (~ k * d)
+  int32_t all_item_begin;  // first 256-row item over all problems (inertia)
+  int32_t tc;              // assigned by the tensor-core screen (no CUDA-core items)
 };
 
 // First work item whose work offset is >= c (work offsets: the problem's
@@ -295,7 +298,8 @@ __global__ void batched_mean_kernel(const BProb* __restrict__ probs, int P, cons
 // After each pass: record the iteration and convergence, reset the change
 // counters.  iter[0] counts passes (the initial one is 1).
 __global__ void batched_step_kernel(int P, int32_t* __restrict__ pchg, int32_t* __restrict__ conv,
-                                    int32_t* __restrict__ last_chg, int32_t* __restrict__ iter) {
+                                    int32_t* __restrict__ last_chg, int32_t* __restrict__ iter,
+                                    int* __restrict__ und_n) {
   const int it = iter[0] + 1;
   for (int p = threadIdx.x; p < P; p += blockDim.x) {
     const int c = pchg[p];
@@ -304,7 +308,10 @@ __global__ void batched_step_kernel(int P, int32_t* __restrict__ pchg, int32_t* 
     pchg[p] = 0;
   }
   __syncthreads();
-  if (threadIdx.x == 0) iter[0] = it;
+  if (threadIdx.x == 0) {
+    iter[0] = it;
+    *und_n = 0;
+  }
 }
 
 // FP64 sum of squared distances to the final centres, per problem.
@@ -315,12 +322,11 @@ __global__ void batched_inertia_kernel(const BProb* __restrict__ probs, int P, i
     int lo = 0, hi = P;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
-      if (probs[mid].item_begin <= item) lo = mid;
+      if (probs[mid].all_item_begin <= item) lo = mid;
       else hi = mid;
     }
-    while (lo + 1 < P && probs[lo + 1].item_begin <= item) lo++;
     const BProb& pr = probs[lo];
-    const int64_t i = (item - pr.item_begin) * kItemRows + threadIdx.x;
+    const int64_t i = (item - pr.all_item_begin) * kItemRows + threadIdx.x;
     double s = 0.0;
     if (pr.active && i < pr.n) {
       const float* x = X + pr.x_off + i * pr.d;
@@ -333,6 +339,343 @@ __global__ void batched_inertia_kernel(const BProb* __restrict__ probs, int P, i
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     if ((threadIdx.x & 31) == 0 && s != 0.0) atomicAdd(&inertia[lo], s);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core tier for problems with 32 <= d <= 64 and k <= 256: each
+// 128-row item of a problem is screened with split-BF16 products (x_hi c_hi +
+// x_hi c_lo + x_lo c_hi, one 64-wide K chunk, FP32 accumulators in TMEM)
+// against the problem's centres staged in shared memory; a row is decided
+// when every other centre's lower bound exceeds the best centre's upper bound
+// (the error bound of the single-problem screen), otherwise its candidate
+// centres are re-scored with fuel's exact f32 arithmetic.  Labels are
+// therefore identical to the CUDA-core tier.
+// ---------------------------------------------------------------------------
+constexpr int kTcRows = 128;
+
+struct BTcArgs {
+  const int32_t* tcp;         // problem ids served here
+  const int32_t* item_begin;  // [ntc + 1] first 128-row item of each
+  int ntc, items;
+  float alpha;                // operand + accumulation error per |x||c|
+  int* status;
+  unsigned long long* undecided;  // rows re-scored exactly (count over the call)
+  int32_t* und_p;                 // this pass's undecided rows: problem, row
+  int32_t* und_i;
+  int* und_n;
+};
+
+
+// |v|^2 in FP32 as 8 interleaved chains + a 3-level tree (error <= (ceil(d/8) + 3) u |v|^2).
+template <class F>
+__device__ __forceinline__ float norm2_blocked(F v, int d) {
+  float p[8];
+#pragma unroll
+  for (int l = 0; l < 8; l++) p[l] = 0.0f;
+  for (int e = 0; e < d; e += 8) {
+#pragma unroll
+    for (int l = 0; l < 8; l++)
+      if (e + l < d) {
+        const float x = v(e + l);
+        p[l] = fmaf(x, x, p[l]);
+      }
+  }
+  return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
+}
+
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(kTcRows, 2) batched_tc_assign_kernel(
+    const BProb* __restrict__ probs, BTcArgs ta, const float* __restrict__ X, const float* __restrict__ C,
+    int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs, int32_t* __restrict__ counts,
+    int32_t* __restrict__ pchg, int first) {
+  extern __shared__ __align__(1024) unsigned char smem_t[];
+  unsigned char* base =
+      reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_t) + 1023) & ~(uintptr_t)1023);
+  unsigned char* sAh = base;                 // [128 rows][64] bf16, SW128
+  unsigned char* sAl = base + 16384;
+  unsigned char* sBh = base + 32768;         // [256 centres][64] bf16, SW128
+  unsigned char* sBl = base + 65536;
+  float* cn2 = reinterpret_cast<float*>(base + 98304);  // [256] |c|^2
+  float* cn = cn2 + 256;                                 // [256] |c|
+  float* xn2 = cn + 256;                                 // [128] |x|^2
+  float* cmax = xn2 + 128;                               // [2] max |c|^2, max |c| of the problem
+  uint64_t* bar = reinterpret_cast<uint64_t*>(cmax + 2);
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bar + 1);
+  int* s_flag = reinterpret_cast<int*>(tmem_holder + 1);  // [0] change count, [1] abort
+  const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) {
+    tcx::mbar_init(bar, 1);
+    s_flag[0] = 0;
+    s_flag[1] = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tcx::smem_u32(tmem_holder)),
+                 "r"(256)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tcx::tc_fence_before();
+  __syncthreads();
+  tcx::tc_fence_after();
+  const uint32_t tmem = *tmem_holder;
+  const int64_t it0 = (int64_t)ta.items * blockIdx.x / gridDim.x;
+  const int64_t it1 = (int64_t)ta.items * (blockIdx.x + 1) / gridDim.x;
+  const double u24 = 5.9604644775390625e-08;
+  int q = -1, p = -1, kp = 0;
+  BProb pr{};
+  float beta = 0.0f, gamma = 0.0f;
+  uint32_t phase = 0;
+  auto flush_chg = [&]() {
+    __syncthreads();
+    if (tid == 0 && p >= 0 && s_flag[0]) atomicAdd(&pchg[p], s_flag[0]);
+    __syncthreads();
+    if (tid == 0) s_flag[0] = 0;
+  };
+  for (int64_t item = it0; item < it1; item++) {
+    if (q < 0 || (q + 1 < ta.ntc && item >= ta.item_begin[q + 1])) {
+      flush_chg();
+      int lo = 0, hi = ta.ntc;
+      while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (ta.item_begin[mid] <= item) lo = mid;
+        else hi = mid;
+      }
+      q = lo;
+      p = ta.tcp[q];
+      pr = probs[p];
+      kp = (pr.k + 15) & ~15;
+      beta = (float)(((pr.d + 7) / 8 + 3 + 9) * u24 * 1.01);
+      gamma = (float)((pr.d + 4) * u24 * 1.01);
+      if (pr.active) {
+        // centres -> BF16 hi / lo in the SW128 layout (zero padded), FP32 norms
+        for (int e = tid; e < kp * 8; e += kTcRows) {
+          const int j = e >> 3, ch = e & 7;
+          uint32_t hw[4], lw[4];
+#pragma unroll
+          for (int l = 0; l < 8; l += 2) {
+            const int t0 = 8 * ch + l;
+            const float c0 = (j < pr.k && t0 < pr.d) ? C[pr.c_off + (int64_t)j * pr.d + t0] : 0.0f;
+            const float c1 = (j < pr.k && t0 + 1 < pr.d) ? C[pr.c_off + (int64_t)j * pr.d + t0 + 1] : 0.0f;
+            const __nv_bfloat162 h = __floats2bfloat162_rn(c0, c1);
+            const float2 hf = __bfloat1622float2(h);
+            const __nv_bfloat162 lo = __floats2bfloat162_rn(c0 - hf.x, c1 - hf.y);
+            hw[l / 2] = *reinterpret_cast<const uint32_t*>(&h);
+            lw[l / 2] = *reinterpret_cast<const uint32_t*>(&lo);
+          }
+          const uint32_t off = (uint32_t)j * 128u + ((uint32_t)(ch ^ (j & 7)) << 4);
+          *reinterpret_cast<uint4*>(sBh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(sBl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+        if (tid == 0) cmax[0] = cmax[1] = 0.0f;
+        __syncthreads();
+        float m2 = 0.0f;
+        for (int j = tid; j < pr.k; j += kTcRows) {
+          const float* cj = C + pr.c_off + (int64_t)j * pr.d;
+          const float v = norm2_blocked([&](int t) { return cj[t]; }, pr.d);
+          cn2[j] = v;
+          cn[j] = sqrtf(v);
+          m2 = fmaxf(m2, v);
+        }
+        // non-negative floats order like their bit patterns
+        atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m2));
+        __syncthreads();
+        if (tid == 0) cmax[1] = sqrtf(cmax[0]);
+      }
+      __syncthreads();
+    }
+    if (!pr.active) continue;
+    // rows -> BF16 hi / lo (zero padded), FP32 norms; thread = row
+    const int64_t i = (item - ta.item_begin[q]) * kTcRows + tid;
+    const bool live = i < pr.n;
+    const float* xr = X + pr.x_off + (live ? i : 0) * pr.d;
+    // 8 chunks of 8 values: BF16 hi / lo packed into 16-byte stores at the
+    // swizzled chunk position; |x|^2 accumulated in the blocked order
+    float pn[8];
+#pragma unroll
+    for (int l = 0; l < 8; l++) pn[l] = 0.0f;
+    const bool vec = ((pr.d & 3) == 0) && ((pr.x_off & 3) == 0);
+#pragma unroll 2
+    for (int j = 0; j < 8; j++) {
+      float x[8];
+      if (live && vec && 8 * j + 7 < pr.d) {
+        const float4 a4 = __ldg(reinterpret_cast<const float4*>(xr + 8 * j));
+        const float4 b4 = __ldg(reinterpret_cast<const float4*>(xr + 8 * j + 4));
+        x[0] = a4.x, x[1] = a4.y, x[2] = a4.z, x[3] = a4.w, x[4] = b4.x, x[5] = b4.y, x[6] = b4.z, x[7] = b4.w;
+      } else {
+#pragma unroll
+        for (int l = 0; l < 8; l++) x[l] = (live && 8 * j + l < pr.d) ? __ldg(xr + 8 * j + l) : 0.0f;
+      }
+      uint32_t hw[4], lw[4];
+#pragma unroll
+      for (int l = 0; l < 8; l += 2) {
+        const __nv_bfloat162 h = __floats2bfloat162_rn(x[l], x[l + 1]);
+        const float2 hf = __bfloat1622float2(h);
+        const __nv_bfloat162 lo = __floats2bfloat162_rn(x[l] - hf.x, x[l + 1] - hf.y);
+        hw[l / 2] = *reinterpret_cast<const uint32_t*>(&h);
+        lw[l / 2] = *reinterpret_cast<const uint32_t*>(&lo);
+        pn[l] = fmaf(x[l], x[l], pn[l]);
+        pn[l + 1] = fmaf(x[l + 1], x[l + 1], pn[l + 1]);
+      }
+      const uint32_t off = (uint32_t)tid * 128u + ((uint32_t)(j ^ (tid & 7)) << 4);
+      *reinterpret_cast<uint4*>(sAh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      *reinterpret_cast<uint4*>(sAl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+    }
+    const float nx = ((pn[0] + pn[1]) + (pn[2] + pn[3])) + ((pn[4] + pn[5]) + (pn[6] + pn[7]));
+    xn2[tid] = nx;
+    // generic-proxy smem writes -> visible to the tensor core's async proxy
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tcx::tc_fence_before();
+    __syncthreads();
+    tcx::tc_fence_after();
+    if (tid == 0) {
+      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kp >> 3) << 17) |
+                             ((uint32_t)(kTcRows >> 4) << 24);
+      const uint64_t ah = tcx::smem_desc_sw128(tcx::smem_u32(sAh)), al = tcx::smem_desc_sw128(tcx::smem_u32(sAl));
+      const uint64_t bh = tcx::smem_desc_sw128(tcx::smem_u32(sBh)), bl = tcx::smem_desc_sw128(tcx::smem_u32(sBl));
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) tcx::umma_bf16(tmem, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : 0u);
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) tcx::umma_bf16(tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
+#pragma unroll
+      for (int kk = 0; kk < 4; kk++) tcx::umma_bf16(tmem, al + 2 * kk, bh + 2 * kk, idesc, 1u);
+      tcx::umma_commit(bar);
+    }
+    const bool ok = tcx::mbar_wait(bar, phase, reinterpret_cast<volatile int*>(s_flag + 1));
+    phase ^= 1;
+    if (__syncthreads_or(!ok)) {
+      if (tid == 0) atomicOr(ta.status, DEV_TIMEOUT);
+      break;
+    }
+    tcx::tc_fence_after();
+    // screen: best centre, then every centre whose lower bound reaches its
+    // upper bound; TMEM read 64 columns per wait
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    const float xl = sqrtf(nx);
+    float best = __int_as_float(0x7f800000);
+    int bj = 0;
+    for (int c0 = 0; c0 < kp; c0 += 64) {
+      uint32_t r[4][16];
+#pragma unroll
+      for (int h = 0; h < 4; h++) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+      tcx::tmem_ld_wait();
+#pragma unroll
+      for (int h = 0; h < 4; h++)
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = c0 + 16 * h + j;
+          if (col < pr.k) {
+            const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
+            if (dt < best) {
+              best = dt;
+              bj = col;
+            }
+          }
+        }
+    }
+    const float hi_b = best + (ta.alpha * xl * cn[bj] + beta * (nx + cn2[bj])) * (1.0f + gamma) + gamma * fabsf(best);
+    // columns above T cannot reach hi_b even with the largest error of the
+    // problem (norm maxima); only the others get the exact per-column test
+    const float amax = (ta.alpha * xl * cmax[1] + beta * (nx + cmax[0])) * (1.0f + gamma);
+    const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
+    bool undecided = false;
+    for (int c0 = 0; c0 < kp; c0 += 64) {
+      uint32_t r[4][16];
+#pragma unroll
+      for (int h = 0; h < 4; h++) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+      tcx::tmem_ld_wait();
+#pragma unroll
+      for (int h = 0; h < 4; h++)
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = c0 + 16 * h + j;
+          const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col < 256 ? col : 0]);
+          if (col < pr.k && col != bj && (!(T > 0.0f) || !(dt > T))) {
+            const float e = (ta.alpha * xl * cn[col] + beta * (nx + cn2[col])) * (1.0f + gamma) + gamma * fabsf(dt);
+            if (!(dt - e > hi_b)) undecided = true;
+          }
+        }
+    }
+    tcx::tc_fence_before();
+    int lab = bj;
+    {
+      const unsigned um = __ballot_sync(0xffffffffu, live && undecided);
+      if ((tid & 31) == 0 && um) atomicAdd(ta.undecided, (unsigned long long)__popc(um));
+    }
+    if (live && undecided) {
+      // the exact re-score kernel decides this row
+      const int u = atomicAdd(ta.und_n, 1);
+      ta.und_p[u] = p;
+      ta.und_i[u] = (int32_t)i;
+    }
+    const int old = live ? (first ? -1 : labels[pr.lab_off + i]) : -1;
+    if (live && !undecided && lab != old) {
+      labels[pr.lab_off + i] = lab;
+      if (!first) atomicAdd(&s_flag[0], 1);
+      atomicAdd(&counts[pr.cnt_off + lab], 1);
+      if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
+      for (int t = 0; t < pr.d; t++) {
+        const float xv = __ldg(xr + t);
+        add_coord(limbs + pr.limb_off + ((int64_t)lab * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
+        if (old >= 0) add_coord(limbs + pr.limb_off + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+      }
+    }
+    __syncthreads();  // TMEM and the A tile are reused by the next item
+  }
+  flush_chg();
+  tcx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tcx::tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+  }
+}
+
+// Exact assignment of the rows the tensor-core screen left undecided: one
+// warp per row, lanes over the centres (fuel's f32 operation order), the
+// smallest (distance, index) key wins -- the first minimum, as in the
+// CUDA-core pass -- then the row's sums move if its label changed.
+template <int KIND, int ORDER>
+__global__ void __launch_bounds__(256) batched_rescore_kernel(
+    const BProb* __restrict__ probs, const int32_t* __restrict__ und_p, const int32_t* __restrict__ und_i,
+    const int* __restrict__ und_n, const float* __restrict__ X, const float* __restrict__ C,
+    int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs, int32_t* __restrict__ counts,
+    int32_t* __restrict__ pchg, int first) {
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int cnt = *und_n;
+  for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < cnt; u += nw) {
+    const int p = und_p[u];
+    const int64_t i = und_i[u];
+    const BProb& pr = probs[p];
+    const float* xr = X + pr.x_off + i * pr.d;
+    uint64_t best = ~0ull;
+    for (int c = lane; c < pr.k; c += 32) {
+      const float dv = exact_dist_scalar<KIND, ORDER>(xr, C + pr.c_off + (int64_t)c * pr.d, pr.d);
+      const uint64_t key = ((uint64_t)__float_as_uint(dv) << 32) | (uint32_t)c;
+      best = key < best ? key : best;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const uint64_t v = ((uint64_t)__shfl_xor_sync(0xffffffffu, (uint32_t)(best >> 32), o) << 32) |
+                         __shfl_xor_sync(0xffffffffu, (uint32_t)best, o);
+      best = v < best ? v : best;
+    }
+    const int lab = (int)(uint32_t)best;
+    const int old = first ? -1 : labels[pr.lab_off + i];
+    if (lab == old) continue;
+    if (lane == 0) {
+      labels[pr.lab_off + i] = lab;
+      if (!first) atomicAdd(&pchg[p], 1);
+      atomicAdd(&counts[pr.cnt_off + lab], 1);
+      if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
+    }
+    for (int t = lane; t < pr.d; t += 32) {
+      const float xv = __ldg(xr + t);
+      add_coord(limbs + pr.limb_off + ((int64_t)lab * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
+      if (old >= 0) add_coord(limbs + pr.limb_off + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+    }
   }
 }
 
@@ -371,13 +714,17 @@ std::map<std::vector<int>, Tuned> g_tuned;
 using namespace fuelg;
 
 extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, int32_t max_iter, int32_t order,
-                                    int32_t flags, fuelg_stats* stats) {
+                                    int32_t precision, int32_t flags, fuelg_stats* stats) {
   if (count < 0 || (count > 0 && !probs) || max_iter < 1) {
     set_error("invalid batched kmeans arguments count=%d max_iter=%d", count, max_iter);
     return ST_EINVAL;
   }
   if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
     set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16) {
+    set_error("unknown precision tier %d", precision);
     return ST_EINVAL;
   }
   for (int p = 0; p < count; p++) {
@@ -422,8 +769,11 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   std::vector<int64_t> xoff(P + 1, 0), kdb(P + 1, 0);
   std::vector<int32_t> rblk(P + 1, 0);
   int64_t xs = 0, cs = 0, ls = 0, ks = 0, kd = 0;
-  int64_t items = 0;
+  int64_t items = 0;      // CUDA-core 256-row items
+  int64_t all_items = 0;  // 256-row items of every problem (inertia)
   int64_t work = 0;
+  std::vector<int32_t> tcp, tc_begin;  // tensor-core problems and their 128-row item starts
+  int64_t tc_items = 0, tc_rows = 0;
   int64_t rb = 0;
   for (int p = 0; p < P; p++) {
     const fuelg_kmeans_problem& q = probs[p];
@@ -434,29 +784,42 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     hp[p].cnt_off = (int32_t)ks;
     hp[p].d = q.d;
     hp[p].k = q.k;
+    // tensor-core tier: split-BF16 screen for 32 <= d <= 64, k <= 256
+    hp[p].tc = (precision != FUELG_PREC_FP32 && q.d >= 32 && q.d <= 64 && q.k <= 256) ? 1 : 0;
     hp[p].item_begin = (int32_t)items;
+    hp[p].all_item_begin = (int32_t)all_items;
     hp[p].cost_begin = work;
     hp[p].item_cost = (int64_t)q.k * q.d + 64;  // distance work + per-row overhead
-    work += hp[p].item_cost * ((q.n + kItemRows - 1) / kItemRows);
+    const int64_t its = hp[p].tc ? 0 : (q.n + kItemRows - 1) / kItemRows;
+    work += hp[p].item_cost * its;
+    all_items += (q.n + kItemRows - 1) / kItemRows;
+    if (hp[p].tc) {
+      tcp.push_back(p);
+      tc_begin.push_back((int32_t)tc_items);
+      tc_items += (q.n + kTcRows - 1) / kTcRows;
+      tc_rows += q.n;
+    }
     xoff[p] = xs;
     kdb[p] = kd;
     rblk[p] = (int32_t)rb;
-    xs += q.n * q.d;
+    xs += (q.n * q.d + 3) & ~3ll;  // 16-byte aligned rows for d % 4 == 0
     cs += (int64_t)q.k * q.d;
     ls += q.n;
     ks += q.k;
     kd += (int64_t)q.k * q.d;
-    items += (q.n + kItemRows - 1) / kItemRows;
+    items += its;
     rb += (q.n * q.d + 65535) / 65536;
   }
   xoff[P] = xs;
   kdb[P] = kd;
   rblk[P] = (int32_t)rb;
-  if (items >= (1ll << 31)) {
+  tc_begin.push_back((int32_t)tc_items);
+  if (all_items >= (1ll << 31) || tc_items >= (1ll << 31)) {
     set_error("batch too large");
     return ST_ENOTSUP;
   }
-  DevBuf dX, dC, dLab, dCnt, dOff, dRb, dRange, dProbs, dKdb, dPchg, dConv, dLast, dIter, dInert, dLimbs;
+  DevBuf dX, dC, dLab, dCnt, dOff, dRb, dRange, dProbs, dKdb, dPchg, dConv, dLast, dIter, dInert, dLimbs, dTcp,
+      dTcb, dSt, dUnd;
   FUELG_TRY(dX.alloc(sizeof(float) * xs));
   FUELG_TRY(dC.alloc(sizeof(float) * cs));
   FUELG_TRY(dLab.alloc(sizeof(int32_t) * ls));
@@ -464,6 +827,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   FUELG_TRY(dOff.alloc(sizeof(int64_t) * (P + 1)));
   FUELG_TRY(dRb.alloc(sizeof(int32_t) * (P + 1)));
   FUELG_TRY(dRange.alloc(sizeof(int) * 3 * P));
+  FUELG_CUDA(cudaMemsetAsync(dX.p, 0, sizeof(float) * xs, s));  // alignment padding between problems reads as 0
   for (int p = 0; p < P; p++) {
     FUELG_CUDA(cudaMemcpyAsync(dX.as<float>() + hp[p].x_off, probs[p].data, sizeof(float) * probs[p].n * probs[p].d,
                                cudaMemcpyDefault, s));
@@ -514,6 +878,13 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   FUELG_TRY(dIter.alloc(sizeof(int32_t)));
   FUELG_TRY(dInert.alloc(sizeof(double) * P));
   FUELG_CUDA(cudaMemcpyAsync(dProbs.p, hp.data(), sizeof(BProb) * P, cudaMemcpyHostToDevice, s));
+  const int ntc = (int)tcp.size();
+  FUELG_TRY(dTcp.alloc(sizeof(int32_t) * std::max(1, ntc)));
+  FUELG_TRY(dTcb.alloc(sizeof(int32_t) * (ntc + 1)));
+  FUELG_TRY(dSt.alloc(sizeof(int) * 4));
+  if (ntc) FUELG_CUDA(cudaMemcpyAsync(dTcp.p, tcp.data(), sizeof(int32_t) * ntc, cudaMemcpyHostToDevice, s));
+  FUELG_CUDA(cudaMemcpyAsync(dTcb.p, tc_begin.data(), sizeof(int32_t) * (ntc + 1), cudaMemcpyHostToDevice, s));
+  FUELG_CUDA(cudaMemsetAsync(dSt.p, 0, sizeof(int) * 4, s));
   FUELG_CUDA(cudaMemcpyAsync(dKdb.p, kdb.data(), sizeof(int64_t) * (P + 1), cudaMemcpyHostToDevice, s));
   FUELG_CUDA(cudaMemsetAsync(dLimbs.p, 0, sizeof(unsigned long long) * limbs_total, s));
   FUELG_CUDA(cudaMemsetAsync(dCnt.p, 0, sizeof(int32_t) * ks, s));
@@ -529,6 +900,33 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
                                          : batched_assign_kernel<KIND_SQDIST, ORDER_ARM>;
   FUELG_CUDA(cudaFuncSetAttribute(k_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   FUELG_CUDA(cudaFuncSetAttribute(k_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto t_init = order == FUELG_ORDER_X86 ? batched_tc_assign_kernel<KIND_PAIRWISE, ORDER_X86>
+                                         : batched_tc_assign_kernel<KIND_PAIRWISE, ORDER_ARM>;
+  auto t_iter = order == FUELG_ORDER_X86 ? batched_tc_assign_kernel<KIND_SQDIST, ORDER_X86>
+                                         : batched_tc_assign_kernel<KIND_SQDIST, ORDER_ARM>;
+  const size_t tsmem = 1024 + 98304 + sizeof(float) * (256 * 2 + 128 + 2) + 64;
+  FUELG_CUDA(cudaFuncSetAttribute(t_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+  FUELG_CUDA(cudaFuncSetAttribute(t_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
+  BTcArgs ta{};
+  ta.tcp = dTcp.as<int32_t>();
+  ta.item_begin = dTcb.as<int32_t>();
+  ta.ntc = ntc;
+  ta.items = (int)tc_items;
+  {
+    // operand rounding of hi + lo (3.01 * 2^-16) + FP32 accumulation of 3 x 64 products
+    const double rel = 3.01 * std::ldexp(1.0, -16) + 3.0 * 64 * std::ldexp(1.0, -23) * (1.0 + std::ldexp(1.0, -7));
+    ta.alpha = (float)(2.0 * rel * 1.01);
+  }
+  ta.status = dSt.as<int>();
+  ta.undecided = reinterpret_cast<unsigned long long*>(dSt.as<int>() + 2);
+  ta.und_n = dSt.as<int>() + 1;
+  FUELG_TRY(dUnd.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, tc_rows)));
+  ta.und_p = dUnd.as<int32_t>();
+  ta.und_i = dUnd.as<int32_t>() + std::max<int64_t>(1, tc_rows);
+  auto r_init = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_PAIRWISE, ORDER_X86>
+                                         : batched_rescore_kernel<KIND_PAIRWISE, ORDER_ARM>;
+  auto r_iter = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_SQDIST, ORDER_X86>
+                                         : batched_rescore_kernel<KIND_SQDIST, ORDER_ARM>;
   int sms = 152;
   {
     int dev = 0;
@@ -546,28 +944,43 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     if (it != g_tuned.end()) bps = it->second.blocks_per_sm;
   }
   auto grid_for = [&](int b) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)sms * b)); };
+  const unsigned tc_grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tc_items, (int64_t)sms * 2));
   const unsigned mean_grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((kd + 255) / 256, (int64_t)sms * 8));
   const int fixed = (flags & FUELG_LLOYD_FIXED_ITERS) ? 1 : 0;
   (void)fixed;  // every pass runs; the reported count follows the changed == 0 stop unless fixed
 
   auto pass = [&](bool first, bool write, unsigned grid) -> int {
-    if (first)
-      k_init<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
-                                           dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                           dPchg.as<int32_t>(), 1, work);
-    else
-      k_iter<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
-                                           dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                           dPchg.as<int32_t>(), 0, work);
-    note_launch();
-    if (write || true) {
-      batched_mean_kernel<<<mean_grid, 256, 0, s>>>(dProbs.as<BProb>(), P, dKdb.as<int64_t>(), kd,
-                                                    dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                                    dC.as<float>(), write ? 1 : 0);
+    if (items > 0) {
+      if (first)
+        k_init<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
+                                             dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
+                                             dPchg.as<int32_t>(), 1, work);
+      else
+        k_iter<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
+                                             dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
+                                             dPchg.as<int32_t>(), 0, work);
       note_launch();
     }
+    if (tc_items > 0) {
+      (first ? t_init : t_iter)<<<tc_grid, kTcRows, tsmem, s>>>(dProbs.as<BProb>(), ta, dX.as<float>(),
+                                                                 dC.as<float>(), dLab.as<int32_t>(),
+                                                                 dLimbs.as<unsigned long long>(),
+                                                                 dCnt.as<int32_t>(), dPchg.as<int32_t>(),
+                                                                 first ? 1 : 0);
+      note_launch();
+      (first ? r_init : r_iter)<<<sms * 8, 256, 0, s>>>(dProbs.as<BProb>(), ta.und_p, ta.und_i, ta.und_n,
+                                                        dX.as<float>(), dC.as<float>(), dLab.as<int32_t>(),
+                                                        dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
+                                                        dPchg.as<int32_t>(), first ? 1 : 0);
+      note_launch();
+    }
+    // canonical counters every pass; new centres only when another pass follows
+    batched_mean_kernel<<<mean_grid, 256, 0, s>>>(dProbs.as<BProb>(), P, dKdb.as<int64_t>(), kd,
+                                                  dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(), dC.as<float>(),
+                                                  write ? 1 : 0);
+    note_launch();
     batched_step_kernel<<<1, 512, 0, s>>>(P, dPchg.as<int32_t>(), dConv.as<int32_t>(), dLast.as<int32_t>(),
-                                          dIter.as<int32_t>());
+                                          dIter.as<int32_t>(), dSt.as<int>() + 1);
     note_launch();
     FUELG_CUDA(cudaGetLastError());
     return ST_OK;
@@ -642,8 +1055,8 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   }
   cudaEventRecord(evh1, s);
   {
-    const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)sms * 8));
-    batched_inertia_kernel<<<ig, kItemRows, 0, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(),
+    const unsigned ig = (unsigned)std::max<int64_t>(1, std::min<int64_t>(all_items, (int64_t)sms * 8));
+    batched_inertia_kernel<<<ig, kItemRows, 0, s>>>(dProbs.as<BProb>(), P, (int)all_items, dX.as<float>(),
                                                     dC.as<float>(), dLab.as<int32_t>(), dInert.as<double>());
     note_launch();
     FUELG_CUDA(cudaGetLastError());
@@ -658,8 +1071,17 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   for (int p = 0; p < P; p++)
     FUELG_CUDA(cudaMemcpyAsync(probs[p].out_centers, dC.as<float>() + hp[p].c_off,
                                sizeof(float) * probs[p].k * probs[p].d, cudaMemcpyDefault, s));
+  int hst4[4] = {0, 0, 0, 0};
+  FUELG_CUDA(cudaMemcpyAsync(hst4, dSt.p, sizeof(hst4), cudaMemcpyDeviceToHost, s));
   cudaEventRecord(ev1, s);
   FUELG_CUDA(cudaStreamSynchronize(s));
+  const int hst = hst4[0];
+  unsigned long long undecided_rows = 0;
+  memcpy(&undecided_rows, hst4 + 2, sizeof(undecided_rows));
+  if (hst & DEV_TIMEOUT) {
+    set_error("a device wait timed out");
+    return ST_ETIMEOUT;
+  }
   int64_t d2h = (int64_t)sizeof(int32_t) * ls + (int64_t)sizeof(float) * cs;
   for (int p = 0; p < P; p++) {
     fuelg_kmeans_problem& q = probs[p];
@@ -688,6 +1110,8 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     for (int p = 0; p < P; p++) evals += hp[p].n * hp[p].k;
     stats->distance_evals = evals * max_iter;
     stats->iterations = max_iter;
+    stats->rescored = (int64_t)undecided_rows;
+    stats->precision_used = tc_items > 0 ? precision : 0;
     stats->kernel_launches = (int32_t)(launch_count() - launches0);
   }
   return ST_OK;

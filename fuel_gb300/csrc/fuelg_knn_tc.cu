@@ -475,15 +475,23 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
             f[4 * v + 2] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z);
             f[4 * v + 3] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w);
           }
-          float mn = f[0];
+          // minimum and pass mask as 4-level trees (short dependency chains)
+          float m8[8];
 #pragma unroll
-          for (int j = 1; j < 16; j++) mn = fminf(mn, f[j]);
+          for (int j = 0; j < 8; j++) m8[j] = fminf(f[2 * j], f[2 * j + 1]);
+#pragma unroll
+          for (int j = 0; j < 4; j++) m8[j] = fminf(m8[2 * j], m8[2 * j + 1]);
+          const float mn = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
           if (mn <= thr) {
             // the few passing columns, one loop trip each; the screened
             // distance is D~ = |q|^2 + (|x|^2 - 2 q.x) in f32
-            unsigned mask = 0;
+            unsigned b8[8];
 #pragma unroll
-            for (int j = 0; j < 16; j++) mask |= (f[j] <= thr ? 1u : 0u) << j;
+            for (int j = 0; j < 8; j++)
+              b8[j] = (f[2 * j] <= thr ? 1u : 0u) | (f[2 * j + 1] <= thr ? 2u : 0u);
+#pragma unroll
+            for (int j = 0; j < 4; j++) b8[j] = b8[2 * j] | (b8[2 * j + 1] << 2);
+            unsigned mask = (b8[0] | (b8[1] << 4)) | ((b8[2] | (b8[3] << 4)) << 8);
             while (mask) {
               const int j = __ffs(mask) - 1;
               mask &= mask - 1;

@@ -188,8 +188,86 @@ class SearchIndex:
         dist_list = [dist[off[i]:off[i + 1]].copy() for i in range(m)]
         return idx_list, dist_list
 
+    def priority_searcher(self, query):
+        """Priority search for one coordinate query row: candidates in
+        ascending (distance, index) order between a skip distance and a
+        cutoff (src/search/linear_scan.rs:70-235)."""
+        return PrioritySearcher(self, query)
+
     def __repr__(self):
         return f"<SearchIndex tree={self.tree!r} dtype={self.dtype!r} shape={self.shape!r}>"
+
+
+class PrioritySearcher:
+    """LinearScanPrioritySearcher (src/search/linear_scan.rs:70-235) over the
+    GPU range scan.  On first use the candidates with skip <= distance <=
+    cutoff are computed (one fuelg_range call with the cutoff as radius, the
+    skip applied to its (distance, index)-ordered hits) and then handed out
+    in order; ``decrease_cutoff`` only ever lowers the cutoff, and candidates
+    past it end the iteration, as in the reference."""
+
+    def __init__(self, index: SearchIndex, query):
+        q = np.ascontiguousarray(np.asarray(query, dtype=index.dtype).reshape(1, -1))
+        if q.shape[1] != index.shape[1]:
+            raise ValueError(f"query must have {index.shape[1]} coordinates")
+        self._index = index
+        self._query = q
+        self.reset()
+
+    def reset(self):
+        self._cand = None
+        self._pos = 0
+        self.cutoff = np.float32(np.inf)
+        self.skip = np.float32(0.0)
+
+    def reset_with_limits(self, cutoff, skip):
+        if not skip >= 0 or not cutoff >= skip:
+            raise ValueError("need 0 <= skip <= cutoff")
+        self.reset()
+        self.cutoff = np.float32(cutoff)
+        self.skip = np.float32(skip)
+
+    def _ensure(self):
+        if self._cand is not None:
+            return
+        idx, dist = self._index.radius_search(self._query, float(self.cutoff), exclude_self=False)
+        keep = dist[0] >= self.skip
+        self._cand = (idx[0][keep], dist[0][keep])
+        self._pos = 0
+
+    def next(self, skip_point=None):
+        """Next (distance, index) or None; skip_point(index) -> True skips a
+        point (SearchFilter)."""
+        self._ensure()
+        idx, dist = self._cand
+        while self._pos < len(idx):
+            i, d = int(idx[self._pos]), dist[self._pos]
+            self._pos += 1
+            if d > self.cutoff:
+                return None
+            if d < self.skip:
+                continue
+            if skip_point is not None and skip_point(i):
+                continue
+            return float(d), i
+        return None
+
+    def all_lower_bound(self):
+        if self._cand is None:
+            return 0.0
+        idx, dist = self._cand
+        for j in range(self._pos, len(idx)):
+            d = dist[j]
+            if d > self.cutoff:
+                break
+            if d >= self.skip:
+                return float(d)
+        return float("inf")
+
+    def decrease_cutoff(self, threshold):
+        if threshold > self.cutoff:
+            raise ValueError("thresholds must only decrease")
+        self.cutoff = np.float32(threshold)
 
 
 def knn_search(data, query, k, *, exclude_self=None, distance="euclidean", tree="auto", seed=None, **kw):

@@ -155,8 +155,12 @@ typedef struct {
   int32_t status;
   double out_inertia;
 } fuelg_kmeans_problem;
+/* precision: FUELG_PREC_FP32 = exact CUDA-core assignment everywhere; BF16 or
+ * SPLIT_BF16 = problems with 32 <= d <= 64 and k <= 256 are screened with
+ * split-BF16 tensor-core products and re-scored exactly where the screen
+ * cannot decide (identical results). */
 int fuelg_kmeans_batched(fuelg_kmeans_problem *problems, int32_t count, int32_t max_iter, int32_t order,
-                         int32_t flags, fuelg_stats *stats);
+                         int32_t precision, int32_t flags, fuelg_stats *stats);
 
 /* kNN serving with continuous batching over a resident index.  No
  * counterpart in the reference (fuel answers one call at a time); it serves

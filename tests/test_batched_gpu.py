@@ -8,7 +8,7 @@ import pytest
 from fuel_gb300 import kmeans, kmeans_batched, workloads
 
 
-def _mixed(count, seed, n_max=20000, dims=(2, 3, 8, 17, 32, 64, 100)):
+def _mixed(count, seed, n_max=20000, dims=(2, 3, 8, 17, 32, 40, 64, 100)):
     rng = np.random.default_rng(seed)
     descs = []
     for i in range(count):
@@ -27,11 +27,12 @@ def _same(a, b):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "split_bf16"])
 @pytest.mark.parametrize("fixed", [False, True])
 @pytest.mark.parametrize("order", ["arm", "x86"])
-def test_batched_equals_single(gpu, fixed, order):
+def test_batched_equals_single(gpu, fixed, order, precision):
     probs = _mixed(24, seed=5 + fixed)
-    got = kmeans_batched(probs, max_iter=12, order=order, fixed_iters=fixed)
+    got = kmeans_batched(probs, max_iter=12, order=order, fixed_iters=fixed, precision=precision)
     for (X, init), g in zip(probs, got):
         ref = kmeans(X, k=init.shape[0], variant="lloyd", init=init, max_iter=12, order=order,
                      fixed_iters=fixed)
