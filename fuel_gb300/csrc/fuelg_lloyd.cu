@@ -40,7 +40,7 @@ ExactSums* exact_sums_new();
 void exact_sums_delete(ExactSums*);
 int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaStream_t stream);
 int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
-                    bool write_centers, float* centers, int32_t* changed, cudaStream_t stream);
+                    bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream);
 int lloyd_tc_rescored_total(TcLloydState* st, cudaStream_t stream, int64_t* out);
 
 namespace {
@@ -377,7 +377,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
       FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
     if (exact)
       return exact_sums_step(es, p.X, lab_new.as<int32_t>(), labels, first, write_centers, C, changed.as<int32_t>(),
-                             stream);
+                             dev_status, stream);
     FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t), stream));
     post_assign_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(lab_new.as<int32_t>(), n, labels,
                                                                        first ? 1 : 0, changed.as<int32_t>()); ::fuelg::note_launch();

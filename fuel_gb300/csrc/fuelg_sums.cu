@@ -73,19 +73,18 @@ __global__ void exp_range_kernel(const float* __restrict__ X, int64_t count, int
 // aggregated in shared memory per block when k fits (integer counts: exact).
 constexpr int kSmemK = 4096;
 
-__global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first, int k,
-                                      int32_t* __restrict__ labels, int32_t* __restrict__ chg_i,
-                                      int32_t* __restrict__ chg_old, int32_t* __restrict__ chg_new,
-                                      int32_t* __restrict__ nchg, int32_t* __restrict__ cin,
-                                      int32_t* __restrict__ cout) {
-  __shared__ int32_t h_in[kSmemK], h_out[kSmemK];
-  griddep_wait();
+__device__ __forceinline__ void commit_body(int bid, int nblk, int32_t* h_in, int32_t* h_out,
+                                            const int32_t* __restrict__ lab_new, int64_t n, int first, int k,
+                                            int32_t* __restrict__ labels, int32_t* __restrict__ chg_i,
+                                            int32_t* __restrict__ chg_old, int32_t* __restrict__ chg_new,
+                                            int32_t* __restrict__ nchg, int32_t* __restrict__ cin,
+                                            int32_t* __restrict__ cout) {
   const bool local = k <= kSmemK;
   if (local)
     for (int j = threadIdx.x; j < k; j += blockDim.x) h_in[j] = h_out[j] = 0;
   __syncthreads();
   const int lane = threadIdx.x & 31;
-  for (int64_t base0 = (int64_t)blockIdx.x * blockDim.x; base0 < n; base0 += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t base0 = (int64_t)bid * blockDim.x; base0 < n; base0 += (int64_t)nblk * blockDim.x) {
     const int64_t i = base0 + threadIdx.x;
     bool ch = false;
     int32_t nw = 0, old = -1;
@@ -123,16 +122,12 @@ __global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64
     }
 }
 
-// Single warp: bucket offsets and the chunk table (in-chunks of cluster
-// 0..k-1, then out-chunks), member counts, and chunk_info[c] = cluster of
-// chunk c (bit 31: an out-chunk).  Warp-shuffle scans over 32-entry tiles.
-__global__ void bucket_plan_kernel(int k, const int32_t* __restrict__ cin, const int32_t* __restrict__ cout,
-                                   int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
-                                   int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts,
-                                   int32_t* __restrict__ chunk_info) {
-  griddep_wait();
+__device__ __forceinline__ void plan_body(int k, const int32_t* __restrict__ cin, const int32_t* __restrict__ cout,
+                                          int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
+                                          int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts,
+                                          int32_t* __restrict__ chunk_info) {
   const int lane = threadIdx.x & 31;
-  if (threadIdx.x >= 32) return;
+  if (threadIdx.x >= 32) return;  // callers run this with warp 0 only
   int32_t carry_c = 0;
   for (int pass = 0; pass < 2; pass++) {
     const int32_t* cnt = pass == 0 ? cin : cout;
@@ -165,16 +160,46 @@ __global__ void bucket_plan_kernel(int k, const int32_t* __restrict__ cin, const
   if (lane == 0) chunk_off[2 * k] = carry_c;
 }
 
-__global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
-                                      const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg, int k,
-                                      const int32_t* __restrict__ off_in, const int32_t* __restrict__ off_out,
-                                      int32_t* __restrict__ cur_in, int32_t* __restrict__ cur_out,
-                                      int32_t* __restrict__ bucket_in, int32_t* __restrict__ bucket_out) {
-  __shared__ int32_t c_in[kSmemK], c_out[kSmemK];
+// Commit, then the last block to finish (a ticket after a fence: no
+// waiting) plans the buckets from the complete histograms.
+__global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first, int k,
+                                      int32_t* __restrict__ labels, int32_t* __restrict__ chg_i,
+                                      int32_t* __restrict__ chg_old, int32_t* __restrict__ chg_new,
+                                      int32_t* __restrict__ nchg, int32_t* __restrict__ cin,
+                                      int32_t* __restrict__ cout, unsigned* __restrict__ done,
+                                      int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
+                                      int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts,
+                                      int32_t* __restrict__ chunk_info) {
+  __shared__ int32_t h_in[kSmemK], h_out[kSmemK];
+  __shared__ unsigned s_last;
   griddep_wait();
+  commit_body(blockIdx.x, gridDim.x, h_in, h_out, lab_new, n, first, k, labels, chg_i, chg_old, chg_new, nchg, cin,
+              cout);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(done, 1u) == gridDim.x - 1 ? 1u : 0u;
+  __syncthreads();
+  if (s_last) {
+    __threadfence();
+    if (threadIdx.x < 32) plan_body(k, cin, cout, off_in, off_out, chunk_off, counts, chunk_info);
+    if (threadIdx.x == 0) *done = 0;
+  }
+}
+
+// Single warp: bucket offsets and the chunk table (in-chunks of cluster
+// 0..k-1, then out-chunks), member counts, and chunk_info[c] = cluster of
+// chunk c (bit 31: an out-chunk).  Warp-shuffle scans over 32-entry tiles.
+
+__device__ __forceinline__ void scatter_body(int bid, int nblk, int32_t* c_in, int32_t* c_out,
+                                             const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
+                                             const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg,
+                                             int k, const int32_t* __restrict__ off_in,
+                                             const int32_t* __restrict__ off_out, int32_t* __restrict__ cur_in,
+                                             int32_t* __restrict__ cur_out, int32_t* __restrict__ bucket_in,
+                                             int32_t* __restrict__ bucket_out) {
   const int cnt = *nchg;
   const bool local = k <= kSmemK;
-  for (int e0 = blockIdx.x * blockDim.x; e0 < cnt; e0 += gridDim.x * blockDim.x) {
+  for (int e0 = bid * blockDim.x; e0 < cnt; e0 += nblk * blockDim.x) {
     const int e = e0 + threadIdx.x;
     const bool v = e < cnt;
     int32_t i = 0, o = -1, w = 0;
@@ -212,6 +237,17 @@ __global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const i
   }
 }
 
+__global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
+                                      const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg, int k,
+                                      const int32_t* __restrict__ off_in, const int32_t* __restrict__ off_out,
+                                      int32_t* __restrict__ cur_in, int32_t* __restrict__ cur_out,
+                                      int32_t* __restrict__ bucket_in, int32_t* __restrict__ bucket_out) {
+  __shared__ int32_t c_in[kSmemK], c_out[kSmemK];
+  griddep_wait();
+  scatter_body(blockIdx.x, gridDim.x, c_in, c_out, chg_i, chg_old, chg_new, nchg, k, off_in, off_out, cur_in, cur_out,
+               bucket_in, bucket_out);
+}
+
 // 64-bit form of fixed_of for L <= 2 (|I(x)| < 2^63 by construction).
 __device__ __forceinline__ unsigned long long fixed_of64(float x, int e_lo, bool negate) {
   const uint32_t bits = __float_as_uint(x);
@@ -226,21 +262,20 @@ __device__ __forceinline__ unsigned long long fixed_of64(float x, int e_lo, bool
 }
 
 // One chunk of <= 32 rows of one cluster, signed; thread per coordinate.
+// Work item w = chunk * ty + slab (slab: 256 coordinates).
 template <int L>
-__global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict__ X, int d, int k, int e_lo,
-                                                         const int32_t* __restrict__ chunk_off,
-                                                         const int32_t* __restrict__ chunk_info,
-                                                         const int32_t* __restrict__ cin,
-                                                         const int32_t* __restrict__ cout,
-                                                         const int32_t* __restrict__ off_in,
-                                                         const int32_t* __restrict__ off_out,
-                                                         const int32_t* __restrict__ bucket_in,
-                                                         const int32_t* __restrict__ bucket_out,
-                                                         unsigned long long* __restrict__ limbs) {
-  griddep_wait();
+__device__ __forceinline__ void accumulate_body(int bid, int nblk, int ty, int32_t* rid, const float* __restrict__ X,
+                                                int d, int k, int e_lo, const int32_t* __restrict__ chunk_off,
+                                                const int32_t* __restrict__ chunk_info,
+                                                const int32_t* __restrict__ cin, const int32_t* __restrict__ cout,
+                                                const int32_t* __restrict__ off_in,
+                                                const int32_t* __restrict__ off_out,
+                                                const int32_t* __restrict__ bucket_in,
+                                                const int32_t* __restrict__ bucket_out,
+                                                unsigned long long* __restrict__ limbs) {
   const int total = chunk_off[2 * k];
-  __shared__ int32_t rid[kRows];
-  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+  for (int w = bid; w < total * ty; w += nblk) {
+    const int c = w / ty, slab = w - c * ty;
     const int32_t info = chunk_info[c];
     const bool out = info < 0;
     const int j = info & 0x7fffffff;
@@ -251,7 +286,7 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
     __syncthreads();
     if (threadIdx.x < kRows) rid[threadIdx.x] = threadIdx.x < rows ? src[threadIdx.x] : -1;
     __syncthreads();
-    for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < d; t += gridDim.y * blockDim.x) {
+    for (int t = slab * blockDim.x + threadIdx.x; t < d; t += ty * blockDim.x) {
       float xv[kRows];
 #pragma unroll
       for (int q = 0; q < kRows; q++) xv[q] = rid[q] >= 0 ? __ldg(X + (int64_t)rid[q] * d + t) : 0.0f;
@@ -278,22 +313,39 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
   }
 }
 
+template <int L>
+__global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict__ X, int d, int k, int e_lo, int ty,
+                                                         const int32_t* __restrict__ chunk_off,
+                                                         const int32_t* __restrict__ chunk_info,
+                                                         const int32_t* __restrict__ cin,
+                                                         const int32_t* __restrict__ cout,
+                                                         const int32_t* __restrict__ off_in,
+                                                         const int32_t* __restrict__ off_out,
+                                                         const int32_t* __restrict__ bucket_in,
+                                                         const int32_t* __restrict__ bucket_out,
+                                                         unsigned long long* __restrict__ limbs) {
+  __shared__ int32_t rid[kRows];
+  griddep_wait();
+  accumulate_body<L>(blockIdx.x, gridDim.x, ty, rid, X, d, k, e_lo, chunk_off, chunk_info, cin, cout, off_in, off_out,
+                     bucket_in, bucket_out, limbs);
+}
+
 // Canonicalise every coordinate's limbs and write the exact mean of non-empty
 // clusters as the correctly rounded f32 centre.
 template <int L>
-__global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, int d, int e_lo,
-                            const int32_t* __restrict__ counts, float* __restrict__ centers, int write_centers,
-                            int32_t* __restrict__ nchg, int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
-                            int nzero) {
-  griddep_wait();
+__device__ __forceinline__ void mean_body(int bid, int nblk, unsigned long long* __restrict__ limbs, int64_t kd,
+                                          int d, int e_lo, const int32_t* __restrict__ counts,
+                                          float* __restrict__ centers, int write_centers,
+                                          int32_t* __restrict__ nchg, int32_t* __restrict__ changed,
+                                          int32_t* __restrict__ zero4k, int nzero) {
   // hand the change count to the host and reset the per-pass counters
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (bid == 0 && threadIdx.x == 0) {
     *changed = *nchg;
     *nchg = 0;
   }
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nzero; e += (int64_t)gridDim.x * blockDim.x)
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < nzero; e += (int64_t)nblk * blockDim.x)
     zero4k[e] = 0;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kd; e += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < kd; e += (int64_t)nblk * blockDim.x) {
     unsigned long long* lp = limbs + e * L;
     unsigned __int128 tot = 0;
 #pragma unroll
@@ -319,13 +371,23 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
   }
 }
 
+template <int L>
+__global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, int d, int e_lo,
+                            const int32_t* __restrict__ counts, float* __restrict__ centers, int write_centers,
+                            int32_t* __restrict__ nchg, int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
+                            int nzero) {
+  griddep_wait();
+  mean_body<L>(blockIdx.x, gridDim.x, limbs, kd, d, e_lo, counts, centers, write_centers, nchg, changed, zero4k,
+               nzero);
+}
+
 }  // namespace
 
 struct ExactSums {
   int L = 0, e_lo = 0, k = 0, d = 0;
   int64_t n = 0;
   Scratch limbs, counts, chg_i, chg_old, chg_new, nchg, cin, cout, off_in, off_out, cur, chunk_off, chunk_info,
-      bucket_in, bucket_out, range;
+      bucket_in, bucket_out, range, done;
   int64_t max_chunks = 0;
 };
 
@@ -379,6 +441,8 @@ int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaS
   FUELG_TRY(s->bucket_out.alloc(sizeof(int32_t) * n, stream));
   s->max_chunks = 2 * (n / kRows) + 2 * (int64_t)k + 2;
   FUELG_TRY(s->chunk_info.alloc(sizeof(int32_t) * s->max_chunks, stream));
+  FUELG_TRY(s->done.alloc(sizeof(unsigned), stream));
+  FUELG_CUDA(cudaMemsetAsync(s->done.p, 0, sizeof(unsigned), stream));
   return ST_OK;
 }
 
@@ -388,7 +452,7 @@ int exact_sums_L(const ExactSums* s) { return s->L; }
 // update the exact sums and counts, and write the new centres.  *changed
 // (device) receives the number of changed labels.
 int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
-                    bool write_centers, float* centers, int32_t* changed, cudaStream_t stream) {
+                    bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream) {
   const int64_t n = s->n;
   const int k = s->k, d = s->d;
   int32_t* cin = s->cin.as<int32_t>();
@@ -397,25 +461,24 @@ int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_
   int32_t* cur_out = cin + 3 * k;
   int32_t* off_in = s->off_in.as<int32_t>();
   int32_t* off_out = off_in + k;
+  const int ty = (d + 255) / 256;
   // counters were zeroed at init and are reset by mean_kernel after every pass
   FUELG_TRY(launch_pdl(commit_changes_kernel, dim3((unsigned)std::min<int64_t>((n + 255) / 256, 2 * 152)), dim3(256),
                        0, stream, lab_new, n, first ? 1 : 0, k, labels, s->chg_i.as<int32_t>(),
-                       s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), cin, cout));
-  FUELG_TRY(launch_pdl(bucket_plan_kernel, dim3(1), dim3(32), 0, stream, k, (const int32_t*)cin,
-                       (const int32_t*)cout, off_in, off_out, s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(),
+                       s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), cin, cout,
+                       s->done.as<unsigned>(), off_in, off_out, s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(),
                        s->chunk_info.as<int32_t>()));
   FUELG_TRY(launch_pdl(bucket_scatter_kernel, dim3(2 * 152), dim3(256), 0, stream,
                        (const int32_t*)s->chg_i.as<int32_t>(), (const int32_t*)s->chg_old.as<int32_t>(),
                        (const int32_t*)s->chg_new.as<int32_t>(), (const int32_t*)s->nchg.as<int32_t>(), k,
                        (const int32_t*)off_in, (const int32_t*)off_out, cur_in, cur_out, s->bucket_in.as<int32_t>(),
                        s->bucket_out.as<int32_t>()));
-  const int ty = (d + 255) / 256;
-  dim3 g((unsigned)std::min<int64_t>(s->max_chunks, std::max(1, 8 * 152 / ty)), ty);
+  const dim3 g((unsigned)std::min<int64_t>(s->max_chunks * ty, 8 * 152));
   const int64_t kd = (int64_t)k * d;
   const unsigned mg = (unsigned)std::min<int64_t>((kd + 255) / 256, 8 * 152);
   auto run = [&](auto Lc) -> int {
     constexpr int LL = decltype(Lc)::value;
-    FUELG_TRY(launch_pdl(accumulate_kernel<LL>, g, dim3(256), 0, stream, X, d, k, s->e_lo,
+    FUELG_TRY(launch_pdl(accumulate_kernel<LL>, g, dim3(256), 0, stream, X, d, k, s->e_lo, ty,
                          (const int32_t*)s->chunk_off.as<int32_t>(), (const int32_t*)s->chunk_info.as<int32_t>(),
                          (const int32_t*)cin, (const int32_t*)cout, (const int32_t*)off_in, (const int32_t*)off_out,
                          (const int32_t*)s->bucket_in.as<int32_t>(), (const int32_t*)s->bucket_out.as<int32_t>(),

@@ -115,7 +115,31 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_holder;
-  // the prologue above overlaps the predecessor; centres and norms come from it
+  // X does not depend on the predecessor kernel: the producer issues the A
+  // (point) tiles of the first NS stages before waiting for it; the centre
+  // tiles (B) and norms come from the predecessor.
+  int pre = 0;
+  if (warp == 0 && lane == 0) {
+    prefetch_tmap(&tmA);
+    if (SPLIT) prefetch_tmap(&tmAlo);
+    const uint64_t pol_a = policy_evict_first();
+    int64_t t = blockIdx.x;
+    int kc = 0;
+    for (int st = 0; st < NS && t < ntiles; st++) {
+      uint8_t* sA = base + (size_t)st * stage_bytes;
+      uint8_t* sB = sA + a_bytes;
+      mbar_expect_tx(&full[st], stage_bytes);
+      const int ax = a.a_tiled ? 0 : kc * BK;
+      const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
+      tma_load_2d_hint(sA, &tmA, ax, ay, &full[st], pol_a);
+      if (SPLIT) tma_load_2d_hint(sB + b_bytes, &tmAlo, ax, ay, &full[st], pol_a);
+      pre++;
+      if (++kc == a.kc) {
+        kc = 0;
+        t += gridDim.x;
+      }
+    }
+  }
   griddep_wait();
   for (int j = threadIdx.x; j < a.kp; j += blockDim.x) {
     snc[j] = a.nc[j];
@@ -125,12 +149,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
 
   if (warp == 0) {
     if (lane == 0) {
-      prefetch_tmap(&tmA);
       prefetch_tmap(&tmB);
-      if (SPLIT) {
-        prefetch_tmap(&tmAlo);
-        prefetch_tmap(&tmBlo);
-      }
+      if (SPLIT) prefetch_tmap(&tmBlo);
       const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
       uint32_t stage = 0, phase = 0;
       uint32_t armed = 0, last_ph = 0;  // per-stage bit: armed at least once / parity of the last arm
@@ -142,24 +162,27 @@ __global__ void __launch_bounds__(kTcThreads, 2)
           break;
         }
         for (int kc = 0; kc < a.kc; kc++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
-            if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-            *abort_flag = 1;
-            break;
-          }
           uint8_t* sA = base + (size_t)stage * stage_bytes;
           uint8_t* sB = sA + a_bytes;
-          mbar_expect_tx(&full[stage], stage_bytes);
           armed |= 1u << stage;
           last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
-          const int ax = a.a_tiled ? 0 : kc * BK;
-          const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
-          tma_load_2d_hint(sA, &tmA, ax, ay, &full[stage], pol_a);
-          tma_load_2d_hint(sB, &tmB, kc * BK, 0, &full[stage], pol_b);
-          if (SPLIT) {
-            tma_load_2d_hint(sB + b_bytes, &tmAlo, ax, ay, &full[stage], pol_a);
-            tma_load_2d_hint(sB + b_bytes + a_bytes, &tmBlo, kc * BK, 0, &full[stage], pol_b);
+          if (pre > 0) {
+            // A already in flight (issued before the dependency wait)
+            pre--;
+          } else {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+              if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+              *abort_flag = 1;
+              break;
+            }
+            mbar_expect_tx(&full[stage], stage_bytes);
+            const int ax = a.a_tiled ? 0 : kc * BK;
+            const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
+            tma_load_2d_hint(sA, &tmA, ax, ay, &full[stage], pol_a);
+            if (SPLIT) tma_load_2d_hint(sB + b_bytes, &tmAlo, ax, ay, &full[stage], pol_a);
           }
+          tma_load_2d_hint(sB, &tmB, kc * BK, 0, &full[stage], pol_b);
+          if (SPLIT) tma_load_2d_hint(sB + b_bytes + a_bytes, &tmBlo, kc * BK, 0, &full[stage], pol_b);
           if (++stage == (uint32_t)NS) {
             stage = 0;
             phase ^= 1;
@@ -366,35 +389,47 @@ __global__ void prep_rows_kernel(const float* __restrict__ X, int64_t rows, int6
     float acc = 0.0f;
     const bool v = r < valid_rows;
     const float* xr = X + r * d;
-    for (int c0 = 4 * lane; c0 < dp; c0 += 128) {
-      float x4[4];
-      if (v && vec && c0 + 3 < d) {
-        const float4 t = __ldg(reinterpret_cast<const float4*>(xr + c0));
-        x4[0] = t.x, x4[1] = t.y, x4[2] = t.z, x4[3] = t.w;
-      } else {
+    // up to 8 chunks of 4 values per lane are loaded before any is used (the
+    // loads overlap), then converted in order (the norm chain keeps its order)
+    for (int cb = 4 * lane; cb < dp; cb += 128 * 8) {
+      float x8[8][4];
 #pragma unroll
-        for (int q = 0; q < 4; q++) x4[q] = (v && c0 + q < d) ? __ldg(xr + c0 + q) : 0.0f;
-      }
-      __nv_bfloat162 h01 = __floats2bfloat162_rn(x4[0], x4[1]);
-      __nv_bfloat162 h23 = __floats2bfloat162_rn(x4[2], x4[3]);
-      uint2 hpack;
-      hpack.x = *reinterpret_cast<uint32_t*>(&h01);
-      hpack.y = *reinterpret_cast<uint32_t*>(&h23);
-      const int64_t off = prep_offset(r, c0, dp, tile_kc);
-      *reinterpret_cast<uint2*>(hi + off) = hpack;
-      if (SPLIT) {
-        const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
-        __nv_bfloat162 l01 = __floats2bfloat162_rn(x4[0] - f01.x, x4[1] - f01.y);
-        __nv_bfloat162 l23 = __floats2bfloat162_rn(x4[2] - f23.x, x4[3] - f23.y);
-        uint2 lpack;
-        lpack.x = *reinterpret_cast<uint32_t*>(&l01);
-        lpack.y = *reinterpret_cast<uint32_t*>(&l23);
-        *reinterpret_cast<uint2*>(lo + off) = lpack;
+      for (int u = 0; u < 8; u++) {
+        const int c0 = cb + 128 * u;
+        if (v && vec && c0 + 3 < d) {
+          const float4 t = __ldg(reinterpret_cast<const float4*>(xr + c0));
+          x8[u][0] = t.x, x8[u][1] = t.y, x8[u][2] = t.z, x8[u][3] = t.w;
+        } else {
+#pragma unroll
+          for (int q = 0; q < 4; q++) x8[u][q] = (v && c0 + q < d) ? __ldg(xr + c0 + q) : 0.0f;
+        }
       }
 #pragma unroll
-      for (int q = 0; q < 4; q++) {
-        acc = fmaf(x4[q], x4[q], acc);
-        anyneg |= x4[q] < 0.0f;
+      for (int u = 0; u < 8; u++) {
+        const int c0 = cb + 128 * u;
+        if (c0 >= dp) break;
+        const float* x4 = x8[u];
+        __nv_bfloat162 h01 = __floats2bfloat162_rn(x4[0], x4[1]);
+        __nv_bfloat162 h23 = __floats2bfloat162_rn(x4[2], x4[3]);
+        uint2 hpack;
+        hpack.x = *reinterpret_cast<uint32_t*>(&h01);
+        hpack.y = *reinterpret_cast<uint32_t*>(&h23);
+        const int64_t off = prep_offset(r, c0, dp, tile_kc);
+        *reinterpret_cast<uint2*>(hi + off) = hpack;
+        if (SPLIT) {
+          const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
+          __nv_bfloat162 l01 = __floats2bfloat162_rn(x4[0] - f01.x, x4[1] - f01.y);
+          __nv_bfloat162 l23 = __floats2bfloat162_rn(x4[2] - f23.x, x4[3] - f23.y);
+          uint2 lpack;
+          lpack.x = *reinterpret_cast<uint32_t*>(&l01);
+          lpack.y = *reinterpret_cast<uint32_t*>(&l23);
+          *reinterpret_cast<uint2*>(lo + off) = lpack;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+          acc = fmaf(x4[q], x4[q], acc);
+          anyneg |= x4[q] < 0.0f;
+        }
       }
     }
 #pragma unroll
