@@ -246,11 +246,15 @@ def run_ours(args):
     pk = peaks()
     value = world * ITERS * args.steps / (t_max / 1e3)
     e2e_value = world * ITERS * args.steps / (e2e_max / 1e3)
-    # roofline of the hot kernel.  Tensor-core tier: one read of the BF16 copy of X
-    # (n*d*2), the BF16 centres (k*d*2) and one int32 label per point.  Plain tier:
-    # one read of X (n*d*4) + the centres (k*d*4) + one 8-byte key per point.
+    # roofline of the hot kernel.  Tensor-core tier: one read of the BF16 copies of X
+    # (n*d*2 each: hi and lo for split-BF16, the one exact scaled-integer copy for
+    # split_bf16_scaled), the BF16 centres (k*d*2 per copy) and one int32 label per
+    # point.  Plain tier: one read of X (n*d*4) + the centres (k*d*4) + one 8-byte
+    # key per point.
     if prec_used != 0:
-        alg_bytes = N * D * 2 * (2 if prec_used == 2 else 1) + K * D * 2 + N * 4
+        x_copies = 2 if prec_used == 2 else 1
+        c_copies = 2 if prec_used == 3 else 1
+        alg_bytes = N * D * 2 * x_copies + K * D * 2 * c_copies + N * 4
         hot_name = "lloyd_tc_kernel (tcgen05 BF16 screen of the Lloyd assignment)"
     else:
         alg_bytes = N * D * 4 + K * D * 4 + N * 8
@@ -300,7 +304,7 @@ def run_ours(args):
                                    f"{sample_iters}), restated fuel CPU Lloyd, {cpu_t:.1f} s"},
         "clocks": clk.summary(),
         "inertia": inertia,
-        "precision_used": {0: "fp32", 1: "bf16", 2: "split_bf16"}[prec_used],
+        "precision_used": _lib.PRECISION_NAMES[prec_used],
         "rescored_fraction": rescored / float(N * ITERS * args.steps),
         "plain_fp32": plain,
         "tc_vs_plain": (value / plain["iters_per_s"]) if plain else None,
@@ -366,7 +370,7 @@ def knn_tc_rate(lib, _lib, torch, args, m_tc=None, plain=True, reps=1, n_index=K
                "queries": m_tc, "queries_per_s": m_tc / (t / 1e3), "ms_per_call": t,
                "distance_evals_per_s": m_tc * float(n) / (t / 1e3), "hot_kernel_ms": hot,
                "hot_kernel_launches": sts[-1].hot_kernel_launches, "rescored": sts[-1].rescored,
-               "precision_used": {0: "fp32", 1: "bf16", 2: "split_bf16"}[sts[-1].precision_used],
+               "precision_used": _lib.PRECISION_NAMES[sts[-1].precision_used],
                "kernel_launches": sts[-1].kernel_launches}
         # tensor pipe: 2*m*n*dp flops in the screen kernel
         dp = ((d + 63) // 64) * 64

@@ -19,6 +19,8 @@ METRIC = {"sqeuclidean": 0, "euclidean": 1}
 ORDER = {"arm": 0, "x86": 1}
 EXCLUDE_NONE, EXCLUDE_LINEAR, EXCLUDE_KPLUS1 = 0, 1, 2
 PRECISION = {"fp32": 0, "bf16": 1, "split_bf16": 2}
+# stats["precision_used"] may also be 3: split_bf16 on scaled-integer data
+PRECISION_NAMES = {0: "fp32", 1: "bf16", 2: "split_bf16", 3: "split_bf16_scaled"}
 LLOYD_FIXED_ITERS = 1
 
 

@@ -534,12 +534,17 @@ __global__ void __launch_bounds__(kTcRows, 2) batched_tc_assign_kernel(
                              ((uint32_t)(kTcRows >> 4) << 24);
       const uint64_t ah = tcx::smem_desc_sw128(tcx::smem_u32(sAh)), al = tcx::smem_desc_sw128(tcx::smem_u32(sAl));
       const uint64_t bh = tcx::smem_desc_sw128(tcx::smem_u32(sBh)), bl = tcx::smem_desc_sw128(tcx::smem_u32(sBl));
+      // K steps of 16 that hold data (the zero columns past d add nothing)
+      const int nks = (pr.d + 15) >> 4;
 #pragma unroll
-      for (int kk = 0; kk < 4; kk++) tcx::umma_bf16(tmem, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : 0u);
+      for (int kk = 0; kk < 4; kk++)
+        if (kk < nks) tcx::umma_bf16(tmem, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : 0u);
 #pragma unroll
-      for (int kk = 0; kk < 4; kk++) tcx::umma_bf16(tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
+      for (int kk = 0; kk < 4; kk++)
+        if (kk < nks) tcx::umma_bf16(tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
 #pragma unroll
-      for (int kk = 0; kk < 4; kk++) tcx::umma_bf16(tmem, al + 2 * kk, bh + 2 * kk, idesc, 1u);
+      for (int kk = 0; kk < 4; kk++)
+        if (kk < nks) tcx::umma_bf16(tmem, al + 2 * kk, bh + 2 * kk, idesc, 1u);
       tcx::umma_commit(bar);
     }
     const bool ok = tcx::mbar_wait(bar, phase, reinterpret_cast<volatile int*>(s_flag + 1));

@@ -172,10 +172,12 @@ int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, 
 void knn_tc_index_free(TcIndex* t);
 int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream);
 // split: hi + lo BF16 operands (accuracy ~2^-16 instead of 2^-8); ignored for
-// integer data whose BF16 screen is exact.
+// integer data whose BF16 screen is exact.  row_k (device, m entries, or
+// nullptr): a smaller k per query row -- row q's first row_k[q] keys (of the
+// kk per row written) are its exact top row_k[q]; the rest are unspecified.
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
                 int split, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
-                int* exact_out);
+                int* exact_out, const int32_t* row_k = nullptr);
 
 // Read-only view of an index handle for concurrent users (the serving loop);
 // with want_tc the tensor-core form is built first when the shape allows it.

@@ -43,14 +43,17 @@ constexpr int kApp = 256;      // appended candidates per query between compacti
 struct KnnTcArgs {
   int64_t m, n;
   int kc;        // K chunks of 64
-  int kk2;       // keys kept per query
+  int ks_last;   // K steps of 16 with data in the last chunk (1..4)
+  int kk2;       // keys kept per query (the list stride)
+  const int32_t* row_k;  // per query row k (rows keep kk2_of(row_k[q]) <= kk2 keys), or nullptr
+  int exact_sq;  // exact squared distances: no margin keys
   int exact;     // D~ is exact (integer data)
   int split;     // hi + lo BF16 operands (three products)
   int stages;
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
   float xmax_n2;     // max |x|^2 over the index (filter slack)
-  uint64_t* lists;   // [S][m][2*kk2 + kApp]: two kept-key buffers + append log per index split
+  uint64_t* lists;   // [S][m][kk2 + kApp]: kept keys + append log per index split
   uint64_t* out_keys;  // [S][m][kk2]
   uint32_t idesc;
   int* status;
@@ -59,6 +62,10 @@ struct KnnTcArgs {
 
 
 constexpr int kSel = 8;  // keys per lane in a selection (appended or prefix): 256 per warp
+
+// Screened keys kept for a query of k neighbours: k plus the margin the
+// error-bound proof needs (none when the screened squared distances are exact).
+__host__ __device__ __forceinline__ int kk2_of(int k, int exact_sq) { return exact_sq ? k : k + (k / 8 > 8 ? k / 8 : 8); }
 
 // Number of held keys below t over the warp.
 __device__ __forceinline__ int warp_count_hi_below(const uint32_t (&hi)[2 * kSel], uint32_t t) {
@@ -70,14 +77,16 @@ __device__ __forceinline__ int warp_count_hi_below(const uint32_t (&hi)[2 * kSel
 
 // Warp-cooperative selection for one query: the union of its
 // na (<= 256) appended keys and its plen (<= kk <= 256) kept keys is reduced
-// to its kk smallest, written unsorted to nxt[0, min(kk, na + plen)).  The
-// kk-th smallest key is found by a bitwise binary search over the
-// distance word (32 steps, counting with a warp reduction) and, only when
-// several keys share that distance, over the index word; keys are unique.
-// No shared memory, no sort.  Returns the kk-th smallest key, or KEY_NONE
-// while fewer than kk are held, on every lane.
-__device__ __noinline__ uint64_t warp_select(const uint64_t* __restrict__ app, int na,
-                                             const uint64_t* __restrict__ cur, int plen, uint64_t* __restrict__ nxt,
+// to its kk smallest, written unsorted back over cur[0, min(kk, na + plen)).
+// The kk-th smallest key is found by a bitwise binary search over the
+// distance word (counting with a warp reduction) and, only when several keys
+// share that distance, over the index word; keys are unique.  Each search
+// starts below the bits that the smallest and largest candidate word share.
+// In place: every lane has read its keys before the first warp-wide
+// exchange, and every store comes after the last.  No shared memory, no sort.
+// Returns the kk-th smallest key, or KEY_NONE while fewer than kk are held,
+// on every lane.
+__device__ __noinline__ uint64_t warp_select(const uint64_t* __restrict__ app, int na, uint64_t* cur, int plen,
                                              int kk, int lane) {
   uint64_t key[2 * kSel];
 #pragma unroll
@@ -87,34 +96,48 @@ __device__ __noinline__ uint64_t warp_select(const uint64_t* __restrict__ app, i
     key[kSel + i] = e < plen ? cur[e] : KEY_NONE;
   }
   uint32_t hi[2 * kSel];
+  uint32_t hmin = 0xffffffffu, hmax = 0;
 #pragma unroll
-  for (int i = 0; i < 2 * kSel; i++) hi[i] = (uint32_t)(key[i] >> 32);
+  for (int i = 0; i < 2 * kSel; i++) {
+    hi[i] = (uint32_t)(key[i] >> 32);
+    if (key[i] != KEY_NONE) {
+      hmin = min(hmin, hi[i]);
+      hmax = max(hmax, hi[i]);
+    }
+  }
   const int total = na + plen;
   uint64_t kth = KEY_NONE;
-  uint32_t H = 0xffffffffu, Lo = 0xffffffffu;  // keep keys <= (H, Lo)
   if (total >= kk) {
-    H = 0;
-    for (int b = 31; b >= 0; b--) {
+    // the kk-th distance word lies in [hmin, hmax]: search the bits below
+    // their common prefix only
+    hmin = __reduce_min_sync(0xffffffffu, hmin);
+    hmax = __reduce_max_sync(0xffffffffu, hmax);
+    int top = hmin == hmax ? -1 : 31 - __clz(hmin ^ hmax);
+    uint32_t H = top >= 0 ? hmin & ~((2u << top) - 1u) : hmin;
+    for (int b = top; b >= 0; b--) {
       const uint32_t t = H | (1u << b);
       if (warp_count_hi_below(hi, t) < kk) H = t;
     }
     // keys below H: fewer than kk; keys with hi == H: the rest is taken from them
     const int below = warp_count_hi_below(hi, H);
     int eq = 0;
-    uint32_t lo_max = 0;
+    uint32_t lmin = 0xffffffffu, lmax = 0;
 #pragma unroll
     for (int i = 0; i < 2 * kSel; i++)
       if (hi[i] == H) {
         eq++;
-        lo_max = max(lo_max, (uint32_t)key[i]);
+        lmin = min(lmin, (uint32_t)key[i]);
+        lmax = max(lmax, (uint32_t)key[i]);
       }
     eq = __reduce_add_sync(0xffffffffu, eq);
+    lmax = __reduce_max_sync(0xffffffffu, lmax);
     const int need = kk - below;
-    if (eq == need) {
-      Lo = __reduce_max_sync(0xffffffffu, lo_max);
-    } else {
-      Lo = 0;
-      for (int b = 31; b >= 0; b--) {
+    uint32_t Lo = lmax;
+    if (eq != need) {
+      lmin = __reduce_min_sync(0xffffffffu, lmin);
+      top = lmin == lmax ? -1 : 31 - __clz(lmin ^ lmax);
+      Lo = top >= 0 ? lmin & ~((2u << top) - 1u) : lmin;
+      for (int b = top; b >= 0; b--) {
         const uint32_t t = Lo | (1u << b);
         int c = 0;
 #pragma unroll
@@ -137,7 +160,7 @@ __device__ __noinline__ uint64_t warp_select(const uint64_t* __restrict__ app, i
   int pos = incl - mine;
 #pragma unroll
   for (int i = 0; i < 2 * kSel; i++)
-    if (key[i] != KEY_NONE && key[i] <= kth) nxt[pos++] = key[i];
+    if (key[i] != KEY_NONE && key[i] <= kth) cur[pos++] = key[i];
   __syncwarp();
   return total >= kk ? kth : KEY_NONE;
 }
@@ -269,7 +292,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
   const int64_t ntiles_all = (a.n + XN - 1) / XN;
   const int64_t tb = ntiles_all * blockIdx.y / gridDim.y;
   const int64_t ntiles = ntiles_all * (blockIdx.y + 1) / gridDim.y - tb;
-  uint64_t* const lists_sp = a.lists + (size_t)blockIdx.y * a.m * (2ull * a.kk2 + kApp);
+  uint64_t* const lists_sp = a.lists + (size_t)blockIdx.y * a.m * ((size_t)a.kk2 + kApp);
   uint64_t* const out_sp = a.out_keys + (size_t)blockIdx.y * a.m * a.kk2;
 
   if (threadIdx.x == 0) {
@@ -279,7 +302,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], kEpi);
+      mbar_init(&acce[b], kEpiWarps);
     }
     mbar_init(afull, 1);
     mbar_init(fin, 1);
@@ -368,13 +391,16 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           const int kc = j % a.kc;
           const uint64_t ad = smem_desc_sw128(smem_u32(sA + (size_t)kc * a_chunk));
           const uint64_t bd = smem_desc_sw128(smem_u32(sB + (size_t)stage * b_bytes));
+          // K steps of 16 that hold data: the zero columns past d add nothing
+          const int nks = kc == a.kc - 1 ? a.ks_last : BK / 16;
 #pragma unroll
           for (int kk = 0; kk < BK / 16; kk++)
-            umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (j | kk) != 0 ? 1u : 0u);
+            if (kk < nks) umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (j | kk) != 0 ? 1u : 0u);
           if (a.split && j < a.kc) {
             const uint64_t al = smem_desc_sw128(smem_u32(sA + (size_t)(a.kc + kc) * a_chunk));
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; kk++) umma_bf16(d_tmem, al + 2 * kk, bd + 2 * kk, a.idesc, 1u);
+            for (int kk = 0; kk < BK / 16; kk++)
+              if (kk < nks) umma_bf16(d_tmem, al + 2 * kk, bd + 2 * kk, a.idesc, 1u);
           }
           umma_commit(&empty[stage]);
           if (++stage == (uint32_t)NS) {
@@ -399,12 +425,13 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     const int64_t qi = q0 + row;
     const bool valid = qi < a.m;
     const float nq = valid ? a.qn2[qi] : 0.0f;
-    const size_t qstride = 2ull * a.kk2 + kApp;
-    uint64_t* app = lists_sp + (valid ? qi : 0) * qstride + 2ull * a.kk2;  // this query's append log
+    const int kkr = (a.row_k != nullptr && valid) ? kk2_of(a.row_k[qi], a.exact_sq) : a.kk2;  // this row's keys
+    const size_t qstride = (size_t)a.kk2 + kApp;
+    uint64_t* app = lists_sp + (valid ? qi : 0) * qstride + a.kk2;  // this query's append log
     float* nsm_w = xnsm + ew * 2 * XN;
     uint64_t tau = KEY_NONE;  // kk2-th key held
     float tau_d = __int_as_float(0x7f800000);
-    int na = 0, half = 0, plen = 0;
+    int na = 0, plen = 0;
     // Screen filter in the shifted domain: a column can enter only if
     // |x|^2 - 2 q.x <= tau - |q|^2 (+ slack covering the rounding of both
     // forms when the data are not exact integers); the screened distance is
@@ -425,16 +452,14 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
         const int src = __ffs(need) - 1;
         need &= need - 1;
         const int sna = __shfl_sync(0xffffffffu, na, src);
-        const int shalf = __shfl_sync(0xffffffffu, half, src);
         const int splen = __shfl_sync(0xffffffffu, plen, src);
+        const int skk = __shfl_sync(0xffffffffu, kkr, src);
         uint64_t* lb = lists_sp + (q0 + g * 32 + src) * qstride;
-        const uint64_t nt = warp_select(lb + 2ull * a.kk2, sna, lb + (size_t)shalf * a.kk2, splen,
-                                        lb + (size_t)(shalf ^ 1) * a.kk2, a.kk2, lane);
+        const uint64_t nt = warp_select(lb + a.kk2, sna, lb, splen, skk, lane);
         if (lane == src) {
           tau = nt;
           tau_d = nt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(nt);
-          half ^= 1;
-          plen = min(a.kk2, plen + na);
+          plen = min(kkr, plen + na);
           na = 0;
         }
       }
@@ -463,28 +488,35 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
 #pragma unroll
         for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
         tmem_ld_wait();
+        // shifted screen values f = |x|^2 - 2 q.x (in place) and each group's
+        // minimum as a 4-level tree (short dependency chains, four groups interleaved)
+        float mnh[4];
 #pragma unroll
         for (int h = 0; h < 4; h++) {
           const float4* n4 = reinterpret_cast<const float4*>(nsm + c0 + 16 * h);
-          float f[16];
 #pragma unroll
           for (int v = 0; v < 4; v++) {
             const float4 q4 = n4[v];
-            f[4 * v] = fmaf(-2.0f, __uint_as_float(r[h][4 * v]), q4.x);
-            f[4 * v + 1] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 1]), q4.y);
-            f[4 * v + 2] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z);
-            f[4 * v + 3] = fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w);
+            r[h][4 * v] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v]), q4.x));
+            r[h][4 * v + 1] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 1]), q4.y));
+            r[h][4 * v + 2] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z));
+            r[h][4 * v + 3] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w));
           }
-          // minimum and pass mask as 4-level trees (short dependency chains)
           float m8[8];
 #pragma unroll
-          for (int j = 0; j < 8; j++) m8[j] = fminf(f[2 * j], f[2 * j + 1]);
+          for (int j = 0; j < 8; j++) m8[j] = fminf(__uint_as_float(r[h][2 * j]), __uint_as_float(r[h][2 * j + 1]));
 #pragma unroll
           for (int j = 0; j < 4; j++) m8[j] = fminf(m8[2 * j], m8[2 * j + 1]);
-          const float mn = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
-          if (mn <= thr) {
+          mnh[h] = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
+        }
+#pragma unroll
+        for (int h = 0; h < 4; h++) {
+          if (mnh[h] <= thr) {
             // the few passing columns, one loop trip each; the screened
             // distance is D~ = |q|^2 + (|x|^2 - 2 q.x) in f32
+            float f[16];
+#pragma unroll
+            for (int j = 0; j < 16; j++) f[j] = __uint_as_float(r[h][j]);
             unsigned b8[8];
 #pragma unroll
             for (int j = 0; j < 8; j++)
@@ -504,14 +536,16 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
               }
             }
           }
-          if (__any_sync(0xffffffffu, na > kApp - 16)) {
-            flush(kApp - 16);
-            thr = threshold();
-          }
+        }
+        // at most 64 appends per lane per chunk: compact before the log can overflow
+        if (__any_sync(0xffffffffu, na > kApp - 64)) {
+          flush(kApp - 64);
+          thr = threshold();
         }
       }
       tc_fence_before();
-      mbar_arrive(&acce[b]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[b]);
     }
     flush(0);
     // kept keys out (unsorted; sorted afterwards), one query at a time per
@@ -519,9 +553,8 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     for (int src = 0; src < 32; src++) {
       const int64_t qs = q0 + g * 32 + src;
       if (qs >= a.m) break;
-      const int shalf = __shfl_sync(0xffffffffu, half, src);
       const int splen = __shfl_sync(0xffffffffu, plen, src);
-      const uint64_t* from = lists_sp + qs * qstride + (size_t)shalf * a.kk2;
+      const uint64_t* from = lists_sp + qs * qstride;
       uint64_t* to = out_sp + qs * a.kk2;
       for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
     }
@@ -577,7 +610,8 @@ __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64
 // fail the proof are flagged for the exact scan.
 template <int ORDER>
 __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __restrict__ X, int d, int64_t m,
-                                   int kk, int kk2, int metric, const uint64_t* __restrict__ keys_in,
+                                   int kk, int kk2, const int32_t* __restrict__ row_k, int metric,
+                                   const uint64_t* __restrict__ keys_in,
                                    uint64_t* __restrict__ keys_out, const float* __restrict__ qn2, float xmax_norm,
                                    float xmax_n2, float alpha, float beta, float gamma,
                                    int32_t* __restrict__ redo, int32_t* __restrict__ nredo) {
@@ -590,12 +624,16 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
   __syncwarp();
   const uint64_t* kin = keys_in + qi * kk2;
   uint64_t* kout = keys_out + qi * kk2;
+  // this row's k and kept keys (the list stride stays kk2)
+  const int kq = row_k != nullptr ? row_k[qi] : kk;
+  const int kk2q = row_k != nullptr ? kk2_of(kq, 0) : kk2;
+  for (int c = kk2q + lane; c < kk2; c += 32) kout[c] = KEY_NONE;
   // exact keys of the candidates, written in place of the screened ones
   const int l = lane & 7, grp = lane >> 3;
   float last_screen = 0.0f;
-  for (int c0 = 0; c0 < kk2; c0 += 4) {
+  for (int c0 = 0; c0 < kk2q; c0 += 4) {
     const int c = c0 + grp;
-    const uint64_t sk = c < kk2 ? kin[c] : KEY_NONE;
+    const uint64_t sk = c < kk2q ? kin[c] : KEY_NONE;
     const bool real = sk != KEY_NONE;
     const uint32_t idx = real ? key_idx(sk) : 0u;
     const float* x = X + (int64_t)idx * d;
@@ -613,7 +651,7 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
       s = ORDER == ORDER_X86 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
     }
     if (metric == METRIC_EUCLIDEAN) s = __fsqrt_rn(s);
-    if (l == 0 && c < kk2) kout[c] = real ? make_key(s, idx) : KEY_NONE;
+    if (l == 0 && c < kk2q) kout[c] = real ? make_key(s, idx) : KEY_NONE;
     if (real) last_screen = fmaxf(last_screen, key_dist(sk));
   }
   // the largest screened distance kept (candidates are sorted by screened key)
@@ -622,7 +660,7 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
   __syncwarp();
   // sort the kk2 exact keys (small: insertion sort by lane 0)
   if (lane == 0) {
-    for (int a1 = 1; a1 < kk2; a1++) {
+    for (int a1 = 1; a1 < kk2q; a1++) {
       const uint64_t v = kout[a1];
       int b = a1 - 1;
       while (b >= 0 && kout[b] > v) {
@@ -632,13 +670,13 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
       kout[b + 1] = v;
     }
     // proof: only needed when every slot was filled (otherwise every point was kept)
-    const bool full_list = kin[kk2 - 1] != KEY_NONE;
+    const bool full_list = kin[kk2q - 1] != KEY_NONE;
     if (full_list) {
       const float nq = qn2[qi];
       const float qn = sqrtf(nq);
       const float e = (alpha * qn * xmax_norm + beta * (nq + xmax_n2)) * (1.0f + gamma) + gamma * last_screen;
       const float lower = last_screen - e;  // every unscreened point's reference squared distance is >= this
-      const uint64_t kth = kout[kk - 1];
+      const uint64_t kth = kout[kq - 1];
       bool ok;
       if (metric == METRIC_EUCLIDEAN) ok = kth != KEY_NONE && lower > 0.0f && key_dist(kth) < __fsqrt_rd(lower);
       else ok = kth != KEY_NONE && key_dist(kth) < lower;
@@ -674,7 +712,7 @@ size_t knn_tc_fixed_smem(int d, int split) {
   const size_t a_bytes = (size_t)(split ? 2 : 1) * (dp / BK) * QM * BK * 2;
   return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * XN * sizeof(float);
 }
-int knn_tc_margin(int kk, bool exact_sq) { return exact_sq ? 0 : std::max(8, kk / 8); }
+int knn_tc_margin(int kk, bool exact_sq) { return kk2_of(kk, exact_sq ? 1 : 0) - kk; }
 }  // namespace
 
 bool knn_tc_supported(int d, int kk, int split) {
@@ -758,7 +796,7 @@ int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream) {
 
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
                 int split, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
-                int* exact_out) {
+                int* exact_out, const int32_t* row_k) {
   const int64_t n = ti->n;
   const int d = ti->d;
   const int dp = ti->dp;
@@ -801,9 +839,10 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     set_error("tensor-core kNN tile does not fit shared memory (d=%d)", d);
     return ST_ENOTSUP;
   }
-  // Index splits: when the query blocks cannot fill the GPU's CTA slots,
-  // each block's scan is split over S index ranges (>= 16 tiles each) whose
-  // sorted kept lists are merged afterwards.
+  // Index splits: when the query blocks cannot fill the GPU's CTA slots, each
+  // block's scan is split over S index ranges (>= 16 tiles each) whose sorted
+  // kept lists are merged afterwards.  Every split keeps its own top-kk2, so
+  // the selection work grows with S.
   const int64_t ntiles_all = (n + XN - 1) / XN;
   const int64_t slots = 152 * kCtasPerSm;
   const int64_t qblocks = (m + QM - 1) / QM;
@@ -811,11 +850,11 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   if (qblocks < slots)
     S = (int)std::max<int64_t>(1, std::min<int64_t>({slots / qblocks, ntiles_all / 16, (int64_t)kMaxSplits}));
   // Bound scratch: batches of queries whose lists take at most ~1 GiB.
-  const size_t per_query = ((size_t)S * (kk2 * 3 + kApp) + kk2 * 2) * 8;  // per split: lists + kept; merged
+  const size_t per_query = ((size_t)S * (kk2 * 2 + kApp) + kk2 * 2) * 8;  // per split: lists + kept; merged
   int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
   mb = std::min<int64_t>(mb, mpad);
   Scratch lists, kept_sp, kept_m, kept2, redo, nredo;
-  FUELG_TRY(lists.alloc((size_t)S * mb * (2 * kk2 + kApp) * 8, stream));
+  FUELG_TRY(lists.alloc((size_t)S * mb * (kk2 + kApp) * 8, stream));
   FUELG_TRY(kept_sp.alloc((size_t)S * mb * kk2 * 8, stream));
   if (S > 1) FUELG_TRY(kept_m.alloc((size_t)mb * kk2 * 8, stream));
   uint64_t* kept = S > 1 ? kept_m.as<uint64_t>() : kept_sp.as<uint64_t>();
@@ -848,7 +887,10 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.m = mcur;
     a.n = n;
     a.kc = kc;
+    a.ks_last = ((d + 15) / 16) - (kc - 1) * (BK / 16);
     a.kk2 = kk2;
+    a.row_k = row_k != nullptr ? row_k + b0 : nullptr;
+    a.exact_sq = margin == 0 ? 1 : 0;
     a.exact = exact ? 1 : 0;
     a.split = split;
     a.stages = stages;
@@ -890,12 +932,14 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     const size_t rsm = (size_t)8 * (d + 4) * sizeof(float);
     const unsigned rg = (unsigned)((mcur * 32 + 255) / 256);
     if (order == ORDER_X86)
-      knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2, metric,
+      knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2,
+                                                              row_k != nullptr ? row_k + b0 : nullptr, metric,
                                                               kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
                                                               gamma, redo.as<int32_t>(), nredo.as<int32_t>());
     else
-      knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2, metric,
+      knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2,
+                                                              row_k != nullptr ? row_k + b0 : nullptr, metric,
                                                               kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
                                                               gamma, redo.as<int32_t>(), nredo.as<int32_t>());

@@ -23,8 +23,11 @@
 #include <cub/device/device_scan.cuh>
 #include <vector>
 
+#include "../../include/fuelg.h"
 #include "fuelg_common.cuh"
 #include "fuelg_internal.h"
+#include "fuelg_prep.cuh"
+#include "fuelg_sums.cuh"
 
 namespace fuelg {
 
@@ -40,8 +43,16 @@ ExactSums* exact_sums_new();
 void exact_sums_delete(ExactSums*);
 int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaStream_t stream);
 int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
-                    bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream);
+                    bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream,
+                    const CentrePrep* cp);
+int exact_sums_update(ExactSums* s, const float* X, bool write_centers, float* centers, int32_t* changed,
+                      const CentrePrep* cp, cudaStream_t stream);
+void exact_sums_commit_view(ExactSums* s, SumsCommit* v);
 int lloyd_tc_rescored_total(TcLloydState* st, cudaStream_t stream, int64_t* out);
+int lloyd_tc_pass_fused(const LloydParams& p, TcLloydState* st, const float* centers, int32_t* labels,
+                        const SumsCommit& sc, int* dev_status, cudaStream_t stream);
+CentrePrep lloyd_tc_centre_prep(TcLloydState* st);
+bool lloyd_tc_scaled(const TcLloydState* st);
 
 namespace {
 
@@ -340,7 +351,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   if (p.precision != 0 && lloyd_tc_supported(d, k) && tc_fits) {
     tc = lloyd_tc_new();
     FUELG_TRY(lloyd_tc_prepare(p, tc, stream));
-    r->precision_used = p.precision;
+    r->precision_used = lloyd_tc_scaled(tc) ? FUELG_PREC_SPLIT_BF16_SCALED : p.precision;
   } else {
     FUELG_TRY(keys.alloc(sizeof(uint64_t) * n, stream));
   }
@@ -371,13 +382,24 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   };
   // one pass: assign, commit labels, update sums, and (if another pass
   // follows) the centres it will use
+  // Tensor-core tier with exact sums: every pass after the first is one
+  // fused screen launch (labels committed, undecided points re-scored, buckets
+  // planned in place), then the sum update, whose centre kernel also writes the
+  // next pass's BF16 centre copies.
+  CentrePrep cprep;
+  if (tc) cprep = lloyd_tc_centre_prep(tc);
+  SumsCommit scv{};
+  if (exact) exact_sums_commit_view(es, &scv);
   auto pass = [&](bool first, bool write_centers) -> int {
-    FUELG_TRY(assign(first));
+    const bool fused = tc && exact && !first && d <= 1024;
+    if (fused) FUELG_TRY(lloyd_tc_pass_fused(p, tc, C, labels, scv, dev_status, stream));
+    else FUELG_TRY(assign(first));
     if (p.tol > 0 && write_centers)
       FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
+    if (fused) return exact_sums_update(es, p.X, write_centers, C, changed.as<int32_t>(), &cprep, stream);
     if (exact)
       return exact_sums_step(es, p.X, lab_new.as<int32_t>(), labels, first, write_centers, C, changed.as<int32_t>(),
-                             dev_status, stream);
+                             dev_status, stream, tc ? &cprep : nullptr);
     FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t), stream));
     post_assign_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(lab_new.as<int32_t>(), n, labels,
                                                                        first ? 1 : 0, changed.as<int32_t>()); ::fuelg::note_launch();

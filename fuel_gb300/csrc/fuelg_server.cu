@@ -4,12 +4,15 @@
 // Requests (query rows + k) are queued on submit.  Each worker owns a CUDA
 // stream and, whenever it is free, takes every queued request that fits its
 // batch (query rows) and the server's device-memory budget, runs them as one
-// kNN batch (top-max(k) keys, exactly the keys each request would get alone:
-// the k smallest (distance, index) keys are a prefix of the k' smallest for
-// k' >= k), and hands each request its own first k columns.  Requests that
+// kNN batch -- one tensor-core launch in which every query row selects only
+// its own request's k (plus the proof margin); the plain tier computes
+// top-max(k) -- exactly the keys each request would get alone: the k smallest
+// (distance, index) keys are a prefix of the k' smallest for k' >= k -- and
+// hands each request its own first k columns.  Requests that
 // arrive while batches are on the GPU are admitted by the next free worker as
 // memory frees up, so their device work overlaps.  Results are bit-identical
 // to a single fuelg_knn call on the same rows.
+#include <algorithm>
 #include <condition_variable>
 #include <chrono>
 #include <cstring>
@@ -72,13 +75,14 @@ size_t request_bytes(int64_t m, int d, int k) {
                       (size_t)(3 * kk2 + 256) * 8 + 64);
 }
 
-int run_batch(fuelg_server* sv, std::vector<Request*>& batch, cudaStream_t s, float* pin_q, int64_t* pin_i,
-              float* pin_d, double* ms_out) {
+int run_batch(fuelg_server* sv, std::vector<Request*>& batch, cudaStream_t s, float* pin_q, int32_t* pin_k,
+              int64_t* pin_i, float* pin_d, double* ms_out) {
   const IndexView& ix = sv->view;
   int64_t m = 0;
   int kmax = 0;
   for (Request* r : batch) {
     memcpy(pin_q + m * ix.d, r->q.data(), sizeof(float) * r->m * ix.d);
+    for (int64_t i = 0; i < r->m; i++) pin_k[m + i] = r->k;
     m += r->m;
     kmax = std::max(kmax, r->k);
   }
@@ -93,20 +97,23 @@ int run_batch(fuelg_server* sv, std::vector<Request*>& batch, cudaStream_t s, fl
     }
   } eg{e0, e1};
   cudaEventRecord(e0, s);
-  Scratch q, keys, oi, od, dstat;
+  Scratch q, rk, keys, oi, od, dstat;
   FUELG_TRY(q.alloc(sizeof(float) * m * ix.d, s));
+  FUELG_TRY(rk.alloc(sizeof(int32_t) * m, s));
   FUELG_TRY(keys.alloc(sizeof(uint64_t) * m * kmax, s));
   FUELG_TRY(oi.alloc(sizeof(int64_t) * m * kmax, s));
   FUELG_TRY(od.alloc(sizeof(float) * m * kmax, s));
   FUELG_TRY(dstat.alloc(sizeof(int), s));
   FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
   FUELG_CUDA(cudaMemcpyAsync(q.p, pin_q, sizeof(float) * m * ix.d, cudaMemcpyHostToDevice, s));
+  FUELG_CUDA(cudaMemcpyAsync(rk.p, pin_k, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
   const int split = sv->precision == FUELG_PREC_SPLIT_BF16 ? 1 : 0;
   if (sv->precision != FUELG_PREC_FP32 && ix.tc && knn_tc_supported(ix.d, kmax, split)) {
+    // one launch for the mixed batch: every row selects only its own k (plus margin)
     int64_t rescored = 0;
     int exact = 0;
     FUELG_TRY(knn_tc_topk(ix.tc, q.as<float>(), m, ix.X, kmax, ix.order, ix.metric, split, keys.as<uint64_t>(),
-                          dstat.as<int>(), s, &rescored, &exact));
+                          dstat.as<int>(), s, &rescored, &exact, rk.as<int32_t>()));
   } else {
     ExactScanParams p;
     p.A = q.as<float>();
@@ -158,9 +165,11 @@ void worker_main(fuelg_server* sv) {
   const int d = sv->view.d;
   // pinned staging for one batch (kmax <= 4095 bounded by submit checks)
   float* pin_q = nullptr;
+  int32_t* pin_k = nullptr;
   int64_t* pin_i = nullptr;
   float* pin_d = nullptr;
   cudaHostAlloc(&pin_q, sizeof(float) * rows * d, cudaHostAllocDefault);
+  cudaHostAlloc(&pin_k, sizeof(int32_t) * rows, cudaHostAllocDefault);
   size_t out_cap = 0;
   for (;;) {
     std::vector<Request*> batch;
@@ -197,7 +206,8 @@ void worker_main(fuelg_server* sv) {
       cudaHostAlloc(&pin_d, sizeof(float) * out_cap, cudaHostAllocDefault);
     }
     double ms = 0.0;
-    const int st = (pin_q && pin_i && pin_d) ? run_batch(sv, batch, s, pin_q, pin_i, pin_d, &ms) : ST_ENOMEM;
+    const int st = (pin_q && pin_k && pin_i && pin_d) ? run_batch(sv, batch, s, pin_q, pin_k, pin_i, pin_d, &ms)
+                                                      : ST_ENOMEM;
     const std::string err = st == ST_OK ? std::string() : std::string(fuelg_last_error());
     {
       std::lock_guard<std::mutex> lk(sv->mu);
@@ -220,6 +230,7 @@ void worker_main(fuelg_server* sv) {
     sv->cv_work.notify_all();
   }
   if (pin_q) cudaFreeHost(pin_q);
+  if (pin_k) cudaFreeHost(pin_k);
   if (pin_i) cudaFreeHost(pin_i);
   if (pin_d) cudaFreeHost(pin_d);
   cudaStreamDestroy(s);

@@ -19,12 +19,12 @@
 #include "fuelg_common.cuh"
 #include "fuelg_exact.cuh"
 #include "fuelg_internal.h"
+#include "fuelg_prep.cuh"
+#include "fuelg_sums.cuh"
 
 namespace fuelg {
 
 namespace {
-
-constexpr int kRows = 32;  // rows per accumulation chunk
 
 __device__ __forceinline__ void range_acc(float x, int& lo, int& hi, int& bad) {
   uint32_t mant;
@@ -71,7 +71,6 @@ __global__ void exp_range_kernel(const float* __restrict__ X, int64_t count, int
 // Changed labels -> change list + per-cluster in/out histograms.  `first`: no
 // previous label (the initial assignment puts every point in).  Histograms are
 // aggregated in shared memory per block when k fits (integer counts: exact).
-constexpr int kSmemK = 4096;
 
 __device__ __forceinline__ void commit_body(int bid, int nblk, int32_t* h_in, int32_t* h_out,
                                             const int32_t* __restrict__ lab_new, int64_t n, int first, int k,
@@ -122,44 +121,6 @@ __device__ __forceinline__ void commit_body(int bid, int nblk, int32_t* h_in, in
     }
 }
 
-__device__ __forceinline__ void plan_body(int k, const int32_t* __restrict__ cin, const int32_t* __restrict__ cout,
-                                          int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
-                                          int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts,
-                                          int32_t* __restrict__ chunk_info) {
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x >= 32) return;  // callers run this with warp 0 only
-  int32_t carry_c = 0;
-  for (int pass = 0; pass < 2; pass++) {
-    const int32_t* cnt = pass == 0 ? cin : cout;
-    int32_t* off = pass == 0 ? off_in : off_out;
-    int32_t carry_m = 0;
-    for (int t0 = 0; t0 < k; t0 += 32) {
-      const int j = t0 + lane;
-      const int32_t c = j < k ? cnt[j] : 0;
-      const int32_t nc = (c + kRows - 1) / kRows;
-      int32_t a = c, b = nc;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int32_t ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
-        if (lane >= o) {
-          a += ua;
-          b += ub;
-        }
-      }
-      if (j < k) {
-        off[j] = carry_m + a - c;
-        const int32_t c0 = carry_c + b - nc;
-        chunk_off[pass * k + j] = c0;
-        for (int q = 0; q < nc; q++) chunk_info[c0 + q] = j | (pass << 31);
-        if (pass == 0) counts[j] += cin[j] - cout[j];
-      }
-      carry_m += __shfl_sync(0xffffffffu, a, 31);
-      carry_c += __shfl_sync(0xffffffffu, b, 31);
-    }
-  }
-  if (lane == 0) chunk_off[2 * k] = carry_c;
-}
-
 // Commit, then the last block to finish (a ticket after a fence: no
 // waiting) plans the buckets from the complete histograms.
 __global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64_t n, int first, int k,
@@ -181,14 +142,10 @@ __global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64
   __syncthreads();
   if (s_last) {
     __threadfence();
-    if (threadIdx.x < 32) plan_body(k, cin, cout, off_in, off_out, chunk_off, counts, chunk_info);
+    if (threadIdx.x < 32) plan_body(threadIdx.x, k, cin, cout, off_in, off_out, chunk_off, counts, chunk_info);
     if (threadIdx.x == 0) *done = 0;
   }
 }
-
-// Single warp: bucket offsets and the chunk table (in-chunks of cluster
-// 0..k-1, then out-chunks), member counts, and chunk_info[c] = cluster of
-// chunk c (bit 31: an out-chunk).  Warp-shuffle scans over 32-entry tiles.
 
 __device__ __forceinline__ void scatter_body(int bid, int nblk, int32_t* c_in, int32_t* c_out,
                                              const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
@@ -330,45 +287,45 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
                      bucket_in, bucket_out, limbs);
 }
 
-// Canonicalise every coordinate's limbs and write the exact mean of non-empty
-// clusters as the correctly rounded f32 centre.
+// Canonicalise one coordinate's limbs and, for a non-empty cluster, write
+// its exact mean as the correctly rounded f32 centre coordinate.
 template <int L>
-__device__ __forceinline__ void mean_body(int bid, int nblk, unsigned long long* __restrict__ limbs, int64_t kd,
-                                          int d, int e_lo, const int32_t* __restrict__ counts,
-                                          float* __restrict__ centers, int write_centers,
-                                          int32_t* __restrict__ nchg, int32_t* __restrict__ changed,
-                                          int32_t* __restrict__ zero4k, int nzero) {
-  // hand the change count to the host and reset the per-pass counters
+__device__ __forceinline__ void mean_elem(unsigned long long* __restrict__ limbs, int64_t e, int d, int e_lo,
+                                          const int32_t* __restrict__ counts, float* __restrict__ centers,
+                                          int write_centers) {
+  unsigned long long* lp = limbs + e * L;
+  unsigned __int128 tot = 0;
+#pragma unroll
+  for (int l = 0; l < L; l++) tot += (unsigned __int128)lp[l] << (32 * l);
+  if constexpr (L < 4) tot &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
+#pragma unroll
+  for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
+  const int j = (int)(e / d);
+  const int cnt = counts[j];
+  if (cnt <= 0 || !write_centers) return;
+  const bool neg = (tot >> (32 * L - 1)) & 1;
+  unsigned __int128 mag = tot;
+  if (neg) {
+    if constexpr (L < 4) {
+      mag = (((unsigned __int128)1) << (32 * (L % 4))) - tot;
+      mag &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
+    } else {
+      mag = (unsigned __int128)0 - tot;
+    }
+  }
+  float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, e_lo);
+  centers[e] = neg ? -v : v;
+}
+
+// Hand the change count to the host and reset the per-pass counters.
+__device__ __forceinline__ void mean_handoff(int bid, int nblk, int32_t* __restrict__ nchg,
+                                             int32_t* __restrict__ changed, int32_t* __restrict__ zero4k, int nzero) {
   if (bid == 0 && threadIdx.x == 0) {
     *changed = *nchg;
     *nchg = 0;
   }
   for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < nzero; e += (int64_t)nblk * blockDim.x)
     zero4k[e] = 0;
-  for (int64_t e = (int64_t)bid * blockDim.x + threadIdx.x; e < kd; e += (int64_t)nblk * blockDim.x) {
-    unsigned long long* lp = limbs + e * L;
-    unsigned __int128 tot = 0;
-#pragma unroll
-    for (int l = 0; l < L; l++) tot += (unsigned __int128)lp[l] << (32 * l);
-    if constexpr (L < 4) tot &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
-#pragma unroll
-    for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
-    const int j = (int)(e / d);
-    const int cnt = counts[j];
-    if (cnt <= 0 || !write_centers) continue;
-    const bool neg = (tot >> (32 * L - 1)) & 1;
-    unsigned __int128 mag = tot;
-    if (neg) {
-      if constexpr (L < 4) {
-        mag = (((unsigned __int128)1) << (32 * (L % 4))) - tot;
-        mag &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
-      } else {
-        mag = (unsigned __int128)0 - tot;
-      }
-    }
-    float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, e_lo);
-    centers[e] = neg ? -v : v;
-  }
 }
 
 template <int L>
@@ -377,8 +334,32 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
                             int32_t* __restrict__ nchg, int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
                             int nzero) {
   griddep_wait();
-  mean_body<L>(blockIdx.x, gridDim.x, limbs, kd, d, e_lo, counts, centers, write_centers, nchg, changed, zero4k,
-               nzero);
+  mean_handoff(blockIdx.x, gridDim.x, nchg, changed, zero4k, nzero);
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kd; e += (int64_t)gridDim.x * blockDim.x)
+    mean_elem<L>(limbs, e, d, e_lo, counts, centers, write_centers);
+}
+
+// The same update, one block per centre row, which then also writes the
+// row's BF16 copies and norms for the next pass's tensor-core screen (block
+// j >= k: a zero padding row of the copies).
+template <int L, bool SPLIT>
+__global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __restrict__ limbs, int k, int d,
+                                                        int e_lo, const int32_t* __restrict__ counts,
+                                                        float* __restrict__ centers, int32_t* __restrict__ nchg,
+                                                        int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
+                                                        int nzero, CentrePrep cp) {
+  griddep_wait();
+  mean_handoff(blockIdx.x, gridDim.x, nchg, changed, zero4k, nzero);
+  if (cp.zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *cp.zero_word = 0;
+  const int j = blockIdx.x;
+  if (j < k)
+    for (int c = threadIdx.x; c < d; c += blockDim.x) mean_elem<L>(limbs, (int64_t)j * d + c, d, e_lo, counts, centers, 1);
+  __syncthreads();  // the row's centre values are visible to warp 0
+  if (threadIdx.x < 32) {
+    const float* row = centers + (int64_t)j * d;
+    const bool vec = ((d & 3) == 0) && ((reinterpret_cast<uintptr_t>(centers) & 15) == 0);
+    prep_row<SPLIT>(row, j, j < k, vec, d, cp.dp, 0, cp.hi, cp.lo, cp.nrm2, cp.nrm, threadIdx.x, cp.scale);
+  }
 }
 
 }  // namespace
@@ -448,26 +429,38 @@ int exact_sums_init(ExactSums* s, const float* X, int64_t n, int d, int k, cudaS
 
 int exact_sums_L(const ExactSums* s) { return s->L; }
 
-// Apply one assignment pass: commit lab_new into labels, record the changes,
-// update the exact sums and counts, and write the new centres.  *changed
+// Device pointers for a fused pass that commits its labels itself.
+void exact_sums_commit_view(ExactSums* s, SumsCommit* v) {
+  const int k = s->k;
+  v->chg_i = s->chg_i.as<int32_t>();
+  v->chg_old = s->chg_old.as<int32_t>();
+  v->chg_new = s->chg_new.as<int32_t>();
+  v->nchg = s->nchg.as<int32_t>();
+  v->cin = s->cin.as<int32_t>();
+  v->cout = v->cin + k;
+  v->off_in = s->off_in.as<int32_t>();
+  v->off_out = v->off_in + k;
+  v->chunk_off = s->chunk_off.as<int32_t>();
+  v->counts = s->counts.as<int32_t>();
+  v->chunk_info = s->chunk_info.as<int32_t>();
+  v->done = s->done.as<unsigned>();
+  v->k = k;
+}
+
+// Update after a committed pass (labels, change list, histograms and plan in
+// place): scatter the changed points into per-cluster buckets, add their
+// exact fixed-point rows into the sums, and write the new centres -- with cp,
+// also the BF16 centre copies the next tensor-core screen reads.  *changed
 // (device) receives the number of changed labels.
-int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
-                    bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream) {
-  const int64_t n = s->n;
+int exact_sums_update(ExactSums* s, const float* X, bool write_centers, float* centers, int32_t* changed,
+                      const CentrePrep* cp, cudaStream_t stream) {
   const int k = s->k, d = s->d;
   int32_t* cin = s->cin.as<int32_t>();
-  int32_t* cout = cin + k;
   int32_t* cur_in = cin + 2 * k;
   int32_t* cur_out = cin + 3 * k;
   int32_t* off_in = s->off_in.as<int32_t>();
   int32_t* off_out = off_in + k;
   const int ty = (d + 255) / 256;
-  // counters were zeroed at init and are reset by mean_kernel after every pass
-  FUELG_TRY(launch_pdl(commit_changes_kernel, dim3((unsigned)std::min<int64_t>((n + 255) / 256, 2 * 152)), dim3(256),
-                       0, stream, lab_new, n, first ? 1 : 0, k, labels, s->chg_i.as<int32_t>(),
-                       s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), cin, cout,
-                       s->done.as<unsigned>(), off_in, off_out, s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(),
-                       s->chunk_info.as<int32_t>()));
   FUELG_TRY(launch_pdl(bucket_scatter_kernel, dim3(2 * 152), dim3(256), 0, stream,
                        (const int32_t*)s->chg_i.as<int32_t>(), (const int32_t*)s->chg_old.as<int32_t>(),
                        (const int32_t*)s->chg_new.as<int32_t>(), (const int32_t*)s->nchg.as<int32_t>(), k,
@@ -476,16 +469,24 @@ int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_
   const dim3 g((unsigned)std::min<int64_t>(s->max_chunks * ty, 8 * 152));
   const int64_t kd = (int64_t)k * d;
   const unsigned mg = (unsigned)std::min<int64_t>((kd + 255) / 256, 8 * 152);
+  const bool prep = cp != nullptr && cp->hi != nullptr && write_centers;
   auto run = [&](auto Lc) -> int {
     constexpr int LL = decltype(Lc)::value;
     FUELG_TRY(launch_pdl(accumulate_kernel<LL>, g, dim3(256), 0, stream, X, d, k, s->e_lo, ty,
                          (const int32_t*)s->chunk_off.as<int32_t>(), (const int32_t*)s->chunk_info.as<int32_t>(),
-                         (const int32_t*)cin, (const int32_t*)cout, (const int32_t*)off_in, (const int32_t*)off_out,
-                         (const int32_t*)s->bucket_in.as<int32_t>(), (const int32_t*)s->bucket_out.as<int32_t>(),
-                         s->limbs.as<unsigned long long>()));
-    FUELG_TRY(launch_pdl(mean_kernel<LL>, dim3(mg), dim3(256), 0, stream, s->limbs.as<unsigned long long>(), kd, d,
-                         s->e_lo, (const int32_t*)s->counts.as<int32_t>(), centers, write_centers ? 1 : 0,
-                         s->nchg.as<int32_t>(), changed, cin, 4 * k));
+                         (const int32_t*)cin, (const int32_t*)(cin + k), (const int32_t*)off_in,
+                         (const int32_t*)off_out, (const int32_t*)s->bucket_in.as<int32_t>(),
+                         (const int32_t*)s->bucket_out.as<int32_t>(), s->limbs.as<unsigned long long>()));
+    if (prep) {
+      auto mk = cp->lo != nullptr ? mean_prep_kernel<LL, true> : mean_prep_kernel<LL, false>;
+      FUELG_TRY(launch_pdl(mk, dim3((unsigned)cp->kp), dim3(256), 0, stream, s->limbs.as<unsigned long long>(), k, d,
+                           s->e_lo, (const int32_t*)s->counts.as<int32_t>(), centers, s->nchg.as<int32_t>(), changed,
+                           cin, 4 * k, *cp));
+    } else {
+      FUELG_TRY(launch_pdl(mean_kernel<LL>, dim3(mg), dim3(256), 0, stream, s->limbs.as<unsigned long long>(), kd, d,
+                           s->e_lo, (const int32_t*)s->counts.as<int32_t>(), centers, write_centers ? 1 : 0,
+                           s->nchg.as<int32_t>(), changed, cin, 4 * k));
+    }
     return ST_OK;
   };
   switch (s->L) {
@@ -495,6 +496,28 @@ int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_
     default: FUELG_TRY(run(std::integral_constant<int, 4>())); break;
   }
   return ST_OK;
+}
+
+// Apply one assignment pass: commit lab_new into labels, record the changes,
+// update the exact sums and counts, and write the new centres (and, with cp,
+// their BF16 copies).  *changed (device) receives the number of changed labels.
+int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_t* labels, bool first,
+                    bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream,
+                    const CentrePrep* cp) {
+  (void)dev_status;
+  const int64_t n = s->n;
+  const int k = s->k;
+  int32_t* cin = s->cin.as<int32_t>();
+  int32_t* cout = cin + k;
+  int32_t* off_in = s->off_in.as<int32_t>();
+  int32_t* off_out = off_in + k;
+  // counters were zeroed at init and are reset by the centre update after every pass
+  FUELG_TRY(launch_pdl(commit_changes_kernel, dim3((unsigned)std::min<int64_t>((n + 255) / 256, 2 * 152)), dim3(256),
+                       0, stream, lab_new, n, first ? 1 : 0, k, labels, s->chg_i.as<int32_t>(),
+                       s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), cin, cout,
+                       s->done.as<unsigned>(), off_in, off_out, s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(),
+                       s->chunk_info.as<int32_t>()));
+  return exact_sums_update(s, X, write_centers, centers, changed, cp, stream);
 }
 
 }  // namespace fuelg

@@ -1,0 +1,64 @@
+// fuelg_sums.cuh -- device pieces of the exact centroid-sum update shared by
+// the update kernels (fuelg_sums.cu) and the fused tensor-core Lloyd pass
+// (fuelg_tc.cu), which commits its labels and plans the buckets itself.
+#pragma once
+
+#include <cstdint>
+
+namespace fuelg {
+
+constexpr int kRows = 32;     // rows per accumulation chunk
+constexpr int kSmemK = 4096;  // clusters whose histograms fit shared memory
+
+// Device state a fused assignment pass writes instead of the commit kernel:
+// the change list (point, old, new label) with its length, the per-cluster
+// in/out histograms, and -- from the last CTA, by ticket -- the bucket plan.
+struct SumsCommit {
+  int32_t *chg_i, *chg_old, *chg_new, *nchg;
+  int32_t *cin, *cout;  // histograms (zeroed by the previous centre update)
+  int32_t *off_in, *off_out, *chunk_off, *counts, *chunk_info;
+  unsigned* done;  // ticket, reset by the last CTA
+  int k;
+};
+
+// One full warp (lane = its lane index): bucket offsets and the chunk table
+// (in-chunks of cluster 0..k-1, then out-chunks), member counts, and
+// chunk_info[c] = cluster of chunk c (bit 31: an out-chunk), from the
+// complete in/out histograms.  Warp-shuffle scans over 32-entry tiles.
+__device__ __forceinline__ void plan_body(int lane, int k, const int32_t* __restrict__ cin,
+                                          const int32_t* __restrict__ cout, int32_t* __restrict__ off_in,
+                                          int32_t* __restrict__ off_out, int32_t* __restrict__ chunk_off,
+                                          int32_t* __restrict__ counts, int32_t* __restrict__ chunk_info) {
+  int32_t carry_c = 0;
+  for (int pass = 0; pass < 2; pass++) {
+    const int32_t* cnt = pass == 0 ? cin : cout;
+    int32_t* off = pass == 0 ? off_in : off_out;
+    int32_t carry_m = 0;
+    for (int t0 = 0; t0 < k; t0 += 32) {
+      const int j = t0 + lane;
+      const int32_t c = j < k ? cnt[j] : 0;
+      const int32_t nc = (c + kRows - 1) / kRows;
+      int32_t a = c, b = nc;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+        if (lane >= o) {
+          a += ua;
+          b += ub;
+        }
+      }
+      if (j < k) {
+        off[j] = carry_m + a - c;
+        const int32_t c0 = carry_c + b - nc;
+        chunk_off[pass * k + j] = c0;
+        for (int q = 0; q < nc; q++) chunk_info[c0 + q] = j | (pass << 31);
+        if (pass == 0) counts[j] += cin[j] - cout[j];
+      }
+      carry_m += __shfl_sync(0xffffffffu, a, 31);
+      carry_c += __shfl_sync(0xffffffffu, b, 31);
+    }
+  }
+  if (lane == 0) chunk_off[2 * k] = carry_c;
+}
+
+}  // namespace fuelg

@@ -35,6 +35,8 @@
 
 #include "fuelg_common.cuh"
 #include "fuelg_internal.h"
+#include "fuelg_prep.cuh"
+#include "fuelg_sums.cuh"
 #include "fuelg_tc_common.cuh"
 
 namespace fuelg {
@@ -45,402 +47,6 @@ namespace {
 
 constexpr int BM = 128;  // points per tile (UMMA M)
 constexpr int kTcThreads = 192;
-
-struct TcArgs {
-  int64_t n;
-  int d, k, kp, kc, stages;
-  const float* nx;  // ||x||^2 per point (f32 of an FP64 sum)
-  const float* xn;  // ||x||
-  const float* nc;  // ||c||^2 per (padded) centre
-  const float* cn;  // ||c||
-  int32_t* lab_new;
-  int32_t* ulist;
-  uint64_t* umask;
-  int32_t* ucount;
-  int mw;
-  float alpha, beta, gamma;
-  uint32_t idesc;
-  uint32_t tmem_cols;
-  int a_tiled;  // A copies are tile-major (see prep_offset)
-  float s_scale;              // nonneg data: sum|x_i c_i| <= dot * s_scale
-  int sep_lo;                 // hi+lo: the hi.lo + lo.hi terms have their own accumulator
-  const int* neg_flag;        // != 0 when X holds a negative value
-  int* status;
-  const volatile int* cancel;
-};
-
-template <bool SPLIT>
-__global__ void __launch_bounds__(kTcThreads, 2)
-    lloyd_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
-                    const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo, TcArgs a) {
-  extern __shared__ __align__(1024) uint8_t smem_raw[];
-  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
-  const uint32_t a_bytes = BM * BK * 2;
-  const uint32_t b_bytes = (uint32_t)a.kp * BK * 2;
-  const uint32_t stage_bytes = (SPLIT ? 2u : 1u) * (a_bytes + b_bytes);
-  const int NS = a.stages;
-  uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)NS * stage_bytes);
-  uint64_t* empty = full + NS;
-  uint64_t* accf = empty + NS;
-  uint64_t* acce = accf + 2;
-  uint64_t* fin = acce + 2;
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
-  float* snc = reinterpret_cast<float*>(tmem_holder + 4);
-  float* scn = snc + a.kp;
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t ntiles = (a.n + BM - 1) / BM;
-
-  if (threadIdx.x == 0) {
-    for (int s = 0; s < NS; s++) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
-    }
-    for (int b = 0; b < 2; b++) {
-      mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], BM);
-    }
-    mbar_init(fin, 1);
-    *abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-  }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
-                 "r"(a.tmem_cols)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  const uint32_t tmem_base = *tmem_holder;
-  // X does not depend on the predecessor kernel: the producer issues the A
-  // (point) tiles of the first NS stages before waiting for it; the centre
-  // tiles (B) and norms come from the predecessor.
-  int pre = 0;
-  if (warp == 0 && lane == 0) {
-    prefetch_tmap(&tmA);
-    if (SPLIT) prefetch_tmap(&tmAlo);
-    const uint64_t pol_a = policy_evict_first();
-    int64_t t = blockIdx.x;
-    int kc = 0;
-    for (int st = 0; st < NS && t < ntiles; st++) {
-      uint8_t* sA = base + (size_t)st * stage_bytes;
-      uint8_t* sB = sA + a_bytes;
-      mbar_expect_tx(&full[st], stage_bytes);
-      const int ax = a.a_tiled ? 0 : kc * BK;
-      const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
-      tma_load_2d_hint(sA, &tmA, ax, ay, &full[st], pol_a);
-      if (SPLIT) tma_load_2d_hint(sB + b_bytes, &tmAlo, ax, ay, &full[st], pol_a);
-      pre++;
-      if (++kc == a.kc) {
-        kc = 0;
-        t += gridDim.x;
-      }
-    }
-  }
-  griddep_wait();
-  for (int j = threadIdx.x; j < a.kp; j += blockDim.x) {
-    snc[j] = a.nc[j];
-    scn[j] = a.cn[j];
-  }
-  __syncthreads();
-
-  if (warp == 0) {
-    if (lane == 0) {
-      prefetch_tmap(&tmB);
-      if (SPLIT) prefetch_tmap(&tmBlo);
-      const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
-      uint32_t stage = 0, phase = 0;
-      uint32_t armed = 0, last_ph = 0;  // per-stage bit: armed at least once / parity of the last arm
-      int tile_no = 0;
-      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, tile_no++) {
-        if (a.cancel != nullptr && *a.cancel) {
-          atomicOr(a.status, DEV_CANCELLED);
-          *abort_flag = 1;
-          break;
-        }
-        for (int kc = 0; kc < a.kc; kc++) {
-          uint8_t* sA = base + (size_t)stage * stage_bytes;
-          uint8_t* sB = sA + a_bytes;
-          armed |= 1u << stage;
-          last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
-          if (pre > 0) {
-            // A already in flight (issued before the dependency wait)
-            pre--;
-          } else {
-            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
-              if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-              *abort_flag = 1;
-              break;
-            }
-            mbar_expect_tx(&full[stage], stage_bytes);
-            const int ax = a.a_tiled ? 0 : kc * BK;
-            const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
-            tma_load_2d_hint(sA, &tmA, ax, ay, &full[stage], pol_a);
-            if (SPLIT) tma_load_2d_hint(sB + b_bytes, &tmAlo, ax, ay, &full[stage], pol_a);
-          }
-          tma_load_2d_hint(sB, &tmB, kc * BK, 0, &full[stage], pol_b);
-          if (SPLIT) tma_load_2d_hint(sB + b_bytes + a_bytes, &tmBlo, kc * BK, 0, &full[stage], pol_b);
-          if (++stage == (uint32_t)NS) {
-            stage = 0;
-            phase ^= 1;
-          }
-        }
-      }
-      // Never leave the CTA with a TMA copy still writing shared memory: wait
-      // (bounded) for the last load armed on every stage.
-      for (int s2 = 0; s2 < NS; s2++)
-        if (armed & (1u << s2)) {
-          volatile int never = 0;
-          if (!mbar_wait(&full[s2], (last_ph >> s2) & 1u, &never)) atomicOr(a.status, DEV_TIMEOUT);
-        }
-    }
-  } else if (warp == 1) {
-    if (lane == 0) {
-      uint32_t stage = 0, phase = 0;
-      int64_t lt = 0;
-      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, lt++) {
-        const uint32_t buf = (uint32_t)(lt & 1), accph = (uint32_t)((lt >> 1) & 1);
-        if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag)) {
-          if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-          *abort_flag = 1;
-          break;
-        }
-        tc_fence_after();
-        // split: hi.hi accumulates at [0, kp), the hi.lo + lo.hi terms at [kp, 2kp)
-        const uint32_t acc_cols = (SPLIT && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
-        const uint32_t d_tmem = tmem_base + buf * acc_cols;
-        const uint32_t d_lo = d_tmem + (a.sep_lo ? (uint32_t)a.kp : 0u);
-        bool ok = true;
-        for (int kc = 0; kc < a.kc; kc++) {
-          if (!mbar_wait(&full[stage], phase, abort_flag)) {
-            if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-            *abort_flag = 1;
-            ok = false;
-            break;
-          }
-          tc_fence_after();
-          uint8_t* sA = base + (size_t)stage * stage_bytes;
-          uint8_t* sB = sA + a_bytes;
-          const uint64_t ad = smem_desc_sw128(smem_u32(sA));
-          const uint64_t bd = smem_desc_sw128(smem_u32(sB));
-#pragma unroll
-          for (int kk = 0; kk < BK / 16; kk++) {
-            // advance 16 BF16 (32 bytes) along K inside the swizzled row
-            umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (kc | kk) != 0 ? 1u : 0u);
-            if (SPLIT) {
-              const uint64_t adlo = smem_desc_sw128(smem_u32(sB + b_bytes));
-              const uint64_t bdlo = smem_desc_sw128(smem_u32(sB + b_bytes + a_bytes));
-              umma_bf16(d_lo, ad + 2 * kk, bdlo + 2 * kk, a.idesc, (a.sep_lo && (kc | kk) == 0) ? 0u : 1u);
-              umma_bf16(d_lo, adlo + 2 * kk, bd + 2 * kk, a.idesc, 1u);
-            }
-          }
-          umma_commit(&empty[stage]);
-          if (++stage == (uint32_t)NS) {
-            stage = 0;
-            phase ^= 1;
-          }
-        }
-        if (!ok) break;
-        umma_commit(&accf[buf]);
-      }
-      // every MMA this thread issued has completed before TMEM is freed
-      umma_commit(fin);
-      volatile int never = 0;
-      if (!mbar_wait(fin, 0, &never)) atomicOr(a.status, DEV_TIMEOUT);
-    }
-  } else {
-    // epilogue: warps 2..5 -> TMEM lane groups 2,3,0,1
-    const int g = warp & 3;
-    const int row = g * 32 + lane;
-    int64_t lt = 0;
-    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
-      const uint32_t buf = (uint32_t)(lt & 1), accph = (uint32_t)((lt >> 1) & 1);
-      if (*abort_flag || !mbar_wait(&accf[buf], accph, abort_flag)) {
-        if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-        *abort_flag = 1;
-        break;
-      }
-      tc_fence_after();
-      const int64_t i = t * BM + row;
-      const bool valid = i < a.n;
-      const float nxi = valid ? a.nx[i] : 0.0f;
-      const float xni = valid ? a.xn[i] : 0.0f;
-      const uint32_t acc_cols = (SPLIT && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
-      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + buf * acc_cols;
-      const bool nonneg = *a.neg_flag == 0;
-      // pass 1: screened argmin (first index wins ties)
-      float best = __int_as_float(0x7f800000), best_dot = 0.0f;
-      int bj = 0;
-      for (int c0 = 0; c0 < a.kp; c0 += 16) {
-        float v[16];
-        tmem_ld16(taddr + c0, v);
-        if (SPLIT && a.sep_lo) {
-          float w[16];
-          tmem_ld16(taddr + a.kp + c0, w);
-#pragma unroll
-          for (int j = 0; j < 16; j++) v[j] += w[j];
-        }
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int col = c0 + j;
-          if (col < a.k) {
-            const float dt = fmaf(-2.0f, v[j], nxi + snc[col]);
-            if (dt < best) {
-              best = dt;
-              bj = col;
-              best_dot = v[j];
-            }
-          }
-        }
-      }
-      // S_j bounds sum_i |x_i c_ij|: |x||c_j| in general, the (inflated) dot product for nonnegative data
-      const float sb = nonneg ? fmaxf(best_dot, 0.0f) * a.s_scale : xni * scn[bj];
-      const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
-      const float hi = best + eb;
-      // pass 2: every other centre whose lower bound reaches the best's upper bound
-      uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
-      for (int c0 = 0; c0 < a.kp; c0 += 16) {
-        float v[16];
-        tmem_ld16(taddr + c0, v);
-        if (SPLIT && a.sep_lo) {
-          float w[16];
-          tmem_ld16(taddr + a.kp + c0, w);
-#pragma unroll
-          for (int j = 0; j < 16; j++) v[j] += w[j];
-        }
-#pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int col = c0 + j;
-          if (col < a.k && col != bj) {
-            const float dt = fmaf(-2.0f, v[j], nxi + snc[col]);
-            const float sj = nonneg ? fmaxf(v[j], 0.0f) * a.s_scale : xni * scn[col];
-            const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
-            if (!(dt - e > hi)) {
-              const uint64_t bit = 1ull << (col & 63);
-              const int w = col >> 6;
-              if (w == 0) m0 |= bit;
-              else if (w == 1) m1 |= bit;
-              else if (w == 2) m2 |= bit;
-              else m3 |= bit;
-            }
-          }
-        }
-      }
-      tc_fence_before();
-      mbar_arrive(&acce[buf]);
-      if (valid) {
-        if ((m0 | m1 | m2 | m3) == 0) {
-          a.lab_new[i] = bj;
-        } else {
-          const uint64_t bit = 1ull << (bj & 63);
-          const int w = bj >> 6;
-          if (w == 0) m0 |= bit;
-          else if (w == 1) m1 |= bit;
-          else if (w == 2) m2 |= bit;
-          else m3 |= bit;
-          a.lab_new[i] = -1;
-          const int u = atomicAdd(a.ucount, 1);
-          a.ulist[u] = (int32_t)i;
-          uint64_t* um = a.umask + (int64_t)u * a.mw;
-          um[0] = m0;
-          if (a.mw > 1) um[1] = m1;
-          if (a.mw > 2) um[2] = m2;
-          if (a.mw > 3) um[3] = m3;
-        }
-      }
-    }
-  }
-  tc_fence_before();
-  __syncthreads();
-  if (warp == 1) {
-    tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(a.tmem_cols)
-                 : "memory");
-  }
-}
-
-// X (f32) -> BF16 hi (and lo = BF16(x - hi)) copies with rows padded to dp
-// (a multiple of 8, zero filled), plus ||x||^2 and ||x||.  One warp per row,
-// four columns per lane per step; the squared norm is an FP32 sum of at most
-// 4*ceil(dp/128) terms per lane and a 5-level tree, so its relative error is
-// below (ceil(d/32) + 9) 2^-24 -- the beta term of the screen's error bound.
-// With tile_kc > 0 the copies are written tile-major -- [row tile of 128][K
-// chunk of 64][128 rows][64 columns] -- so that every TMA box the screen loads
-// is one contiguous 16 KB block of HBM; dp is then tile_kc * 64.
-__device__ __forceinline__ int64_t prep_offset(int64_t r, int c, int dp, int tile_kc) {
-  if (tile_kc == 0) return r * dp + c;
-  return (((r >> 7) * tile_kc + (c >> 6)) * 128 + (r & 127)) * 64 + (c & 63);
-}
-
-template <bool SPLIT>
-__global__ void prep_rows_kernel(const float* __restrict__ X, int64_t rows, int64_t valid_rows, int d, int dp,
-                                 int tile_kc, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
-                                 float* __restrict__ nrm2, float* __restrict__ nrm, int* __restrict__ neg_flag,
-                                 int32_t* __restrict__ zero_word) {
-  griddep_wait();
-  if (zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *zero_word = 0;
-  bool anyneg = false;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  const bool vec = ((d & 3) == 0) && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
-  for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < rows; r += (int64_t)gridDim.x * nw) {
-    float acc = 0.0f;
-    const bool v = r < valid_rows;
-    const float* xr = X + r * d;
-    // up to 8 chunks of 4 values per lane are loaded before any is used (the
-    // loads overlap), then converted in order (the norm chain keeps its order)
-    for (int cb = 4 * lane; cb < dp; cb += 128 * 8) {
-      float x8[8][4];
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int c0 = cb + 128 * u;
-        if (v && vec && c0 + 3 < d) {
-          const float4 t = __ldg(reinterpret_cast<const float4*>(xr + c0));
-          x8[u][0] = t.x, x8[u][1] = t.y, x8[u][2] = t.z, x8[u][3] = t.w;
-        } else {
-#pragma unroll
-          for (int q = 0; q < 4; q++) x8[u][q] = (v && c0 + q < d) ? __ldg(xr + c0 + q) : 0.0f;
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        const int c0 = cb + 128 * u;
-        if (c0 >= dp) break;
-        const float* x4 = x8[u];
-        __nv_bfloat162 h01 = __floats2bfloat162_rn(x4[0], x4[1]);
-        __nv_bfloat162 h23 = __floats2bfloat162_rn(x4[2], x4[3]);
-        uint2 hpack;
-        hpack.x = *reinterpret_cast<uint32_t*>(&h01);
-        hpack.y = *reinterpret_cast<uint32_t*>(&h23);
-        const int64_t off = prep_offset(r, c0, dp, tile_kc);
-        *reinterpret_cast<uint2*>(hi + off) = hpack;
-        if (SPLIT) {
-          const float2 f01 = __bfloat1622float2(h01), f23 = __bfloat1622float2(h23);
-          __nv_bfloat162 l01 = __floats2bfloat162_rn(x4[0] - f01.x, x4[1] - f01.y);
-          __nv_bfloat162 l23 = __floats2bfloat162_rn(x4[2] - f23.x, x4[3] - f23.y);
-          uint2 lpack;
-          lpack.x = *reinterpret_cast<uint32_t*>(&l01);
-          lpack.y = *reinterpret_cast<uint32_t*>(&l23);
-          *reinterpret_cast<uint2*>(lo + off) = lpack;
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) {
-          acc = fmaf(x4[q], x4[q], acc);
-          anyneg |= x4[q] < 0.0f;
-        }
-      }
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-    if (lane == 0) {
-      nrm2[r] = acc;
-      nrm[r] = sqrtf(acc);
-    }
-  }
-  if (neg_flag != nullptr && __any_sync(0xffffffffu, anyneg) && (threadIdx.x & 31) == 0) atomicOr(neg_flag, 1);
-}
 
 // Exact re-score of the undecided points: each candidate centre is scored
 // with the reference's own f32 operation order, first minimum wins.  One warp
@@ -503,14 +109,506 @@ __device__ __forceinline__ float warp_candidate_dist(const float* __restrict__ x
   }
 }
 
+// One warp re-scores one undecided point x against its candidate centres
+// (bit j of um[0..mw) set: centre j), PER at a time (this lane's slot is
+// lane / G); returns the first centre with the smallest exact distance, on
+// every lane.
+template <int KIND, int ORDER>
+__device__ __forceinline__ int rescore_point(const float* __restrict__ x, const float* __restrict__ C, int d, int mw,
+                                             const uint64_t* __restrict__ um, int lane) {
+  constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
+  constexpr int G = LANE8 ? 8 : (KIND == KIND_SQDIST ? 32 : 1);  // lanes per candidate
+  constexpr int PER = 32 / G;                                      // candidates per warp step
+  uint64_t best = KEY_NONE;
+  int w = 0;
+  uint64_t m = um[0];
+  const int slot = lane / G;
+  for (;;) {
+    int got = 0, j = 0;
+    while (got < PER) {
+      while (m == 0 && w + 1 < mw) m = um[++w];
+      if (m == 0) break;
+      const int b = __ffsll((long long)m) - 1;
+      m &= m - 1;
+      if (got == slot) j = w * 64 + b;
+      got++;
+    }
+    if (got == 0) break;
+    const bool mine = slot < got;
+    if (!mine) j = 0;  // idle slots score centre 0 and discard it
+    // lloyd.rs:166-168 calls sqdist(centre, point); the initial pairwise
+    // kernel takes (point, centre).  The squares are identical either way.
+    const float dist = warp_candidate_dist<KIND, ORDER>(x, C + (int64_t)j * d, d, lane);
+    if (mine && (lane % G) == 0) {
+      const uint64_t key = make_key(dist, (uint32_t)j);
+      best = key < best ? key : best;
+    }
+    if (got < PER) break;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const uint64_t o = __shfl_xor_sync(0xffffffffu, best, off);
+    best = o < best ? o : best;
+  }
+  return (int)key_idx(best);
+}
+
+struct TcArgs {
+  int64_t n;
+  int d, k, kp, kc, stages;
+  const float* nx;  // ||x||^2 per point (f32 of an FP64 sum)
+  const float* xn;  // ||x||
+  const float* nc;  // ||c||^2 per (padded) centre
+  const float* cn;  // ||c||
+  int32_t* lab_new;
+  int32_t* ulist;
+  uint64_t* umask;
+  int32_t* ucount;
+  int mw;
+  float alpha, beta, gamma;
+  uint32_t idesc;
+  uint32_t tmem_cols;
+  int a_tiled;  // A copies are tile-major (see prep_offset)
+  float s_scale;              // nonneg data: sum|x_i c_i| <= dot * s_scale
+  int sep_lo;                 // hi+lo: the hi.lo + lo.hi terms have their own accumulator
+  const int* neg_flag;        // != 0 when X holds a negative value
+  int* status;
+  const volatile int* cancel;
+  // Fused pass (every pass after the first of a k-means call): the labels of
+  // decided points are committed here (change list, histograms); the
+  // undecided ones go to ulist for the re-score kernel, which commits them
+  // and plans the buckets -- no lab_new and no commit kernel.
+  int fused;
+  int32_t* labels;
+  SumsCommit sc;
+};
+
+// MODE: kBf16 (A, B single BF16), kSplit (A and B hi + lo: three products),
+// kScaledA (A exact in BF16 -- integers of a scaled copy -- and B hi + lo: two
+// products; the A lo term of the split form is identically zero).
+constexpr int kBf16 = 0, kSplit = 1, kScaledA = 2;
+
+template <int MODE>
+__global__ void __launch_bounds__(kTcThreads, 2)
+    lloyd_tc_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmAlo,
+                    const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmBlo, TcArgs a) {
+  extern __shared__ __align__(1024) uint8_t smem_raw[];
+  uint8_t* base = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_bytes = BM * BK * 2;
+  const uint32_t b_bytes = (uint32_t)a.kp * BK * 2;
+  constexpr bool ALO = MODE == kSplit, BLO = MODE != kBf16;
+  const uint32_t stage_bytes = (ALO ? 2u : 1u) * a_bytes + (BLO ? 2u : 1u) * b_bytes;
+  // stage layout: A | B | A lo (kSplit) | B lo (kSplit, kScaledA)
+  const uint32_t off_alo = a_bytes + b_bytes, off_blo = (ALO ? 2u : 1u) * a_bytes + b_bytes;
+  const int NS = a.stages;
+  uint64_t* full = reinterpret_cast<uint64_t*>(base + (size_t)NS * stage_bytes);
+  uint64_t* empty = full + NS;
+  uint64_t* accf = empty + NS;
+  uint64_t* acce = accf + 2;
+  uint64_t* fin = acce + 2;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+  float* snc = reinterpret_cast<float*>(tmem_holder + 4);
+  float* scn = snc + a.kp;
+  int32_t* h_in = reinterpret_cast<int32_t*>(scn + a.kp);  // fused: per-CTA in/out histograms
+  int32_t* h_out = h_in + a.kp;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t ntiles = (a.n + BM - 1) / BM;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < NS; s++) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&accf[b], 1);
+      mbar_init(&acce[b], BM);
+    }
+    mbar_init(fin, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                 "r"(a.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_holder;
+  // X does not depend on the predecessor kernel: the producer issues the A
+  // (point) tiles of the first NS stages before waiting for it; the centre
+  // tiles (B) and norms come from the predecessor.
+  int pre = 0;
+  if (warp == 0 && lane == 0) {
+    prefetch_tmap(&tmA);
+    if (ALO) prefetch_tmap(&tmAlo);
+    const uint64_t pol_a = policy_evict_first();
+    int64_t t = blockIdx.x;
+    int kc = 0;
+    for (int st = 0; st < NS && t < ntiles; st++) {
+      uint8_t* sA = base + (size_t)st * stage_bytes;
+      uint8_t* sB = sA + a_bytes;
+      mbar_expect_tx(&full[st], stage_bytes);
+      const int ax = a.a_tiled ? 0 : kc * BK;
+      const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
+      tma_load_2d_hint(sA, &tmA, ax, ay, &full[st], pol_a);
+      if (ALO) tma_load_2d_hint(sA + off_alo, &tmAlo, ax, ay, &full[st], pol_a);
+      pre++;
+      if (++kc == a.kc) {
+        kc = 0;
+        t += gridDim.x;
+      }
+    }
+  }
+  griddep_wait();
+  for (int j = threadIdx.x; j < a.kp; j += blockDim.x) {
+    snc[j] = a.nc[j];
+    scn[j] = a.cn[j];
+    h_in[j] = 0;
+    h_out[j] = 0;
+  }
+  __syncthreads();
+
+  if (warp == 0) {
+    if (lane == 0) {
+      prefetch_tmap(&tmB);
+      if (BLO) prefetch_tmap(&tmBlo);
+      const uint64_t pol_a = policy_evict_first(), pol_b = policy_evict_last();
+      uint32_t stage = 0, phase = 0;
+      uint32_t armed = 0, last_ph = 0;  // per-stage bit: armed at least once / parity of the last arm
+      int tile_no = 0;
+      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, tile_no++) {
+        if (a.cancel != nullptr && *a.cancel) {
+          atomicOr(a.status, DEV_CANCELLED);
+          *abort_flag = 1;
+          break;
+        }
+        for (int kc = 0; kc < a.kc; kc++) {
+          uint8_t* sA = base + (size_t)stage * stage_bytes;
+          uint8_t* sB = sA + a_bytes;
+          armed |= 1u << stage;
+          last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
+          if (pre > 0) {
+            // A already in flight (issued before the dependency wait)
+            pre--;
+          } else {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+              if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+              *abort_flag = 1;
+              break;
+            }
+            mbar_expect_tx(&full[stage], stage_bytes);
+            const int ax = a.a_tiled ? 0 : kc * BK;
+            const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
+            tma_load_2d_hint(sA, &tmA, ax, ay, &full[stage], pol_a);
+            if (ALO) tma_load_2d_hint(sA + off_alo, &tmAlo, ax, ay, &full[stage], pol_a);
+          }
+          tma_load_2d_hint(sB, &tmB, kc * BK, 0, &full[stage], pol_b);
+          if (BLO) tma_load_2d_hint(sA + off_blo, &tmBlo, kc * BK, 0, &full[stage], pol_b);
+          if (++stage == (uint32_t)NS) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      // Never leave the CTA with a TMA copy still writing shared memory: wait
+      // (bounded) for the last load armed on every stage.
+      for (int s2 = 0; s2 < NS; s2++)
+        if (armed & (1u << s2)) {
+          volatile int never = 0;
+          if (!mbar_wait(&full[s2], (last_ph >> s2) & 1u, &never)) atomicOr(a.status, DEV_TIMEOUT);
+        }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      uint32_t stage = 0, phase = 0;
+      int64_t lt = 0;
+      for (int64_t t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x, lt++) {
+        const uint32_t buf = (uint32_t)(lt & 1), accph = (uint32_t)((lt >> 1) & 1);
+        if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag)) {
+          if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        // split: hi.hi accumulates at [0, kp), the hi.lo + lo.hi terms at [kp, 2kp)
+        const uint32_t acc_cols = (BLO && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
+        const uint32_t d_tmem = tmem_base + buf * acc_cols;
+        const uint32_t d_lo = d_tmem + (a.sep_lo ? (uint32_t)a.kp : 0u);
+        bool ok = true;
+        for (int kc = 0; kc < a.kc; kc++) {
+          if (!mbar_wait(&full[stage], phase, abort_flag)) {
+            if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+            *abort_flag = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          uint8_t* sA = base + (size_t)stage * stage_bytes;
+          uint8_t* sB = sA + a_bytes;
+          const uint64_t ad = smem_desc_sw128(smem_u32(sA));
+          const uint64_t bd = smem_desc_sw128(smem_u32(sB));
+#pragma unroll
+          for (int kk = 0; kk < BK / 16; kk++) {
+            // advance 16 BF16 (32 bytes) along K inside the swizzled row
+            umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (kc | kk) != 0 ? 1u : 0u);
+            if (BLO) {
+              const uint64_t bdlo = smem_desc_sw128(smem_u32(sA + off_blo));
+              umma_bf16(d_lo, ad + 2 * kk, bdlo + 2 * kk, a.idesc, (a.sep_lo && (kc | kk) == 0) ? 0u : 1u);
+            }
+            if (ALO) {
+              const uint64_t adlo = smem_desc_sw128(smem_u32(sA + off_alo));
+              umma_bf16(d_lo, adlo + 2 * kk, bd + 2 * kk, a.idesc, 1u);
+            }
+          }
+          umma_commit(&empty[stage]);
+          if (++stage == (uint32_t)NS) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+        if (!ok) break;
+        umma_commit(&accf[buf]);
+      }
+      // every MMA this thread issued has completed before TMEM is freed
+      umma_commit(fin);
+      volatile int never = 0;
+      if (!mbar_wait(fin, 0, &never)) atomicOr(a.status, DEV_TIMEOUT);
+    }
+  } else {
+    // epilogue: warps 2..5 -> TMEM lane groups 2,3,0,1
+    const int g = warp & 3;
+    const int row = g * 32 + lane;
+    // fused: commit a label (warp-collective; act: this lane has one) --
+    // change list by one reservation per warp, histograms in shared memory
+    auto commit = [&](bool act, int64_t i, int lb) {
+      int old = -1;
+      bool ch = false;
+      if (act) {
+        old = a.labels[i];
+        ch = lb != old;
+        if (ch) a.labels[i] = lb;
+      }
+      const unsigned chm = __ballot_sync(0xffffffffu, ch);
+      if (chm) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(a.sc.nchg, __popc(chm));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (ch) {
+          const int pos = base + __popc(chm & ((1u << lane) - 1u));
+          a.sc.chg_i[pos] = (int32_t)i;
+          a.sc.chg_old[pos] = old;
+          a.sc.chg_new[pos] = lb;
+          atomicAdd(&h_in[lb], 1);
+          atomicAdd(&h_out[old], 1);
+        }
+      }
+    };
+    int64_t lt = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
+      const uint32_t buf = (uint32_t)(lt & 1), accph = (uint32_t)((lt >> 1) & 1);
+      const bool ok = !*abort_flag && mbar_wait(&accf[buf], accph, abort_flag);
+      if (!ok) {
+        if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+        *abort_flag = 1;
+      }
+      if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
+      tc_fence_after();
+      const int64_t i = t * BM + row;
+      const bool valid = i < a.n;
+      const float nxi = valid ? a.nx[i] : 0.0f;
+      const float xni = valid ? a.xn[i] : 0.0f;
+      const uint32_t acc_cols = (BLO && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
+      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + buf * acc_cols;
+      const bool nonneg = *a.neg_flag == 0;
+      // pass 1: screened argmin (first index wins ties)
+      float best = __int_as_float(0x7f800000), best_dot = 0.0f;
+      int bj = 0;
+      for (int c0 = 0; c0 < a.kp; c0 += 16) {
+        float v[16];
+        tmem_ld16(taddr + c0, v);
+        if (BLO && a.sep_lo) {
+          float w[16];
+          tmem_ld16(taddr + a.kp + c0, w);
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] += w[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = c0 + j;
+          if (col < a.k) {
+            const float dt = fmaf(-2.0f, v[j], nxi + snc[col]);
+            if (dt < best) {
+              best = dt;
+              bj = col;
+              best_dot = v[j];
+            }
+          }
+        }
+      }
+      // S_j bounds sum_i |x_i c_ij|: |x||c_j| in general, the (inflated) dot product for nonnegative data
+      const float sb = nonneg ? fmaxf(best_dot, 0.0f) * a.s_scale : xni * scn[bj];
+      const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
+      const float hi = best + eb;
+      // pass 2: every other centre whose lower bound reaches the best's upper bound
+      uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+      for (int c0 = 0; c0 < a.kp; c0 += 16) {
+        float v[16];
+        tmem_ld16(taddr + c0, v);
+        if (BLO && a.sep_lo) {
+          float w[16];
+          tmem_ld16(taddr + a.kp + c0, w);
+#pragma unroll
+          for (int j = 0; j < 16; j++) v[j] += w[j];
+        }
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const int col = c0 + j;
+          if (col < a.k && col != bj) {
+            const float dt = fmaf(-2.0f, v[j], nxi + snc[col]);
+            const float sj = nonneg ? fmaxf(v[j], 0.0f) * a.s_scale : xni * scn[col];
+            const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
+            if (!(dt - e > hi)) {
+              const uint64_t bit = 1ull << (col & 63);
+              const int w = col >> 6;
+              if (w == 0) m0 |= bit;
+              else if (w == 1) m1 |= bit;
+              else if (w == 2) m2 |= bit;
+              else m3 |= bit;
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acce[buf]);
+      const bool und = (m0 | m1 | m2 | m3) != 0;
+      if (a.fused) commit(valid && !und, i, bj);  // undecided points: committed by the re-score kernel
+      if (valid) {
+        if (!und) {
+          if (!a.fused) a.lab_new[i] = bj;
+        } else {
+          const uint64_t bit = 1ull << (bj & 63);
+          const int w = bj >> 6;
+          if (w == 0) m0 |= bit;
+          else if (w == 1) m1 |= bit;
+          else if (w == 2) m2 |= bit;
+          else m3 |= bit;
+          if (!a.fused) a.lab_new[i] = -1;
+          const int u = atomicAdd(a.ucount, 1);
+          a.ulist[u] = (int32_t)i;
+          uint64_t* um = a.umask + (int64_t)u * a.mw;
+          um[0] = m0;
+          if (a.mw > 1) um[1] = m1;
+          if (a.mw > 2) um[2] = m2;
+          if (a.mw > 3) um[3] = m3;
+        }
+      }
+    }
+    if (a.fused) {
+      // this CTA's histograms into the global ones
+      named_bar_sync(1, BM);
+      for (int j = threadIdx.x - 64; j < a.k; j += BM) {
+        if (h_in[j]) atomicAdd(&a.sc.cin[j], h_in[j]);
+        if (h_out[j]) atomicAdd(&a.sc.cout[j], h_out[j]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(a.tmem_cols)
+                 : "memory");
+  }
+}
+
+// X (f32) -> BF16 hi (and lo) copies, norms: one warp per row (prep_row in
+// fuelg_prep.cuh).
+template <bool SPLIT>
+__global__ void prep_rows_kernel(const float* __restrict__ X, int64_t rows, int64_t valid_rows, int d, int dp,
+                                 int tile_kc, __nv_bfloat16* __restrict__ hi, __nv_bfloat16* __restrict__ lo,
+                                 float* __restrict__ nrm2, float* __restrict__ nrm, int* __restrict__ neg_flag,
+                                 int32_t* __restrict__ zero_word, float scale) {
+  griddep_wait();
+  if (zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *zero_word = 0;
+  bool anyneg = false;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const bool vec = ((d & 3) == 0) && ((reinterpret_cast<uintptr_t>(X) & 15) == 0);
+  for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < rows; r += (int64_t)gridDim.x * nw)
+    anyneg |= prep_row<SPLIT>(X + r * d, r, r < valid_rows, vec, d, dp, tile_kc, hi, lo, nrm2, nrm, lane, scale);
+  if (neg_flag != nullptr && __any_sync(0xffffffffu, anyneg) && (threadIdx.x & 31) == 0) atomicOr(neg_flag, 1);
+}
+
+// Smallest non-zero and largest |x| over X (as ordered float bits): out[0]
+// (start 0x7f800000) and out[1] (start 0).
+__global__ void abs_range_kernel(const float* __restrict__ X, int64_t count, unsigned* __restrict__ out) {
+  unsigned lo = 0x7f800000u, hi = 0u;
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, nth = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t e = tid; e < count; e += nth) {
+    const unsigned b = __float_as_uint(X[e]) & 0x7fffffffu;
+    if (b != 0u) lo = min(lo, b);
+    hi = max(hi, b);
+  }
+  lo = __reduce_min_sync(0xffffffffu, lo);
+  hi = __reduce_max_sync(0xffffffffu, hi);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[0], lo);
+    atomicMax(&out[1], hi);
+  }
+}
+
+// Scaled-integer copy of X for the kScaledA screen: every value x must be
+// s * I (|I| <= 256, I = rint(x / s)) to within |x - I s| <= 2^-21 |x|; the
+// copy holds I (exact in BF16), tile-major like prep_rows_kernel, with the
+// norms of x itself.  Any value outside the form sets *fail.
+__global__ void prep_scaled_kernel(const float* __restrict__ X, int64_t rows, int64_t valid_rows, int d, int dp,
+                                   int tile_kc, float s, __nv_bfloat16* __restrict__ q, float* __restrict__ nrm2,
+                                   float* __restrict__ nrm, int* __restrict__ neg_flag, int* __restrict__ fail) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  bool anyneg = false, bad = false;
+  for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < rows; r += (int64_t)gridDim.x * nw) {
+    const bool v = r < valid_rows;
+    const float* xr = X + r * d;
+    float acc = 0.0f;
+    for (int c0 = 4 * lane; c0 < dp; c0 += 128) {
+      float x4[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) x4[t] = (v && c0 + t < d) ? __ldg(xr + c0 + t) : 0.0f;
+      float i4[4];
+#pragma unroll
+      for (int t = 0; t < 4; t++) {
+        i4[t] = rintf(__fdiv_rn(x4[t], s));
+        bad |= !(fabsf(i4[t]) <= 256.0f) || !(fabsf(fmaf(-i4[t], s, x4[t])) <= 4.76837158203125e-07f * fabsf(x4[t]));
+        acc = fmaf(x4[t], x4[t], acc);
+        anyneg |= x4[t] < 0.0f;
+      }
+      __nv_bfloat162 h01 = __floats2bfloat162_rn(i4[0], i4[1]);
+      __nv_bfloat162 h23 = __floats2bfloat162_rn(i4[2], i4[3]);
+      uint2 pk;
+      pk.x = *reinterpret_cast<uint32_t*>(&h01);
+      pk.y = *reinterpret_cast<uint32_t*>(&h23);
+      *reinterpret_cast<uint2*>(q + prep_offset(r, c0, dp, tile_kc)) = pk;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (lane == 0) {
+      nrm2[r] = acc;
+      nrm[r] = sqrtf(acc);
+    }
+  }
+  if (__any_sync(0xffffffffu, anyneg) && lane == 0) atomicOr(neg_flag, 1);
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(fail, 1);
+}
+
 template <int KIND, int ORDER>
 __global__ void rescore_kernel(const float* __restrict__ X, const float* __restrict__ C, int d, int mw,
                                const int32_t* __restrict__ ulist, const uint64_t* __restrict__ umask,
                                const int32_t* __restrict__ ucount, int32_t* __restrict__ lab_new,
                                unsigned long long* __restrict__ tally) {
-  constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
-  constexpr int G = LANE8 ? 8 : (KIND == KIND_SQDIST ? 32 : 1);  // lanes per candidate
-  constexpr int PER = 32 / G;                                      // candidates per warp step
   const int lane = threadIdx.x & 31;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -518,40 +616,8 @@ __global__ void rescore_kernel(const float* __restrict__ X, const float* __restr
   if (blockIdx.x == 0 && threadIdx.x == 0) *tally += (unsigned long long)cnt;
   for (int64_t u = gw; u < cnt; u += nwarps) {
     const int64_t i = ulist[u];
-    const float* x = X + i * d;
-    uint64_t best = KEY_NONE;
-    // walk the candidate bits PER at a time; this lane's slot is lane / G
-    int w = 0;
-    uint64_t m = umask[u * mw];
-    const int slot = lane / G;
-    for (;;) {
-      int got = 0, j = 0;
-      while (got < PER) {
-        while (m == 0 && w + 1 < mw) m = umask[u * mw + (++w)];
-        if (m == 0) break;
-        const int b = __ffsll((long long)m) - 1;
-        m &= m - 1;
-        if (got == slot) j = w * 64 + b;
-        got++;
-      }
-      if (got == 0) break;
-      const bool mine = slot < got;
-      if (!mine) j = 0;  // idle slots score centre 0 and discard it
-      // lloyd.rs:166-168 calls sqdist(centre, point); the initial pairwise
-      // kernel takes (point, centre).  The squares are identical either way.
-      const float dist = warp_candidate_dist<KIND, ORDER>(x, C + (int64_t)j * d, d, lane);
-      if (mine && (lane % G) == 0) {
-        const uint64_t key = make_key(dist, (uint32_t)j);
-        best = key < best ? key : best;
-      }
-      if (got < PER) break;
-    }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      const uint64_t o = __shfl_xor_sync(0xffffffffu, best, off);
-      best = o < best ? o : best;
-    }
-    if (lane == 0) lab_new[i] = (int32_t)key_idx(best);
+    const int lb = rescore_point<KIND, ORDER>(X + i * d, C, d, mw, umask + u * mw, lane);
+    if (lane == 0) lab_new[i] = lb;
   }
 }
 
@@ -565,11 +631,13 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
                                                            const uint64_t* __restrict__ umask,
                                                            const int32_t* __restrict__ ucount,
                                                            int32_t* __restrict__ lab_new,
-                                                           unsigned long long* __restrict__ tally) {
+                                                           unsigned long long* __restrict__ tally,
+                                                           int32_t* __restrict__ labels, SumsCommit sc, int commit) {
   constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
   constexpr int G = LANE8 ? 8 : 32;
   constexpr int PER = 32 / G;
   extern __shared__ __align__(16) float rs_smem[];
+  __shared__ unsigned s_last;
   griddep_wait();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   float* xs = rs_smem + (size_t)wib * (PER + 1) * ds;
@@ -629,7 +697,36 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
       const uint64_t o = __shfl_xor_sync(0xffffffffu, best, off);
       best = o < best ? o : best;
     }
-    if (lane == 0) lab_new[i] = (int32_t)key_idx(best);
+    if (lane == 0) {
+      const int32_t lb = (int32_t)key_idx(best);
+      if (!commit) {
+        lab_new[i] = lb;
+      } else {
+        // fused pass: commit this point's label (few points: global atomics)
+        const int32_t old = labels[i];
+        if (lb != old) {
+          labels[i] = lb;
+          const int pos = atomicAdd(sc.nchg, 1);
+          sc.chg_i[pos] = (int32_t)i;
+          sc.chg_old[pos] = old;
+          sc.chg_new[pos] = lb;
+          atomicAdd(&sc.cin[lb], 1);
+          atomicAdd(&sc.cout[old], 1);
+        }
+      }
+    }
+  }
+  if (!commit) return;
+  // the last block to finish (a ticket after a fence) plans the buckets from
+  // the complete histograms
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(sc.done, 1u) == gridDim.x - 1 ? 1u : 0u;
+  __syncthreads();
+  if (s_last && threadIdx.x < 32) {
+    __threadfence();
+    plan_body(lane, sc.k, sc.cin, sc.cout, sc.off_in, sc.off_out, sc.chunk_off, sc.counts, sc.chunk_info);
+    if (lane == 0) *sc.done = 0;
   }
 }
 
@@ -639,6 +736,8 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
 // once per k-means call; the centre copy every iteration.
 struct TcLloydState {
   bool split = false;
+  int mode = kBf16;    // kBf16, kSplit or kScaledA (split tier on scaled-integer data)
+  float scale = 1.0f;  // kScaledA: X = scale * (integer copy); centre copies hold fl(scale * c)
   int dp = 0, kp = 0, kc = 0, mw = 0, stages = 0;
   int64_t arows = 0;  // rows of the tile-major A copies (whole tiles)
   int ctas_per_sm = 1;
@@ -657,8 +756,55 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   st->kp = (p.k + 15) & ~15;
   st->kc = (st->dp + BK - 1) / BK;
   st->mw = (st->kp + 63) / 64;
+  st->arows = ((n + BM - 1) / BM) * BM;
+  const size_t xb = (size_t)st->arows * st->kc * BK * 2;
+  FUELG_TRY(st->xhi.alloc(xb, stream));
+  FUELG_TRY(st->xnrm2.alloc(sizeof(float) * st->arows, stream));
+  FUELG_TRY(st->xnrm.alloc(sizeof(float) * st->arows, stream));
+  FUELG_TRY(st->negf.alloc(sizeof(int), stream));
+  FUELG_CUDA(cudaMemsetAsync(st->negf.p, 0, sizeof(int), stream));
+  // Split tier on data that are integers |I| <= 256 times one scale s (to
+  // within 2^-21 relative; quantised data such as 8-bit pixel values / 255):
+  // the scaled copy I is exact in BF16, so the A lo term of the split form is
+  // zero and A is one BF16 copy (half the bytes) -- kScaledA.  s = the smallest
+  // non-zero |x|; the conversion kernel verifies every value.
+  st->mode = st->split ? kSplit : kBf16;
+  st->scale = 1.0f;
+  if (st->split && getenv("FUELG_TC_NO_SCALED") == nullptr) {
+    Scratch rng, fail;
+    FUELG_TRY(rng.alloc(sizeof(unsigned) * 2, stream));
+    FUELG_TRY(fail.alloc(sizeof(int), stream));
+    const unsigned init[2] = {0x7f800000u, 0u};
+    FUELG_CUDA(cudaMemcpyAsync(rng.p, init, sizeof(init), cudaMemcpyHostToDevice, stream));
+    FUELG_CUDA(cudaMemsetAsync(fail.p, 0, sizeof(int), stream));
+    abs_range_kernel<<<8 * 152, 256, 0, stream>>>(p.X, n * (int64_t)p.d, rng.as<unsigned>());
+    ::fuelg::note_launch();
+    unsigned hr[2];
+    FUELG_CUDA(cudaMemcpyAsync(hr, rng.p, sizeof(hr), cudaMemcpyDeviceToHost, stream));
+    FUELG_CUDA(cudaStreamSynchronize(stream));
+    float lo, hi;
+    memcpy(&lo, &hr[0], sizeof(float));
+    memcpy(&hi, &hr[1], sizeof(float));
+    if (hr[0] < 0x7f800000u && hr[1] < 0x7f800000u && (double)hi <= 256.0 * (double)lo * (1.0 + 1e-6)) {
+      prep_scaled_kernel<<<8 * 152, 256, 0, stream>>>(p.X, st->arows, n, p.d, st->kc * BK, st->kc, lo,
+                                                      st->xhi.as<__nv_bfloat16>(), st->xnrm2.as<float>(),
+                                                      st->xnrm.as<float>(), st->negf.as<int>(), fail.as<int>());
+      ::fuelg::note_launch();
+      FUELG_CUDA(cudaGetLastError());
+      int hf = 1;
+      FUELG_CUDA(cudaMemcpyAsync(&hf, fail.p, sizeof(int), cudaMemcpyDeviceToHost, stream));
+      FUELG_CUDA(cudaStreamSynchronize(stream));
+      if (hf == 0) {
+        st->mode = kScaledA;
+        st->scale = lo;
+      } else {
+        FUELG_CUDA(cudaMemsetAsync(st->negf.p, 0, sizeof(int), stream));
+      }
+    }
+  }
+  const bool alo = st->mode == kSplit, blo = st->mode != kBf16;
   const size_t a_bytes = BM * BK * 2, b_bytes = (size_t)st->kp * BK * 2;
-  const size_t stage_bytes = (st->split ? 2 : 1) * (a_bytes + b_bytes);
+  const size_t stage_bytes = (alo ? 2 : 1) * a_bytes + (blo ? 2 : 1) * b_bytes;
   // Tunables (defaults measured on GB300): FUELG_TC_STAGES pipeline depth,
   // FUELG_TC_CTAS_PER_SM resident CTAs per SM (shared memory is divided).
   int per_sm = 2;
@@ -669,78 +815,67 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   stages = std::max(2, std::min(8, stages));
   {
     uint32_t cols = 32;
-    st->sep_lo = st->split && st->kp <= 128;
+    st->sep_lo = blo && st->kp <= 128;
     while (cols < (uint32_t)((st->sep_lo ? 4 : 2) * st->kp)) cols <<= 1;
     if (cols * per_sm > 512) per_sm = 1;
     if (per_sm == 1 && getenv("FUELG_TC_STAGES") == nullptr) stages = std::max(2, std::min(8, (int)((200 * 1024) / stage_bytes)));
   }
   st->ctas_per_sm = per_sm;
   st->stages = stages;
-  st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 8 * st->kp;
+  st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 16 * st->kp + 16;
   if (st->smem > 227 * 1024) {
     set_error("tensor-core Lloyd tile does not fit shared memory (k=%d)", p.k);
     return ST_ENOTSUP;
   }
-  st->arows = ((n + BM - 1) / BM) * BM;
-  const size_t xb = (size_t)st->arows * st->kc * BK * 2;
-  FUELG_TRY(st->xhi.alloc(xb, stream));
-  if (st->split) FUELG_TRY(st->xlo.alloc(xb, stream));
-  FUELG_TRY(st->xnrm2.alloc(sizeof(float) * st->arows, stream));
-  FUELG_TRY(st->xnrm.alloc(sizeof(float) * st->arows, stream));
+  if (alo) FUELG_TRY(st->xlo.alloc(xb, stream));
   const size_t cb = (size_t)st->kp * st->dp * 2;
   FUELG_TRY(st->chi.alloc(cb, stream));
-  if (st->split) FUELG_TRY(st->clo.alloc(cb, stream));
+  if (blo) FUELG_TRY(st->clo.alloc(cb, stream));
   FUELG_TRY(st->cnrm2.alloc(sizeof(float) * st->kp, stream));
   FUELG_TRY(st->cnrm.alloc(sizeof(float) * st->kp, stream));
   FUELG_TRY(st->ulist.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(st->umask.alloc(sizeof(uint64_t) * n * st->mw, stream));
   FUELG_TRY(st->ucount.alloc(sizeof(int32_t), stream));
-  FUELG_TRY(st->negf.alloc(sizeof(int), stream));
-  FUELG_CUDA(cudaMemsetAsync(st->negf.p, 0, sizeof(int), stream));
   FUELG_TRY(st->rescored_total.alloc(sizeof(unsigned long long), stream));
   FUELG_CUDA(cudaMemsetAsync(st->rescored_total.p, 0, sizeof(unsigned long long), stream));
-  if (st->split)
-    prep_rows_kernel<true><<<8 * 152, 256, 0, stream>>>(p.X, st->arows, n, p.d, st->kc * BK, st->kc,
-                                                         st->xhi.as<__nv_bfloat16>(),
-                                                         st->xlo.as<__nv_bfloat16>(), st->xnrm2.as<float>(),
-                                                         st->xnrm.as<float>(), st->negf.as<int>(), nullptr);
-  else
-    prep_rows_kernel<false><<<8 * 152, 256, 0, stream>>>(p.X, st->arows, n, p.d, st->kc * BK, st->kc,
-                                                          st->xhi.as<__nv_bfloat16>(),
-                                                          nullptr, st->xnrm2.as<float>(), st->xnrm.as<float>(), st->negf.as<int>(),
-                                                          nullptr);
-  ::fuelg::note_launch();
-  FUELG_CUDA(cudaGetLastError());
+  if (st->mode != kScaledA) {
+    auto pk = alo ? prep_rows_kernel<true> : prep_rows_kernel<false>;
+    pk<<<8 * 152, 256, 0, stream>>>(p.X, st->arows, n, p.d, st->kc * BK, st->kc, st->xhi.as<__nv_bfloat16>(),
+                                    alo ? st->xlo.as<__nv_bfloat16>() : (__nv_bfloat16*)nullptr,
+                                    st->xnrm2.as<float>(), st->xnrm.as<float>(), st->negf.as<int>(), nullptr, 1.0f);
+    ::fuelg::note_launch();
+    FUELG_CUDA(cudaGetLastError());
+  }
   // A: tile-major [arows * kc, 64] -- each box is one contiguous 16 KB block
   FUELG_TRY(tcx::make_map_bf16(&st->tmA, st->xhi.p, st->arows * st->kc, BK, BM));
   FUELG_TRY(tcx::make_map_bf16(&st->tmB, st->chi.p, st->kp, st->dp, st->kp));
-  if (st->split) {
-    FUELG_TRY(tcx::make_map_bf16(&st->tmAlo, st->xlo.p, st->arows * st->kc, BK, BM));
-    FUELG_TRY(tcx::make_map_bf16(&st->tmBlo, st->clo.p, st->kp, st->dp, st->kp));
-  } else {
-    st->tmAlo = st->tmA;
-    st->tmBlo = st->tmB;
-  }
-  auto kern = st->split ? lloyd_tc_kernel<true> : lloyd_tc_kernel<false>;
+  st->tmAlo = st->tmA;
+  st->tmBlo = st->tmB;
+  if (alo) FUELG_TRY(tcx::make_map_bf16(&st->tmAlo, st->xlo.p, st->arows * st->kc, BK, BM));
+  if (blo) FUELG_TRY(tcx::make_map_bf16(&st->tmBlo, st->clo.p, st->kp, st->dp, st->kp));
+  auto kern = st->mode == kScaledA ? lloyd_tc_kernel<kScaledA>
+              : st->mode == kSplit ? lloyd_tc_kernel<kSplit> : lloyd_tc_kernel<kBf16>;
   FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)st->smem));
   return ST_OK;
 }
 
-int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* lab_new,
-                    int* dev_status, cudaStream_t stream) {
+namespace {
+// One screen launch.  fused == nullptr: lab_new receives every label (the
+// undecided ones from the re-score kernel launched after it); otherwise the
+// pass commits into fused->labels itself (TcArgs).  prep: convert the centres
+// first (else the previous centre update wrote their BF16 copies).
+int tc_pass(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* lab_new,
+            int32_t* labels, const SumsCommit* fused, bool prep, int* dev_status, cudaStream_t stream) {
   const int64_t n = p.n;
   // centre copies and norms for this iteration (padded rows are zero); block 0
   // also clears the undecided-point counter for this pass
-  if (st->split)
-    FUELG_TRY(launch_pdl(prep_rows_kernel<true>, dim3((st->kp + 7) / 8), dim3(256), 0, stream, centers,
-                         (int64_t)st->kp, (int64_t)p.k, p.d, st->dp, 0, st->chi.as<__nv_bfloat16>(),
-                         st->clo.as<__nv_bfloat16>(), st->cnrm2.as<float>(), st->cnrm.as<float>(), (int*)nullptr,
-                         st->ucount.as<int32_t>()));
-  else
-    FUELG_TRY(launch_pdl(prep_rows_kernel<false>, dim3((st->kp + 7) / 8), dim3(256), 0, stream, centers,
-                         (int64_t)st->kp, (int64_t)p.k, p.d, st->dp, 0, st->chi.as<__nv_bfloat16>(),
-                         (__nv_bfloat16*)nullptr, st->cnrm2.as<float>(), st->cnrm.as<float>(), (int*)nullptr,
-                         st->ucount.as<int32_t>()));
+  if (prep) {
+    auto pk = st->split ? prep_rows_kernel<true> : prep_rows_kernel<false>;
+    FUELG_TRY(launch_pdl(pk, dim3((st->kp + 7) / 8), dim3(256), 0, stream, centers, (int64_t)st->kp, (int64_t)p.k,
+                         p.d, st->dp, 0, st->chi.as<__nv_bfloat16>(),
+                         st->split ? st->clo.as<__nv_bfloat16>() : (__nv_bfloat16*)nullptr, st->cnrm2.as<float>(),
+                         st->cnrm.as<float>(), (int*)nullptr, st->ucount.as<int32_t>(), st->scale));
+  }
   TcArgs a{};
   a.n = n;
   a.d = p.d;
@@ -766,11 +901,18 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
   // S = sum_i |x_i c_i| <= |x||c| (for nonnegative data S = x.c itself).  The
   // distance takes 2 x.c.  Norms and epilogue roundings stay within beta
   // (|x|^2 + |c|^2); fuel's own f32 sum of d squares within (d + 4) 2^-24 of
-  // the distance (gamma).
+  // the distance (gamma).  kScaledA: x = s I + e with |e| <= 2^-21 |x| and I
+  // exact; B = hi + lo of fl(s c) is within (2^-16 + 2^-24)|s c| of s c, so the
+  // operand error is (2^-16 + 2 2^-24)(1 + d) + d with d = 2^-21 (taken as
+  // 2^-20), and the two accumulators add KP 2^-23 (1 + 2u) + KP 2^-23 2.01 u.
   const double KP = (double)st->kc * BK;
   const double u8 = std::ldexp(1.0, -8), u23 = std::ldexp(1.0, -23), u24 = std::ldexp(1.0, -24);
   double rel;
-  if (st->split && st->sep_lo)
+  if (st->mode == kScaledA) {
+    const double dl = std::ldexp(1.0, -20);
+    rel = (std::ldexp(1.0, -16) + 2 * u24) * (1.0 + dl) + dl +
+          (KP * u23 * (1.0 + 2 * u8) + (st->sep_lo ? 1.0 : 2.0) * KP * u23 * 2.01 * u8) * (1.0 + dl) + u24;
+  } else if (st->split && st->sep_lo)
     rel = 3.01 * std::ldexp(1.0, -16) + KP * u23 * (1.0 + 2 * u8) + 2.0 * KP * u23 * 2.01 * u8 + u24;
   else if (st->split)
     rel = 3.01 * std::ldexp(1.0, -16) + 3.0 * KP * u23 * (1.0 + 2 * u8);
@@ -795,14 +937,19 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int64_t ntiles = (n + BM - 1) / BM;
   const int grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * st->ctas_per_sm);
+  if (fused) {
+    a.fused = 1;
+    a.labels = labels;
+    a.sc = *fused;
+  }
   HotTimer* ht = hot_timer();
   if (ht) ht->begin(stream);
-  if (st->split)
-    FUELG_TRY(launch_pdl(lloyd_tc_kernel<true>, dim3(grid), dim3(kTcThreads), st->smem, stream, st->tmA, st->tmAlo,
-                         st->tmB, st->tmBlo, a));
-  else
-    FUELG_TRY(launch_pdl(lloyd_tc_kernel<false>, dim3(grid), dim3(kTcThreads), st->smem, stream, st->tmA,
-                         st->tmAlo, st->tmB, st->tmBlo, a));
+  {
+    auto kern = st->mode == kScaledA ? lloyd_tc_kernel<kScaledA>
+                : st->mode == kSplit ? lloyd_tc_kernel<kSplit> : lloyd_tc_kernel<kBf16>;
+    FUELG_TRY(launch_pdl(kern, dim3(grid), dim3(kTcThreads), st->smem, stream, st->tmA, st->tmAlo, st->tmB,
+                         st->tmBlo, a));
+  }
   if (ht) ht->end(stream);
   FUELG_CUDA(cudaGetLastError());
   const int rgrid = 8 * sms;
@@ -828,14 +975,17 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
         FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         FUELG_TRY(launch_pdl(kfn, dim3(g2), dim3(128), sm, stream, p.X, centers, p.d, ds, st->mw,
                              (const int32_t*)a.ulist, (const uint64_t*)a.umask, (const int32_t*)a.ucount, a.lab_new,
-                             st->rescored_total.as<unsigned long long>()));
+                             st->rescored_total.as<unsigned long long>(), labels, a.sc, fused ? 1 : 0));
       } else {
         auto kfn = rescore_smem_kernel<KIND_SQDIST, ORDER_ARM>;
         FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         FUELG_TRY(launch_pdl(kfn, dim3(g2), dim3(128), sm, stream, p.X, centers, p.d, ds, st->mw,
                              (const int32_t*)a.ulist, (const uint64_t*)a.umask, (const int32_t*)a.ucount, a.lab_new,
-                             st->rescored_total.as<unsigned long long>()));
+                             st->rescored_total.as<unsigned long long>(), labels, a.sc, fused ? 1 : 0));
       }
+    } else if (fused) {
+      set_error("the fused Lloyd pass needs d <= 1024");
+      return ST_EINVAL;
     } else if (p.order == ORDER_X86) {
       rescore_kernel<KIND_SQDIST, ORDER_X86><<<rgrid, 256, 0, stream>>>(p.X, centers, p.d, st->mw, a.ulist, a.umask,
                                                                        a.ucount, a.lab_new, st->rescored_total.as<unsigned long long>()); ::fuelg::note_launch();
@@ -846,6 +996,37 @@ int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers
   }
 FUELG_CUDA(cudaGetLastError());
   return ST_OK;
+}
+
+}  // namespace
+
+int lloyd_assign_tc(const LloydParams& p, TcLloydState* st, const float* centers, bool first, int32_t* lab_new,
+                    int* dev_status, cudaStream_t stream) {
+  return tc_pass(p, st, centers, first, lab_new, nullptr, nullptr, true, dev_status, stream);
+}
+
+// A later pass: the screen commits the decided labels, the re-score kernel
+// the undecided ones and plans the buckets (d <= 1024).  The centre copies
+// were written by the previous centre update (lloyd_tc_centre_prep), which
+// also cleared the undecided-point counter.
+int lloyd_tc_pass_fused(const LloydParams& p, TcLloydState* st, const float* centers, int32_t* labels,
+                        const SumsCommit& sc, int* dev_status, cudaStream_t stream) {
+  return tc_pass(p, st, centers, false, nullptr, labels, &sc, false, dev_status, stream);
+}
+
+bool lloyd_tc_scaled(const TcLloydState* st) { return st->mode == kScaledA; }
+
+CentrePrep lloyd_tc_centre_prep(TcLloydState* st) {
+  CentrePrep cp;
+  cp.hi = st->chi.as<__nv_bfloat16>();
+  cp.lo = st->split ? st->clo.as<__nv_bfloat16>() : nullptr;
+  cp.nrm2 = st->cnrm2.as<float>();
+  cp.nrm = st->cnrm.as<float>();
+  cp.dp = st->dp;
+  cp.kp = st->kp;
+  cp.zero_word = st->ucount.as<int32_t>();
+  cp.scale = st->scale;
+  return cp;
 }
 
 int lloyd_tc_rescored_total(TcLloydState* st, cudaStream_t stream, int64_t* out) {

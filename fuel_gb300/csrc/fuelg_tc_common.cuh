@@ -112,6 +112,10 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
 }
 // Named barrier over nthreads threads that also ORs a per-thread flag: every
 // participant gets the same answer, so a loop exit taken on it is uniform.
+__device__ __forceinline__ void named_bar_sync(int bar_id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "r"(nthreads) : "memory");
+}
+
 __device__ __forceinline__ int named_bar_or(int bar_id, int nthreads, int v) {
   int r;
   asm volatile(

@@ -53,6 +53,11 @@ extern "C" {
 #define FUELG_PREC_FP32 0       /* plain FP32 CUDA-core distances (exact reference order)  */
 #define FUELG_PREC_BF16 1       /* tcgen05 BF16 screen + exact FP32 re-score (d >= 32)     */
 #define FUELG_PREC_SPLIT_BF16 2 /* tcgen05 split-BF16 (hi+lo) screen + exact FP32 re-score */
+/* Reported in fuelg_stats.precision_used only: the split-BF16 tier found the
+   data to be small integers times one scale (e.g. 8-bit values / 255), so the
+   point operand is exact in BF16 and its lo half (zero) is neither stored nor
+   read.  Requested as FUELG_PREC_SPLIT_BF16.                                  */
+#define FUELG_PREC_SPLIT_BF16_SCALED 3
 
 #define FUELG_LLOYD_FIXED_ITERS 1 /* run exactly max_iter iterations (ignore changed==0 stop) */
 

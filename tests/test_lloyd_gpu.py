@@ -62,6 +62,8 @@ def test_lloyd_sparse_config_reduced(gpu, oracle, precision):
     """The k=64, d=784 sparse 0..255/255 workload at n=7,000, 10 iterations."""
     X, init = workloads.lloyd_sparse(n=7000)
     r = kmeans(X, k=64, variant="lloyd", max_iter=10, init=init, fixed_iters=True, precision=precision)
+    # 8-bit values / 255: the split tier runs on the exact scaled-integer copy
+    assert r.stats["precision_used"] == {"fp32": 0, "split_bf16": 3}[precision]
     c, lab, it, inert = oracle.lloyd_exact(X, 64, init, max_iter=10, threads=threads(), fixed_iters=True)
     assert r.n_iter == 10 == it
     assert np.array_equal(r.labels, lab)
@@ -150,6 +152,48 @@ def test_tc_tier_matches_exact_run(gpu, precision):
     # the hi+lo screen decides almost every point without re-scoring
     if precision == "split_bf16":
         assert b.stats["rescored"] < 0.2 * 9000 * 12
+
+
+def quantised(n, d, k, seed, scale=np.float32(0.37), top=200):
+    """Integers in [-top, top] (cluster centres + noise, clipped) times one f32 scale."""
+    rng = np.random.default_rng(seed)
+    c = rng.integers(-top // 2, top // 2, size=(k, d))
+    q = np.clip(c[rng.integers(0, k, n)] + rng.integers(-20, 21, size=(n, d)), -top, top)
+    return (q.astype(np.float32) * scale).astype(np.float32)
+
+
+@pytest.mark.parametrize("order", ["arm", "x86"])
+@pytest.mark.parametrize("d,k", [(100, 20), (784, 64), (48, 130)])
+def test_tc_scaled_integer_data_per_iteration(gpu, oracle, order, d, k, monkeypatch):
+    """Split tier on integer-times-scale data: the point operand is exact in
+    BF16 (one copy, two products); assignments stay bit-identical.  The same
+    data forced through the plain split form agrees."""
+    n = 2500
+    X = quantised(n, d, k, d + k)
+    init = X[np.random.default_rng(3).choice(n, k, replace=False)]
+    for t in (1, 2, 4):
+        r = kmeans(X, k=k, variant="lloyd", max_iter=t, init=init, order=order, fixed_iters=True,
+                   precision="split_bf16")
+        assert r.stats["precision_used"] == 3
+        lab, _ = oracle.lloyd_assign(X, r.centers, initial=(t == 1), order=order, threads=threads())
+        assert np.array_equal(r.labels, lab), f"iteration {t}: {np.sum(r.labels != lab)} labels differ"
+    monkeypatch.setenv("FUELG_TC_NO_SCALED", "1")
+    r2 = kmeans(X, k=k, variant="lloyd", max_iter=4, init=init, order=order, fixed_iters=True, precision="split_bf16")
+    assert r2.stats["precision_used"] == 2
+    assert np.array_equal(r2.labels, r.labels)
+    assert np.array_equal(r2.centers.view(np.uint32), r.centers.view(np.uint32))
+
+
+def test_tc_scaled_detection_rejects_off_grid_values(gpu, oracle):
+    """One value off the integer grid: the plain split form is used, same result."""
+    X = quantised(2000, 64, 10, 4)
+    X[17, 5] += np.float32(0.001)
+    init = X[:10].copy()
+    r = kmeans(X, k=10, variant="lloyd", max_iter=5, init=init, fixed_iters=True, precision="split_bf16")
+    assert r.stats["precision_used"] == 2
+    c, lab, it, _ = oracle.lloyd_exact(X, 10, init, max_iter=5, threads=threads(), fixed_iters=True)
+    assert np.array_equal(r.labels, lab)
+    assert np.array_equal(r.centers.view(np.uint32), c.view(np.uint32))
 
 
 def test_tc_tier_small_d_falls_back_to_exact(gpu):

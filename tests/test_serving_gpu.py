@@ -19,7 +19,7 @@ def _mix(rng, d, count, max_rows=300):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "split_bf16"])
 def test_serving_results_equal_alone(gpu, precision):
     rng = np.random.default_rng(3)
     X = workloads.unit_normal_rows(60000, 96, seed=0)
@@ -36,6 +36,26 @@ def test_serving_results_equal_alone(gpu, precision):
     assert st["queries"] == sum(Q.shape[0] for Q, _ in reqs)
     assert st["max_batch_requests"] > 1  # submitted together -> merged
     assert all(h.latency_ms is not None and h.latency_ms >= 0 for h in handles)
+
+
+@pytest.mark.gpu
+def test_serving_mixed_k_integer_data(gpu):
+    """Integer data (exact BF16 screen, no proof margin): one tensor-core
+    launch per batch with every row selecting its own k matches each request
+    answered alone."""
+    rng = np.random.default_rng(5)
+    X = workloads.knn_geometric(n=40000, d=64, seed=3)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="bf16")
+    reqs = [(X[rng.integers(0, X.shape[0], size=int(m))].copy(), int(k))
+            for m, k in zip(rng.integers(1, 200, size=24), rng.choice([1, 3, 10, 57, 100], size=24))]
+    alone = [ix.knn(Q, k, exclude_self=False) for Q, k in reqs]
+    with Server(ix, precision="bf16", max_batch_queries=4096, workers=1) as sv:
+        got = [h.result() for h in [sv.submit(Q, k) for Q, k in reqs]]
+        st = sv.stats()
+    for (gi, gd), (ai, ad) in zip(got, alone):
+        np.testing.assert_array_equal(gi, ai)
+        np.testing.assert_array_equal(gd.view(np.uint32), ad.view(np.uint32))
+    assert st["max_batch_requests"] > 1
 
 
 @pytest.mark.gpu
