@@ -474,9 +474,10 @@ def serving_rates():
     from fuel_gb300 import workloads
     X = workloads.unit_normal_rows(SERVE_N, SERVE_D, seed=0)
     tc = serving_run("split_bf16", SERVE_SECONDS_TC, X)
+    tc16 = serving_run("fp16", SERVE_SECONDS_TC, X)
     plain = serving_run("fp32", SERVE_SECONDS_PLAIN, X)
     return {"workload": f"knn serving n={SERVE_N} d={SERVE_D} unit-norm rows, Poisson {SERVE_RATE:.0f} req/s, "
-                        "batch log-U[1,4096], k in {1,10,100}", "tc": tc, "plain_fp32": plain}
+                        "batch log-U[1,4096], k in {1,10,100}", "tc": tc, "tc_fp16": tc16, "plain_fp32": plain}
 
 
 def run_profile(args):

@@ -308,12 +308,18 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
 }  // extern "C"
 
 namespace fuelg {
-int index_view_get(fuelg_index* ix, bool want_tc, bool want_split, IndexView* out) {
+int index_view_get(fuelg_index* ix, int want_tier, IndexView* out) {
   std::lock_guard<std::mutex> lk(ix->mu);
   cudaSetDevice(ix->device);
-  if (want_tc && !ix->tc && ix->n > 0 && knn_tc_supported(ix->d, 1, 0))
+  if (want_tier >= 0 && !ix->tc && ix->n > 0 && knn_tc_supported(ix->d, 1, TC_BF16))
     FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, ix->stream, &ix->tc));
-  if (want_split && ix->tc && knn_tc_supported(ix->d, 1, 1)) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, ix->stream));
+  if (want_tier == TC_SPLIT && ix->tc) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, ix->stream));
+  out->f16 = false;
+  if (want_tier == TC_F16 && ix->tc) {
+    const int rc = knn_tc_index_add_f16(ix->tc, ix->X, ix->stream);
+    if (rc != ST_OK && rc != ST_ENOTSUP) return rc;
+    out->f16 = rc == ST_OK;  // else values outside the FP16 range: the plain tier serves
+  }
   out->device = ix->device;
   out->n = ix->n;
   out->d = ix->d;
@@ -364,7 +370,7 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
     set_error("unknown exclude mode %d", exclude_mode);
     return ST_EINVAL;
   }
-  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16) {
+  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_F16 || precision == FUELG_PREC_SPLIT_BF16_SCALED) {
     set_error("unknown precision tier %d", precision);
     return ST_EINVAL;
   }
@@ -402,17 +408,25 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   p.kk = kk;
   int used = FUELG_PREC_FP32;
   int64_t rescored = 0;
-  const int split = precision == FUELG_PREC_SPLIT_BF16 ? 1 : 0;
-  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk, split) && ix->n > 0) {
+  const int tier = precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT : precision == FUELG_PREC_F16 ? TC_F16 : TC_BF16;
+  bool tc_done = false;
+  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk, tier) && ix->n > 0) {
     int exact = 0;
     if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
-    if (split) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, s));
-    FUELG_TRY(knn_tc_topk(ix->tc, p.A, m, ix->X, kk, ix->order, ix->metric, split, keys.as<uint64_t>(),
-                          dstat.as<int>(), s, &rescored, &exact));
-    used = (split && !exact) ? FUELG_PREC_SPLIT_BF16 : FUELG_PREC_BF16;
-  } else {
-    FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
+    if (tier == TC_SPLIT) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, s));
+    int rc = tier == TC_F16 ? knn_tc_index_add_f16(ix->tc, ix->X, s) : ST_OK;
+    // values outside the FP16 range (index or queries): the plain tier answers
+    if (rc == ST_OK)
+      rc = knn_tc_topk(ix->tc, p.A, m, ix->X, kk, ix->order, ix->metric, tier, keys.as<uint64_t>(),
+                       dstat.as<int>(), s, &rescored, &exact);
+    if (rc != ST_OK && rc != ST_ENOTSUP) return rc;
+    if (rc == ST_OK) {
+      tc_done = true;
+      // integer data run the exact one-product screen whatever the split request
+      used = tier == TC_F16 ? FUELG_PREC_F16 : (tier == TC_SPLIT && !exact) ? FUELG_PREC_SPLIT_BF16 : FUELG_PREC_BF16;
+    }
   }
+  if (!tc_done) FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
   FUELG_TRY(finalize_knn(keys.as<uint64_t>(), m, kk, k, exclude_mode, static_cast<int64_t*>(oi.dptr),
                          static_cast<float*>(od.dptr), s));
   int64_t d2h = 0;

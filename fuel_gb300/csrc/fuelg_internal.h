@@ -162,21 +162,27 @@ int finalize_knn(const uint64_t* keys, int64_t m, int kk, int k, int exclude_mod
 int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
                          void* scratch, size_t scratch_bytes, cudaStream_t stream);
 
-// Tensor-core kNN (fuelg_knn_tc.cu): top-kk keys per query [m, kk] via a BF16
+// Tensor-core kNN (fuelg_knn_tc.cu): top-kk keys per query [m, kk] via a
 // tcgen05 screen; exact for integer data, otherwise re-scored and proven.
-bool knn_tc_supported(int d, int kk, int split);
+// Operand tiers: BF16 (one product, error ~2^-8), split BF16 (hi + lo, three
+// products, ~2^-16), FP16 (one product, ~2^-11; values within the FP16 range).
+constexpr int TC_BF16 = 0, TC_SPLIT = 1, TC_F16 = 2;
+bool knn_tc_supported(int d, int kk, int tier);
 // Resident tensor-core form of an index: BF16 copy padded to whole tiles, FP32
 // norms, integer census and the index-side bounds; built once per handle.
 struct TcIndex;
 int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, TcIndex** out);
 void knn_tc_index_free(TcIndex* t);
 int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream);
-// split: hi + lo BF16 operands (accuracy ~2^-16 instead of 2^-8); ignored for
-// integer data whose BF16 screen is exact.  row_k (device, m entries, or
+// FP16 copy of the index; ST_ENOTSUP when a value lies outside the FP16 range.
+int knn_tc_index_add_f16(TcIndex* t, const float* X32, cudaStream_t stream);
+// tier: TC_BF16 / TC_SPLIT / TC_F16 operands; integer data whose BF16 screen
+// is exact always use BF16 (no margin, no re-score); FP16 falls back to the
+// split tier when the queries leave the FP16 range.  row_k (device, m entries, or
 // nullptr): a smaller k per query row -- row q's first row_k[q] keys (of the
 // kk per row written) are its exact top row_k[q]; the rest are unspecified.
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
-                int split, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
+                int tier, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
                 int* exact_out, const int32_t* row_k = nullptr);
 
 // Read-only view of an index handle for concurrent users (the serving loop);
@@ -189,11 +195,13 @@ struct IndexView {
   int order = 0;
   const float* X = nullptr;
   const TcIndex* tc = nullptr;
+  bool f16 = false;  // the index has its FP16 copy (FP16 tier)
 };
 }  // namespace fuelg
 struct fuelg_index;
 namespace fuelg {
-int index_view_get(fuelg_index* ix, bool want_tc, bool want_split, IndexView* out);
+// want_tier (TC_*, or -1 for none): build that tensor-core form of the index.
+int index_view_get(fuelg_index* ix, int want_tier, IndexView* out);
 
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,

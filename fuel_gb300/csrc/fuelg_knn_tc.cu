@@ -21,6 +21,8 @@
 #include <cmath>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "fuelg_common.cuh"
 #include "fuelg_internal.h"
 #include "fuelg_tc_common.cuh"
@@ -46,7 +48,7 @@ struct KnnTcArgs {
   int ks_last;   // K steps of 16 with data in the last chunk (1..4)
   int kk2;       // keys kept per query (the list stride)
   const int32_t* row_k;  // per query row k (rows keep kk2_of(row_k[q]) <= kk2 keys), or nullptr
-  int exact_sq;  // exact squared distances: no margin keys
+  int margin_mode;  // kk2_of mode of this launch
   int exact;     // D~ is exact (integer data)
   int split;     // hi + lo BF16 operands (three products)
   int stages;
@@ -62,10 +64,16 @@ struct KnnTcArgs {
 
 
 constexpr int kSel = 8;  // keys per lane in a selection (appended or prefix): 256 per warp
+constexpr float kF16Max = 65504.0f;  // largest finite FP16 value
 
 // Screened keys kept for a query of k neighbours: k plus the margin the
-// error-bound proof needs (none when the screened squared distances are exact).
-__host__ __device__ __forceinline__ int kk2_of(int k, int exact_sq) { return exact_sq ? k : k + (k / 8 > 8 ? k / 8 : 8); }
+// error-bound proof needs.  Margin modes: 0 exact screened squared distances
+// (none), 1 BF16 / split BF16 (max(8, k/8)), 2 FP16 (max(8, k/4): its larger
+// screen error needs more ranks between the k-th and the last kept key).
+__host__ __device__ __forceinline__ int kk2_of(int k, int mode) {
+  const int m = mode == 0 ? 0 : (mode == 1 ? k / 8 : k / 4);
+  return mode == 0 ? k : k + (m > 8 ? m : 8);
+}
 
 // Number of held keys below t over the warp.
 __device__ __forceinline__ int warp_count_hi_below(const uint32_t (&hi)[2 * kSel], uint32_t t) {
@@ -425,7 +433,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     const int64_t qi = q0 + row;
     const bool valid = qi < a.m;
     const float nq = valid ? a.qn2[qi] : 0.0f;
-    const int kkr = (a.row_k != nullptr && valid) ? kk2_of(a.row_k[qi], a.exact_sq) : a.kk2;  // this row's keys
+    const int kkr = (a.row_k != nullptr && valid) ? kk2_of(a.row_k[qi], a.margin_mode) : a.kk2;  // this row's keys
     const size_t qstride = (size_t)a.kk2 + kApp;
     uint64_t* app = lists_sp + (valid ? qi : 0) * qstride + a.kk2;  // this query's append log
     float* nsm_w = xnsm + ew * 2 * XN;
@@ -570,8 +578,9 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
 // Rows -> BF16 copy padded to dp columns and rows_pad rows (zeros), |row|^2 in
 // FP32, plus an integer-data census: flags[0] |= non-integer or |v| > 256,
 // flags[1] = max |v| (as float bits; non-negative so integer order works).
+template <bool F16>
 __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64_t rows_pad, int d, int dp,
-                                __nv_bfloat16* __restrict__ out, __nv_bfloat16* __restrict__ out_lo,
+                                void* __restrict__ out, __nv_bfloat16* __restrict__ out_lo,
                                 float* __restrict__ n2, int* __restrict__ flags) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   int bad = 0;
@@ -580,9 +589,13 @@ __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64
     float acc = 0.0f;
     for (int c = lane; c < dp; c += 32) {
       const float x = (r < rows && c < d) ? __ldg(X + r * d + c) : 0.0f;
-      const __nv_bfloat16 hi = __float2bfloat16_rn(x);
-      out[r * dp + c] = hi;
-      if (out_lo) out_lo[r * dp + c] = __float2bfloat16_rn(x - __bfloat162float(hi));
+      if (F16) {
+        static_cast<__half*>(out)[r * dp + c] = __float2half_rn(x);
+      } else {
+        const __nv_bfloat16 hi = __float2bfloat16_rn(x);
+        static_cast<__nv_bfloat16*>(out)[r * dp + c] = hi;
+        if (out_lo) out_lo[r * dp + c] = __float2bfloat16_rn(x - __bfloat162float(hi));
+      }
       acc = fmaf(x, x, acc);
       if (x != rintf(x) || fabsf(x) > 256.0f) bad = 1;
       vmax = fmaxf(vmax, fabsf(x));
@@ -610,10 +623,10 @@ __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64
 // fail the proof are flagged for the exact scan.
 template <int ORDER>
 __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __restrict__ X, int d, int64_t m,
-                                   int kk, int kk2, const int32_t* __restrict__ row_k, int metric,
-                                   const uint64_t* __restrict__ keys_in,
+                                   int kk, int kk2, const int32_t* __restrict__ row_k, int margin_mode,
+                                   int metric, const uint64_t* __restrict__ keys_in,
                                    uint64_t* __restrict__ keys_out, const float* __restrict__ qn2, float xmax_norm,
-                                   float xmax_n2, float alpha, float beta, float gamma,
+                                   float xmax_n2, float alpha, float beta, float gamma, float abs_a,
                                    int32_t* __restrict__ redo, int32_t* __restrict__ nredo) {
   extern __shared__ __align__(16) float qsm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -626,7 +639,7 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
   uint64_t* kout = keys_out + qi * kk2;
   // this row's k and kept keys (the list stride stays kk2)
   const int kq = row_k != nullptr ? row_k[qi] : kk;
-  const int kk2q = row_k != nullptr ? kk2_of(kq, 0) : kk2;
+  const int kk2q = row_k != nullptr ? kk2_of(kq, margin_mode) : kk2;
   for (int c = kk2q + lane; c < kk2; c += 32) kout[c] = KEY_NONE;
   // exact keys of the candidates, written in place of the screened ones
   const int l = lane & 7, grp = lane >> 3;
@@ -674,7 +687,8 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
     if (full_list) {
       const float nq = qn2[qi];
       const float qn = sqrtf(nq);
-      const float e = (alpha * qn * xmax_norm + beta * (nq + xmax_n2)) * (1.0f + gamma) + gamma * last_screen;
+      const float e = (alpha * qn * xmax_norm + beta * (nq + xmax_n2)) * (1.0f + gamma) + gamma * last_screen +
+                      abs_a * (qn + xmax_norm);
       const float lower = last_screen - e;  // every unscreened point's reference squared distance is >= this
       const uint64_t kth = kout[kq - 1];
       bool ok;
@@ -712,14 +726,14 @@ size_t knn_tc_fixed_smem(int d, int split) {
   const size_t a_bytes = (size_t)(split ? 2 : 1) * (dp / BK) * QM * BK * 2;
   return 1024 + a_bytes + 8 * 32 + 16 + (size_t)kEpiWarps * 2 * XN * sizeof(float);
 }
-int knn_tc_margin(int kk, bool exact_sq) { return kk2_of(kk, exact_sq ? 1 : 0) - kk; }
+int margin_mode_of(int tier) { return tier == TC_F16 ? 2 : 1; }
 }  // namespace
 
-bool knn_tc_supported(int d, int kk, int split) {
+bool knn_tc_supported(int d, int kk, int tier) {
   if (d < 32 || d > 256 || kk < 1) return false;
   // kept keys per query are selected 8 per lane by one warp
-  if (kk + knn_tc_margin(kk, false) > 32 * kSel) return false;
-  return knn_tc_fixed_smem(d, split) + 2 * (size_t)XN * BK * 2 <= kSmemPerCta;
+  if (kk2_of(kk, margin_mode_of(tier)) > 32 * kSel) return false;
+  return knn_tc_fixed_smem(d, tier == TC_SPLIT) + 2 * (size_t)XN * BK * 2 <= kSmemPerCta;
 }
 
 // Top-kk keys of every query via the tensor-core screen.  out_keys: [m, kk]
@@ -729,11 +743,12 @@ struct TcIndex {
   int d = 0, dp = 0;
   __nv_bfloat16* xb = nullptr;  // [npad, dp] BF16, zero padded
   __nv_bfloat16* xlo = nullptr; // [npad, dp] BF16 of x - xb (split tier; built on first use)
+  __half* xh = nullptr;         // [npad, dp] FP16 (FP16 tier; built on first use)
   float* xn2 = nullptr;         // [npad] FP32 |x|^2 (padded rows 0)
   bool integer = false;         // every value an integer with |v| <= 256
   float vmax = 0.0f;            // max |v|
   float xmax_n2 = 0.0f;         // max |x|^2
-  CUtensorMap tmX, tmXlo;
+  CUtensorMap tmX, tmXlo, tmXh;
 };
 
 void knn_tc_index_free(TcIndex* t) {
@@ -741,6 +756,7 @@ void knn_tc_index_free(TcIndex* t) {
   if (t->xb) cudaFree(t->xb);
   if (t->xn2) cudaFree(t->xn2);
   if (t->xlo) cudaFree(t->xlo);
+  if (t->xh) cudaFree(t->xh);
   delete t;
 }
 
@@ -760,7 +776,8 @@ int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, 
   Scratch flags;
   FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
   FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 2, stream));
-  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, n, t->npad, d, t->dp, t->xb, nullptr, t->xn2, flags.as<int>());
+  knn_prep_kernel<false><<<8 * 152, 256, 0, stream>>>(X32, n, t->npad, d, t->dp, t->xb, nullptr, t->xn2,
+                                                      flags.as<int>());
   ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   int hf[2];
@@ -785,8 +802,8 @@ int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream) {
   FUELG_TRY(hi.alloc((size_t)t->npad * t->dp * 2, stream));
   FUELG_TRY(n2.alloc(sizeof(float) * t->npad, stream));
   FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
-  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(X32, t->n, t->npad, t->d, t->dp, hi.as<__nv_bfloat16>(), t->xlo,
-                                               n2.as<float>(), flags.as<int>());
+  knn_prep_kernel<false><<<8 * 152, 256, 0, stream>>>(X32, t->n, t->npad, t->d, t->dp, hi.as<__nv_bfloat16>(),
+                                                      t->xlo, n2.as<float>(), flags.as<int>());
   ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   FUELG_TRY(make_map_bf16(&t->tmXlo, t->xlo, t->npad, t->dp, XN));
@@ -794,16 +811,41 @@ int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream) {
   return ST_OK;
 }
 
+int knn_tc_index_add_f16(TcIndex* t, const float* X32, cudaStream_t stream) {
+  if (t->xh) return ST_OK;
+  if (!(t->vmax <= kF16Max)) {
+    set_error("index values exceed the FP16 range (max |v| = %g)", (double)t->vmax);
+    return ST_ENOTSUP;
+  }
+  FUELG_CUDA(cudaMalloc(&t->xh, (size_t)t->npad * t->dp * 2));
+  Scratch n2, flags;
+  FUELG_TRY(n2.alloc(sizeof(float) * t->npad, stream));
+  FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
+  knn_prep_kernel<true><<<8 * 152, 256, 0, stream>>>(X32, t->n, t->npad, t->d, t->dp, t->xh, nullptr,
+                                                     n2.as<float>(), flags.as<int>());
+  ::fuelg::note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  FUELG_TRY(make_map_bf16(&t->tmXh, t->xh, t->npad, t->dp, XN));  // 2-byte elements: same box geometry
+  FUELG_CUDA(cudaStreamSynchronize(stream));
+  return ST_OK;
+}
+
 int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32, int kk, int order, int metric,
-                int split, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
+                int tier, uint64_t* out_keys, int* dev_status, cudaStream_t stream, int64_t* rescored,
                 int* exact_out, const int32_t* row_k) {
   const int64_t n = ti->n;
   const int d = ti->d;
   const int dp = ti->dp;
   const int kc = dp / BK;
   const int64_t mpad = ((m + QM - 1) / QM) * QM;
+  const bool f16 = tier == TC_F16;
+  int split = tier == TC_SPLIT ? 1 : 0;
   if (split && !ti->xlo) {
     set_error("split-BF16 kNN needs the index residual copy");
+    return ST_ENOTSUP;
+  }
+  if (f16 && !ti->xh) {
+    set_error("FP16 kNN needs the index FP16 copy");
     return ST_ENOTSUP;
   }
   Scratch qb, qlo, qn2, flags;
@@ -812,22 +854,32 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   FUELG_TRY(qn2.alloc(sizeof(float) * mpad, stream));
   FUELG_TRY(flags.alloc(sizeof(int) * 2, stream));
   FUELG_CUDA(cudaMemsetAsync(flags.p, 0, sizeof(int) * 2, stream));
-  knn_prep_kernel<<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.as<__nv_bfloat16>(),
-                                               split ? qlo.as<__nv_bfloat16>() : nullptr, qn2.as<float>(),
-                                               flags.as<int>()); ::fuelg::note_launch();
+  if (f16)
+    knn_prep_kernel<true><<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.p, nullptr, qn2.as<float>(),
+                                                       flags.as<int>());
+  else
+    knn_prep_kernel<false><<<8 * 152, 256, 0, stream>>>(Q32, m, mpad, d, dp, qb.p,
+                                                        split ? qlo.as<__nv_bfloat16>() : nullptr, qn2.as<float>(),
+                                                        flags.as<int>());
+  ::fuelg::note_launch();
   FUELG_CUDA(cudaGetLastError());
   int hf[2];
   FUELG_CUDA(cudaMemcpyAsync(hf, flags.p, sizeof(hf), cudaMemcpyDeviceToHost, stream));
   FUELG_CUDA(cudaStreamSynchronize(stream));
   float qmax;
   memcpy(&qmax, &hf[1], sizeof(float));
+  if (f16 && !(qmax <= kF16Max)) {
+    set_error("query values exceed the FP16 range (max |q| = %g)", (double)qmax);
+    return ST_ENOTSUP;
+  }
   const float vmax = std::max(qmax, ti->vmax);
   const bool integer = hf[0] == 0 && ti->integer;
   const bool exact = integer && 2.0 * dp * (double)vmax * vmax < 16777216.0;
   *exact_out = exact ? 1 : 0;
-  if (exact) split = 0;  // integer data: the plain BF16 screen is already exact
+  if (exact) split = 0;  // integer data: the one-product screen (BF16 or FP16) is already exact
   // screened keys kept per query: exact sqeuclidean needs none extra
-  const int margin = knn_tc_margin(kk, exact && metric == METRIC_SQEUCLIDEAN);
+  const int mmode = (exact && metric == METRIC_SQEUCLIDEAN) ? 0 : margin_mode_of(tier);
+  const int margin = kk2_of(kk, mmode) - kk;
   const int kk2 = kk + margin;
 
   const size_t b_bytes = (size_t)XN * BK * 2;
@@ -867,10 +919,16 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   // integer data aside, keep the error-bound constants of the Lloyd screen
   const double u8 = std::ldexp(1.0, -8), u23 = std::ldexp(1.0, -23), u24 = std::ldexp(1.0, -24);
-  // operand rounding (2u + u^2 per BF16 product; 3.01 * 2^-16 with hi + lo)
-  // plus FP32 accumulation in the tensor core over dp (3 dp) products
+  // operand rounding (2u + u^2 per BF16 product with u = 2^-8; 3.01 * 2^-16
+  // with hi + lo; u = 2^-11 per FP16 value in the normal range) plus FP32
+  // accumulation in the tensor core over dp (3 dp) products.  FP16 values below
+  // 2^-14 round with an absolute error of at most 2^-25 instead: the distance
+  // (2 q.x) takes 2^-24 (|q|_1 + |x|_1) <= 2^-24 sqrt(dp) (|q| + |x|) more.
+  const double u11 = std::ldexp(1.0, -11);
   const double rel = split ? 3.01 * std::ldexp(1.0, -16) + 3.0 * dp * u23 * (1.0 + 2 * u8)
+                     : f16 ? (2 * u11 + u11 * u11) + dp * u23 * (1.0 + 2 * u11)
                            : (2 * u8 + u8 * u8) + dp * u23 * (1.0 + 2 * u8);
+  const float abs_a = (f16 && !exact) ? (float)(u24 * std::sqrt((double)dp) * 1.01) : 0.0f;
   // exact integer data: the screen and fuel's own f32 sum are both exact
   const float alpha = exact ? 0.0f : (float)(2.0 * rel * 1.01);
   // (+3 u: the screened value is rounded as fl(|q|^2 + fl(|x|^2 - 2 q.x)))
@@ -890,7 +948,7 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.ks_last = ((d + 15) / 16) - (kc - 1) * (BK / 16);
     a.kk2 = kk2;
     a.row_k = row_k != nullptr ? row_k + b0 : nullptr;
-    a.exact_sq = margin == 0 ? 1 : 0;
+    a.margin_mode = mmode;
     a.exact = exact ? 1 : 0;
     a.split = split;
     a.stages = stages;
@@ -899,7 +957,9 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.xmax_n2 = xmax_n2;
     a.lists = lists.as<uint64_t>();
     a.out_keys = kept_sp.as<uint64_t>();
-    a.idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(XN >> 3) << 17) | ((uint32_t)(QM >> 4) << 24);
+    // instruction descriptor: D=F32, A=B=BF16 (format 1) or FP16 (format 0), K-major, N=XN, M=QM
+    a.idesc = (1u << 4) | (f16 ? 0u : (1u << 7) | (1u << 10)) | ((uint32_t)(XN >> 3) << 17) |
+              ((uint32_t)(QM >> 4) << 24);
     a.status = dev_status;
     a.cancel = cancel_word_device();
     // the query map addresses rows b0.. through the y coordinate
@@ -909,7 +969,8 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     else tmQl = tmQb;
     const dim3 grid((unsigned)((mcur + QM - 1) / QM), (unsigned)S);
     if (ht) ht->begin(stream);
-    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, ti->tmX, tmQl, split ? ti->tmXlo : ti->tmX, a);
+    const CUtensorMap& tmXs = f16 ? ti->tmXh : ti->tmX;
+    kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, tmXs, tmQl, split ? ti->tmXlo : tmXs, a);
     ::fuelg::note_launch();
     if (ht) ht->end(stream);
     FUELG_CUDA(cudaGetLastError());
@@ -933,16 +994,16 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     const unsigned rg = (unsigned)((mcur * 32 + 255) / 256);
     if (order == ORDER_X86)
       knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2,
-                                                              row_k != nullptr ? row_k + b0 : nullptr, metric,
+                                                              row_k != nullptr ? row_k + b0 : nullptr, mmode, metric,
                                                               kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
-                                                              gamma, redo.as<int32_t>(), nredo.as<int32_t>());
+                                                              gamma, abs_a, redo.as<int32_t>(), nredo.as<int32_t>());
     else
       knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2,
-                                                              row_k != nullptr ? row_k + b0 : nullptr, metric,
+                                                              row_k != nullptr ? row_k + b0 : nullptr, mmode, metric,
                                                               kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
-                                                              gamma, redo.as<int32_t>(), nredo.as<int32_t>());
+                                                              gamma, abs_a, redo.as<int32_t>(), nredo.as<int32_t>());
     ::fuelg::note_launch();
     FUELG_CUDA(cudaGetLastError());
     // first kk exact keys of every query

@@ -107,14 +107,20 @@ int run_batch(fuelg_server* sv, std::vector<Request*>& batch, cudaStream_t s, fl
   FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
   FUELG_CUDA(cudaMemcpyAsync(q.p, pin_q, sizeof(float) * m * ix.d, cudaMemcpyHostToDevice, s));
   FUELG_CUDA(cudaMemcpyAsync(rk.p, pin_k, sizeof(int32_t) * m, cudaMemcpyHostToDevice, s));
-  const int split = sv->precision == FUELG_PREC_SPLIT_BF16 ? 1 : 0;
-  if (sv->precision != FUELG_PREC_FP32 && ix.tc && knn_tc_supported(ix.d, kmax, split)) {
+  const int tier = sv->precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT
+                   : sv->precision == FUELG_PREC_F16    ? TC_F16
+                                                        : TC_BF16;
+  int rc = ST_ENOTSUP;
+  if (sv->precision != FUELG_PREC_FP32 && ix.tc && (tier != TC_F16 || ix.f16) &&
+      knn_tc_supported(ix.d, kmax, tier)) {
     // one launch for the mixed batch: every row selects only its own k (plus margin)
     int64_t rescored = 0;
     int exact = 0;
-    FUELG_TRY(knn_tc_topk(ix.tc, q.as<float>(), m, ix.X, kmax, ix.order, ix.metric, split, keys.as<uint64_t>(),
-                          dstat.as<int>(), s, &rescored, &exact, rk.as<int32_t>()));
-  } else {
+    rc = knn_tc_topk(ix.tc, q.as<float>(), m, ix.X, kmax, ix.order, ix.metric, tier, keys.as<uint64_t>(),
+                     dstat.as<int>(), s, &rescored, &exact, rk.as<int32_t>());
+    if (rc != ST_OK && rc != ST_ENOTSUP) return rc;  // ENOTSUP: queries outside the FP16 range
+  }
+  if (rc != ST_OK) {
     ExactScanParams p;
     p.A = q.as<float>();
     p.m = m;
@@ -247,14 +253,19 @@ int fuelg_server_create(fuelg_index* ix, int32_t precision, int64_t max_batch_qu
     return ST_EINVAL;
   }
   *out = nullptr;
-  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16 || max_batch_queries < 1 ||
+  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_F16 || precision == FUELG_PREC_SPLIT_BF16_SCALED ||
+      max_batch_queries < 1 ||
       budget_bytes < 1 || workers < 1 || workers > 16) {
     set_error("invalid server arguments (precision=%d max_batch=%lld budget=%lld workers=%d)", precision,
               (long long)max_batch_queries, (long long)budget_bytes, workers);
     return ST_EINVAL;
   }
   IndexView v;
-  FUELG_TRY(index_view_get(ix, precision != FUELG_PREC_FP32, precision == FUELG_PREC_SPLIT_BF16, &v));
+  const int want = precision == FUELG_PREC_FP32         ? -1
+                   : precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT
+                   : precision == FUELG_PREC_F16        ? TC_F16
+                                                        : TC_BF16;
+  FUELG_TRY(index_view_get(ix, want, &v));
   fuelg_server* sv = new fuelg_server();
   sv->view = v;
   sv->precision = precision;

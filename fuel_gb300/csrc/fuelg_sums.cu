@@ -288,11 +288,12 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
 }
 
 // Canonicalise one coordinate's limbs and, for a non-empty cluster, write
-// its exact mean as the correctly rounded f32 centre coordinate.
+// its exact mean as the correctly rounded f32 centre coordinate.  Returns the
+// coordinate's centre value after the update.
 template <int L>
-__device__ __forceinline__ void mean_elem(unsigned long long* __restrict__ limbs, int64_t e, int d, int e_lo,
-                                          const int32_t* __restrict__ counts, float* __restrict__ centers,
-                                          int write_centers) {
+__device__ __forceinline__ float mean_elem(unsigned long long* __restrict__ limbs, int64_t e, int d, int e_lo,
+                                           const int32_t* __restrict__ counts, float* __restrict__ centers,
+                                           int write_centers) {
   unsigned long long* lp = limbs + e * L;
   unsigned __int128 tot = 0;
 #pragma unroll
@@ -302,7 +303,7 @@ __device__ __forceinline__ void mean_elem(unsigned long long* __restrict__ limbs
   for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
   const int j = (int)(e / d);
   const int cnt = counts[j];
-  if (cnt <= 0 || !write_centers) return;
+  if (cnt <= 0 || !write_centers) return centers[e];
   const bool neg = (tot >> (32 * L - 1)) & 1;
   unsigned __int128 mag = tot;
   if (neg) {
@@ -314,7 +315,9 @@ __device__ __forceinline__ void mean_elem(unsigned long long* __restrict__ limbs
     }
   }
   float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, e_lo);
-  centers[e] = neg ? -v : v;
+  v = neg ? -v : v;
+  centers[e] = v;
+  return v;
 }
 
 // Hand the change count to the host and reset the per-pass counters.
@@ -339,26 +342,41 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
     mean_elem<L>(limbs, e, d, e_lo, counts, centers, write_centers);
 }
 
-// The same update, one block per centre row, which then also writes the
-// row's BF16 copies and norms for the next pass's tensor-core screen (block
-// j >= k: a zero padding row of the copies).
+// The same update, one block per centre row, which also writes the row's
+// BF16 copies (of fl(scale * c)) and norms for the next pass's tensor-core
+// screen (block j >= k: a zero padding row of the copies).  Every thread
+// converts the coordinates it computed; the squared norm is a per-thread FP32
+// sum of ceil(dp/256) terms and an 8-level tree, within (ceil(d/32) + 9) 2^-24
+// relative -- the beta term of the screen's bound.
 template <int L, bool SPLIT>
 __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __restrict__ limbs, int k, int d,
                                                         int e_lo, const int32_t* __restrict__ counts,
                                                         float* __restrict__ centers, int32_t* __restrict__ nchg,
                                                         int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
                                                         int nzero, CentrePrep cp) {
+  __shared__ float part[8];
   griddep_wait();
   mean_handoff(blockIdx.x, gridDim.x, nchg, changed, zero4k, nzero);
   if (cp.zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *cp.zero_word = 0;
   const int j = blockIdx.x;
-  if (j < k)
-    for (int c = threadIdx.x; c < d; c += blockDim.x) mean_elem<L>(limbs, (int64_t)j * d + c, d, e_lo, counts, centers, 1);
-  __syncthreads();  // the row's centre values are visible to warp 0
-  if (threadIdx.x < 32) {
-    const float* row = centers + (int64_t)j * d;
-    const bool vec = ((d & 3) == 0) && ((reinterpret_cast<uintptr_t>(centers) & 15) == 0);
-    prep_row<SPLIT>(row, j, j < k, vec, d, cp.dp, 0, cp.hi, cp.lo, cp.nrm2, cp.nrm, threadIdx.x, cp.scale);
+  float acc = 0.0f;
+  for (int c = threadIdx.x; c < cp.dp; c += blockDim.x) {
+    const float v = (j < k && c < d) ? mean_elem<L>(limbs, (int64_t)j * d + c, d, e_lo, counts, centers, 1) : 0.0f;
+    const float t = __fmul_rn(cp.scale, v);
+    const __nv_bfloat16 h = __float2bfloat16_rn(t);
+    cp.hi[(int64_t)j * cp.dp + c] = h;
+    if (SPLIT) cp.lo[(int64_t)j * cp.dp + c] = __float2bfloat16_rn(t - __bfloat162float(h));
+    acc = fmaf(v, v, acc);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float a01 = part[0] + part[1], a23 = part[2] + part[3], a45 = part[4] + part[5], a67 = part[6] + part[7];
+    const float nn = (a01 + a23) + (a45 + a67);
+    cp.nrm2[j] = nn;
+    cp.nrm[j] = sqrtf(nn);
   }
 }
 

@@ -969,7 +969,7 @@ int tc_pass(const LloydParams& p, TcLloydState* st, const float* centers, bool f
     if (p.d <= 1024) {
       const int per = p.order == ORDER_X86 ? 1 : 4;
       const size_t sm = (size_t)4 * (per + 1) * ds * sizeof(float);
-      const int g2 = 4 * sms;
+      const int g2 = 2 * sms;  // one wave: a few hundred points per pass after the first
       if (p.order == ORDER_X86) {
         auto kfn = rescore_smem_kernel<KIND_SQDIST, ORDER_X86>;
         FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));

@@ -73,7 +73,9 @@ class SearchIndex:
     """Persistent linear-scan index held in GB300 memory.
 
     Parameters mirror ``fuel.search.SearchIndex`` (python/fuel/search.py:230).
-    ``precision`` ('fp32' | 'bf16' | 'split_bf16') picks the tier and
+    ``precision`` ('fp32' | 'bf16' | 'split_bf16' | 'fp16') picks the tier
+    (every tier returns the exact reference answer; the tensor-core tiers
+    screen in BF16, hi+lo BF16 or FP16 and re-score) and
     ``order`` ('arm' | 'x86') the summation profile to reproduce (default: the
     profile fuel compiles on this host).  ``precompute=K`` is accepted; the
     exact answer is computed on every call with the k+1 exclude-self rule of

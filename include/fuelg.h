@@ -58,6 +58,10 @@ extern "C" {
    point operand is exact in BF16 and its lo half (zero) is neither stored nor
    read.  Requested as FUELG_PREC_SPLIT_BF16.                                  */
 #define FUELG_PREC_SPLIT_BF16_SCALED 3
+/* kNN / range only: tcgen05 FP16 screen (one product, ~2^-11 operand rounding,
+   a wider proof margin) + exact FP32 re-score; values must lie within the FP16
+   range (|v| <= 65504), otherwise the plain FP32 tier answers.               */
+#define FUELG_PREC_F16 4
 
 #define FUELG_LLOYD_FIXED_ITERS 1 /* run exactly max_iter iterations (ignore changed==0 stop) */
 

@@ -261,3 +261,65 @@ def test_knn_tc_split_unit_rows_certified(gpu, oracle):
     redo = (st["rescored"] - 300 * kk2) / X.shape[0]
     assert redo <= 0.02 * 300, f"{redo} of 300 queries needed the exact rescan"
     assert_same(g, oracle.knn(X, Q, 100, threads=threads()))
+
+
+@pytest.mark.parametrize("d", [32, 96, 128])
+@pytest.mark.parametrize("metric", ["sqeuclidean", "euclidean"])
+@pytest.mark.parametrize("order", ["arm", "x86"])
+def test_knn_tc_fp16_general_data(gpu, oracle, d, metric, order):
+    """FP16 screen (one product, wider proof margin): bit-exact like every tier."""
+    rng = np.random.default_rng(d + 303)
+    X = rng.normal(size=(4000, d)).astype(np.float32)
+    Q = rng.normal(size=(257, d)).astype(np.float32)
+    ix = SearchIndex(X, distance=metric, tree="linear", precision="fp16", order=order)
+    for k in (1, 10, 100):
+        g = ix.knn(Q, k, exclude_self=False)
+        assert ix.last_stats["precision_used"] == 4
+        assert_same(g, oracle.knn(X, Q, k, metric=metric, order=order, threads=threads()))
+
+
+def test_knn_tc_fp16_unit_rows_certified(gpu, oracle):
+    """Unit-norm rows (d=96): the FP16 screen with its margin certifies nearly
+    every query without the exact rescan; results bit-exact."""
+    X = workloads.unit_normal_rows(60000, 96, seed=0)
+    Q = workloads.unit_normal_rows(300, 96, seed=5)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="fp16")
+    for k, kk2 in ((1, 9), (10, 18), (100, 125)):
+        g = ix.knn(Q, k, exclude_self=False)
+        st = ix.last_stats
+        assert st["precision_used"] == 4
+        redo = (st["rescored"] - 300 * kk2) / X.shape[0]
+        assert redo <= 0.02 * 300, f"k={k}: {redo} of 300 queries needed the exact rescan"
+        assert_same(g, oracle.knn(X, Q, k, threads=threads()))
+
+
+def test_knn_tc_fp16_tiny_and_integer_values(gpu, oracle):
+    """Values in the FP16 subnormal range (absolute rounding term of the bound)
+    and integer data (exact one-product screen) stay bit-exact."""
+    rng = np.random.default_rng(17)
+    X = (rng.normal(size=(3000, 64)) * 1e-5).astype(np.float32)
+    Q = (rng.normal(size=(200, 64)) * 1e-5).astype(np.float32)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="fp16")
+    for k in (1, 10):
+        assert_same(ix.knn(Q, k, exclude_self=False), oracle.knn(X, Q, k, threads=threads()))
+        assert ix.last_stats["precision_used"] == 4
+    Xi = workloads.knn_geometric(n=5000, d=128)
+    g = gpu_knn(Xi, Xi, 50, mode="linear", precision="fp16")
+    assert_same(g, oracle.knn(Xi, Xi, 50, exclude="linear", threads=threads()))
+
+
+def test_knn_tc_fp16_out_of_range_uses_plain_tier(gpu, oracle):
+    """Values beyond the FP16 range: the plain FP32 tier answers (same bar)."""
+    rng = np.random.default_rng(23)
+    X = rng.normal(size=(2000, 48)).astype(np.float32)
+    X[7, 3] = 1e6
+    Q = rng.normal(size=(100, 48)).astype(np.float32)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="fp16")
+    g = ix.knn(Q, 10, exclude_self=False)
+    assert ix.last_stats["precision_used"] == 0
+    assert_same(g, oracle.knn(X, Q, 10, threads=threads()))
+    ix2 = SearchIndex(Q, distance="sqeuclidean", tree="linear", precision="fp16")
+    Qbig = X[:20].copy()  # one query row holds 1e6
+    g2 = ix2.knn(Qbig, 5, exclude_self=False)
+    assert ix2.last_stats["precision_used"] == 0
+    assert_same(g2, oracle.knn(Q, Qbig, 5, threads=threads()))

@@ -19,7 +19,7 @@ def _mix(rng, d, count, max_rows=300):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32", "bf16", "split_bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "split_bf16", "fp16"])
 def test_serving_results_equal_alone(gpu, precision):
     rng = np.random.default_rng(3)
     X = workloads.unit_normal_rows(60000, 96, seed=0)
