@@ -260,9 +260,10 @@ def run_ours(args):
         alg_bytes = N * D * 4 + K * D * 4 + N * 8
         hot_name = "scan_topk_kernel (exact FP32 Lloyd assignment)"
     avg_launch_ms = hot_ms / max(1, hot_n)
-    # DRAM bytes (read + write) per launch of the split-BF16 screen on this
-    # workload, from an ncu capture of the same kernel: 233.8 MB + 3.2 MB
-    traffic = 237.0e6 if prec_used == 2 else None
+    # DRAM bytes (read + write) per launch of the screen on this workload, from
+    # ncu captures of the same kernel: split-BF16 233.8 MB + 3.2 MB; the scaled
+    # integer copy (8-bit values / 255) 117.6 MB + 3.0 MB
+    traffic = {2: 237.0e6, 3: 120.6e6}.get(prec_used)
     achieved = alg_bytes / (avg_launch_ms / 1e3) / 1e9
     hbm_peak = pk.get("hbm_gbs", 6800.0)
 

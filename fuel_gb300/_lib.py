@@ -68,6 +68,7 @@ SIGNATURES = {
     "fuelg_range_size": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "fuelg_range_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
     "fuelg_range_free": (ctypes.c_int, [_vp]),
+    "fuelg_pairwise": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, _vp, ctypes.POINTER(Stats)]),
     "fuelg_kmeans_lloyd": (ctypes.c_int, [_vp, _i64, _i32, _i32, _vp, _i32, _dbl, _i32, _i32, _i32, _vp, _vp,
                                           ctypes.POINTER(_i32), ctypes.POINTER(_dbl), ctypes.POINTER(Stats)]),
     "fuelg_lloyd_assign": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),

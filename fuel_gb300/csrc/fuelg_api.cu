@@ -446,6 +446,61 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   return ST_OK;
 }
 
+int fuelg_pairwise(const float* X, int64_t n, int32_t d, int32_t metric, int32_t order, int32_t form, float* out,
+                   fuelg_stats* stats) {
+  if (n < 0 || d < 1 || (n > 0 && !X)) {
+    set_error("invalid pairwise arguments n=%lld d=%d", (long long)n, d);
+    return ST_EINVAL;
+  }
+  if (metric != FUELG_METRIC_SQEUCLIDEAN && metric != FUELG_METRIC_EUCLIDEAN) {
+    set_error("unknown metric %d", metric);
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  if (form != FUELG_PAIRWISE_CONDENSED && form != FUELG_PAIRWISE_SQUARE) {
+    set_error("unknown pairwise form %d", form);
+    return ST_EINVAL;
+  }
+  const int64_t outs = form == FUELG_PAIRWISE_CONDENSED ? n * (n - 1) / 2 : n * n;
+  if (outs > 0 && !out) {
+    set_error("out is NULL");
+    return ST_EINVAL;
+  }
+  FUELG_TRY(begin_call());
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (outs <= 0) return ST_OK;
+  cudaStream_t s;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  CallMeter meter;
+  Timer tm(s);
+  InBuf xb;
+  FUELG_TRY(xb.init(X, (size_t)n * d * sizeof(float), s));
+  OutBuf ob;
+  FUELG_TRY(ob.init(out, (size_t)outs * sizeof(float), s));
+  FUELG_TRY(pairwise_launch(static_cast<const float*>(xb.dptr), n, d, metric, order, form,
+                            static_cast<float*>(ob.dptr), s));
+  int64_t d2h = 0;
+  FUELG_TRY(ob.flush(s, &d2h));
+  const double ms = tm.stop();
+  FUELG_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = xb.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = form == FUELG_PAIRWISE_CONDENSED ? outs : n * (n + 1) / 2;
+    stats->precision_used = FUELG_PREC_FP32;
+    meter.fill(stats);
+  }
+  return ST_OK;
+}
+
 int fuelg_range(fuelg_index* ix, const float* queries, int64_t m, double radius, int32_t exclude_self,
                 fuelg_range_result** out, fuelg_stats* stats) {
   if (!ix || !out) {

@@ -203,6 +203,10 @@ namespace fuelg {
 // want_tier (TC_*, or -1 for none): build that tensor-core form of the index.
 int index_view_get(fuelg_index* ix, int want_tier, IndexView* out);
 
+// All pairwise distances (fuelg_pairwise.cu): condensed or square form, out on the device.
+int pairwise_launch(const float* X, int64_t n, int d, int metric, int order, int form, float* out,
+                    cudaStream_t stream);
+
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
                 float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream);

@@ -385,11 +385,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     const int row = g * 32 + lane;
     // fused: commit a label (warp-collective; act: this lane has one) --
     // change list by one reservation per warp, histograms in shared memory
-    auto commit = [&](bool act, int64_t i, int lb) {
-      int old = -1;
+    auto commit = [&](bool act, int64_t i, int lb, int old) {
       bool ch = false;
       if (act) {
-        old = a.labels[i];
         ch = lb != old;
         if (ch) a.labels[i] = lb;
       }
@@ -409,8 +407,15 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
     };
     int64_t lt = 0;
+    const bool nonneg = *a.neg_flag == 0;
     for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
       const uint32_t buf = (uint32_t)(lt & 1), accph = (uint32_t)((lt >> 1) & 1);
+      // this point's norms and current label, loaded while the tile's MMAs run
+      const int64_t i = t * BM + row;
+      const bool valid = i < a.n;
+      const float nxi = valid ? a.nx[i] : 0.0f;
+      const float xni = valid ? a.xn[i] : 0.0f;
+      const int32_t old_lab = (a.fused && valid) ? a.labels[i] : -1;
       const bool ok = !*abort_flag && mbar_wait(&accf[buf], accph, abort_flag);
       if (!ok) {
         if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
@@ -418,13 +423,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       }
       if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
       tc_fence_after();
-      const int64_t i = t * BM + row;
-      const bool valid = i < a.n;
-      const float nxi = valid ? a.nx[i] : 0.0f;
-      const float xni = valid ? a.xn[i] : 0.0f;
       const uint32_t acc_cols = (BLO && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
       const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + buf * acc_cols;
-      const bool nonneg = *a.neg_flag == 0;
       // pass 1: screened argmin (first index wins ties)
       float best = __int_as_float(0x7f800000), best_dot = 0.0f;
       int bj = 0;
@@ -486,7 +486,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       tc_fence_before();
       mbar_arrive(&acce[buf]);
       const bool und = (m0 | m1 | m2 | m3) != 0;
-      if (a.fused) commit(valid && !und, i, bj);  // undecided points: committed by the re-score kernel
+      if (a.fused) commit(valid && !und, i, bj, old_lab);  // undecided points: committed by the re-score kernel
       if (valid) {
         if (!und) {
           if (!a.fused) a.lab_new[i] = bj;

@@ -286,3 +286,68 @@ def range_search(data, query, radius, *, exclude_self=None, distance="euclidean"
     query = _ensure_float(query)
     index = SearchIndex(data, distance=distance, tree=tree, seed=seed, **kw)
     return index.radius_search(query, radius, exclude_self=exclude_self)
+
+
+def _condensed_n(length: int) -> int:
+    """n with n*(n-1)/2 == length (python/fuel/search.py:50-57)."""
+    import math
+    if length < 0:
+        raise ValueError("condensed distance vector length must be non-negative")
+    n = (1 + math.isqrt(1 + 8 * length)) // 2
+    if n * (n - 1) // 2 != length:
+        raise ValueError("condensed distance vector length must be n*(n-1)/2 for some integer n")
+    return n
+
+
+def pairwise_distances(data, distance="euclidean", form="condensed", *, order=None):
+    """All pairwise distances of a point set (python/fuel/search.py:92-150).
+
+    ``form='condensed'``: the lower triangle as one vector, pair (i, j) with
+    j < i at ``i*(i-1)//2 + j``; ``form='square'``: the symmetric matrix.
+    Raw float32 points with distance ``euclidean``/``l2`` or
+    ``sqeuclidean``/``squared_euclidean`` run on the GPU (fuelg_pairwise),
+    bit-identical to fuel's distance in the chosen summation ``order``;
+    ``distance='precomputed'`` converts between the forms as fuel does (a 1-D
+    input is a scipy ``pdist`` vector, pairs (a, b) with a < b).
+    """
+    data = _ensure_float(data)
+    distance = str(distance).lower()
+    form = str(form).lower()
+    if form not in ("condensed", "square"):
+        raise ValueError("form must be 'condensed' or 'square'")
+    if distance == "precomputed":
+        if data.ndim == 1:
+            n = _condensed_n(data.shape[0])
+            ti, tj = np.tril_indices(n, -1)  # i > j
+            internal = data[tj * (2 * n - tj - 1) // 2 + (ti - tj - 1)]
+            if form == "condensed":
+                return internal
+            sq = np.zeros((n, n), dtype=data.dtype)
+            sq[ti, tj] = internal
+            sq[tj, ti] = internal
+            return sq
+        if data.ndim == 2:
+            if data.shape[0] != data.shape[1]:
+                raise ValueError("precomputed distance matrix must be square")
+            if form == "square":
+                return data
+            return data[np.tril_indices(data.shape[0], -1)].copy()
+        raise ValueError("precomputed data must be a square matrix or condensed distance vector")
+    if data.ndim != 2:
+        raise ValueError("data must be a 2D array of observations when distance is not 'precomputed'")
+    metric = _parse_distance(distance)
+    _require_f32(data, "data")
+    order = order or _lib.default_order()
+    if order not in _lib.ORDER:
+        raise ValueError(f"order must be one of {sorted(_lib.ORDER)}")
+    X = np.ascontiguousarray(data)
+    n, d = X.shape
+    square = form == "square"
+    if d == 0:  # every distance between empty rows is 0
+        return np.zeros((n, n) if square else n * (n - 1) // 2, dtype=np.float32)
+    out = np.empty(n * n if square else n * (n - 1) // 2, dtype=np.float32)
+    st = _lib.Stats()
+    _lib.check(_lib.load().fuelg_pairwise(_lib.ptr(X), n, d, _lib.METRIC[metric], _lib.ORDER[order],
+                                          1 if square else 0, _lib.ptr(out), ctypes.byref(st)))
+    pairwise_distances.last_stats = st.as_dict()
+    return out.reshape(n, n) if square else out

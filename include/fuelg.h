@@ -118,6 +118,20 @@ int fuelg_range_size(const fuelg_range_result *res, int64_t *m, int64_t *total);
 int fuelg_range_copy(const fuelg_range_result *res, int64_t *offsets, int64_t *idx, float *dist);
 int fuelg_range_free(fuelg_range_result *res);
 
+/* All pairwise distances of one point set.  Replaces
+ * fuel.search.pairwise_distances for raw f32 points (python/fuel/search.py:
+ * 92-150 -> _compute_pairwise_distances[_condensed]_f32, python/mod.rs:74-124
+ * -> compute_pairwise_condensed / compute_pairwise_dense,
+ * src/api/condensed_distance_matrix.rs:16-48, square_distance_matrix.rs:11-40).
+ * form FUELG_PAIRWISE_CONDENSED: out[i*(i-1)/2 + j] for j < i (n*(n-1)/2
+ * values); FUELG_PAIRWISE_SQUARE: out[i*n + j], n*n values.  Values are
+ * bit-identical to the reference distance in the given summation order.
+ * X and out may be host or device pointers. */
+#define FUELG_PAIRWISE_CONDENSED 0
+#define FUELG_PAIRWISE_SQUARE 1
+int fuelg_pairwise(const float *X, int64_t n, int32_t d, int32_t metric, int32_t order, int32_t form, float *out,
+                   fuelg_stats *stats);
+
 /* Lloyd k-means with fixed initial centres.  Replaces lloyd_f32
  * (python/kmeans.rs:188-218, 355) -> cluster::kmeans::lloyd
  * (src/cluster/kmeans/lloyd.rs:118-202) with InitMethod::Fixed

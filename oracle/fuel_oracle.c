@@ -624,6 +624,50 @@ int fo_range_f64(const double *X, int64_t n, int64_t d, const double *Q, int64_t
                  int order, int exclude_self, int threads, int64_t **offsets, int64_t **idx, double **dist) {
     return fo_range_any(1, X, n, d, Q, m, radius, metric, order, exclude_self, threads, offsets, idx, (void **)dist);
 }
+/* ------------------------------------------------------------------------ */
+/* Pairwise distance matrix of one point set (fuel.search.pairwise_distances */
+/* for raw f32 points): compute_pairwise_condensed,                         */
+/* src/api/condensed_distance_matrix.rs:22-48 -- rows i = 1..n-1, j = 0..i-1 */
+/* in order, out[i*(i-1)/2 + j] = distance(points[i], points[j]) -- and     */
+/* compute_pairwise_dense, src/api/square_distance_matrix.rs:11-40 --      */
+/* row[j] = distance(points[i], points[j]) for j >= i, mirrored to (j, i).  */
+/* distance = DistanceFunction<SquaredEuclidean> (FO_KIND_KNN order), sqrt  */
+/* for Euclidean (src/distance/euclidean.rs:7-9).                           */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    const float *X;
+    int64_t n, d;
+    int metric, order, square;
+    float *out;
+} fo_pw_ctx;
+
+static float fo_pw_value(const fo_pw_ctx *c, int64_t i, int64_t j) {
+    float v = fo_dist_f32(FO_KIND_KNN, c->order, c->X + i * c->d, c->X + j * c->d, c->d);
+    if (c->metric == FO_METRIC_EUCLIDEAN) v = sqrtf(v);
+    return v;
+}
+
+static void fo_pw_task(void *ctx, int64_t i) {
+    const fo_pw_ctx *c = (const fo_pw_ctx *)ctx;
+    if (!c->square) {
+        for (int64_t j = 0; j < i; j++) c->out[i * (i - 1) / 2 + j] = fo_pw_value(c, i, j);
+        return;
+    }
+    for (int64_t j = i; j < c->n; j++) {
+        const float v = fo_pw_value(c, i, j);
+        c->out[i * c->n + j] = v;
+        if (j > i) c->out[j * c->n + i] = v;
+    }
+}
+
+int fo_pairwise_dist_f32(const float *X, int64_t n, int64_t d, int metric, int order, int square, int threads,
+                         float *out) {
+    if (n < 0 || d < 0) return 1;
+    fo_pw_ctx c = {X, n, d, metric, order, square, out};
+    fo_parallel_for(threads, n, fo_pw_task, &c);
+    return 0;
+}
+
 void fo_free(void *p) { free(p); }
 
 /* ------------------------------------------------------------------------ */

@@ -74,6 +74,8 @@ def load():
                                      ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp)]
     lib.fo_free.restype = None
     lib.fo_free.argtypes = [vp]
+    lib.fo_pairwise_dist_f32.restype = i32
+    lib.fo_pairwise_dist_f32.argtypes = [vp, i64, i64, i32, i32, i32, i32, vp]
     lib.fo_lloyd_f32.restype = i32
     lib.fo_lloyd_f32.argtypes = [vp, i64, i64, i64, vp, i64, dbl, i32, i32, i32, vp, vp,
                                  ctypes.POINTER(i64), ctypes.POINTER(dbl), ctypes.POINTER(i64)]
@@ -114,6 +116,23 @@ def pairwise_sqdist(p1, p2, order: str | None = None) -> np.ndarray:
     fn = lib.fo_pairwise_sqdist_f64 if is64 else lib.fo_pairwise_sqdist_f32
     fn(ORDERS[order], _p(p1), p1.shape[0], _p(p2), p2.shape[0], p1.shape[1], _p(out))
     return out
+
+
+def pairwise_distances(X, metric: str = "euclidean", form: str = "condensed", order: str | None = None,
+                       threads: int = 1) -> np.ndarray:
+    """fuel.search.pairwise_distances for raw f32 points (python/fuel/search.py:92-150):
+    the condensed lower triangle (pair (i, j), j < i, at i*(i-1)/2 + j) or the
+    square matrix, each value distance(X[i], X[j]) in the reference's order."""
+    lib = load()
+    order = order or host_order()
+    X = _f(X, np.float32)
+    n, d = X.shape
+    square = form == "square"
+    out = np.empty(n * n if square else n * (n - 1) // 2, dtype=np.float32)
+    rc = lib.fo_pairwise_dist_f32(_p(X), n, d, METRICS[metric], ORDERS[order], int(square), threads, _p(out))
+    if rc:
+        raise ValueError("pairwise_distances: invalid arguments")
+    return out.reshape(n, n) if square else out
 
 
 def knn(X, Q, k: int, metric: str = "sqeuclidean", order: str | None = None, exclude: str = "none",
