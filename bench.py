@@ -317,6 +317,31 @@ def run_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def pairwise_rate(lib, _lib, torch, args):
+    """pairwise_distances on the configs[0] points (n=20,000, d=16): condensed and
+    square forms, device-resident output; roofline = bytes written / kernel time."""
+    from fuel_gb300 import workloads
+    X = workloads.knn_plain()
+    n, d = X.shape
+    Xd = torch.from_numpy(X).cuda()
+    out = {}
+    for form, nout in ((0, n * (n - 1) // 2), (1, n * n)):
+        o = torch.empty(nout, dtype=torch.float32, device="cuda")
+        sts = []
+        for i in range(max(3, args.warmup) + max(1, args.steps)):
+            st = _lib.Stats()
+            _lib.check(lib.fuelg_pairwise(_lib.ptr(Xd), n, d, 1, _lib.ORDER[_lib.default_order()], form, _lib.ptr(o),
+                                          ctypes.byref(st)))
+            sts.append(st)
+        sts = sts[max(3, args.warmup):]
+        hot = sum(s.hot_kernel_ms for s in sts) / len(sts)
+        out["condensed" if form == 0 else "square"] = {
+            "kernel_ms": hot, "pairs_per_s": n * (n - 1) / 2 / (hot / 1e3),
+            "written_gbs": nout * 4 / (hot / 1e3) / 1e9}
+        del o
+    return {"workload": f"pairwise euclidean n={n} d={d}", **out}
+
+
 def knn_plain_rate(lib, _lib, torch, args):
     from fuel_gb300 import workloads
     X = workloads.knn_plain()
@@ -513,6 +538,8 @@ def run_profile(args):
         print(json.dumps({"profile": "serving", **serving_rates()}))
     elif args.profile == "batched":
         print(json.dumps({"profile": "batched", **batched_rate(count=args.batched_problems, plain=False)}))
+    elif args.profile == "pairwise":
+        print(json.dumps({"profile": "pairwise", **pairwise_rate(lib, _lib, torch, args)}))
     else:
         args.steps = max(1, args.steps)
         print(json.dumps({"profile": "knn_plain", **knn_plain_rate(lib, _lib, torch, args)}))
@@ -525,7 +552,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--precision", choices=["fp32", "bf16", "split_bf16"], default="split_bf16")
-    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain", "serving", "batched"], default=None)
+    ap.add_argument("--profile", choices=["lloyd", "knn_tc", "knn_plain", "serving", "batched", "pairwise"],
+                    default=None)
     ap.add_argument("--iters", type=int, default=ITERS, help="Lloyd iterations per call (--profile lloyd)")
     ap.add_argument("--knn-queries", type=int, default=20_000, help="query count (--profile knn_tc)")
     ap.add_argument("--knn-n", type=int, default=KNN_N, help="index rows (--profile knn_tc)")

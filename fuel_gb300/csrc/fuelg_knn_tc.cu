@@ -452,9 +452,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     };
     // Lanes whose append log passed `lim` entries are reduced to their kk2
     // smallest keys, one query at a time, by the whole warp.
-    auto flush = [&](int lim) {
-      unsigned need = __ballot_sync(0xffffffffu, na > lim);
-      if (!need) return;
+    auto flush_rows = [&](unsigned need) {
       __syncwarp();
       while (need) {
         const int src = __ffs(need) - 1;
@@ -471,6 +469,10 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           na = 0;
         }
       }
+    };
+    auto flush = [&](int lim) {
+      const unsigned need = __ballot_sync(0xffffffffu, na > lim);
+      if (need) flush_rows(need);
     };
     float thr = threshold();
     // norms of the tile's XN columns: 4 per lane, fetched one tile ahead
@@ -546,8 +548,9 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           }
         }
         // at most 64 appends per lane per chunk: compact before the log can overflow
-        if (__any_sync(0xffffffffu, na > kApp - 64)) {
-          flush(kApp - 64);
+        const unsigned full = __ballot_sync(0xffffffffu, na > kApp - 64);
+        if (full) {
+          flush_rows(full);
           thr = threshold();
         }
       }

@@ -13,10 +13,15 @@
 // (x_i - x_j)^2 == (x_j - x_i)^2 exactly, so the mirrored half of the square
 // form is the same value.
 //
-// Kernel: one CTA per 32 x 32 tile of the lower tile triangle (row tile >=
-// column tile); 256 threads, 2 x 2 pairs each with 8 lane accumulators;
-// 64-column chunks of both row blocks staged in shared memory.  Small d is
-// bound by the output writes (HBM), large d by FP32 issue.
+// Kernels: one CTA per tile of the lower tile triangle (row tile >= column
+// tile), 256 threads.  d <= 128 (pairwise_rows_kernel): 64 x 64 tiles, whole
+// rows of both blocks in shared memory, 4 x 4 pairs per thread computed lane by
+// lane -- lane l's sum over the 8-blocks is finished before it is added to the
+// running total, which is the reference's order (acc_0 + acc_1 + ... + acc_7,
+// then the tail) with 2 registers per pair instead of 9.  Larger d
+// (pairwise_kernel): 32 x 32 tiles, 64-column chunks, 2 x 2 pairs with 8 lane
+// accumulators each.  Small d is bound by FP32 issue and the output writes
+// (HBM), large d by FP32 issue.
 #include <cmath>
 
 #include "../../include/fuelg.h"
@@ -140,13 +145,108 @@ __global__ void __launch_bounds__(256) pairwise_kernel(const float* __restrict__
   }
 }
 
+constexpr int PR = 64;      // rows-kernel tile edge
+constexpr int kRowsMaxD = 128;
+
+template <int ORDER, int METRIC, int FORM>
+__global__ void __launch_bounds__(256) pairwise_rows_kernel(const float* __restrict__ X, int64_t n, int d,
+                                                            int64_t ntb, float* __restrict__ out) {
+  constexpr bool FMA8 = ORDER == ORDER_X86;
+  extern __shared__ float rs[];  // [2][PR][d + 1]: row block i, row block j
+  __shared__ float st[PR][PR + 1];
+  const int S = d + 1;  // odd stride: the 16 rows a half-warp reads sit in different banks
+  float* sa = rs;
+  float* sb = rs + PR * S;
+  const int64_t t = blockIdx.x;
+  int64_t bi = (int64_t)((std::sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while (bi * (bi + 1) / 2 > t) bi--;
+  while ((bi + 1) * (bi + 2) / 2 <= t) bi++;
+  const int64_t bj = t - bi * (bi + 1) / 2;
+  if (bi >= ntb) return;
+  const int64_t i0 = bi * PR, j0 = bj * PR;
+  for (int e = threadIdx.x; e < PR * d; e += 256) {
+    const int r = e / d, c = e - r * d;
+    const int64_t gi = i0 + r, gj = j0 + r;
+    sa[r * S + c] = gi < n ? __ldg(X + gi * d + c) : 0.0f;
+    sb[r * S + c] = gj < n ? __ldg(X + gj * d + c) : 0.0f;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // rows ty + 16a, cols tx + 16b
+  const int sd = d & ~7;
+  float sum[4][4];
+#pragma unroll 1
+  for (int l = 0; l < 8; l++) {
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) acc[a][b] = 0.0f;
+    for (int c = l; c < sd; c += 8) {
+      float xa[4], yb[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) xa[a] = sa[(ty + 16 * a) * S + c];
+#pragma unroll
+      for (int b = 0; b < 4; b++) yb[b] = sb[(tx + 16 * b) * S + c];
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+          const float df = __fsub_rn(xa[a], yb[b]);
+          acc[a][b] = FMA8 ? __fmaf_rn(df, df, acc[a][b]) : __fadd_rn(sq_rn(df), acc[a][b]);
+        }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) sum[a][b] = l == 0 ? acc[a][b] : __fadd_rn(sum[a][b], acc[a][b]);
+  }
+  for (int c = sd; c < d; c++) {
+    float xa[4], yb[4];
+#pragma unroll
+    for (int a = 0; a < 4; a++) xa[a] = sa[(ty + 16 * a) * S + c];
+#pragma unroll
+    for (int b = 0; b < 4; b++) yb[b] = sb[(tx + 16 * b) * S + c];
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+      for (int b = 0; b < 4; b++) {
+        const float df = __fsub_rn(xa[a], yb[b]);
+        sum[a][b] = FMA8 ? __fmaf_rn(df, df, sum[a][b]) : __fadd_rn(sum[a][b], sq_rn(df));
+      }
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+    const int64_t gi = i0 + ty + 16 * a;
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int64_t gj = j0 + tx + 16 * b;
+      const float v = METRIC == METRIC_EUCLIDEAN ? __fsqrt_rn(sum[a][b]) : sum[a][b];
+      if (FORM == FUELG_PAIRWISE_CONDENSED) {
+        if (gi < n && gj < gi) out[gi * (gi - 1) / 2 + gj] = v;
+      } else {
+        if (gi < n && gj < n) out[gi * n + gj] = v;
+        st[ty + 16 * a][tx + 16 * b] = v;
+      }
+    }
+  }
+  if (FORM == FUELG_PAIRWISE_SQUARE && bi != bj) {  // the mirrored tile (j, i), row by row
+    __syncthreads();
+    for (int e = threadIdx.x; e < PR * PR; e += 256) {
+      const int rj = e / PR, ci = e - rj * PR;
+      const int64_t gj = j0 + rj, gi = i0 + ci;
+      if (gj < n && gi < n) out[gj * n + gi] = st[ci][rj];
+    }
+  }
+}
+
 }  // namespace
 
 int pairwise_launch(const float* X, int64_t n, int d, int metric, int order, int form, float* out,
                     cudaStream_t stream) {
   if (n < 2 && form == FUELG_PAIRWISE_CONDENSED) return ST_OK;
   if (n < 1) return ST_OK;
-  const int64_t ntb = (n + PT - 1) / PT;
+  const bool rows = d <= kRowsMaxD;
+  const int64_t ntb = (n + (rows ? PR : PT) - 1) / (rows ? PR : PT);
   const int64_t tiles = ntb * (ntb + 1) / 2;
   if (tiles > 0x7fffffffll) {
     set_error("pairwise: %lld points need more tiles than one launch holds", (long long)n);
@@ -154,7 +254,17 @@ int pairwise_launch(const float* X, int64_t n, int d, int metric, int order, int
   }
   HotTimer* ht = hot_timer();
   if (ht) ht->begin(stream);
-#define FUELG_PW(O, M, F) pairwise_kernel<O, M, F><<<(unsigned)tiles, 256, 0, stream>>>(X, n, d, ntb, out)
+  const size_t rsm = (size_t)2 * PR * (d + 1) * sizeof(float);
+  auto launch = [&](auto kr, auto kc) -> int {
+    if (rows) {
+      FUELG_CUDA(cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm));
+      kr<<<(unsigned)tiles, 256, rsm, stream>>>(X, n, d, ntb, out);
+    } else {
+      kc<<<(unsigned)tiles, 256, 0, stream>>>(X, n, d, ntb, out);
+    }
+    return ST_OK;
+  };
+#define FUELG_PW(O, M, F) FUELG_TRY(launch(pairwise_rows_kernel<O, M, F>, pairwise_kernel<O, M, F>))
   const bool x86 = order == ORDER_X86, eu = metric == METRIC_EUCLIDEAN, cond = form == FUELG_PAIRWISE_CONDENSED;
   if (x86 && eu && cond) FUELG_PW(ORDER_X86, METRIC_EUCLIDEAN, FUELG_PAIRWISE_CONDENSED);
   else if (x86 && eu) FUELG_PW(ORDER_X86, METRIC_EUCLIDEAN, FUELG_PAIRWISE_SQUARE);

@@ -36,7 +36,8 @@ def test_precomputed_conversions_cpu():
 @pytest.mark.parametrize("order", ["arm", "x86"])
 @pytest.mark.parametrize("metric", ["euclidean", "sqeuclidean"])
 @pytest.mark.parametrize("form", ["condensed", "square"])
-@pytest.mark.parametrize("n,d", [(1, 5), (2, 3), (33, 1), (70, 7), (129, 64), (300, 100), (257, 784)])
+@pytest.mark.parametrize("n,d", [(1, 5), (2, 3), (33, 1), (70, 7), (129, 64), (300, 100), (150, 128), (140, 129),
+                                 (257, 784)])
 def test_pairwise_matches_oracle(gpu, oracle, order, metric, form, n, d):
     rng = np.random.default_rng(n * 31 + d)
     X = rng.normal(size=(n, d)).astype(np.float32)
