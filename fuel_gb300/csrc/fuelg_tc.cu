@@ -223,7 +223,7 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(&accf[b], 1);
-      mbar_init(&acce[b], BM);
+      mbar_init(&acce[b], BM / 32);  // one arrive per epilogue warp
     }
     mbar_init(fin, 1);
     *abort_flag = 0;
@@ -425,9 +425,60 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       tc_fence_after();
       const uint32_t acc_cols = (BLO && a.sep_lo ? 2u : 1u) * (uint32_t)a.kp;
       const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + buf * acc_cols;
-      // pass 1: screened argmin (first index wins ties)
       float best = __int_as_float(0x7f800000), best_dot = 0.0f;
       int bj = 0;
+      uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+      if (a.kp <= 64) {
+        // The row's kp <= 64 dot products in registers: two TMEM round trips,
+        // then the accumulator is released before the screen arithmetic.
+        float v[64];
+#pragma unroll
+        for (int h0 = 0; h0 < 4; h0 += 2) {
+          uint32_t rh[2][16], rl[2][16];
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+            if (16 * (h0 + h) < a.kp) {
+              tmem_ld16_nowait(taddr + 16 * (h0 + h), rh[h]);
+              if (BLO && a.sep_lo) tmem_ld16_nowait(taddr + a.kp + 16 * (h0 + h), rl[h]);
+            }
+          tmem_ld_wait();
+#pragma unroll
+          for (int h = 0; h < 2; h++)
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+              float x = 16 * (h0 + h) < a.kp ? __uint_as_float(rh[h][j]) : 0.0f;
+              if (BLO && a.sep_lo && 16 * (h0 + h) < a.kp) x += __uint_as_float(rl[h][j]);
+              v[16 * (h0 + h) + j] = x;
+            }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[buf]);
+        // pass 1: screened argmin (first index wins ties)
+#pragma unroll
+        for (int col = 0; col < 64; col++)
+          if (col < a.k) {
+            const float dt = fmaf(-2.0f, v[col], nxi + snc[col]);
+            if (dt < best) {
+              best = dt;
+              bj = col;
+              best_dot = v[col];
+            }
+          }
+        const float sb = nonneg ? fmaxf(best_dot, 0.0f) * a.s_scale : xni * scn[bj];
+        const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
+        const float hi = best + eb;
+        // pass 2: every other centre whose lower bound reaches the best's upper bound
+#pragma unroll
+        for (int col = 0; col < 64; col++)
+          if (col < a.k && col != bj) {
+            const float dt = fmaf(-2.0f, v[col], nxi + snc[col]);
+            const float sj = nonneg ? fmaxf(v[col], 0.0f) * a.s_scale : xni * scn[col];
+            const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
+            if (!(dt - e > hi)) m0 |= 1ull << col;
+          }
+      } else {
+      // pass 1: screened argmin (first index wins ties)
       for (int c0 = 0; c0 < a.kp; c0 += 16) {
         float v[16];
         tmem_ld16(taddr + c0, v);
@@ -455,7 +506,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
       const float hi = best + eb;
       // pass 2: every other centre whose lower bound reaches the best's upper bound
-      uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
       for (int c0 = 0; c0 < a.kp; c0 += 16) {
         float v[16];
         tmem_ld16(taddr + c0, v);
@@ -484,7 +534,9 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         }
       }
       tc_fence_before();
-      mbar_arrive(&acce[buf]);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[buf]);
+      }
       const bool und = (m0 | m1 | m2 | m3) != 0;
       if (a.fused) commit(valid && !und, i, bj, old_lab);  // undecided points: committed by the re-score kernel
       if (valid) {
