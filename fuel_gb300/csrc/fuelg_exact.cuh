@@ -48,8 +48,30 @@ __device__ __forceinline__ float rn_ratio_f32(unsigned __int128 A, unsigned long
   int sh = 0;
   if (bitsA - bitsC < 27) sh = 27 - (bitsA - bitsC);
   const unsigned __int128 A2 = A << sh;
-  const unsigned __int128 q = A2 / cnt;
-  const unsigned __int128 r = A2 - q * cnt;
+  // exact quotient and remainder: one 64-bit division when A2 fits 64 bits (the
+  // common case), else long division by 32-bit digits (cnt < 2^32), else the
+  // generic 128-bit division
+  unsigned __int128 q, r;
+  if ((A2 >> 64) == 0) {
+    const unsigned long long a64 = (unsigned long long)A2;
+    const unsigned long long q64 = a64 / cnt;
+    q = q64;
+    r = a64 - q64 * cnt;
+  } else if ((cnt >> 32) == 0) {
+    unsigned long long rr = 0;
+    q = 0;
+#pragma unroll
+    for (int w = 3; w >= 0; w--) {
+      const unsigned long long cur = (rr << 32) | (unsigned long long)(uint32_t)(A2 >> (32 * w));
+      const unsigned long long qw = cur / cnt;  // < 2^32: rr < cnt < 2^32
+      rr = cur - qw * cnt;
+      q = (q << 32) | qw;
+    }
+    r = rr;
+  } else {
+    q = A2 / cnt;
+    r = A2 - q * cnt;
+  }
   const int p = q >> 64 ? 128 - __clzll((long long)(unsigned long long)(q >> 64))
                         : 64 - __clzll((long long)(unsigned long long)q);
   const int drop = p - 24;

@@ -84,6 +84,23 @@ def test_wide_exponent_range_uses_fp64_sums(gpu, oracle):
         assert np.array_equal(r.labels, lab)
 
 
+@pytest.mark.parametrize("scale_bits", [(-20, 20), (-45, 30)])
+def test_multi_limb_exact_sums(gpu, oracle, scale_bits):
+    """Exponent ranges that need 2-3 limbs of exact sums (quotients beyond 64
+    bits in the mean rounding): centres and labels bit-exact against the
+    exact-mean oracle, plain and tensor-core tiers."""
+    lo, hi = scale_bits
+    X = mixture(2000, 40, 6, 11)
+    rng = np.random.default_rng(12)
+    X *= np.exp2(rng.integers(lo, hi, size=X.shape)).astype(np.float32)
+    init = X[:6].copy()
+    c, lab, it, _ = oracle.lloyd_exact(X, 6, init, max_iter=5, threads=threads(), fixed_iters=True)
+    for prec in ("fp32", "split_bf16"):
+        r = kmeans(X, k=6, variant="lloyd", max_iter=5, init=init, fixed_iters=True, precision=prec)
+        assert np.array_equal(r.labels, lab)
+        assert np.array_equal(r.centers.view(np.uint32), c.view(np.uint32))
+
+
 def test_fixed_iters_and_stop_rule(gpu):
     X = mixture(2000, 4, 3, 9)
     r1 = kmeans(X, k=3, variant="lloyd", max_iter=50, init="first")
