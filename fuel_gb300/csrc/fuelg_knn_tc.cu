@@ -907,6 +907,9 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   // Bound scratch: batches of queries whose lists take at most ~1 GiB.
   const size_t per_query = ((size_t)S * (kk2 * 2 + kApp) + kk2 * 2) * 8;  // per split: lists + kept; merged
   int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
+  // when the queries need several batches (S = 1): whole waves of query blocks
+  // per batch, so every batch but the last fills the GPU's CTA slots evenly
+  if (mb < mpad && mb >= slots * QM) mb = mb / (slots * QM) * (slots * QM);
   mb = std::min<int64_t>(mb, mpad);
   Scratch lists, kept_sp, kept_m, kept2, redo, nredo;
   FUELG_TRY(lists.alloc((size_t)S * mb * (kk2 + kApp) * 8, stream));
