@@ -19,6 +19,7 @@
 // queries that fail the proof are re-run through the exact scan.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include <cuda_fp16.h>
@@ -55,8 +56,14 @@ struct KnnTcArgs {
   const float* qn2;  // |q|^2 per query row
   const float* xn2;  // |x|^2 per index row (padded rows: 0)
   float xmax_n2;     // max |x|^2 over the index (filter slack)
-  uint64_t* lists;   // [S][m][kk2 + kApp]: kept keys + append log per index split
-  uint64_t* out_keys;  // [S][m][kk2]
+  uint64_t* lists;     // [CTA][QM][kk2 + kApp]: kept keys + append log of the rows a CTA works on
+  uint64_t* out_keys;  // [piece][QM][kk2]: each piece's kept keys
+  // Work decomposition: CTA c works through pieces [cta_pb[c], cta_pb[c+1]);
+  // piece p = query block piece_qb[p] against index tiles [piece_t0[p], piece_t1[p]).
+  const int32_t* piece_qb;
+  const int32_t* piece_t0;
+  const int32_t* piece_t1;
+  const int32_t* cta_pb;
   uint32_t idesc;
   int* status;
   const volatile int* cancel;
@@ -235,20 +242,25 @@ __global__ void __launch_bounds__(256) sort_rows_kernel(uint64_t* __restrict__ k
 
 constexpr int kMaxSplits = 128;
 
-// One warp per query: k-way merge of the S (<= kMaxSplits) sorted split
-// lists in[s][q][0, kk2) into out[q][0, kk2); lane l owns lists l, l+32, ...
-__global__ void __launch_bounds__(256) merge_tc_splits_kernel(const uint64_t* __restrict__ in, int64_t m, int S,
-                                                              int kk2, uint64_t* __restrict__ out) {
+// One warp per query: k-way merge of the sorted lists its query block's
+// pieces kept -- piece p holds rows in[p][0, QM)[0, kk2); the block's pieces are
+// [qb_pb[qb], qb_pb[qb + 1]), at most kMaxSplits -- into out[q][0, kk2); lane l
+// owns pieces l, l+32, ...
+__global__ void __launch_bounds__(256) merge_tc_splits_kernel(const uint64_t* __restrict__ in, int64_t m,
+                                                              const int32_t* __restrict__ qb_pb, int kk2,
+                                                              uint64_t* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (q >= m) return;
+  const int64_t qb = q / QM, row = q - qb * QM;
+  const int p0 = qb_pb[qb], S = qb_pb[qb + 1] - p0;
   int pos[kMaxSplits / 32];
   uint64_t head[kMaxSplits / 32];
 #pragma unroll
   for (int t = 0; t < kMaxSplits / 32; t++) {
     const int sp = lane + 32 * t;
     pos[t] = 0;
-    head[t] = sp < S ? in[((size_t)sp * m + q) * kk2] : KEY_NONE;
+    head[t] = sp < S ? in[((size_t)(p0 + sp) * QM + row) * kk2] : KEY_NONE;
   }
   for (int j = 0; j < kk2; j++) {
     uint64_t mn = head[0];
@@ -267,7 +279,7 @@ __global__ void __launch_bounds__(256) merge_tc_splits_kernel(const uint64_t* __
       if (head[t] == mn) {  // keys are unique: one list advances
         const int sp = lane + 32 * t;
         pos[t]++;
-        head[t] = pos[t] < kk2 ? in[((size_t)sp * m + q) * kk2 + pos[t]] : KEY_NONE;
+        head[t] = pos[t] < kk2 ? in[((size_t)(p0 + sp) * QM + row) * kk2 + pos[t]] : KEY_NONE;
       }
   }
 }
@@ -289,19 +301,18 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
   uint64_t* accf = empty + NS;
   uint64_t* acce = accf + 2;
   uint64_t* afull = acce + 2;
-  uint64_t* fin = afull + 1;
+  uint64_t* aempty = afull + 1;  // the MMAs reading a piece's query tile are done
+  uint64_t* fin = aempty + 1;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
-  float* xnsm = reinterpret_cast<float*>(tmem_holder + 4);  // [kEpiWarps][2][XN] index norms
+  // [kEpiWarps][2][XN] index norms, read as float4: 16-byte aligned
+  float* xnsm = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(tmem_holder + 2) + 15) & ~(uintptr_t)15);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t q0 = (int64_t)blockIdx.x * QM;
-  // index split blockIdx.y of gridDim.y: tiles [tb, tb + ntiles)
-  const int64_t ntiles_all = (a.n + XN - 1) / XN;
-  const int64_t tb = ntiles_all * blockIdx.y / gridDim.y;
-  const int64_t ntiles = ntiles_all * (blockIdx.y + 1) / gridDim.y - tb;
-  uint64_t* const lists_sp = a.lists + (size_t)blockIdx.y * a.m * ((size_t)a.kk2 + kApp);
-  uint64_t* const out_sp = a.out_keys + (size_t)blockIdx.y * a.m * a.kk2;
+  // this CTA's pieces: (query block, index tile range), worked through in order
+  const int pb = a.cta_pb[blockIdx.x], pe = a.cta_pb[blockIdx.x + 1];
+  const size_t qstride = (size_t)a.kk2 + kApp;
+  uint64_t* const lists_cta = a.lists + (size_t)blockIdx.x * QM * qstride;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < NS; s++) {
@@ -313,6 +324,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
       mbar_init(&acce[b], kEpiWarps);
     }
     mbar_init(afull, 1);
+    mbar_init(aempty, 1);
     mbar_init(fin, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -333,91 +345,112 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
       prefetch_tmap(&tmQ);
       prefetch_tmap(&tmX);
       const uint64_t pol_q = policy_evict_first(), pol_x = policy_evict_last();
-      // the query tile, once
-      mbar_expect_tx(afull, (uint32_t)(a.split ? 2 : 1) * a.kc * a_chunk);
-      for (int kc = 0; kc < a.kc; kc++) tma_load_2d_hint(sA + (size_t)kc * a_chunk, &tmQ, kc * BK, (int)q0, afull, pol_q);
-      if (a.split)
-        for (int kc = 0; kc < a.kc; kc++)
-          tma_load_2d_hint(sA + (size_t)(a.kc + kc) * a_chunk, &tmQlo, kc * BK, (int)q0, afull, pol_q);
       uint32_t stage = 0, phase = 0, armed = 0, last_ph = 0;
-      for (int64_t t = 0; t < ntiles && !*abort_flag; t++) {
-        if ((t & 63) == 63 && a.cancel != nullptr && *a.cancel) {
-          atomicOr(a.status, DEV_CANCELLED);
+      int loaded = 0;  // query tiles loaded (afull phases)
+      for (int p = pb; p < pe && !*abort_flag; p++) {
+        const int li = p - pb;
+        const int q0 = a.piece_qb[p] * QM;
+        if (li > 0 && !mbar_wait(aempty, (uint32_t)((li - 1) & 1), abort_flag)) {
+          if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
           *abort_flag = 1;
           break;
         }
-        for (int j = 0; j < nb; j++) {
-          if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
-            if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+        // the piece's query tile (hi chunks, then lo chunks in split mode)
+        mbar_expect_tx(afull, (uint32_t)(a.split ? 2 : 1) * a.kc * a_chunk);
+        for (int kc = 0; kc < a.kc; kc++) tma_load_2d_hint(sA + (size_t)kc * a_chunk, &tmQ, kc * BK, q0, afull, pol_q);
+        if (a.split)
+          for (int kc = 0; kc < a.kc; kc++)
+            tma_load_2d_hint(sA + (size_t)(a.kc + kc) * a_chunk, &tmQlo, kc * BK, q0, afull, pol_q);
+        loaded++;
+        for (int64_t t = a.piece_t0[p]; t < a.piece_t1[p] && !*abort_flag; t++) {
+          if ((t & 63) == 63 && a.cancel != nullptr && *a.cancel) {
+            atomicOr(a.status, DEV_CANCELLED);
             *abort_flag = 1;
             break;
           }
-          mbar_expect_tx(&full[stage], b_bytes);
-          armed |= 1u << stage;
-          last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
-          tma_load_2d_hint(sB + (size_t)stage * b_bytes, j < a.kc ? &tmX : &tmXlo, (j % a.kc) * BK,
-                           (int)((tb + t) * XN), &full[stage], pol_x);
-          if (++stage == (uint32_t)NS) {
-            stage = 0;
-            phase ^= 1;
+          for (int j = 0; j < nb; j++) {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+              if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+              *abort_flag = 1;
+              break;
+            }
+            mbar_expect_tx(&full[stage], b_bytes);
+            armed |= 1u << stage;
+            last_ph = (last_ph & ~(1u << stage)) | (phase << stage);
+            tma_load_2d_hint(sB + (size_t)stage * b_bytes, j < a.kc ? &tmX : &tmXlo, (j % a.kc) * BK,
+                             (int)(t * XN), &full[stage], pol_x);
+            if (++stage == (uint32_t)NS) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
         }
       }
+      // never leave a TMA copy writing shared memory: wait (bounded) for the
+      // last query tile and the last load armed on every stage
       volatile int never = 0;
-      if (!mbar_wait(afull, 0, &never)) atomicOr(a.status, DEV_TIMEOUT);
+      if (loaded > 0 && !mbar_wait(afull, (uint32_t)((loaded - 1) & 1), &never)) atomicOr(a.status, DEV_TIMEOUT);
       for (int s2 = 0; s2 < NS; s2++)
         if (armed & (1u << s2))
           if (!mbar_wait(&full[s2], (last_ph >> s2) & 1u, &never)) atomicOr(a.status, DEV_TIMEOUT);
     }
   } else if (warp == 1) {
     if (lane == 0) {
-      bool ok = mbar_wait(afull, 0, abort_flag);
-      if (!ok) {
-        if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-        *abort_flag = 1;
-      }
-      tc_fence_after();
       uint32_t stage = 0, phase = 0;
-      for (int64_t t = 0; ok && t < ntiles && !*abort_flag; t++) {
-        const uint32_t buf = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
-        if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag)) {
+      int64_t gt = 0;  // tiles so far over all pieces: accumulator buffer and parity
+      bool ok = true;
+      for (int p = pb; ok && p < pe && !*abort_flag; p++) {
+        const int li = p - pb;
+        if (!mbar_wait(afull, (uint32_t)(li & 1), abort_flag)) {
           if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
           *abort_flag = 1;
           break;
         }
         tc_fence_after();
-        const uint32_t d_tmem = tmem_base + buf * XN;
-        for (int j = 0; j < nb; j++) {
-          if (!mbar_wait(&full[stage], phase, abort_flag)) {
+        for (int64_t t = a.piece_t0[p]; ok && t < a.piece_t1[p] && !*abort_flag; t++, gt++) {
+          const uint32_t buf = (uint32_t)(gt & 1), accph = (uint32_t)((gt >> 1) & 1);
+          if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag)) {
             if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
             *abort_flag = 1;
             ok = false;
             break;
           }
           tc_fence_after();
-          // B = x_hi[kc]: q_hi . x_hi (+ q_lo . x_hi); B = x_lo[kc]: q_hi . x_lo
-          const int kc = j % a.kc;
-          const uint64_t ad = smem_desc_sw128(smem_u32(sA + (size_t)kc * a_chunk));
-          const uint64_t bd = smem_desc_sw128(smem_u32(sB + (size_t)stage * b_bytes));
-          // K steps of 16 that hold data: the zero columns past d add nothing
-          const int nks = kc == a.kc - 1 ? a.ks_last : BK / 16;
-#pragma unroll
-          for (int kk = 0; kk < BK / 16; kk++)
-            if (kk < nks) umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (j | kk) != 0 ? 1u : 0u);
-          if (a.split && j < a.kc) {
-            const uint64_t al = smem_desc_sw128(smem_u32(sA + (size_t)(a.kc + kc) * a_chunk));
+          const uint32_t d_tmem = tmem_base + buf * XN;
+          for (int j = 0; j < nb; j++) {
+            if (!mbar_wait(&full[stage], phase, abort_flag)) {
+              if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+              *abort_flag = 1;
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            // B = x_hi[kc]: q_hi . x_hi (+ q_lo . x_hi); B = x_lo[kc]: q_hi . x_lo
+            const int kc = j % a.kc;
+            const uint64_t ad = smem_desc_sw128(smem_u32(sA + (size_t)kc * a_chunk));
+            const uint64_t bd = smem_desc_sw128(smem_u32(sB + (size_t)stage * b_bytes));
+            // K steps of 16 that hold data: the zero columns past d add nothing
+            const int nks = kc == a.kc - 1 ? a.ks_last : BK / 16;
 #pragma unroll
             for (int kk = 0; kk < BK / 16; kk++)
-              if (kk < nks) umma_bf16(d_tmem, al + 2 * kk, bd + 2 * kk, a.idesc, 1u);
+              if (kk < nks) umma_bf16(d_tmem, ad + 2 * kk, bd + 2 * kk, a.idesc, (j | kk) != 0 ? 1u : 0u);
+            if (a.split && j < a.kc) {
+              const uint64_t al = smem_desc_sw128(smem_u32(sA + (size_t)(a.kc + kc) * a_chunk));
+#pragma unroll
+              for (int kk = 0; kk < BK / 16; kk++)
+                if (kk < nks) umma_bf16(d_tmem, al + 2 * kk, bd + 2 * kk, a.idesc, 1u);
+            }
+            umma_commit(&empty[stage]);
+            if (++stage == (uint32_t)NS) {
+              stage = 0;
+              phase ^= 1;
+            }
           }
-          umma_commit(&empty[stage]);
-          if (++stage == (uint32_t)NS) {
-            stage = 0;
-            phase ^= 1;
-          }
+          if (!ok) break;
+          umma_commit(&accf[buf]);
         }
-        if (!ok) break;
-        umma_commit(&accf[buf]);
+        // the query tile may be replaced once these MMAs are done
+        umma_commit(aempty);
       }
       umma_commit(fin);
       volatile int never = 0;
@@ -430,144 +463,154 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
     const int g = warp & 3;
     const int ew = warp - 2;
     const int row = g * 32 + lane;  // TMEM lane = query row of the tile
-    const int64_t qi = q0 + row;
-    const bool valid = qi < a.m;
-    const float nq = valid ? a.qn2[qi] : 0.0f;
-    const int kkr = (a.row_k != nullptr && valid) ? kk2_of(a.row_k[qi], a.margin_mode) : a.kk2;  // this row's keys
-    const size_t qstride = (size_t)a.kk2 + kApp;
-    uint64_t* app = lists_sp + (valid ? qi : 0) * qstride + a.kk2;  // this query's append log
     float* nsm_w = xnsm + ew * 2 * XN;
-    uint64_t tau = KEY_NONE;  // kk2-th key held
-    float tau_d = __int_as_float(0x7f800000);
-    int na = 0, plen = 0;
-    // Screen filter in the shifted domain: a column can enter only if
-    // |x|^2 - 2 q.x <= tau - |q|^2 (+ slack covering the rounding of both
-    // forms when the data are not exact integers); the screened distance is
-    // formed only for the rare columns that pass.
-    auto threshold = [&]() -> float {
-      if (!valid) return -__int_as_float(0x7f800000);
-      if (tau == KEY_NONE) return __int_as_float(0x7f800000);
-      const float th = tau_d - nq;
-      return a.exact ? th : th + (nq + a.xmax_n2 + tau_d) * 3.814697265625e-06f;  // 2^-18
-    };
-    // Lanes whose append log passed `lim` entries are reduced to their kk2
-    // smallest keys, one query at a time, by the whole warp.
-    auto flush_rows = [&](unsigned need) {
-      __syncwarp();
-      while (need) {
-        const int src = __ffs(need) - 1;
-        need &= need - 1;
-        const int sna = __shfl_sync(0xffffffffu, na, src);
-        const int splen = __shfl_sync(0xffffffffu, plen, src);
-        const int skk = __shfl_sync(0xffffffffu, kkr, src);
-        uint64_t* lb = lists_sp + (q0 + g * 32 + src) * qstride;
-        const uint64_t nt = warp_select(lb + a.kk2, sna, lb, splen, skk, lane);
-        if (lane == src) {
-          tau = nt;
-          tau_d = nt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(nt);
-          plen = min(kkr, plen + na);
-          na = 0;
-        }
-      }
-    };
-    auto flush = [&](int lim) {
-      const unsigned need = __ballot_sync(0xffffffffu, na > lim);
-      if (need) flush_rows(need);
-    };
-    float thr = threshold();
-    // norms of the tile's XN columns: 4 per lane, fetched one tile ahead
-    float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + tb * XN) + lane);
-    for (int64_t t = 0; t < ntiles; t++) {
-      const uint32_t b = (uint32_t)(t & 1), accph = (uint32_t)((t >> 1) & 1);
-      const int64_t p0 = (tb + t) * XN;
-      float* nsm = nsm_w + b * XN;
-      reinterpret_cast<float4*>(nsm)[lane] = pn;
-      if (t + 1 < ntiles) pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + p0 + XN) + lane);
-      bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag);
-      if (!ok) {
-        if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
-        *abort_flag = 1;
-      }
-      if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
-      __syncwarp();
-      tc_fence_after();
-      const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN;
-#pragma unroll 1
-      for (int c0 = 0; c0 < XN; c0 += 64) {
-        uint32_t r[4][16];
-#pragma unroll
-        for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
-        tmem_ld_wait();
-        // shifted screen values f = |x|^2 - 2 q.x (in place) and each group's
-        // minimum as a 4-level tree (short dependency chains, four groups interleaved)
-        float mnh[4];
-#pragma unroll
-        for (int h = 0; h < 4; h++) {
-          const float4* n4 = reinterpret_cast<const float4*>(nsm + c0 + 16 * h);
-#pragma unroll
-          for (int v = 0; v < 4; v++) {
-            const float4 q4 = n4[v];
-            r[h][4 * v] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v]), q4.x));
-            r[h][4 * v + 1] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 1]), q4.y));
-            r[h][4 * v + 2] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z));
-            r[h][4 * v + 3] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w));
+    uint64_t* const app = lists_cta + row * qstride + a.kk2;  // this row's append log
+    int64_t gt = 0;  // tiles so far over all pieces (accumulator buffer and parity)
+    bool alive = true;
+    for (int p = pb; alive && p < pe; p++) {
+      const int64_t q0 = (int64_t)a.piece_qb[p] * QM;
+      const int64_t qi = q0 + row;
+      const bool valid = qi < a.m;
+      const float nq = valid ? a.qn2[qi] : 0.0f;
+      const int kkr = (a.row_k != nullptr && valid) ? kk2_of(a.row_k[qi], a.margin_mode) : a.kk2;  // this row's keys
+      uint64_t tau = KEY_NONE;  // kk2-th key held
+      float tau_d = __int_as_float(0x7f800000);
+      int na = 0, plen = 0;
+      // Screen filter in the shifted domain: a column can enter only if
+      // |x|^2 - 2 q.x <= tau - |q|^2 (+ slack covering the rounding of both
+      // forms when the data are not exact integers); the screened distance is
+      // formed only for the rare columns that pass.
+      auto threshold = [&]() -> float {
+        if (!valid) return -__int_as_float(0x7f800000);
+        if (tau == KEY_NONE) return __int_as_float(0x7f800000);
+        const float th = tau_d - nq;
+        return a.exact ? th : th + (nq + a.xmax_n2 + tau_d) * 3.814697265625e-06f;  // 2^-18
+      };
+      // Lanes whose append log passed `lim` entries are reduced to their kk2
+      // smallest keys, one query at a time, by the whole warp.
+      auto flush_rows = [&](unsigned need) {
+        __syncwarp();
+        while (need) {
+          const int src = __ffs(need) - 1;
+          need &= need - 1;
+          const int sna = __shfl_sync(0xffffffffu, na, src);
+          const int splen = __shfl_sync(0xffffffffu, plen, src);
+          const int skk = __shfl_sync(0xffffffffu, kkr, src);
+          uint64_t* lb = lists_cta + (g * 32 + src) * qstride;
+          const uint64_t nt = warp_select(lb + a.kk2, sna, lb, splen, skk, lane);
+          if (lane == src) {
+            tau = nt;
+            tau_d = nt == KEY_NONE ? __int_as_float(0x7f800000) : key_dist(nt);
+            plen = min(kkr, plen + na);
+            na = 0;
           }
-          float m8[8];
-#pragma unroll
-          for (int j = 0; j < 8; j++) m8[j] = fminf(__uint_as_float(r[h][2 * j]), __uint_as_float(r[h][2 * j + 1]));
-#pragma unroll
-          for (int j = 0; j < 4; j++) m8[j] = fminf(m8[2 * j], m8[2 * j + 1]);
-          mnh[h] = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
         }
+      };
+      float thr = threshold();
+      const int64_t t0 = a.piece_t0[p], t1 = a.piece_t1[p];
+      // norms of the tile's XN columns: 4 per lane, fetched one tile ahead
+      float4 pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + t0 * XN) + lane);
+      for (int64_t t = t0; t < t1; t++, gt++) {
+        const uint32_t b = (uint32_t)(gt & 1), accph = (uint32_t)((gt >> 1) & 1);
+        const int64_t p0 = t * XN;
+        float* nsm = nsm_w + b * XN;
+        reinterpret_cast<float4*>(nsm)[lane] = pn;
+        if (t + 1 < t1) pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + p0 + XN) + lane);
+        bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag);
+        if (!ok) {
+          if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
+          *abort_flag = 1;
+        }
+        if (!__all_sync(0xffffffffu, ok)) {  // warp-uniform exit
+          alive = false;
+          break;
+        }
+        __syncwarp();
+        tc_fence_after();
+        const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN;
+#pragma unroll 1
+        for (int c0 = 0; c0 < XN; c0 += 64) {
+          uint32_t r[4][16];
 #pragma unroll
-        for (int h = 0; h < 4; h++) {
-          if (mnh[h] <= thr) {
-            // the few passing columns, one loop trip each; the screened
-            // distance is D~ = |q|^2 + (|x|^2 - 2 q.x) in f32
-            float f[16];
+          for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+          tmem_ld_wait();
+          // shifted screen values f = |x|^2 - 2 q.x (in place) and each group's
+          // minimum as a 4-level tree (short dependency chains, four groups interleaved)
+          float mnh[4];
 #pragma unroll
-            for (int j = 0; j < 16; j++) f[j] = __uint_as_float(r[h][j]);
-            unsigned b8[8];
+          for (int h = 0; h < 4; h++) {
+            const float4* n4 = reinterpret_cast<const float4*>(nsm + c0 + 16 * h);
 #pragma unroll
-            for (int j = 0; j < 8; j++)
-              b8[j] = (f[2 * j] <= thr ? 1u : 0u) | (f[2 * j + 1] <= thr ? 2u : 0u);
+            for (int v = 0; v < 4; v++) {
+              const float4 q4 = n4[v];
+              r[h][4 * v] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v]), q4.x));
+              r[h][4 * v + 1] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 1]), q4.y));
+              r[h][4 * v + 2] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z));
+              r[h][4 * v + 3] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w));
+            }
+            float m8[8];
 #pragma unroll
-            for (int j = 0; j < 4; j++) b8[j] = b8[2 * j] | (b8[2 * j + 1] << 2);
-            unsigned mask = (b8[0] | (b8[1] << 4)) | ((b8[2] | (b8[3] << 4)) << 8);
-            while (mask) {
-              const int j = __ffs(mask) - 1;
-              mask &= mask - 1;
-              const int64_t p = p0 + c0 + 16 * h + j;
-              float dt = nq + sel16(f, j);
-              if (!a.exact) dt = fmaxf(dt, 0.0f);
-              if (dt <= tau_d && p < a.n) {
-                const uint64_t key = make_key(dt, (uint32_t)p);
-                if (key < tau) app[na++] = key;
+            for (int j = 0; j < 8; j++) m8[j] = fminf(__uint_as_float(r[h][2 * j]), __uint_as_float(r[h][2 * j + 1]));
+#pragma unroll
+            for (int j = 0; j < 4; j++) m8[j] = fminf(m8[2 * j], m8[2 * j + 1]);
+            mnh[h] = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
+          }
+#pragma unroll
+          for (int h = 0; h < 4; h++) {
+            if (mnh[h] <= thr) {
+              // the few passing columns, one loop trip each; the screened
+              // distance is D~ = |q|^2 + (|x|^2 - 2 q.x) in f32
+              float f[16];
+#pragma unroll
+              for (int j = 0; j < 16; j++) f[j] = __uint_as_float(r[h][j]);
+              unsigned b8[8];
+#pragma unroll
+              for (int j = 0; j < 8; j++)
+                b8[j] = (f[2 * j] <= thr ? 1u : 0u) | (f[2 * j + 1] <= thr ? 2u : 0u);
+#pragma unroll
+              for (int j = 0; j < 4; j++) b8[j] = b8[2 * j] | (b8[2 * j + 1] << 2);
+              unsigned mask = (b8[0] | (b8[1] << 4)) | ((b8[2] | (b8[3] << 4)) << 8);
+              while (mask) {
+                const int j = __ffs(mask) - 1;
+                mask &= mask - 1;
+                const int64_t pt = p0 + c0 + 16 * h + j;
+                float dt = nq + sel16(f, j);
+                if (!a.exact) dt = fmaxf(dt, 0.0f);
+                if (dt <= tau_d && pt < a.n) {
+                  const uint64_t key = make_key(dt, (uint32_t)pt);
+                  if (key < tau) app[na++] = key;
+                }
               }
             }
           }
+          // at most 64 appends per lane per chunk: compact before the log can overflow
+          const unsigned full = __ballot_sync(0xffffffffu, na > kApp - 64);
+          if (full) {
+            flush_rows(full);
+            thr = threshold();
+          }
         }
-        // at most 64 appends per lane per chunk: compact before the log can overflow
-        const unsigned full = __ballot_sync(0xffffffffu, na > kApp - 64);
-        if (full) {
-          flush_rows(full);
-          thr = threshold();
-        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&acce[b]);
       }
-      tc_fence_before();
+      if (!alive) break;
+      {
+        const unsigned need = __ballot_sync(0xffffffffu, na > 0);
+        if (need) flush_rows(need);
+      }
+      // kept keys out (unsorted; sorted afterwards), one query at a time per
+      // warp (coalesced); slots past the held count are KEY_NONE.  Piece p's
+      // lists sit at rows [p*QM, p*QM + QM) of the output.
       __syncwarp();
-      if (lane == 0) mbar_arrive(&acce[b]);
-    }
-    flush(0);
-    // kept keys out (unsorted; sorted afterwards), one query at a time per
-    // warp (coalesced); slots past the held count are KEY_NONE
-    for (int src = 0; src < 32; src++) {
-      const int64_t qs = q0 + g * 32 + src;
-      if (qs >= a.m) break;
-      const int splen = __shfl_sync(0xffffffffu, plen, src);
-      const uint64_t* from = lists_sp + qs * qstride;
-      uint64_t* to = out_sp + qs * a.kk2;
-      for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
+      for (int src = 0; src < 32; src++) {
+        if (q0 + g * 32 + src >= a.m) break;
+        const int splen = __shfl_sync(0xffffffffu, plen, src);
+        const uint64_t* from = lists_cta + (g * 32 + src) * qstride;
+        uint64_t* to = a.out_keys + ((size_t)p * QM + g * 32 + src) * a.kk2;
+        for (int o = lane; o < a.kk2; o += 32) to[o] = o < splen ? from[o] : KEY_NONE;
+      }
+      __syncwarp();
     }
   }
   tc_fence_before();
@@ -894,28 +937,103 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     set_error("tensor-core kNN tile does not fit shared memory (d=%d)", d);
     return ST_ENOTSUP;
   }
-  // Index splits: when the query blocks cannot fill the GPU's CTA slots, each
-  // block's scan is split over S index ranges (>= 16 tiles each) whose sorted
-  // kept lists are merged afterwards.  Every split keeps its own top-kk2, so
-  // the selection work grows with S.
+  // Work decomposition.  The queries run in batches.  A batch of whole waves
+  // (a multiple of the GPU's CTA slots in query blocks) has one CTA per
+  // block: the hardware hands blocks to free slots as they come, which
+  // evens out blocks of unequal cost.  A batch of less than a wave (a small
+  // query count, or the last part of a large one) would leave slots idle, so
+  // there each block's index scan is cut into s equal tile ranges (quanta);
+  // the quanta, block-major, are dealt out L at a time to consecutive CTAs,
+  // L = ceil(quanta / slots).  s is the count (quanta of >= 16 tiles, at most
+  // kMaxSplits - 2 pieces per block) that minimises the longest CTA's work,
+  // L (ntiles / s + 4) tiles with 4 tiles' worth charged per piece for its
+  // pipeline refill and its list's start.  A CTA's quanta fall into pieces at
+  // query-block boundaries; a block cut into several pieces gets one kept
+  // list per piece, merged afterwards.
   const int64_t ntiles_all = (n + XN - 1) / XN;
   const int64_t slots = 152 * kCtasPerSm;
-  const int64_t qblocks = (m + QM - 1) / QM;
-  int S = 1;
-  if (qblocks < slots)
-    S = (int)std::max<int64_t>(1, std::min<int64_t>({slots / qblocks, ntiles_all / 16, (int64_t)kMaxSplits}));
-  // Bound scratch: batches of queries whose lists take at most ~1 GiB.
-  const size_t per_query = ((size_t)S * (kk2 * 2 + kApp) + kk2 * 2) * 8;  // per split: lists + kept; merged
-  int64_t mb = std::max<int64_t>(QM, (int64_t)((1ull << 30) / per_query) / QM * QM);
-  // when the queries need several batches (S = 1): whole waves of query blocks
-  // per batch, so every batch but the last fills the GPU's CTA slots evenly
-  if (mb < mpad && mb >= slots * QM) mb = mb / (slots * QM) * (slots * QM);
-  mb = std::min<int64_t>(mb, mpad);
-  Scratch lists, kept_sp, kept_m, kept2, redo, nredo;
-  FUELG_TRY(lists.alloc((size_t)S * mb * (kk2 + kApp) * 8, stream));
-  FUELG_TRY(kept_sp.alloc((size_t)S * mb * kk2 * 8, stream));
-  if (S > 1) FUELG_TRY(kept_m.alloc((size_t)mb * kk2 * 8, stream));
-  uint64_t* kept = S > 1 ? kept_m.as<uint64_t>() : kept_sp.as<uint64_t>();
+  const int64_t wave_q = slots * QM;
+  constexpr int kMaxQuanta = kMaxSplits - 2;
+  auto quanta_of = [&](int64_t qbl) -> int {
+    int best = 1;
+    double best_cost = 0.0;
+    for (int sq = 1; sq <= kMaxQuanta; sq++) {
+      if (sq > 1 && ntiles_all / sq < 16) break;
+      const int64_t L = (qbl * sq + slots - 1) / slots;
+      const double cost = (double)L * ((double)ntiles_all / sq + 4.0);
+      if (sq == 1 || cost < best_cost) best = sq, best_cost = cost;
+    }
+    // tunable: FUELG_KNN_QUANTA fixes s
+    if (const char* e = getenv("FUELG_KNN_QUANTA"))
+      best = (int)std::max<int64_t>(1, std::min<int64_t>({(int64_t)atoi(e), (int64_t)kMaxQuanta, ntiles_all}));
+    return best;
+  };
+  struct Batch {
+    int64_t b0, mcur, G, P;
+    bool merge;
+    std::vector<int32_t> tab;  // piece_qb[P] piece_t0[P] piece_t1[P] cta_pb[G+1] qb_pb[blocks+1]
+  };
+  // Bound scratch: whole-wave batches whose lists take at most ~1 GiB.
+  const int64_t mb_waves =
+      std::max<int64_t>(1, (int64_t)((1ull << 30) / ((size_t)(3 * kk2 + kApp) * 8)) / wave_q) * wave_q;
+  std::vector<Batch> batches;
+  size_t lists_rows = 0, kept_rows = 0, merge_rows = 0, tab_max = 0;
+  int64_t mb = 0;  // largest batch
+  for (int64_t b0 = 0; b0 < m;) {
+    const int64_t rem = m - b0;
+    Batch bt;
+    bt.b0 = b0;
+    bt.mcur = rem >= wave_q ? std::min<int64_t>(mb_waves, rem / wave_q * wave_q) : rem;
+    const int64_t qbl = (bt.mcur + QM - 1) / QM;
+    const int sq = bt.mcur >= wave_q ? 1 : quanta_of(qbl);
+    const int64_t nq_all = qbl * sq;
+    const int64_t L = bt.mcur >= wave_q ? 1 : (nq_all + slots - 1) / slots;
+    bt.G = (nq_all + L - 1) / L;
+    std::vector<int32_t> pq, pt0, pt1, cpb(1, 0), qpb(1, 0);
+    for (int64_t c = 0; c < bt.G; c++) {
+      const int64_t qe = std::min<int64_t>(nq_all, (c + 1) * L);
+      for (int64_t qu = c * L; qu < qe;) {
+        // a run of this CTA's quanta inside one block is one piece
+        const int64_t blk = qu / sq, j0 = qu - blk * sq;
+        const int64_t j1 = std::min<int64_t>(sq, j0 + (qe - qu));
+        pq.push_back((int32_t)blk);
+        pt0.push_back((int32_t)(ntiles_all * j0 / sq));
+        pt1.push_back((int32_t)(ntiles_all * j1 / sq));
+        qu += j1 - j0;
+      }
+      cpb.push_back((int32_t)pq.size());
+    }
+    bt.P = (int64_t)pq.size();
+    bt.merge = false;
+    for (int64_t p = 0, blk = 0; p < bt.P; p++) {
+      if (pt0[p] != 0 || pt1[p] != ntiles_all) bt.merge = true;
+      while (blk < pq[p]) qpb.push_back((int32_t)p), blk++;
+      if (p + 1 == bt.P) qpb.push_back((int32_t)bt.P);
+    }
+    for (int64_t blk = 0; blk < qbl; blk++)
+      if (qpb[blk + 1] - qpb[blk] > kMaxSplits) {
+        set_error("kNN work decomposition cuts a query block into more than %d pieces", kMaxSplits);
+        return ST_EINVAL;
+      }
+    bt.tab.reserve(3 * bt.P + bt.G + 1 + qbl + 1);
+    bt.tab.insert(bt.tab.end(), pq.begin(), pq.end());
+    bt.tab.insert(bt.tab.end(), pt0.begin(), pt0.end());
+    bt.tab.insert(bt.tab.end(), pt1.begin(), pt1.end());
+    bt.tab.insert(bt.tab.end(), cpb.begin(), cpb.end());
+    bt.tab.insert(bt.tab.end(), qpb.begin(), qpb.end());
+    lists_rows = std::max(lists_rows, (size_t)bt.G * QM);
+    kept_rows = std::max(kept_rows, (size_t)bt.P * QM);
+    if (bt.merge) merge_rows = std::max(merge_rows, (size_t)bt.mcur);
+    tab_max = std::max(tab_max, bt.tab.size());
+    mb = std::max(mb, bt.mcur);
+    b0 += bt.mcur;
+    batches.push_back(std::move(bt));
+  }
+  Scratch lists, kept_sp, kept_m, kept2, redo, nredo, plan;
+  FUELG_TRY(lists.alloc(lists_rows * (kk2 + kApp) * 8, stream));
+  FUELG_TRY(kept_sp.alloc(kept_rows * kk2 * 8, stream));
+  if (merge_rows) FUELG_TRY(kept_m.alloc(merge_rows * kk2 * 8, stream));
+  FUELG_TRY(plan.alloc(sizeof(int32_t) * tab_max, stream));
   if (margin) {
     FUELG_TRY(kept2.alloc((size_t)mb * kk2 * 8, stream));
     FUELG_TRY(redo.alloc(sizeof(int32_t) * mb, stream));
@@ -945,8 +1063,9 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
   const float xmax_norm = sqrtf(xmax_n2) * (1.0f + 1e-6f);
   int64_t total_redo = 0;
   HotTimer* ht = hot_timer();
-  for (int64_t b0 = 0; b0 < m; b0 += mb) {
-    const int64_t mcur = std::min<int64_t>(mb, m - b0);
+  for (const Batch& bt : batches) {
+    const int64_t b0 = bt.b0, mcur = bt.mcur, G = bt.G, P = bt.P;
+    const bool merge = bt.merge;
     KnnTcArgs a{};
     a.m = mcur;
     a.n = n;
@@ -963,6 +1082,15 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     a.xmax_n2 = xmax_n2;
     a.lists = lists.as<uint64_t>();
     a.out_keys = kept_sp.as<uint64_t>();
+    // this batch's pieces
+    FUELG_CUDA(cudaMemcpyAsync(plan.p, bt.tab.data(), bt.tab.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               stream));
+    const int32_t* dtab = plan.as<int32_t>();
+    a.piece_qb = dtab;
+    a.piece_t0 = dtab + P;
+    a.piece_t1 = dtab + 2 * P;
+    a.cta_pb = dtab + 3 * P;
+    const int32_t* qb_pb = dtab + 3 * P + G + 1;
     // instruction descriptor: D=F32, A=B=BF16 (format 1) or FP16 (format 0), K-major, N=XN, M=QM
     a.idesc = (1u << 4) | (f16 ? 0u : (1u << 7) | (1u << 10)) | ((uint32_t)(XN >> 3) << 17) |
               ((uint32_t)(QM >> 4) << 24);
@@ -973,7 +1101,7 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     FUELG_TRY(make_map_bf16(&tmQb, qb.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
     if (split) FUELG_TRY(make_map_bf16(&tmQl, qlo.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
     else tmQl = tmQb;
-    const dim3 grid((unsigned)((mcur + QM - 1) / QM), (unsigned)S);
+    const dim3 grid((unsigned)G);
     if (ht) ht->begin(stream);
     const CUtensorMap& tmXs = f16 ? ti->tmXh : ti->tmX;
     kern<<<grid, kThreadsKT, smem, stream>>>(tmQb, tmXs, tmQl, split ? ti->tmXlo : tmXs, a);
@@ -981,14 +1109,17 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     if (ht) ht->end(stream);
     FUELG_CUDA(cudaGetLastError());
     uint64_t* dst = out_keys + b0 * kk;
-    // each query's kept keys in (distance, index) order
-    sort_rows_kernel<<<(unsigned)((S * mcur * 32 + 255) / 256), 256, 0, stream>>>(kept_sp.as<uint64_t>(),
-                                                                                   S * mcur, kk2);
+    // each piece's kept keys in (distance, index) order; with one piece per
+    // block the pieces' rows are the queries' rows
+    const int64_t srows = merge ? P * QM : mcur;
+    sort_rows_kernel<<<(unsigned)((srows * 32 + 255) / 256), 256, 0, stream>>>(kept_sp.as<uint64_t>(), srows, kk2);
     ::fuelg::note_launch();
-    if (S > 1) {
-      merge_tc_splits_kernel<<<(unsigned)((mcur * 32 + 255) / 256), 256, 0, stream>>>(kept_sp.as<uint64_t>(), mcur, S,
-                                                                                      kk2, kept);
+    uint64_t* kept = kept_sp.as<uint64_t>();
+    if (merge) {
+      merge_tc_splits_kernel<<<(unsigned)((mcur * 32 + 255) / 256), 256, 0, stream>>>(kept_sp.as<uint64_t>(), mcur,
+                                                                                      qb_pb, kk2, kept_m.as<uint64_t>());
       ::fuelg::note_launch();
+      kept = kept_m.as<uint64_t>();
     }
     FUELG_CUDA(cudaGetLastError());
     if (margin == 0) {
