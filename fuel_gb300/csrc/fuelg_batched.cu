@@ -314,7 +314,8 @@ __global__ void batched_step_kernel(int P, int32_t* __restrict__ pchg, int32_t* 
   }
 }
 
-// FP64 sum of squared distances to the final centres, per problem.
+// Sum of squared distances to the final centres, per problem (near-FP64:
+// SqDiffAcc per row, FP64 across rows).
 __global__ void batched_inertia_kernel(const BProb* __restrict__ probs, int P, int items_total,
                                        const float* __restrict__ X, const float* __restrict__ C,
                                        const int32_t* __restrict__ labels, double* __restrict__ inertia) {
@@ -331,10 +332,12 @@ __global__ void batched_inertia_kernel(const BProb* __restrict__ probs, int P, i
     if (pr.active && i < pr.n) {
       const float* x = X + pr.x_off + i * pr.d;
       const float* c = C + pr.c_off + (int64_t)labels[pr.lab_off + i] * pr.d;
+      SqDiffAcc sa;
       for (int t = 0; t < pr.d; t++) {
-        const double df = (double)x[t] - (double)c[t];
-        s += df * df;
+        sa.add(x[t], c[t]);
+        if ((t & 31) == 31) sa.renorm();
       }
+      s = sa.value();
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);

@@ -380,4 +380,49 @@ __host__ __device__ inline int smem_row_stride(int d) {
   return s;
 }
 
+// Sum of squared differences (x - c)^2 to near-FP64 accuracy on FP32
+// arithmetic (the FP64 pipe runs at a small fraction of the FP32 rate):
+// x - c = dh + dl exactly (Knuth's two-sum), dh^2 = p + pe exactly (FMA), so
+// (x - c)^2 = p + (pe + dl (2 dh + dl)), the second part within 2^-46 of p
+// relative; the p terms go into a float-float accumulator (two-sum, the
+// rounding errors collected in a second float).  pe is exact for |dh| >=
+// 2^-50 (its bits are multiples of 2^-146, above the subnormal step); an
+// element with 0 < |dh| < 2^-50 or |dh| >= 2^60 (or a non-finite difference)
+// is added in FP64 instead.  renorm() folds the low float back into the
+// high one (a fast two-sum); calling it every few dozen terms keeps the low
+// part within a few ulps of the high one, so the relative error stays near
+// 2^-40 per renormalised run of terms.
+__device__ __forceinline__ void two_sum_f32(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+struct SqDiffAcc {
+  float sh = 0.0f, sl = 0.0f;
+  double slow = 0.0;
+  __device__ __forceinline__ void add(float xv, float cv) {
+    float dh, dl;
+    two_sum_f32(xv, -cv, dh, dl);
+    const float ad = fabsf(dh);
+    if (!(ad < 0x1p60f && (ad >= 0x1p-50f || ad == 0.0f))) {  // rare: FP64
+      const double df = (double)xv - (double)cv;
+      slow = fma(df, df, slow);
+      dh = 0.0f;
+      dl = 0.0f;
+    }
+    const float p = __fmul_rn(dh, dh);
+    const float q = __fmaf_rn(dl, __fadd_rn(__fadd_rn(dh, dh), dl), __fmaf_rn(dh, dh, -p));
+    float e;
+    two_sum_f32(sh, p, sh, e);
+    sl = __fadd_rn(sl, __fadd_rn(e, q));
+  }
+  __device__ __forceinline__ void renorm() {
+    const float s = __fadd_rn(sh, sl);
+    sl = __fsub_rn(sl, __fsub_rn(s, sh));
+    sh = s;
+  }
+  __device__ __forceinline__ double value() const { return ((double)sh + (double)sl) + slow; }
+};
+
 }  // namespace fuelg

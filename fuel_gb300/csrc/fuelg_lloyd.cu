@@ -145,22 +145,51 @@ __global__ void reduce_update_kernel(const double* __restrict__ partial, int d, 
   }
 }
 
-// Per-block FP64 partials of sum_i ||x_i - c_{l_i}||^2 (differences in double).
+// Per-block FP64 partials of sum_i ||x_i - c_{l_i}||^2, to near-FP64
+// accuracy on FP32 arithmetic (one SqDiffAcc per lane, renormalised every
+// 32 terms at most, converted to FP64 once).
 __global__ void inertia_partial_kernel(const float* __restrict__ X, int64_t n, int d, const float* __restrict__ C,
                                        const int32_t* __restrict__ labels, double* __restrict__ partial) {
   __shared__ double red[32];
   double acc = 0.0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const bool vec = (d & 3) == 0 && ((reinterpret_cast<uintptr_t>(X) | reinterpret_cast<uintptr_t>(C)) & 15) == 0;
+  SqDiffAcc sa;  // this lane's terms over all its rows, renormalised every <= 32 terms
   for (int64_t i = (int64_t)blockIdx.x * nw + warp; i < n; i += (int64_t)gridDim.x * nw) {
     const float* x = X + i * d;
     const float* c = C + (int64_t)labels[i] * d;
-    double s = 0.0;
-    for (int t = lane; t < d; t += 32) {
-      const double df = (double)x[t] - (double)c[t];
-      s = fma(df, df, s);
+    if (vec) {
+      // up to 8 float4 of the row and of its centre per lane in flight at once
+      for (int cb = 4 * lane; cb < d; cb += 128 * 8) {
+        float4 xv[8], cv[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          const int c0 = cb + 128 * u;
+          if (c0 < d) {
+            xv[u] = __ldg(reinterpret_cast<const float4*>(x + c0));
+            cv[u] = __ldg(reinterpret_cast<const float4*>(c + c0));
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+          if (cb + 128 * u >= d) break;
+          sa.add(xv[u].x, cv[u].x);
+          sa.add(xv[u].y, cv[u].y);
+          sa.add(xv[u].z, cv[u].z);
+          sa.add(xv[u].w, cv[u].w);
+        }
+        sa.renorm();
+      }
+    } else {
+      for (int t0 = lane; t0 < d; t0 += 32 * 32) {
+        const int t1 = min(d, t0 + 32 * 32);
+#pragma unroll 4
+        for (int t = t0; t < t1; t += 32) sa.add(__ldg(x + t), __ldg(c + t));
+        sa.renorm();
+      }
     }
-    acc += s;
   }
+  acc = sa.value();
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
   if (lane == 0) red[warp] = acc;

@@ -287,23 +287,20 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
                      bucket_in, bucket_out, limbs);
 }
 
-// Canonicalise one coordinate's limbs and, for a non-empty cluster, write
-// its exact mean as the correctly rounded f32 centre coordinate.  Returns the
-// coordinate's centre value after the update.
+// Canonicalise one coordinate's limbs (lv: their values, lp: where they
+// live) and, for a non-empty cluster (cnt > 0) when write_centers, write its
+// exact mean as the correctly rounded f32 centre coordinate to *cptr.
+// Returns the coordinate's centre value after the update (oldc: before it).
 template <int L>
-__device__ __forceinline__ float mean_elem(unsigned long long* __restrict__ limbs, int64_t e, int d, int e_lo,
-                                           const int32_t* __restrict__ counts, float* __restrict__ centers,
-                                           int write_centers) {
-  unsigned long long* lp = limbs + e * L;
+__device__ __forceinline__ float mean_of(unsigned long long* __restrict__ lp, const unsigned long long* lv, int cnt,
+                                         int e_lo, float* __restrict__ cptr, float oldc, int write_centers) {
   unsigned __int128 tot = 0;
 #pragma unroll
-  for (int l = 0; l < L; l++) tot += (unsigned __int128)lp[l] << (32 * l);
+  for (int l = 0; l < L; l++) tot += (unsigned __int128)lv[l] << (32 * l);
   if constexpr (L < 4) tot &= (((unsigned __int128)1) << (32 * (L % 4))) - 1;
 #pragma unroll
   for (int l = 0; l < L; l++) lp[l] = (unsigned long long)((tot >> (32 * l)) & 0xffffffffu);
-  const int j = (int)(e / d);
-  const int cnt = counts[j];
-  if (cnt <= 0 || !write_centers) return centers[e];
+  if (cnt <= 0 || !write_centers) return oldc;
   const bool neg = (tot >> (32 * L - 1)) & 1;
   unsigned __int128 mag = tot;
   if (neg) {
@@ -316,8 +313,20 @@ __device__ __forceinline__ float mean_elem(unsigned long long* __restrict__ limb
   }
   float v = mag == 0 ? 0.0f : rn_ratio_f32(mag, (unsigned long long)cnt, e_lo);
   v = neg ? -v : v;
-  centers[e] = v;
+  *cptr = v;
   return v;
+}
+
+// mean_of for coordinate e of the [k][d] sums.
+template <int L>
+__device__ __forceinline__ float mean_elem(unsigned long long* __restrict__ limbs, int64_t e, int d, int e_lo,
+                                           const int32_t* __restrict__ counts, float* __restrict__ centers,
+                                           int write_centers) {
+  unsigned long long* lp = limbs + e * L;
+  unsigned long long lv[L];
+#pragma unroll
+  for (int l = 0; l < L; l++) lv[l] = lp[l];
+  return mean_of<L>(lp, lv, counts[(int)(e / d)], e_lo, centers + e, centers[e], write_centers);
 }
 
 // Hand the change count to the host and reset the per-pass counters.
@@ -360,13 +369,39 @@ __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __re
   if (cp.zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *cp.zero_word = 0;
   const int j = blockIdx.x;
   float acc = 0.0f;
-  for (int c = threadIdx.x; c < cp.dp; c += blockDim.x) {
-    const float v = (j < k && c < d) ? mean_elem<L>(limbs, (int64_t)j * d + c, d, e_lo, counts, centers, 1) : 0.0f;
+  // the limbs, old centre values and count this thread needs, loaded before
+  // any is used (one memory round trip for rows of up to kPer * 256 columns)
+  constexpr int kPer = 4;
+  unsigned long long lv[kPer][L];
+  float oldc[kPer];
+  const int cnt = j < k ? counts[j] : 0;
+#pragma unroll
+  for (int u = 0; u < kPer; u++) {
+    const int c = threadIdx.x + u * 256;
+    const bool v = j < k && c < d;
+    const int64_t e = (int64_t)j * d + c;
+#pragma unroll
+    for (int l = 0; l < L; l++) lv[u][l] = v ? limbs[e * L + l] : 0ull;
+    oldc[u] = v ? centers[e] : 0.0f;
+  }
+  auto emit = [&](int c, float v) {
     const float t = __fmul_rn(cp.scale, v);
     const __nv_bfloat16 h = __float2bfloat16_rn(t);
     cp.hi[(int64_t)j * cp.dp + c] = h;
     if (SPLIT) cp.lo[(int64_t)j * cp.dp + c] = __float2bfloat16_rn(t - __bfloat162float(h));
     acc = fmaf(v, v, acc);
+  };
+#pragma unroll
+  for (int u = 0; u < kPer; u++) {
+    const int c = threadIdx.x + u * 256;
+    if (c >= cp.dp) break;
+    const int64_t e = (int64_t)j * d + c;
+    const float v = (j < k && c < d) ? mean_of<L>(limbs + e * L, lv[u], cnt, e_lo, centers + e, oldc[u], 1) : 0.0f;
+    emit(c, v);
+  }
+  for (int c = threadIdx.x + kPer * 256; c < cp.dp; c += blockDim.x) {
+    const float v = (j < k && c < d) ? mean_elem<L>(limbs, (int64_t)j * d + c, d, e_lo, counts, centers, 1) : 0.0f;
+    emit(c, v);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);

@@ -24,40 +24,63 @@ struct SumsCommit {
 // One full warp (lane = its lane index): bucket offsets and the chunk table
 // (in-chunks of cluster 0..k-1, then out-chunks), member counts, and
 // chunk_info[c] = cluster of chunk c (bit 31: an out-chunk), from the
-// complete in/out histograms.  Warp-shuffle scans over 32-entry tiles.
+// complete in/out histograms.  Warp-shuffle scans over 32-entry tiles.  The
+// histograms and counts of the first kPlanPre tiles (k <= 128) are loaded
+// up front, so a small k costs one round trip to memory, not one per tile.
+constexpr int kPlanPre = 4;
 __device__ __forceinline__ void plan_body(int lane, int k, const int32_t* __restrict__ cin,
                                           const int32_t* __restrict__ cout, int32_t* __restrict__ off_in,
                                           int32_t* __restrict__ off_out, int32_t* __restrict__ chunk_off,
                                           int32_t* __restrict__ counts, int32_t* __restrict__ chunk_info) {
-  int32_t carry_c = 0;
-  for (int pass = 0; pass < 2; pass++) {
-    const int32_t* cnt = pass == 0 ? cin : cout;
-    int32_t* off = pass == 0 ? off_in : off_out;
-    int32_t carry_m = 0;
-    for (int t0 = 0; t0 < k; t0 += 32) {
-      const int j = t0 + lane;
-      const int32_t c = j < k ? cnt[j] : 0;
-      const int32_t nc = (c + kRows - 1) / kRows;
-      int32_t a = c, b = nc;
+  int32_t pin[kPlanPre], pout[kPlanPre], pcnt[kPlanPre];
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int32_t ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
-        if (lane >= o) {
-          a += ua;
-          b += ub;
-        }
+  for (int t = 0; t < kPlanPre; t++) {
+    const int j = 32 * t + lane;
+    const bool v = j < k;
+    pin[t] = v ? cin[j] : 0;
+    pout[t] = v ? cout[j] : 0;
+    pcnt[t] = v ? counts[j] : 0;
+  }
+  int32_t carry_c = 0;
+  // one 32-cluster tile of one pass, given this lane's histogram entry c
+  auto tile = [&](int pass, int t0, int32_t c, int32_t& carry_m) {
+    const int j = t0 + lane;
+    int32_t* off = pass == 0 ? off_in : off_out;
+    const int32_t nc = (c + kRows - 1) / kRows;
+    int32_t a = c, b = nc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+      if (lane >= o) {
+        a += ua;
+        b += ub;
       }
-      if (j < k) {
-        off[j] = carry_m + a - c;
-        const int32_t c0 = carry_c + b - nc;
-        chunk_off[pass * k + j] = c0;
-        for (int q = 0; q < nc; q++) chunk_info[c0 + q] = j | (pass << 31);
-        if (pass == 0) counts[j] += cin[j] - cout[j];
-      }
-      carry_m += __shfl_sync(0xffffffffu, a, 31);
-      carry_c += __shfl_sync(0xffffffffu, b, 31);
+    }
+    if (j < k) {
+      off[j] = carry_m + a - c;
+      const int32_t c0 = carry_c + b - nc;
+      chunk_off[pass * k + j] = c0;
+      for (int q = 0; q < nc; q++) chunk_info[c0 + q] = j | (pass << 31);
+    }
+    carry_m += __shfl_sync(0xffffffffu, a, 31);
+    carry_c += __shfl_sync(0xffffffffu, b, 31);
+  };
+  for (int pass = 0; pass < 2; pass++) {
+    int32_t carry_m = 0;
+#pragma unroll
+    for (int t = 0; t < kPlanPre; t++)
+      if (32 * t < k) tile(pass, 32 * t, pass == 0 ? pin[t] : pout[t], carry_m);
+    for (int t0 = 32 * kPlanPre; t0 < k; t0 += 32) {
+      const int j = t0 + lane;
+      tile(pass, t0, j < k ? (pass == 0 ? cin[j] : cout[j]) : 0, carry_m);
     }
   }
+#pragma unroll
+  for (int t = 0; t < kPlanPre; t++) {
+    const int j = 32 * t + lane;
+    if (j < k) counts[j] = pcnt[t] + pin[t] - pout[t];
+  }
+  for (int j = 32 * kPlanPre + lane; j < k; j += 32) counts[j] += cin[j] - cout[j];
   if (lane == 0) chunk_off[2 * k] = carry_c;
 }
 

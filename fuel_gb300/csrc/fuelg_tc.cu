@@ -251,7 +251,6 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     int kc = 0;
     for (int st = 0; st < NS && t < ntiles; st++) {
       uint8_t* sA = base + (size_t)st * stage_bytes;
-      uint8_t* sB = sA + a_bytes;
       mbar_expect_tx(&full[st], stage_bytes);
       const int ax = a.a_tiled ? 0 : kc * BK;
       const int ay = a.a_tiled ? (int)((t * a.kc + kc) * BM) : (int)(t * BM);
@@ -622,28 +621,49 @@ __global__ void prep_scaled_kernel(const float* __restrict__ X, int64_t rows, in
                                    float* __restrict__ nrm, int* __restrict__ neg_flag, int* __restrict__ fail) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   bool anyneg = false, bad = false;
+  const bool vec = (d & 3) == 0 && (reinterpret_cast<uintptr_t>(X) & 15) == 0;
+  // I = rint(x * fl(1/s)): for x within 2^-21 relative of I s with |I| <= 256
+  // the product is within 2^-12 of I, so this is rint(x / s); any other x
+  // fails the check below whichever integer it rounds to.
+  const float inv_s = __frcp_rn(s);
   for (int64_t r = (int64_t)blockIdx.x * nw + warp; r < rows; r += (int64_t)gridDim.x * nw) {
     const bool v = r < valid_rows;
     const float* xr = X + r * d;
     float acc = 0.0f;
-    for (int c0 = 4 * lane; c0 < dp; c0 += 128) {
-      float x4[4];
+    // up to 8 chunks of 4 values per lane are loaded before any is used
+    for (int cb = 4 * lane; cb < dp; cb += 128 * 8) {
+      float x8[8][4];
 #pragma unroll
-      for (int t = 0; t < 4; t++) x4[t] = (v && c0 + t < d) ? __ldg(xr + c0 + t) : 0.0f;
-      float i4[4];
+      for (int u = 0; u < 8; u++) {
+        const int c0 = cb + 128 * u;
+        if (v && vec && c0 + 3 < d) {
+          const float4 t4 = __ldg(reinterpret_cast<const float4*>(xr + c0));
+          x8[u][0] = t4.x, x8[u][1] = t4.y, x8[u][2] = t4.z, x8[u][3] = t4.w;
+        } else {
 #pragma unroll
-      for (int t = 0; t < 4; t++) {
-        i4[t] = rintf(__fdiv_rn(x4[t], s));
-        bad |= !(fabsf(i4[t]) <= 256.0f) || !(fabsf(fmaf(-i4[t], s, x4[t])) <= 4.76837158203125e-07f * fabsf(x4[t]));
-        acc = fmaf(x4[t], x4[t], acc);
-        anyneg |= x4[t] < 0.0f;
+          for (int t = 0; t < 4; t++) x8[u][t] = (v && c0 + t < d) ? __ldg(xr + c0 + t) : 0.0f;
+        }
       }
-      __nv_bfloat162 h01 = __floats2bfloat162_rn(i4[0], i4[1]);
-      __nv_bfloat162 h23 = __floats2bfloat162_rn(i4[2], i4[3]);
-      uint2 pk;
-      pk.x = *reinterpret_cast<uint32_t*>(&h01);
-      pk.y = *reinterpret_cast<uint32_t*>(&h23);
-      *reinterpret_cast<uint2*>(q + prep_offset(r, c0, dp, tile_kc)) = pk;
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        const int c0 = cb + 128 * u;
+        if (c0 >= dp) break;
+        const float* x4 = x8[u];
+        float i4[4];
+#pragma unroll
+        for (int t = 0; t < 4; t++) {
+          i4[t] = rintf(__fmul_rn(x4[t], inv_s));
+          bad |= !(fabsf(i4[t]) <= 256.0f) || !(fabsf(fmaf(-i4[t], s, x4[t])) <= 4.76837158203125e-07f * fabsf(x4[t]));
+          acc = fmaf(x4[t], x4[t], acc);
+          anyneg |= x4[t] < 0.0f;
+        }
+        __nv_bfloat162 h01 = __floats2bfloat162_rn(i4[0], i4[1]);
+        __nv_bfloat162 h23 = __floats2bfloat162_rn(i4[2], i4[3]);
+        uint2 pk;
+        pk.x = *reinterpret_cast<uint32_t*>(&h01);
+        pk.y = *reinterpret_cast<uint32_t*>(&h23);
+        *reinterpret_cast<uint2*>(q + prep_offset(r, c0, dp, tile_kc)) = pk;
+      }
     }
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
@@ -701,6 +721,8 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
   const bool v4 = (d & 3) == 0;
   for (int64_t u = gw; u < cnt; u += nwarps) {
     const int64_t i = ulist[u];
+    // the committed label, read now: off the path after the distances
+    const int32_t old = (commit && lane == 0) ? labels[i] : 0;
     const float* x = X + i * d;
     __syncwarp();
     if (v4)
@@ -755,7 +777,6 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
         lab_new[i] = lb;
       } else {
         // fused pass: commit this point's label (few points: global atomics)
-        const int32_t old = labels[i];
         if (lb != old) {
           labels[i] = lb;
           const int pos = atomicAdd(sc.nchg, 1);
