@@ -46,7 +46,7 @@ int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_
                     bool write_centers, float* centers, int32_t* changed, int* dev_status, cudaStream_t stream,
                     const CentrePrep* cp);
 int exact_sums_update(ExactSums* s, const float* X, bool write_centers, float* centers, int32_t* changed,
-                      const CentrePrep* cp, cudaStream_t stream);
+                      const CentrePrep* cp, cudaStream_t stream, bool plan_in_scatter);
 void exact_sums_commit_view(ExactSums* s, SumsCommit* v);
 int lloyd_tc_rescored_total(TcLloydState* st, cudaStream_t stream, int64_t* out);
 int lloyd_tc_pass_fused(const LloydParams& p, TcLloydState* st, const float* centers, int32_t* labels,
@@ -412,9 +412,9 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   // one pass: assign, commit labels, update sums, and (if another pass
   // follows) the centres it will use
   // Tensor-core tier with exact sums: every pass after the first is one
-  // fused screen launch (labels committed, undecided points re-scored, buckets
-  // planned in place), then the sum update, whose centre kernel also writes the
-  // next pass's BF16 centre copies.
+  // fused screen launch (labels committed) and its re-score of the undecided
+  // points, then the sum update -- its scatter kernel plans the buckets, its
+  // centre kernel also writes the next pass's BF16 centre copies.
   CentrePrep cprep;
   if (tc) cprep = lloyd_tc_centre_prep(tc);
   SumsCommit scv{};
@@ -425,7 +425,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
     else FUELG_TRY(assign(first));
     if (p.tol > 0 && write_centers)
       FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
-    if (fused) return exact_sums_update(es, p.X, write_centers, C, changed.as<int32_t>(), &cprep, stream);
+    if (fused) return exact_sums_update(es, p.X, write_centers, C, changed.as<int32_t>(), &cprep, stream, true);
     if (exact)
       return exact_sums_step(es, p.X, lab_new.as<int32_t>(), labels, first, write_centers, C, changed.as<int32_t>(),
                              dev_status, stream, tc ? &cprep : nullptr);

@@ -194,14 +194,32 @@ __device__ __forceinline__ void scatter_body(int bid, int nblk, int32_t* c_in, i
   }
 }
 
+// plan != 0 (the fused pass, k <= kPlanMaxK): the histograms are complete
+// but unplanned -- every block derives the bucket offsets it needs in shared
+// memory, and block 0's second warp writes the full plan (offsets, chunk
+// table, counts) for the accumulation kernel.
 __global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const int32_t* __restrict__ chg_old,
                                       const int32_t* __restrict__ chg_new, const int32_t* __restrict__ nchg, int k,
-                                      const int32_t* __restrict__ off_in, const int32_t* __restrict__ off_out,
+                                      int32_t* __restrict__ off_in, int32_t* __restrict__ off_out,
                                       int32_t* __restrict__ cur_in, int32_t* __restrict__ cur_out,
-                                      int32_t* __restrict__ bucket_in, int32_t* __restrict__ bucket_out) {
+                                      int32_t* __restrict__ bucket_in, int32_t* __restrict__ bucket_out, int plan,
+                                      const int32_t* __restrict__ cin, const int32_t* __restrict__ cout,
+                                      int32_t* __restrict__ chunk_off, int32_t* __restrict__ counts,
+                                      int32_t* __restrict__ chunk_info) {
   __shared__ int32_t c_in[kSmemK], c_out[kSmemK];
+  __shared__ int32_t s_off[2 * kPlanMaxK];
   griddep_wait();
-  scatter_body(blockIdx.x, gridDim.x, c_in, c_out, chg_i, chg_old, chg_new, nchg, k, off_in, off_out, cur_in, cur_out,
+  const int32_t* oin = off_in;
+  const int32_t* oout = off_out;
+  if (plan) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) plan_offsets(lane, k, cin, cout, s_off, s_off + kPlanMaxK);
+    if (warp == 1 && blockIdx.x == 0) plan_body(lane, k, cin, cout, off_in, off_out, chunk_off, counts, chunk_info);
+    __syncthreads();
+    oin = s_off;
+    oout = s_off + kPlanMaxK;
+  }
+  scatter_body(blockIdx.x, gridDim.x, c_in, c_out, chg_i, chg_old, chg_new, nchg, k, oin, oout, cur_in, cur_out,
                bucket_in, bucket_out);
 }
 
@@ -496,17 +514,21 @@ void exact_sums_commit_view(ExactSums* s, SumsCommit* v) {
   v->chunk_off = s->chunk_off.as<int32_t>();
   v->counts = s->counts.as<int32_t>();
   v->chunk_info = s->chunk_info.as<int32_t>();
-  v->done = s->done.as<unsigned>();
   v->k = k;
 }
 
-// Update after a committed pass (labels, change list, histograms and plan in
-// place): scatter the changed points into per-cluster buckets, add their
-// exact fixed-point rows into the sums, and write the new centres -- with cp,
-// also the BF16 centre copies the next tensor-core screen reads.  *changed
-// (device) receives the number of changed labels.
+// Update after a committed pass (labels, change list and histograms in
+// place; the bucket plan too unless plan_in_scatter): scatter the changed
+// points into per-cluster buckets, add their exact fixed-point rows into the
+// sums, and write the new centres -- with cp, also the BF16 centre copies the
+// next tensor-core screen reads.  *changed (device) receives the number of
+// changed labels.  plan_in_scatter needs k <= kPlanMaxK.
 int exact_sums_update(ExactSums* s, const float* X, bool write_centers, float* centers, int32_t* changed,
-                      const CentrePrep* cp, cudaStream_t stream) {
+                      const CentrePrep* cp, cudaStream_t stream, bool plan_in_scatter) {
+  if (plan_in_scatter && s->k > kPlanMaxK) {
+    set_error("the scatter-side bucket plan needs k <= %d", kPlanMaxK);
+    return ST_EINVAL;
+  }
   const int k = s->k, d = s->d;
   int32_t* cin = s->cin.as<int32_t>();
   int32_t* cur_in = cin + 2 * k;
@@ -516,9 +538,10 @@ int exact_sums_update(ExactSums* s, const float* X, bool write_centers, float* c
   const int ty = (d + 255) / 256;
   FUELG_TRY(launch_pdl(bucket_scatter_kernel, dim3(2 * 152), dim3(256), 0, stream,
                        (const int32_t*)s->chg_i.as<int32_t>(), (const int32_t*)s->chg_old.as<int32_t>(),
-                       (const int32_t*)s->chg_new.as<int32_t>(), (const int32_t*)s->nchg.as<int32_t>(), k,
-                       (const int32_t*)off_in, (const int32_t*)off_out, cur_in, cur_out, s->bucket_in.as<int32_t>(),
-                       s->bucket_out.as<int32_t>()));
+                       (const int32_t*)s->chg_new.as<int32_t>(), (const int32_t*)s->nchg.as<int32_t>(), k, off_in,
+                       off_out, cur_in, cur_out, s->bucket_in.as<int32_t>(), s->bucket_out.as<int32_t>(),
+                       plan_in_scatter ? 1 : 0, (const int32_t*)cin, (const int32_t*)(cin + k),
+                       s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(), s->chunk_info.as<int32_t>()));
   const dim3 g((unsigned)std::min<int64_t>(s->max_chunks * ty, 8 * 152));
   const int64_t kd = (int64_t)k * d;
   const unsigned mg = (unsigned)std::min<int64_t>((kd + 255) / 256, 8 * 152);
@@ -570,7 +593,7 @@ int exact_sums_step(ExactSums* s, const float* X, const int32_t* lab_new, int32_
                        s->chg_old.as<int32_t>(), s->chg_new.as<int32_t>(), s->nchg.as<int32_t>(), cin, cout,
                        s->done.as<unsigned>(), off_in, off_out, s->chunk_off.as<int32_t>(), s->counts.as<int32_t>(),
                        s->chunk_info.as<int32_t>()));
-  return exact_sums_update(s, X, write_centers, centers, changed, cp, stream);
+  return exact_sums_update(s, X, write_centers, centers, changed, cp, stream, false);
 }
 
 }  // namespace fuelg

@@ -11,13 +11,13 @@ constexpr int kRows = 32;     // rows per accumulation chunk
 constexpr int kSmemK = 4096;  // clusters whose histograms fit shared memory
 
 // Device state a fused assignment pass writes instead of the commit kernel:
-// the change list (point, old, new label) with its length, the per-cluster
-// in/out histograms, and -- from the last CTA, by ticket -- the bucket plan.
+// the change list (point, old, new label) with its length and the
+// per-cluster in/out histograms; the bucket plan is made by the scatter
+// kernel that follows.
 struct SumsCommit {
   int32_t *chg_i, *chg_old, *chg_new, *nchg;
   int32_t *cin, *cout;  // histograms (zeroed by the previous centre update)
   int32_t *off_in, *off_out, *chunk_off, *counts, *chunk_info;
-  unsigned* done;  // ticket, reset by the last CTA
   int k;
 };
 
@@ -82,6 +82,45 @@ __device__ __forceinline__ void plan_body(int lane, int k, const int32_t* __rest
   }
   for (int j = 32 * kPlanPre + lane; j < k; j += 32) counts[j] += cin[j] - cout[j];
   if (lane == 0) chunk_off[2 * k] = carry_c;
+}
+
+// Clusters a scatter kernel plans for itself (the fused tensor-core pass
+// has k <= 256).
+constexpr int kPlanMaxK = 256;
+
+// One full warp: the bucket offsets alone (exclusive prefix sums of the in
+// and out histograms) into oin / oout -- shared memory of the calling block.
+// All histogram entries are loaded before the scans (one round trip).
+__device__ __forceinline__ void plan_offsets(int lane, int k, const int32_t* __restrict__ cin,
+                                             const int32_t* __restrict__ cout, int32_t* oin, int32_t* oout) {
+  int32_t vi[kPlanMaxK / 32], vo[kPlanMaxK / 32];
+#pragma unroll
+  for (int t = 0; t < kPlanMaxK / 32; t++) {
+    const int j = 32 * t + lane;
+    vi[t] = j < k ? cin[j] : 0;
+    vo[t] = j < k ? cout[j] : 0;
+  }
+  int32_t ci = 0, co = 0;
+#pragma unroll
+  for (int t = 0; t < kPlanMaxK / 32; t++) {
+    if (32 * t >= k) break;
+    int32_t a = vi[t], b = vo[t];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int32_t ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+      if (lane >= o) {
+        a += ua;
+        b += ub;
+      }
+    }
+    const int j = 32 * t + lane;
+    if (j < k) {
+      oin[j] = ci + a - vi[t];
+      oout[j] = co + b - vo[t];
+    }
+    ci += __shfl_sync(0xffffffffu, a, 31);
+    co += __shfl_sync(0xffffffffu, b, 31);
+  }
 }
 
 }  // namespace fuelg

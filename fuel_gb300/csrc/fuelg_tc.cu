@@ -704,23 +704,28 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
                                                            const int32_t* __restrict__ ucount,
                                                            int32_t* __restrict__ lab_new,
                                                            unsigned long long* __restrict__ tally,
-                                                           int32_t* __restrict__ labels, SumsCommit sc, int commit) {
+                                                           int32_t* __restrict__ labels, SumsCommit sc, int commit,
+                                                           int64_t cap) {
   constexpr bool LANE8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
   constexpr int G = LANE8 ? 8 : 32;
   constexpr int PER = 32 / G;
   extern __shared__ __align__(16) float rs_smem[];
-  __shared__ unsigned s_last;
   griddep_wait();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   float* xs = rs_smem + (size_t)wib * (PER + 1) * ds;
   float* cs = xs + ds;
   const int64_t gw = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  // the warp's first list entry and candidate word are read with the count
+  // (cap: entries the list and mask buffers hold)
+  const int64_t g0 = gw < cap ? gw : 0;
+  const int64_t i_next = ulist[g0];
+  const uint64_t m_next = umask[g0 * mw];
   const int cnt = *ucount;
   if (blockIdx.x == 0 && threadIdx.x == 0) *tally += (unsigned long long)cnt;
   const bool v4 = (d & 3) == 0;
   for (int64_t u = gw; u < cnt; u += nwarps) {
-    const int64_t i = ulist[u];
+    const int64_t i = u == gw ? i_next : ulist[u];
     // the committed label, read now: off the path after the distances
     const int32_t old = (commit && lane == 0) ? labels[i] : 0;
     const float* x = X + i * d;
@@ -731,7 +736,7 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
       for (int e = lane; e < d; e += 32) xs[e] = __ldg(x + e);
     uint64_t best = KEY_NONE;
     int w = 0;
-    uint64_t m = umask[u * mw];
+    uint64_t m = u == gw ? m_next : umask[u * mw];
     const int slot = lane / G;
     for (;;) {
       int got = 0, j = 0;
@@ -788,18 +793,6 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
         }
       }
     }
-  }
-  if (!commit) return;
-  // the last block to finish (a ticket after a fence) plans the buckets from
-  // the complete histograms
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) s_last = atomicAdd(sc.done, 1u) == gridDim.x - 1 ? 1u : 0u;
-  __syncthreads();
-  if (s_last && threadIdx.x < 32) {
-    __threadfence();
-    plan_body(lane, sc.k, sc.cin, sc.cout, sc.off_in, sc.off_out, sc.chunk_off, sc.counts, sc.chunk_info);
-    if (lane == 0) *sc.done = 0;
   }
 }
 
@@ -1048,13 +1041,15 @@ int tc_pass(const LloydParams& p, TcLloydState* st, const float* centers, bool f
         FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         FUELG_TRY(launch_pdl(kfn, dim3(g2), dim3(128), sm, stream, p.X, centers, p.d, ds, st->mw,
                              (const int32_t*)a.ulist, (const uint64_t*)a.umask, (const int32_t*)a.ucount, a.lab_new,
-                             st->rescored_total.as<unsigned long long>(), labels, a.sc, fused ? 1 : 0));
+                             st->rescored_total.as<unsigned long long>(), labels, a.sc, fused ? 1 : 0,
+                             (int64_t)p.n));
       } else {
         auto kfn = rescore_smem_kernel<KIND_SQDIST, ORDER_ARM>;
         FUELG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
         FUELG_TRY(launch_pdl(kfn, dim3(g2), dim3(128), sm, stream, p.X, centers, p.d, ds, st->mw,
                              (const int32_t*)a.ulist, (const uint64_t*)a.umask, (const int32_t*)a.ucount, a.lab_new,
-                             st->rescored_total.as<unsigned long long>(), labels, a.sc, fused ? 1 : 0));
+                             st->rescored_total.as<unsigned long long>(), labels, a.sc, fused ? 1 : 0,
+                             (int64_t)p.n));
       }
     } else if (fused) {
       set_error("the fused Lloyd pass needs d <= 1024");
