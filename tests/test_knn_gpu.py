@@ -323,3 +323,40 @@ def test_knn_tc_fp16_out_of_range_uses_plain_tier(gpu, oracle):
     g2 = ix2.knn(Qbig, 5, exclude_self=False)
     assert ix2.last_stats["precision_used"] == 0
     assert_same(g2, oracle.knn(Q, Qbig, 5, threads=threads()))
+
+
+# ---------------------------------------------------------------------------
+# Work decomposition of the tensor-core scan: whole waves of query blocks run
+# one CTA per block; a batch of less than a wave cuts each block's index scan
+# into equal tile ranges whose kept lists are merged.  Results must not depend
+# on the cut.
+# ---------------------------------------------------------------------------
+def test_knn_tc_multiwave_with_split_tail(gpu, oracle):
+    """40,000 queries = 313 blocks: one whole wave (304 blocks) plus a 9-block
+    tail whose 32-tile scans are cut in two and merged."""
+    rng = np.random.default_rng(41)
+    X = rng.normal(size=(4096, 32)).astype(np.float32)
+    Q = rng.normal(size=(40_000, 32)).astype(np.float32)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision="bf16")
+    g = ix.knn(Q, 10, exclude_self=False)
+    assert ix.last_stats["precision_used"] == 1
+    assert_same(g, oracle.knn(X, Q, 10, threads=threads()))
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp16", "split_bf16"])
+def test_knn_tc_quanta_invariance(gpu, oracle, monkeypatch, precision):
+    """Forcing 1, 2, 5, 9 or 37 tile ranges per query block gives the same
+    keys as the default cut and as the oracle (one piece per block, pieces
+    merged across CTAs, a CTA holding pieces of several blocks)."""
+    rng = np.random.default_rng(43)
+    X = rng.normal(size=(20_000, 64)).astype(np.float32)
+    Q = rng.normal(size=(1000, 64)).astype(np.float32)
+    ix = SearchIndex(X, distance="sqeuclidean", tree="linear", precision=precision)
+    want = {k: oracle.knn(X, Q, k, threads=threads()) for k in (1, 50)}
+    for k in (1, 50):
+        assert_same(ix.knn(Q, k, exclude_self=False), want[k])
+    for s in ("1", "2", "5", "9", "37"):
+        monkeypatch.setenv("FUELG_KNN_QUANTA", s)
+        for k in (1, 50):
+            assert_same(ix.knn(Q, k, exclude_self=False), want[k])
+    monkeypatch.delenv("FUELG_KNN_QUANTA")

@@ -252,3 +252,45 @@ def test_sharded_lloyd_with_engine_assign(oracle, gpu):
     np.testing.assert_array_equal(lab, rl)
     assert it == rit
     assert abs(inert - rinert) <= 1e-9 * abs(rinert)
+
+
+@pytest.mark.gpu
+def test_pinned_host_inputs_match_device_inputs(gpu):
+    """fuelg_kmeans_lloyd through the C ABI: pinned host inputs (aligned, and
+    4 bytes off a 16-byte boundary) give the same centres, labels and inertia
+    bits as device-resident inputs, and report their staged bytes."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    from fuel_gb300 import _lib
+    lib = _lib.load()
+    n, d, k, iters = 6000, 64, 16, 12
+    X, init = workloads.lloyd_sparse(n, d, k)
+    assert X.nbytes >= 1 << 20
+
+    def run(xp, cp):
+        oc = np.empty((k, d), np.float32)
+        ol = np.empty(n, np.int64)
+        it, inert, st = ctypes.c_int32(), ctypes.c_double(), _lib.Stats()
+        _lib.check(lib.fuelg_kmeans_lloyd(xp, n, d, k, cp, iters, 0.0, _lib.PRECISION["split_bf16"],
+                                          _lib.ORDER["arm"], _lib.LLOYD_FIXED_ITERS, _lib.ptr(oc), _lib.ptr(ol),
+                                          ctypes.byref(it), ctypes.byref(inert), ctypes.byref(st)))
+        return oc, ol, inert.value, st.h2d_bytes
+
+    Xd = torch.from_numpy(X).cuda()
+    Cd = torch.from_numpy(init).cuda()
+    ref = run(_lib.ptr(Xd), _lib.ptr(Cd))
+    assert ref[3] == 0
+    # aligned pinned buffers
+    Xh = torch.empty((n, d), dtype=torch.float32, pin_memory=True)
+    Xh.copy_(torch.from_numpy(X))
+    Ch = torch.empty((k, d), dtype=torch.float32, pin_memory=True)
+    Ch.copy_(torch.from_numpy(init))
+    # a pinned buffer 4 bytes off a 16-byte boundary
+    flat = torch.empty(n * d + 1, dtype=torch.float32, pin_memory=True)
+    flat[1:].copy_(torch.from_numpy(X.ravel()))
+    for xp in (_lib.ptr(Xh), ctypes.c_void_p(flat.data_ptr() + 4)):
+        got = run(xp, _lib.ptr(Ch))
+        assert got[3] == X.nbytes + init.nbytes
+        np.testing.assert_array_equal(got[0].view(np.uint32), ref[0].view(np.uint32))
+        np.testing.assert_array_equal(got[1], ref[1])
+        assert got[2] == ref[2]
