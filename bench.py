@@ -318,7 +318,7 @@ def run_ours(args):
 
 
 def pairwise_rate(lib, _lib, torch, args):
-    """pairwise_distances on the configs[0] points (n=20,000, d=16): condensed and
+    """pairwise_distances on the kNN self-join points (n=20,000, d=16): condensed and
     square forms, device-resident output; roofline = bytes written / kernel time."""
     from fuel_gb300 import workloads
     X = workloads.knn_plain()
