@@ -264,13 +264,18 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     }
   }
   griddep_wait();
-  for (int j = threadIdx.x; j < a.kp; j += blockDim.x) {
-    snc[j] = a.nc[j];
-    scn[j] = a.cn[j];
-    h_in[j] = 0;
-    h_out[j] = 0;
+  // The centre norms and the per-CTA histograms belong to the epilogue: its
+  // warps stage them behind their own barrier, so the producer's first
+  // centre chunk goes out without waiting for these loads.
+  if (warp >= 2) {
+    for (int j = threadIdx.x - 64; j < a.kp; j += BM) {
+      snc[j] = a.nc[j];
+      scn[j] = a.cn[j];
+      h_in[j] = 0;
+      h_out[j] = 0;
+    }
+    named_bar_sync(1, BM);
   }
-  __syncthreads();
 
   if (warp == 0) {
     if (lane == 0) {
