@@ -64,6 +64,7 @@ SIGNATURES = {
     "fuelg_index_info": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
                                         ctypes.POINTER(_i32)]),
     "fuelg_knn": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
+    "fuelg_knn_ties": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _i32, _pp, ctypes.POINTER(Stats)]),
     "fuelg_range": (ctypes.c_int, [_vp, _vp, _i64, _dbl, _i32, _pp, ctypes.POINTER(Stats)]),
     "fuelg_range_size": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "fuelg_range_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp]),

@@ -22,6 +22,13 @@ _LLOYD_FAMILY = {
     "s_hamerly", "simp_hamerly", "simplified_hamerly", "exponion", "shallot",
 }
 _OTHER = {"hartigan_wong", "hartigan_wong_quick", "macqueen", "kmedians"}
+# variants whose reference result carries no inertia (KMeansResult::without_inertia:
+# src/cluster/kmeans/elkan.rs:267, selkan.rs:223, hamerly.rs:270, shamerly.rs:234,
+# exponion.rs:230, shallot.rs:297)
+_WITHOUT_INERTIA = {
+    "elkan", "s_elkan", "simp_elkan", "simplified_elkan", "hamerly", "s_hamerly", "simp_hamerly",
+    "simplified_hamerly", "exponion", "shallot",
+}
 
 
 class KMeansResult:
@@ -76,7 +83,9 @@ def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, ini
     Returns ``KMeansResult(centers float32[k, d], labels int64[n], n_iter,
     inertia, inertia_bound=None)``.  ``n_iter`` counts the initial assignment
     as iteration 1 (src/cluster/kmeans/util.rs:40).  ``inertia`` is the FP64
-    sum of squared distances of the final pass.  ``fixed_iters=True`` runs
+    sum of squared distances of the final pass, or None for the bound-based
+    variants, whose reference results carry none (``stats["inertia_fp64"]``
+    has it for every variant).  ``fixed_iters=True`` runs
     exactly ``max_iter`` iterations (benchmark mode).
     """
     v = str(variant).lower()
@@ -111,8 +120,10 @@ def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, ini
         _lib.ptr(X), n, d, k, _lib.ptr(C0), max(1, max_iter), float(tol), _lib.PRECISION[precision],
         _lib.ORDER[order], _lib.LLOYD_FIXED_ITERS if fixed_iters else 0, _lib.ptr(centers), _lib.ptr(labels),
         ctypes.byref(iters), ctypes.byref(inertia), ctypes.byref(st)))
-    res = KMeansResult(centers, labels, int(iters.value), float(inertia.value), None)
+    res = KMeansResult(centers, labels, int(iters.value),
+                       None if v in _WITHOUT_INERTIA else float(inertia.value), None)
     res.stats = st.as_dict()
+    res.stats["inertia_fp64"] = float(inertia.value)
     return res
 
 

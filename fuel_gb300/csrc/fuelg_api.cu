@@ -356,14 +356,56 @@ int fuelg_index_info(const fuelg_index* ix, int64_t* n, int32_t* d, int32_t* met
   return ST_OK;
 }
 
-int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32_t exclude_mode, int32_t precision,
-              int64_t* out_idx, float* out_dist, fuelg_stats* stats) {
+}  // extern "C"
+
+namespace {
+
+// Top-kk (distance, index) keys of m query rows against the index, by the
+// requested precision tier (the plain FP32 scan where the tensor-core tier does
+// not serve the shape or the value range).  *used: the tier that ran.
+int index_topk(fuelg_index* ix, const float* Q, int64_t m, int kk, int precision, uint64_t* keys, int* dstat,
+               cudaStream_t s, int* used, int64_t* rescored) {
+  ExactScanParams p;
+  p.A = Q;
+  p.m = m;
+  p.B = ix->X;
+  p.n = ix->n;
+  p.d = ix->d;
+  p.kind = KIND_KNN;
+  p.order = ix->order;
+  p.metric = ix->metric;
+  p.kk = kk;
+  *used = FUELG_PREC_FP32;
+  *rescored = 0;
+  const int tier = precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT : precision == FUELG_PREC_F16 ? TC_F16 : TC_BF16;
+  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk, tier) && ix->n > 0) {
+    int exact = 0;
+    if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
+    if (tier == TC_SPLIT) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, s));
+    int rc = tier == TC_F16 ? knn_tc_index_add_f16(ix->tc, ix->X, s) : ST_OK;
+    // values outside the FP16 range (index or queries): the plain tier answers
+    if (rc == ST_OK)
+      rc = knn_tc_topk(ix->tc, Q, m, ix->X, kk, ix->order, ix->metric, tier, keys, dstat, s, rescored, &exact);
+    if (rc != ST_OK && rc != ST_ENOTSUP) return rc;
+    if (rc == ST_OK) {
+      // integer data run the exact one-product screen whatever the split request
+      *used = tier == TC_F16 ? FUELG_PREC_F16 : (tier == TC_SPLIT && !exact) ? FUELG_PREC_SPLIT_BF16 : FUELG_PREC_BF16;
+      return ST_OK;
+    }
+    *rescored = 0;
+  }
+  return exact_topk(p, keys, dstat, s);
+}
+
+int check_knn_args(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32_t exclude_mode,
+                   int32_t precision) {
   if (!ix) {
     set_error("index is NULL");
     return ST_EINVAL;
   }
-  if (m < 0 || k < 0 || (m > 0 && !queries) || (m > 0 && k > 0 && (!out_idx || !out_dist))) {
-    set_error("invalid knn arguments m=%lld k=%d", (long long)m, k);
+  if (m < 0 || k < 0 || (m > 0 && !queries && m != ix->n)) {
+    set_error("invalid knn arguments m=%lld k=%d (queries may be NULL only for the index's own %lld rows)",
+              (long long)m, k, (long long)ix->n);
     return ST_EINVAL;
   }
   if (exclude_mode < FUELG_EXCLUDE_NONE || exclude_mode > FUELG_EXCLUDE_KPLUS1) {
@@ -378,6 +420,20 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
     set_error("k=%d exceeds the supported maximum of 4095", k);
     return ST_ENOTSUP;
   }
+  return ST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32_t exclude_mode, int32_t precision,
+              int64_t* out_idx, float* out_dist, fuelg_stats* stats) {
+  FUELG_TRY(check_knn_args(ix, queries, m, k, exclude_mode, precision));
+  if (m > 0 && k > 0 && (!out_idx || !out_dist)) {
+    set_error("invalid knn arguments: output buffers are NULL");
+    return ST_EINVAL;
+  }
   std::lock_guard<std::mutex> lk(ix->mu);
   FUELG_TRY(begin_call());
   cudaSetDevice(ix->device);
@@ -388,7 +444,8 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   CallMeter meter;
   Timer tm(s);
   InBuf q;
-  FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(float), s));
+  if (queries) FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(float), s));
+  const float* Q = queries ? static_cast<const float*>(q.dptr) : ix->X;
   OutBuf oi, od;
   FUELG_TRY(oi.init(out_idx, (size_t)m * k * sizeof(int64_t), s));
   FUELG_TRY(od.init(out_dist, (size_t)m * k * sizeof(float), s));
@@ -396,37 +453,9 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   FUELG_TRY(keys.alloc((size_t)m * kk * sizeof(uint64_t), s));
   FUELG_TRY(dstat.alloc(sizeof(int), s));
   FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
-  ExactScanParams p;
-  p.A = static_cast<const float*>(q.dptr);
-  p.m = m;
-  p.B = ix->X;
-  p.n = ix->n;
-  p.d = ix->d;
-  p.kind = KIND_KNN;
-  p.order = ix->order;
-  p.metric = ix->metric;
-  p.kk = kk;
   int used = FUELG_PREC_FP32;
   int64_t rescored = 0;
-  const int tier = precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT : precision == FUELG_PREC_F16 ? TC_F16 : TC_BF16;
-  bool tc_done = false;
-  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk, tier) && ix->n > 0) {
-    int exact = 0;
-    if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
-    if (tier == TC_SPLIT) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, s));
-    int rc = tier == TC_F16 ? knn_tc_index_add_f16(ix->tc, ix->X, s) : ST_OK;
-    // values outside the FP16 range (index or queries): the plain tier answers
-    if (rc == ST_OK)
-      rc = knn_tc_topk(ix->tc, p.A, m, ix->X, kk, ix->order, ix->metric, tier, keys.as<uint64_t>(),
-                       dstat.as<int>(), s, &rescored, &exact);
-    if (rc != ST_OK && rc != ST_ENOTSUP) return rc;
-    if (rc == ST_OK) {
-      tc_done = true;
-      // integer data run the exact one-product screen whatever the split request
-      used = tier == TC_F16 ? FUELG_PREC_F16 : (tier == TC_SPLIT && !exact) ? FUELG_PREC_SPLIT_BF16 : FUELG_PREC_BF16;
-    }
-  }
-  if (!tc_done) FUELG_TRY(exact_topk(p, keys.as<uint64_t>(), dstat.as<int>(), s));
+  FUELG_TRY(index_topk(ix, Q, m, kk, precision, keys.as<uint64_t>(), dstat.as<int>(), s, &used, &rescored));
   FUELG_TRY(finalize_knn(keys.as<uint64_t>(), m, kk, k, exclude_mode, static_cast<int64_t*>(oi.dptr),
                          static_cast<float*>(od.dptr), s));
   int64_t d2h = 0;
@@ -443,6 +472,84 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
     stats->rescored = rescored;
     meter.fill(stats);
   }
+  return ST_OK;
+}
+
+int fuelg_knn_ties(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32_t exclude_mode,
+                   int32_t precision, fuelg_range_result** out, fuelg_stats* stats) {
+  if (!out) {
+    set_error("out is NULL");
+    return ST_EINVAL;
+  }
+  *out = nullptr;
+  FUELG_TRY(check_knn_args(ix, queries, m, k, exclude_mode, precision));
+  std::lock_guard<std::mutex> lk(ix->mu);
+  FUELG_TRY(begin_call());
+  cudaSetDevice(ix->device);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaStream_t s = ix->stream;
+  fuelg_range_result* r = new fuelg_range_result();
+  r->m = m;
+  // linear-index rule searches k, the k+1 rule k+1; both drop self afterwards
+  const int kq = exclude_mode == FUELG_EXCLUDE_KPLUS1 ? k + 1 : k;
+  if (m == 0 || kq == 0 || ix->n == 0) {
+    int st = ST_OK;
+    if (cudaMalloc(&r->off, sizeof(int64_t) * (m + 1)) != cudaSuccess ||
+        cudaMemset(r->off, 0, sizeof(int64_t) * (m + 1)) != cudaSuccess) {
+      cudaGetLastError();
+      set_error("cannot allocate the result offsets");
+      st = ST_ENOMEM;
+    }
+    if (st != ST_OK) {
+      fuelg_range_free(r);
+      return st;
+    }
+    *out = r;
+    return ST_OK;
+  }
+  CallMeter meter;
+  Timer tm(s);
+  auto run = [&]() -> int {
+    InBuf q;
+    if (queries) FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(float), s));
+    const float* Q = queries ? static_cast<const float*>(q.dptr) : ix->X;
+    const int kk = ties_spare_kk(kq, ix->n);
+    Scratch keys, dstat;
+    FUELG_TRY(keys.alloc((size_t)m * kk * sizeof(uint64_t), s));
+    FUELG_TRY(dstat.alloc(sizeof(int), s));
+    FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
+    int used = FUELG_PREC_FP32;
+    int64_t rescored = 0, range_rows = 0;
+    FUELG_TRY(index_topk(ix, Q, m, kk, precision, keys.as<uint64_t>(), dstat.as<int>(), s, &used, &rescored));
+    ExactScanParams base;
+    base.A = Q;
+    base.m = m;
+    base.B = ix->X;
+    base.n = ix->n;
+    base.d = ix->d;
+    base.kind = KIND_KNN;
+    base.order = ix->order;
+    base.metric = ix->metric;
+    FUELG_TRY(knn_ties_lists(keys.as<uint64_t>(), m, kk, kq, exclude_mode != FUELG_EXCLUDE_NONE, base, &r->off,
+                             &r->idx, &r->dist, &r->total, &range_rows, dstat.as<int>(), s));
+    const double ms = tm.stop();
+    FUELG_TRY(read_dev_status(dstat.as<int>(), s));
+    if (stats) {
+      stats->device_ms = ms;
+      stats->h2d_bytes = q.h2d;
+      stats->distance_evals = m * ix->n + range_rows * ix->n;
+      stats->precision_used = used;
+      stats->rescored = rescored;
+      meter.fill(stats);
+    }
+    return ST_OK;
+  };
+  const int st = run();
+  if (st != ST_OK) {
+    fuelg_range_free(r);
+    return st;
+  }
+  *out = r;
   return ST_OK;
 }
 

@@ -208,8 +208,22 @@ int pairwise_launch(const float* X, int64_t n, int d, int metric, int order, int
                     cudaStream_t stream);
 
 // Range search, CSR output on the device.  Allocates *off/*idx/*dist with cudaMalloc.
+// radii (device, p.m entries, or nullptr): a radius per query row instead of `radius`.
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
-                float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream);
+                float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream, const float* radii = nullptr);
+
+// -------- tie-inclusive kNN lists (fuelg_ties.cu) ------------------------------
+// Keys kept per query for tie-inclusive lists of kq neighbours (kq plus spare ranks).
+int ties_spare_kk(int kq, int64_t n);
+// From sorted top-kk keys [m, kk] (device; kk from ties_spare_kk), the lists
+// {i : dist(q, i) <= D_kq} of every query row, sorted by (distance, index),
+// index r dropped from row r when drop_self; rows with more ties than spare
+// ranks are answered by an exact range scan of base (queries base.A, index
+// base.B).  CSR output allocated with cudaMalloc (freed by the caller, also on
+// error); *range_rows = rows that took the range scan.
+int knn_ties_lists(const uint64_t* keys, int64_t m, int kk, int kq, int drop_self, const ExactScanParams& base,
+                   int64_t** d_off, int64_t** d_idx, float** d_dist, int64_t* total, int64_t* range_rows,
+                   int* dev_status, cudaStream_t s);
 
 // -------- Lloyd (fuelg_lloyd.cu) -------------------------------------------
 struct LloydParams {

@@ -548,9 +548,9 @@ int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int6
 namespace {
 
 template <int KIND, int ORDER, bool FILL>
-__global__ void __launch_bounds__(kThreads) range_kernel(ScanArgs a, float radius, int exclude_self,
-                                                         int64_t* __restrict__ counts, const int64_t* __restrict__ offs,
-                                                         uint64_t* __restrict__ out) {
+__global__ void __launch_bounds__(kThreads) range_kernel(ScanArgs a, float radius, const float* __restrict__ radii,
+                                                         int exclude_self, int64_t* __restrict__ counts,
+                                                         const int64_t* __restrict__ offs, uint64_t* __restrict__ out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* qt = reinterpret_cast<float*>(smem_raw);
   float* xt = qt + a.qpb * a.qs;
@@ -568,6 +568,7 @@ __global__ void __launch_bounds__(kThreads) range_kernel(ScanArgs a, float radiu
   stage_rows(qt, a.qs, a.A, q0, (int)min((int64_t)a.qpb, a.m - q0), a.d, a.a_vec4);
   int64_t c = 0;
   int64_t pos = (FILL && active) ? offs[qi * S + s_total] : 0;
+  if (radii && active) radius = radii[qi];  // per-row radius (tie-inclusive kNN rows)
   const float* qrow = qt + qloc * a.qs;
   for (int64_t t0 = p_begin; t0 < p_end; t0 += a.pt) {
     __syncthreads();
@@ -610,17 +611,17 @@ __global__ void split_keys_kernel(const uint64_t* __restrict__ keys, int64_t tot
 }
 
 template <int KIND, int ORDER>
-int launch_range(const ScanArgs& a, const Plan& pl, int64_t qblocks, float radius, int ex, int64_t* counts,
-                 const int64_t* offs, uint64_t* out, bool fill, cudaStream_t s) {
+int launch_range(const ScanArgs& a, const Plan& pl, int64_t qblocks, float radius, const float* radii, int ex,
+                 int64_t* counts, const int64_t* offs, uint64_t* out, bool fill, cudaStream_t s) {
   dim3 grid((unsigned)qblocks, (unsigned)pl.S_grid);
   if (fill) {
     auto kern = range_kernel<KIND, ORDER, true>;
     FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-    kern<<<grid, kThreads, pl.smem, s>>>(a, radius, ex, counts, offs, out); ::fuelg::note_launch();
+    kern<<<grid, kThreads, pl.smem, s>>>(a, radius, radii, ex, counts, offs, out); ::fuelg::note_launch();
   } else {
     auto kern = range_kernel<KIND, ORDER, false>;
     FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-    kern<<<grid, kThreads, pl.smem, s>>>(a, radius, ex, counts, offs, out); ::fuelg::note_launch();
+    kern<<<grid, kThreads, pl.smem, s>>>(a, radius, radii, ex, counts, offs, out); ::fuelg::note_launch();
   }
   FUELG_CUDA(cudaGetLastError());
   return ST_OK;
@@ -629,7 +630,7 @@ int launch_range(const ScanArgs& a, const Plan& pl, int64_t qblocks, float radiu
 }  // namespace
 
 int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_t** d_off, int64_t** d_idx,
-                float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream) {
+                float** d_dist, int64_t* total, int* dev_status, cudaStream_t stream, const float* radii) {
   (void)dev_status;
   *d_off = nullptr;
   *d_idx = nullptr;
@@ -671,10 +672,10 @@ int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_
       return ST_EINVAL;
     }
     return p.order == ORDER_X86
-               ? launch_range<KIND_KNN, ORDER_X86>(a, pl, qblocks, radius, exclude_self, counts.as<int64_t>(), offs,
-                                                   out, fill, stream)
-               : launch_range<KIND_KNN, ORDER_ARM>(a, pl, qblocks, radius, exclude_self, counts.as<int64_t>(), offs,
-                                                   out, fill, stream);
+               ? launch_range<KIND_KNN, ORDER_X86>(a, pl, qblocks, radius, radii, exclude_self, counts.as<int64_t>(),
+                                                   offs, out, fill, stream)
+               : launch_range<KIND_KNN, ORDER_ARM>(a, pl, qblocks, radius, radii, exclude_self, counts.as<int64_t>(),
+                                                   offs, out, fill, stream);
   };
   FUELG_TRY(run(false, nullptr, nullptr));
   size_t tb = 0;

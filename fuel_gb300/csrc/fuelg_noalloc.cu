@@ -1,13 +1,16 @@
 // fuelg_noalloc.cu -- an allocation-free variant of the exact linear-scan kNN.
 //
-// Some callers cannot allocate device memory at all: code running while a CUDA
-// graph is being captured (where cudaMalloc is not permitted), callers whose
-// GPU memory is owned by another allocator or budgeted up front, and embedded
-// hosts that must not grow their footprint after start-up.  fuelg_knn_noalloc
-// serves them: it takes device-resident inputs and outputs and keeps every
-// temporary in one statically sized device array that lives in this module.
+// Some callers cannot allocate device memory: hosts whose GPU memory belongs to
+// another allocator (a framework's caching pool, a memory budget fixed at
+// start-up) and embedded users that must not grow their footprint once they are
+// running.  fuelg_knn_noalloc serves them: it takes device-resident inputs and
+// outputs and keeps every temporary in one statically sized device array that
+// lives in this module.  The call waits for its stream to finish and reads a
+// status word back before it returns.
 #include <cstring>
 #include <mutex>
+
+#include <cuda.h>
 
 #include "../../include/fuelg.h"
 #include "fuelg_common.cuh"
@@ -23,11 +26,33 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
+struct ScratchSlot {
+  CUcontext ctx = nullptr;  // context the address was resolved in
+  void* ptr = nullptr;
+};
+ScratchSlot g_scratch[kMaxDevices];
 
-// Device address of g_noalloc_scratch on the current device, looked up once per
-// device (host code must not use the symbol itself: on the host it is only a
-// stand-in, not a device address).
+// cuCtxGetCurrent through the runtime's driver entry point (no link-time
+// dependency on libcuda).
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+CtxGetCurrentFn ctx_get_current() {
+  static CtxGetCurrentFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(p);
+  }
+  return fn;
+}
+
+// Device address of g_noalloc_scratch for the current device and context.  It
+// is looked up with cudaGetSymbolAddress on the first call on a device (host
+// code must not use the symbol itself: on the host it is only a stand-in, not a
+// device address) and looked up again when the calling thread's current context
+// is not the one the cached address came from (a context made through the
+// driver API, or the primary context re-created after cudaDeviceReset).
 int noalloc_scratch(void** out) {
   int dev = 0;
   FUELG_CUDA(cudaGetDevice(&dev));
@@ -35,30 +60,52 @@ int noalloc_scratch(void** out) {
     set_error("device ordinal %d outside the supported range", dev);
     return ST_ENOTSUP;
   }
+  CtxGetCurrentFn get_ctx = ctx_get_current();
+  if (!get_ctx) {
+    set_error("cuCtxGetCurrent is unavailable from the driver");
+    return ST_ECUDA;
+  }
+  CUcontext ctx = nullptr;
+  if (get_ctx(&ctx) == CUDA_SUCCESS && ctx == nullptr) {
+    // no context yet on this thread: cudaSetDevice makes the device's primary
+    // context current (a context the caller made current is left alone)
+    FUELG_CUDA(cudaSetDevice(dev));
+    get_ctx(&ctx);
+  }
+  if (ctx == nullptr) {
+    set_error("no current CUDA context on device %d", dev);
+    return ST_ECUDA;
+  }
   std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (g_scratch_ptr[dev] == nullptr) {
+  ScratchSlot& slot = g_scratch[dev];
+  if (slot.ptr == nullptr || slot.ctx != ctx) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || p == nullptr) {
       cudaGetLastError();
+      slot = ScratchSlot{};
       set_error("cannot resolve the static scratch on device %d: %s", dev, cudaGetErrorString(e));
       return ST_ECUDA;
     }
-    g_scratch_ptr[dev] = p;
+    slot.ctx = ctx;
+    slot.ptr = p;
   }
-  *out = g_scratch_ptr[dev];
+  *out = slot.ptr;
   return ST_OK;
 }
 
-bool device_accessible(const void* p) {
+// Memory the kernels on the current device can read and write without a copy:
+// device memory of this device, managed memory, or mapped host memory.  Device
+// memory of another GPU is refused (peer access is not assumed).
+bool device_accessible(const void* p, int dev) {
   if (!p) return false;
   cudaPointerAttributes at;
   if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged ||
-         (at.type == cudaMemoryTypeHost && at.devicePointer != nullptr);
+  if (at.type == cudaMemoryTypeDevice) return at.device == dev;
+  return at.type == cudaMemoryTypeManaged || (at.type == cudaMemoryTypeHost && at.devicePointer != nullptr);
 }
 
 }  // namespace
@@ -90,10 +137,13 @@ extern "C" int fuelg_knn_noalloc(const float* data, int64_t n, int32_t d, const 
     return ST_ENOTSUP;
   }
   if (m == 0 || k == 0) return ST_OK;
-  // no staging: everything must already be reachable from the device
-  if ((n > 0 && !device_accessible(data)) || !device_accessible(queries) || !device_accessible(out_idx) ||
-      !device_accessible(out_dist)) {
-    set_error("fuelg_knn_noalloc needs device-accessible data, queries and outputs (it cannot stage host buffers)");
+  // no staging: everything must already be reachable from the current device
+  int dev = 0;
+  FUELG_CUDA(cudaGetDevice(&dev));
+  if ((n > 0 && !device_accessible(data, dev)) || !device_accessible(queries, dev) ||
+      !device_accessible(out_idx, dev) || !device_accessible(out_dist, dev)) {
+    set_error("fuelg_knn_noalloc needs data, queries and outputs in memory of the current device (or managed / "
+              "mapped memory); it cannot stage host buffers");
     return ST_EINVAL;
   }
   void* scratch = nullptr;

@@ -77,9 +77,16 @@ class SearchIndex:
     (every tier returns the exact reference answer; the tensor-core tiers
     screen in BF16, hi+lo BF16 or FP16 and re-score) and
     ``order`` ('arm' | 'x86') the summation profile to reproduce (default: the
-    profile fuel compiles on this host).  ``precompute=K`` is accepted; the
-    exact answer is computed on every call with the k+1 exclude-self rule of
-    the precomputed path (python/search.rs:1163-1170).
+    profile fuel compiles on this host).  ``precompute=K`` builds, on the GPU,
+    the tie-inclusive kNN table of every indexed point to ``min(K, n)``
+    neighbours, as PrecomputedKnnSearcher::new does (src/search/precomputed.rs:
+    36-55, python/search.rs:1362-1366); self-join queries with ``k + 1 <=
+    max_k`` (exclude_self) or ``k <= max_k`` are then served from the table
+    with subset_with_ties (precomputed.rs:60-89) and the k+1 exclude rule of
+    the precomputed path (python/search.rs:1154-1173); other queries are
+    computed by the scan.  (The reference serves every external query from
+    row 0 of its table, python/search.rs:578-585 with precomputed.rs:81-85;
+    that is not reproduced.)
     """
 
     def __init__(self, data, *, distance="euclidean", tree=None, seed=None, precompute=None, precision="fp32",
@@ -118,6 +125,11 @@ class SearchIndex:
         self._handle = handle
         self.index = self
         self.last_stats = None
+        self._table = None
+        if precompute is not None:
+            max_k = min(int(precompute), host.shape[0])
+            if max_k > 0:
+                self._table = (max_k,) + self._ties_csr(None, host.shape[0], max_k, _lib.EXCLUDE_NONE)
 
     def __del__(self):
         h = getattr(self, "_handle", None)
@@ -153,6 +165,10 @@ class SearchIndex:
         if k < 0:
             raise OverflowError("can't convert negative int to unsigned")
         m = query.shape[0]
+        if (self._table is not None and k > 0 and self._same_source(query)
+                and (k + 1 if exclude_self else k) <= self._table[0]):
+            self.last_stats = {"served_from": "precomputed table", "max_k": self._table[0]}
+            return self._knn_from_table(m, k, exclude_self)
         q = np.ascontiguousarray(query)
         idx = np.empty((m, k), np.int64)
         dist = np.empty((m, k), np.float32)
@@ -166,6 +182,62 @@ class SearchIndex:
         self.last_stats = st.as_dict()
         return idx, dist
 
+    def _ties_csr(self, q, m, k, mode):
+        """fuelg_knn_ties -> (offsets int64[m+1], idx int64[], dist float32[]);
+        q None: the index's own rows are the queries."""
+        lib = _lib.load()
+        res = ctypes.c_void_p()
+        st = _lib.Stats()
+        _lib.check(lib.fuelg_knn_ties(self._handle, None if q is None else _lib.ptr(q), m, k, mode,
+                                      _lib.PRECISION[self.precision], ctypes.byref(res), ctypes.byref(st)))
+        try:
+            off, idx, dist = _take_csr(lib, res, m)
+        finally:
+            lib.fuelg_range_free(res)
+        self.last_stats = st.as_dict()
+        return off, idx, dist
+
+    def knn_with_ties(self, query, k, *, exclude_self=None):
+        """Tie-inclusive kNN lists: ([int64 arrays], [float32 arrays]) per
+        query row -- the k nearest points plus every point tied with the k-th
+        distance, sorted by (distance, index), as KNNHeap::into_vec returns
+        them (src/api/search.rs:80-151); exclude_self drops index i from row i
+        after the search (the linear-index rule, python/search.rs:485-488, or
+        the k+1 rule of a precomputed index, :1163-1170)."""
+        query, exclude_self = self._prepare_query(query, exclude_self)
+        k = int(k)
+        if k < 0:
+            raise OverflowError("can't convert negative int to unsigned")
+        q = np.ascontiguousarray(query)
+        m = q.shape[0]
+        if exclude_self:
+            mode = _lib.EXCLUDE_KPLUS1 if self.precompute is not None else _lib.EXCLUDE_LINEAR
+        else:
+            mode = _lib.EXCLUDE_NONE
+        off, idx, dist = self._ties_csr(q, m, k, mode)
+        return ([idx[off[i]:off[i + 1]].copy() for i in range(m)],
+                [dist[off[i]:off[i + 1]].copy() for i in range(m)])
+
+    def _knn_from_table(self, m, k, exclude_self):
+        """subset_with_ties of every row's table entry (src/search/precomputed.rs:
+        60-67), self dropped, truncated to k (python/search.rs:1154-1173, 1195-1216).
+        Every row holds at least max_k >= kq entries, so the first kq columns of
+        each row decide the answer."""
+        max_k, off, idx, dist = self._table
+        kq = k + 1 if exclude_self else k
+        cols = off[:-1, None] + np.arange(kq)[None, :]
+        gi = idx[cols]
+        gd = dist[cols]
+        if exclude_self:
+            is_self = gi == np.arange(m)[:, None]
+            has = is_self.any(axis=1)
+            p = np.where(has, np.argmax(is_self, axis=1), kq)
+            j = np.arange(k)[None, :]
+            src = j + (j >= p[:, None])
+            gi = np.take_along_axis(gi, src, axis=1)
+            gd = np.take_along_axis(gd, src, axis=1)
+        return np.ascontiguousarray(gi[:, :k]), np.ascontiguousarray(gd[:, :k])
+
     def radius_search(self, query, radius, *, exclude_self=None):
         """([int64 arrays], [float32 arrays]) per query row, sorted by (distance, index)."""
         query, exclude_self = self._prepare_query(query, exclude_self)
@@ -177,12 +249,7 @@ class SearchIndex:
         _lib.check(lib.fuelg_range(self._handle, _lib.ptr(q), m, float(radius), int(exclude_self),
                                    ctypes.byref(res), ctypes.byref(st)))
         try:
-            mm, tot = ctypes.c_int64(), ctypes.c_int64()
-            _lib.check(lib.fuelg_range_size(res, ctypes.byref(mm), ctypes.byref(tot)))
-            off = np.empty(m + 1, np.int64)
-            idx = np.empty(max(1, tot.value), np.int64)
-            dist = np.empty(max(1, tot.value), np.float32)
-            _lib.check(lib.fuelg_range_copy(res, _lib.ptr(off), _lib.ptr(idx), _lib.ptr(dist)))
+            off, idx, dist = _take_csr(lib, res, m)
         finally:
             lib.fuelg_range_free(res)
         self.last_stats = st.as_dict()
@@ -198,6 +265,17 @@ class SearchIndex:
 
     def __repr__(self):
         return f"<SearchIndex tree={self.tree!r} dtype={self.dtype!r} shape={self.shape!r}>"
+
+
+def _take_csr(lib, res, m):
+    """Copy a fuelg_range_result to host arrays (offsets[m+1], idx[], dist[])."""
+    mm, tot = ctypes.c_int64(), ctypes.c_int64()
+    _lib.check(lib.fuelg_range_size(res, ctypes.byref(mm), ctypes.byref(tot)))
+    off = np.empty(m + 1, np.int64)
+    idx = np.empty(max(1, tot.value), np.int64)
+    dist = np.empty(max(1, tot.value), np.float32)
+    _lib.check(lib.fuelg_range_copy(res, _lib.ptr(off), _lib.ptr(idx), _lib.ptr(dist)))
+    return off, idx[:tot.value], dist[:tot.value]
 
 
 class PrioritySearcher:

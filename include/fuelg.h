@@ -103,9 +103,26 @@ int fuelg_index_info(const fuelg_index *index, int64_t *n, int32_t *d, int32_t *
  * linear index (python/search.rs:560-568 -> linear_scan_knn_batch :471-491 ->
  * linear_scan_knn, src/api/search.rs:169-184).  out_idx / out_dist are
  * [m, k] row-major (int64 / f32).  exclude_mode selects the exclude-self rule
- * (FUELG_EXCLUDE_*), which drops index i from query row i. */
+ * (FUELG_EXCLUDE_*), which drops index i from query row i.  queries may be
+ * NULL when m equals the index size: the index's own rows are then the
+ * queries (an all-points self-join with no upload). */
 int fuelg_knn(fuelg_index *index, const float *queries, int64_t m, int32_t k, int32_t exclude_mode, int32_t precision,
               int64_t *out_idx, float *out_dist, fuelg_stats *stats);
+
+/* Tie-inclusive k nearest neighbours: for every query row the k nearest
+ * points plus every point tied with the k-th distance, sorted by (distance,
+ * index) -- the list KNNHeap::into_vec returns (src/api/search.rs:80-151) and
+ * fuel's KnnSearch::search_knn contract (src/api/search.rs:268-270) promises.
+ * exclude_mode as for fuelg_knn: FUELG_EXCLUDE_LINEAR searches k and then
+ * drops index i from row i (python/search.rs:485-488), FUELG_EXCLUDE_KPLUS1
+ * searches k+1 and drops self (python/search.rs:1163-1170).  With k = max_k
+ * over the index's own rows (queries NULL, m = n, FUELG_EXCLUDE_NONE) this is
+ * the table PrecomputedKnnSearcher::new builds (src/search/precomputed.rs:36-55).
+ * The lists are CSR, owned by *out (fuelg_range_size / _copy / _free).  Rows
+ * with more ties than the call's spare ranks are completed by an exact range
+ * scan at their k-th distance. */
+int fuelg_knn_ties(fuelg_index *index, const float *queries, int64_t m, int32_t k, int32_t exclude_mode,
+                   int32_t precision, fuelg_range_result **out, fuelg_stats *stats);
 
 /* All points with distance <= radius (radius is cast to f32 as
  * python/search.rs:781-783 does), sorted by (distance, index).  Replaces
@@ -215,23 +232,25 @@ int fuelg_server_stats(fuelg_server *s, int64_t *batches, int64_t *queries, int6
 int fuelg_server_destroy(fuelg_server *s);
 
 /* Allocation-free exact kNN.  No counterpart in the reference: it exists for
- * callers that cannot allocate device memory -- code recording a CUDA graph
- * (cudaMalloc is not allowed during capture), hosts whose GPU memory belongs to
- * another allocator or is budgeted up front, and embedded callers that must
- * not grow their footprint after start-up.  Same results as fuelg_knn on a
- * linear index built from `data` with the same metric and order.
- *  - data [n, d], queries [m, d], out_idx / out_dist [m, k] must be device
- *    (or managed / mapped) memory: host buffers are rejected with
- *    FUELG_EINVAL, since staging them would need an allocation.
+ * callers that cannot allocate device memory -- hosts whose GPU memory belongs
+ * to another allocator (a framework's caching pool) or is budgeted up front,
+ * and embedded callers that must not grow their footprint after start-up.
+ * Same results as fuelg_knn on a linear index built from `data` with the same
+ * metric and order.
+ *  - data [n, d], queries [m, d], out_idx / out_dist [m, k] must be memory of
+ *    the current device (or managed / mapped memory): host buffers and device
+ *    memory of another GPU are rejected with FUELG_EINVAL, since staging them
+ *    would need an allocation.
  *  - every temporary lives in one static 32 MiB device array of the library,
  *    held by each GPU that loads it until the process exits; queries are
- *    processed in batches that fit it; k <= 4095.
- *  - the first call on a device resolves that array's address; make it before
- *    any stream capture.
+ *    processed in batches that fit it; k <= 4095 (FUELG_ENOTSUP beyond).
+ *  - the first call on a device (and the first call in a different CUDA
+ *    context) resolves that array's address with cudaGetSymbolAddress.
  *  - all calls share the array and leave their contents in it, so calls that
  *    overlap on the GPU (different streams, host threads) race: serialise them.
  *  - work is ordered on `stream` (a cudaStream_t, NULL = legacy default); the
- *    call returns after that stream has finished it; no cancellation. */
+ *    call waits for that stream to finish and reads a device status word back
+ *    before it returns; no cancellation. */
 int fuelg_knn_noalloc(const float *data, int64_t n, int32_t d, const float *queries, int64_t m, int32_t k,
                       int32_t metric, int32_t order, int32_t exclude_mode, int64_t *out_idx, float *out_dist,
                       void *stream);

@@ -315,6 +315,26 @@ def knn_with_ties(X, q, k: int, metric: str = "sqeuclidean", order: str | None =
     return idx[:cnt].copy(), dd[:cnt].copy()
 
 
+def knn_ties(X, Q, k: int, metric: str = "sqeuclidean", order: str | None = None, exclude: str = "none"):
+    """Tie-inclusive lists of every query row as CSR (offsets, idx, dist):
+    linear_scan_knn's KNNHeap::into_vec list (k, or k+1 for exclude='kplus1'),
+    then index i dropped from row i for exclude 'linear' / 'kplus1'
+    (python/search.rs:485-488, 1163-1170)."""
+    Q = _f(Q, np.float32)
+    kq = k + 1 if exclude == "kplus1" else k
+    offs, ids, ds = [0], [], []
+    for i in range(Q.shape[0]):
+        ii, dd = knn_with_ties(X, Q[i], kq, metric=metric, order=order)
+        if exclude != "none":
+            keep = ii != i
+            ii, dd = ii[keep], dd[keep]
+        ids.append(ii)
+        ds.append(dd)
+        offs.append(offs[-1] + len(ii))
+    cat = (lambda parts, dt: np.concatenate(parts).astype(dt) if parts else np.empty(0, dt))
+    return np.array(offs, np.int64), cat(ids, np.int64), cat(ds, np.float32)
+
+
 # --------------------------------------------------------------------------
 # Exact-mean Lloyd: fuel's assignment order, centres = correctly rounded f32
 # of the exact mean of each cluster's member rows.
