@@ -43,6 +43,15 @@ class Stats(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ErrorReport(ctypes.Structure):
+    """fuelg_error_report (include/fuelg.h)."""
+    _fields_ = [("max_abs_err", ctypes.c_double), ("max_rel_err", ctypes.c_double), ("pairs", ctypes.c_int64),
+                ("near_ties", ctypes.c_int64), ("order_flips", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class KMeansProblem(ctypes.Structure):
     """fuelg_kmeans_problem (include/fuelg.h)."""
     _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_int64), ("d", ctypes.c_int32), ("k", ctypes.c_int32),
@@ -65,6 +74,8 @@ SIGNATURES = {
                                         ctypes.POINTER(_i32)]),
     "fuelg_knn": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
     "fuelg_knn_ties": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _i32, _pp, ctypes.POINTER(Stats)]),
+    "fuelg_knn_error": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, ctypes.POINTER(ErrorReport)]),
+    "fuelg_fp32_rate": (ctypes.c_int, [ctypes.POINTER(_dbl)]),
     "fuelg_range": (ctypes.c_int, [_vp, _vp, _i64, _dbl, _i32, _pp, ctypes.POINTER(Stats)]),
     "fuelg_range_size": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(_i64)]),
     "fuelg_range_copy": (ctypes.c_int, [_vp, _vp, _vp, _vp]),

@@ -553,6 +553,38 @@ int fuelg_knn_ties(fuelg_index* ix, const float* queries, int64_t m, int32_t k, 
   return ST_OK;
 }
 
+int fuelg_knn_error(fuelg_index* ix, const float* queries, int64_t m, int32_t k, const int64_t* idx,
+                    const float* dist, fuelg_error_report* out) {
+  if (!ix || !out || m < 0 || k < 0 || (m > 0 && k > 0 && (!idx || !dist)) || (m > 0 && !queries && m != ix->n)) {
+    set_error("invalid knn_error arguments");
+    return ST_EINVAL;
+  }
+  memset(out, 0, sizeof(*out));
+  std::lock_guard<std::mutex> lk(ix->mu);
+  FUELG_TRY(begin_call());
+  cudaSetDevice(ix->device);
+  if (m == 0 || k == 0 || ix->n == 0) return ST_OK;
+  cudaStream_t s = ix->stream;
+  InBuf q, bi, bd;
+  if (queries) FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(float), s));
+  FUELG_TRY(bi.init(idx, (size_t)m * k * sizeof(int64_t), s));
+  FUELG_TRY(bd.init(dist, (size_t)m * k * sizeof(float), s));
+  const float* Q = queries ? static_cast<const float*>(q.dptr) : ix->X;
+  return knn_error_report(Q, ix->X, m, ix->d, k, ix->metric, static_cast<const int64_t*>(bi.dptr),
+                          static_cast<const float*>(bd.dptr), &out->max_abs_err, &out->max_rel_err, &out->pairs,
+                          &out->near_ties, &out->order_flips, s);
+}
+
+int fuelg_fp32_rate(double* tera_fma_per_s) {
+  if (!tera_fma_per_s) {
+    set_error("tera_fma_per_s is NULL");
+    return ST_EINVAL;
+  }
+  FUELG_TRY(begin_call());
+  double ms = 0.0;
+  return fp32_issue_rate(tera_fma_per_s, &ms);
+}
+
 int fuelg_pairwise(const float* X, int64_t n, int32_t d, int32_t metric, int32_t order, int32_t form, float* out,
                    fuelg_stats* stats) {
   if (n < 0 || d < 1 || (n > 0 && !X)) {

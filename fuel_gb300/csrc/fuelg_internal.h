@@ -225,6 +225,18 @@ int knn_ties_lists(const uint64_t* keys, int64_t m, int kk, int kq, int drop_sel
                    int64_t** d_off, int64_t** d_idx, float** d_dist, int64_t* total, int64_t* range_rows,
                    int* dev_status, cudaStream_t s);
 
+// -------- accuracy report and FP32 issue rate (fuelg_check.cu) ----------------
+// FP64 check of returned kNN rows (Q [m, d], X the index, idx / dist [m, k],
+// all device): max |d - D| and max |d - D| / D over the returned pairs, the
+// number of pairs, adjacent neighbours within one f32 ulp, and adjacent
+// neighbours that FP64 distances order the other way.
+int knn_error_report(const float* Q, const float* X, int64_t m, int d, int k, int metric, const int64_t* idx,
+                     const float* dist, double* max_abs, double* max_rel, int64_t* pairs, int64_t* near_ties,
+                     int64_t* flips, cudaStream_t s);
+// Sustained FP32 FMA issue rate of the current device (10^12 FMA/s; one FMA
+// is one lane operation, two flops), best of five CUDA-event-timed launches.
+int fp32_issue_rate(double* tera_fma_per_s, double* ms);
+
 // -------- Lloyd (fuelg_lloyd.cu) -------------------------------------------
 struct LloydParams {
   const float* X = nullptr;  // [n, d] device

@@ -124,6 +124,31 @@ int fuelg_knn(fuelg_index *index, const float *queries, int64_t m, int32_t k, in
 int fuelg_knn_ties(fuelg_index *index, const float *queries, int64_t m, int32_t k, int32_t exclude_mode,
                    int32_t precision, fuelg_range_result **out, fuelg_stats *stats);
 
+/* Accuracy of returned kNN rows against FP64.  No counterpart in the
+ * reference (fuel's distances are f32 throughout); it checks results of
+ * fuelg_knn / fuelg_server_* against distances formed in double: for every
+ * returned pair (idx >= 0) of rows [m, k] (host or device arrays; queries NULL
+ * = the index's own rows, as for fuelg_knn) the f32 distance is compared with
+ * the FP64 one, adjacent neighbours whose f32 distances are equal or one ulp
+ * apart are counted as near_ties, and adjacent neighbours that the FP64
+ * distances (index breaking exact ties, DistPair order, src/api/search.rs:23-30)
+ * rank the other way are counted as order_flips -- the only places where the
+ * reference's f32 lists can differ from an FP64 ranking. */
+typedef struct {
+    double max_abs_err;  /* max |d_f32 - d_fp64| over the returned pairs            */
+    double max_rel_err;  /* max |d_f32 - d_fp64| / d_fp64 (pairs with d_fp64 > 0)   */
+    int64_t pairs;       /* returned (query, neighbour) pairs checked               */
+    int64_t near_ties;   /* adjacent neighbours within one f32 ulp (or equal)       */
+    int64_t order_flips; /* adjacent neighbours ranked the other way by FP64        */
+} fuelg_error_report;
+int fuelg_knn_error(fuelg_index *index, const float *queries, int64_t m, int32_t k, const int64_t *idx,
+                    const float *dist, fuelg_error_report *out);
+
+/* Sustained FP32 FMA issue rate of the current GPU in 10^12 FMA/s (an FMA is
+ * one lane operation; two flops): the denominator of the plain FP32 tiers'
+ * roofline.  No counterpart in the reference. */
+int fuelg_fp32_rate(double *tera_fma_per_s);
+
 /* All points with distance <= radius (radius is cast to f32 as
  * python/search.rs:781-783 does), sorted by (distance, index).  Replaces
  * SearchIndex::radius_search (python/search.rs:776-790 -> linear_scan_range,

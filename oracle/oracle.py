@@ -361,50 +361,89 @@ def rn_f32_ratio(S: int, cnt: int, e_lo: int) -> np.float32:
 
 def fixed_point(X: np.ndarray):
     """Exact integer form of f32 data: X == I * 2**e_lo.  Returns (I, e_lo)
-    with I int64 when the sums of up to len(X) rows fit, else Python ints."""
+    with I int64 when the sums of up to len(X) rows fit, else Python ints.
+    Only the non-zero entries are decoded."""
     X = np.ascontiguousarray(X, np.float32)
-    bits = X.view(np.uint32).astype(np.int64)
+    flat = X.view(np.uint32).ravel()
+    pos = np.flatnonzero(flat & 0x7FFFFFFF)
+    if pos.size == 0:
+        return np.zeros(X.shape, np.int64), 0
+    bits = flat[pos].astype(np.int64)
     eb = (bits >> 23) & 0xFF
     mant = (bits & 0x7FFFFF) | np.where(eb != 0, 1 << 23, 0)
     unit = np.where(eb == 0, -149, eb - 150)
-    nz = mant != 0
-    if not nz.any():
-        return np.zeros(X.shape, np.int64), 0
-    ctz = np.zeros_like(mant)
-    mm = np.where(nz, mant, 1)
-    while True:
-        odd = (mm & 1) == 1
-        if odd.all():
-            break
-        ctz += np.where(odd, 0, 1)
-        mm = np.where(odd, mm, mm >> 1)
+    # trailing zeros from the lowest set bit (a power of two below 2**24: exact in float64)
+    ctz = np.log2((mant & -mant).astype(np.float64)).astype(np.int64)
+    mm = mant >> ctz
     # mant = mm * 2**ctz with mm odd, so X = mm * 2**(unit + ctz)
     low = unit + ctz
-    e_lo = int(low[nz].min())
-    e_hi = int((unit[nz] + np.floor(np.log2(mant[nz])).astype(np.int64)).max())
+    e_lo = int(low.min())
+    e_hi = int((unit + np.floor(np.log2(mant)).astype(np.int64)).max())
     sign = np.where((bits >> 31) & 1, -1, 1)
     width = e_hi - e_lo + 1 + int(np.ceil(np.log2(X.shape[0] + 1))) + 1
     if width <= 62:
-        I = np.where(nz, sign * (mm << (low - e_lo)), 0)
-        return I.astype(np.int64), e_lo
-    obj = np.empty(X.shape, dtype=object)
-    flat_m, flat_s, flat_l, flat_z = mm.ravel(), sign.ravel(), low.ravel(), nz.ravel()
-    out = obj.ravel()
-    for t in range(out.size):
-        out[t] = int(flat_s[t]) * (int(flat_m[t]) << int(flat_l[t] - e_lo)) if flat_z[t] else 0
-    return obj, e_lo
+        I = np.zeros(flat.size, np.int64)
+        I[pos] = sign * (mm << (low - e_lo))
+        return I.reshape(X.shape), e_lo
+    obj = np.zeros(flat.size, dtype=object)
+    for t, p_ in enumerate(pos):
+        obj[p_] = int(sign[t]) * (int(mm[t]) << int(low[t] - e_lo))
+    return obj.reshape(X.shape), e_lo
 
 
-def exact_means(I, e_lo, labels, k, prev):
+def exact_means(I, e_lo, labels, k, prev, If64=None):
+    """Correctly rounded f32 means of every cluster's member rows (I * 2**e_lo);
+    empty clusters keep their previous centre.  With If64 (the float64 copy of
+    an int64 I whose column sums of |I| stay below 2**53) the sums are one
+    exact float64 matrix product and the rounding is vectorised
+    (_rn_f32_ratio_vec); otherwise exact Python integers per coordinate."""
     C = np.array(prev, np.float32, copy=True)
+    labels = np.asarray(labels)
+    cnt = np.bincount(labels, minlength=k)[:k]
+    if If64 is not None and labels.shape[0] < (1 << 26):
+        onehot = np.zeros((k, labels.shape[0]), np.float64)
+        onehot[labels, np.arange(labels.shape[0])] = 1.0
+        S = onehot @ If64  # every partial sum is an integer below 2**53: exact in any order
+        live = cnt > 0
+        C[live] = _rn_f32_ratio_vec(S[live], cnt[live], e_lo)
+        return C
     for j in range(k):
         rows = np.nonzero(labels == j)[0]
         if len(rows) == 0:
             continue
         S = I[rows].sum(axis=0)
-        cnt = len(rows)
-        C[j] = [rn_f32_ratio(int(s), cnt, e_lo) for s in S]
+        C[j] = [rn_f32_ratio(int(v), len(rows), e_lo) for v in S]
     return C
+
+
+def _rn_f32_ratio_vec(S, cnt, e_lo):
+    """Vectorised rn_f32_ratio for exact integer sums S (float64 [r, d],
+    |S| < 2**53) and counts cnt (< 2**26): the float64 quotient rounded to f32,
+    then corrected against the exact rounding boundaries of that f32 (the
+    midpoints to its neighbours, times cnt, are exact float64 products), so
+    double rounding cannot slip through.  Results that are zero or subnormal
+    for a non-zero sum are recomputed with rn_f32_ratio."""
+    cnt = np.asarray(cnt, np.float64)[:, None]
+    neg = S < 0
+    T = np.ldexp(np.abs(S), e_lo)
+    c = (T / cnt).astype(np.float32)
+    up = np.nextafter(c, np.float32(np.inf))
+    dn = np.nextafter(c, np.float32(0.0))
+    c64 = c.astype(np.float64)
+    m_hi = (c64 + up.astype(np.float64)) * 0.5 * cnt
+    m_lo = (c64 + dn.astype(np.float64)) * 0.5 * cnt
+    c_even = (c.view(np.uint32) & 1) == 0
+    out = c.copy()
+    out = np.where(T > m_hi, up, out)
+    out = np.where(T == m_hi, np.where(c_even, c, up), out)
+    out = np.where(T < m_lo, dn, out)
+    out = np.where((T == m_lo) & (T > 0), np.where(c_even, c, dn), out)
+    out = np.where(neg, -out, out).astype(np.float32)
+    bad = (np.abs(S) > 0) & (np.abs(out) < np.float32(1.1754944e-38))
+    for r, j in zip(*np.nonzero(bad)):
+        e = int(round(float(np.abs(S[r, j]))))
+        out[r, j] = rn_f32_ratio(-e if neg[r, j] else e, int(cnt[r, 0]), e_lo)
+    return out
 
 
 def lloyd_exact(X, k: int, init, max_iter: int = 300, order: str | None = None, threads: int = 1,
@@ -417,9 +456,12 @@ def lloyd_exact(X, k: int, init, max_iter: int = 300, order: str | None = None, 
     X = np.ascontiguousarray(X, np.float32)
     C = np.ascontiguousarray(init, np.float32).copy()
     I, e_lo = fixed_point(X)
+    If64 = None
+    if I.dtype == np.int64 and float(np.abs(I).sum(axis=0, dtype=np.float64).max(initial=0.0)) < 2.0 ** 52:
+        If64 = I.astype(np.float64)
     labels, _ = lloyd_assign(X, C, initial=True, order=order, threads=threads)
     if max_iter > 1:
-        C = exact_means(I, e_lo, labels, k, C)
+        C = exact_means(I, e_lo, labels, k, C, If64)
     it = 1
     while it < max_iter:
         it += 1
@@ -427,7 +469,7 @@ def lloyd_exact(X, k: int, init, max_iter: int = 300, order: str | None = None, 
         changed = int((new != labels).sum())
         labels = new
         if it < max_iter:
-            C = exact_means(I, e_lo, labels, k, C)
+            C = exact_means(I, e_lo, labels, k, C, If64)
         if not fixed_iters and changed == 0:
             break
     return C, labels, it, lloyd_inertia_fp64(X, C, labels)

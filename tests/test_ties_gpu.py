@@ -58,12 +58,12 @@ MODES = {"none": _lib.EXCLUDE_NONE, "linear": _lib.EXCLUDE_LINEAR, "kplus1": _li
 def test_ties_plain_tie_heavy(gpu, lib, oracle, exclude, k):
     """Integer data with few distinct values: long tie runs at the k-th distance."""
     rng = np.random.default_rng(k)
-    X = rng.integers(0, 3, size=(1500, 6)).astype(np.float32)
+    X = rng.integers(0, 3, size=(1500, 4)).astype(np.float32)  # 81 distinct points, ~18 copies each
     got = _csr(lib, X, X, k, MODES[exclude], "fp32")
     ref = oracle.knn_ties(X, X, k, exclude=exclude)
     _assert_same(got, ref)
     lens = np.diff(ref[0])
-    assert lens.max() > k + 10, "the data must produce tie runs longer than the spare ranks"
+    assert lens.max() > k + 1 + max(8, (k + 1) // 4), "the data must produce tie runs longer than the spare ranks"
 
 
 @pytest.mark.parametrize("metric", ["sqeuclidean", "euclidean"])
