@@ -19,7 +19,7 @@ METRIC = {"sqeuclidean": 0, "euclidean": 1}
 ORDER = {"arm": 0, "x86": 1}
 EXCLUDE_NONE, EXCLUDE_LINEAR, EXCLUDE_KPLUS1 = 0, 1, 2
 # fp16: kNN / serving only (tcgen05 FP16 screen; values within the FP16 range)
-PRECISION = {"fp32": 0, "bf16": 1, "split_bf16": 2, "fp16": 4}
+PRECISION = {"auto": -1, "fp32": 0, "bf16": 1, "split_bf16": 2, "fp16": 4}
 # stats["precision_used"] may also be 3: split_bf16 on scaled-integer data
 PRECISION_NAMES = {0: "fp32", 1: "bf16", 2: "split_bf16", 3: "split_bf16_scaled", 4: "fp16"}
 LLOYD_FIXED_ITERS = 1

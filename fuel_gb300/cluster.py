@@ -76,7 +76,7 @@ def _init_centers(data: np.ndarray, k: int, init, seed):
     return np.ascontiguousarray(arr, np.float32)
 
 
-def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, init=None, precision="fp32",
+def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, init=None, precision=None,
            order=None, fixed_iters=False):
     """K-means clustering (Euclidean space) on the GPU.
 
@@ -86,7 +86,11 @@ def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, ini
     sum of squared distances of the final pass, or None for the bound-based
     variants, whose reference results carry none (``stats["inertia_fp64"]``
     has it for every variant).  ``fixed_iters=True`` runs
-    exactly ``max_iter`` iterations (benchmark mode).
+    exactly ``max_iter`` iterations (benchmark mode).  ``precision`` (None /
+    'auto' | 'fp32' | 'bf16' | 'split_bf16') picks the assignment tier; every
+    tier gives the same result, and the default runs the split-BF16 tensor-core
+    screen where it serves the shape (d >= 32, n >= 16384), the plain FP32
+    scan otherwise.
     """
     v = str(variant).lower()
     if v in _OTHER:
@@ -111,6 +115,9 @@ def kmeans(data, *, k, variant="simp_elkan", max_iter=300, tol=0, seed=None, ini
     X = np.ascontiguousarray(data)
     n, d = X.shape
     C0 = _init_centers(X, k, init, seed)
+    precision = "auto" if precision is None else precision
+    if precision not in _lib.PRECISION or precision == "fp16":
+        raise ValueError("precision must be one of 'auto', 'fp32', 'bf16', 'split_bf16'")
     centers = np.empty((k, d), np.float32)
     labels = np.empty(n, np.int64)
     iters = ctypes.c_int32(0)
@@ -148,7 +155,7 @@ def lloyd_assign(data, centers, *, initial=False, order=None):
     return labels, best
 
 
-def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False, precision="split_bf16"):
+def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False, precision="auto"):
     """Many independent Lloyd k-means problems in one engine call.
 
     ``problems``: iterable of ``(data float32[n, d], init float32[k, d])``.

@@ -2,6 +2,7 @@
 // buffers, status codes, cancellation and per-call measurements.
 #include <cstdarg>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 
@@ -397,6 +398,105 @@ int index_topk(fuelg_index* ix, const float* Q, int64_t m, int kk, int precision
   return exact_topk(p, keys, dstat, s);
 }
 
+// ---- precision autotuner ---------------------------------------------------
+// Buckets (d, floor(log2 n), ceil(log2 kk), value class) -> tier, shared by all
+// indexes of the process, loaded from / appended to FUELG_TUNE_CACHE.
+struct TuneKey {
+  int d, nb, kb, cls;
+  bool operator<(const TuneKey& o) const {
+    return d != o.d ? d < o.d : nb != o.nb ? nb < o.nb : kb != o.kb ? kb < o.kb : cls < o.cls;
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, int> g_tune;
+bool g_tune_loaded = false;
+
+int ilog2_floor(int64_t v) {
+  int r = 0;
+  while (v > 1) {
+    v >>= 1;
+    r++;
+  }
+  return r;
+}
+
+void tune_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = getenv("FUELG_TUNE_CACHE");
+  if (!path) return;
+  FILE* f = fopen(path, "r");
+  if (!f) return;
+  char kind[16];
+  TuneKey key;
+  int tier;
+  while (fscanf(f, "%15s %d %d %d %d %d", kind, &key.d, &key.nb, &key.kb, &key.cls, &tier) == 6)
+    if (strcmp(kind, "knn") == 0 && (tier == FUELG_PREC_BF16 || tier == FUELG_PREC_SPLIT_BF16 ||
+                                     tier == FUELG_PREC_F16 || tier == FUELG_PREC_FP32))
+      g_tune[key] = tier;
+  fclose(f);
+}
+
+void tune_store_locked(const TuneKey& key, int tier) {
+  g_tune[key] = tier;
+  const char* path = getenv("FUELG_TUNE_CACHE");
+  if (!path) return;
+  if (FILE* f = fopen(path, "a")) {
+    fprintf(f, "knn %d %d %d %d %d\n", key.d, key.nb, key.kb, key.cls, tier);
+    fclose(f);
+  }
+}
+
+// The tier a FUELG_PREC_AUTO kNN call runs.  Called with ix->mu held.
+int resolve_knn_precision(fuelg_index* ix, const float* Q, int64_t m, int kk, int* dstat, cudaStream_t s,
+                          int* out) {
+  *out = FUELG_PREC_FP32;
+  if (ix->n == 0 || !knn_tc_supported(ix->d, kk, TC_BF16)) return ST_OK;
+  if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
+  const int cls = knn_tc_index_class(ix->tc);
+  if (cls == TC_CLASS_INTEGER) {
+    *out = FUELG_PREC_BF16;  // exact screen, no margin, no re-score
+    return ST_OK;
+  }
+  const TuneKey key{ix->d, ilog2_floor(ix->n), ilog2_floor(2 * (int64_t)kk - 1), cls};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      *out = it->second;
+      return ST_OK;
+    }
+  }
+  // time the eligible tiers on the first rows of this call (each run twice:
+  // the first builds the tier's index copy and warms up)
+  const int64_t mt = std::min<int64_t>(m, 4096);
+  Scratch keys;
+  FUELG_TRY(keys.alloc((size_t)mt * kk * sizeof(uint64_t), s));
+  const int cand_f16[3] = {FUELG_PREC_F16, FUELG_PREC_SPLIT_BF16, FUELG_PREC_BF16};
+  const int cand_wide[2] = {FUELG_PREC_SPLIT_BF16, FUELG_PREC_BF16};
+  const int* cand = cls == TC_CLASS_F16_RANGE ? cand_f16 : cand_wide;
+  const int nc = cls == TC_CLASS_F16_RANGE ? 3 : 2;
+  int best = FUELG_PREC_SPLIT_BF16;
+  float best_ms = 1e30f;
+  for (int c = 0; c < nc; c++) {
+    int used = 0;
+    int64_t resc = 0;
+    FUELG_TRY(index_topk(ix, Q, mt, kk, cand[c], keys.as<uint64_t>(), dstat, s, &used, &resc));
+    Timer tm(s);
+    FUELG_TRY(index_topk(ix, Q, mt, kk, cand[c], keys.as<uint64_t>(), dstat, s, &used, &resc));
+    const float ms = (float)tm.stop();
+    if (used == cand[c] && ms < best_ms) {
+      best_ms = ms;
+      best = cand[c];
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_store_locked(key, best);
+  *out = best;
+  return ST_OK;
+}
+
 int check_knn_args(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32_t exclude_mode,
                    int32_t precision) {
   if (!ix) {
@@ -412,7 +512,7 @@ int check_knn_args(fuelg_index* ix, const float* queries, int64_t m, int32_t k, 
     set_error("unknown exclude mode %d", exclude_mode);
     return ST_EINVAL;
   }
-  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_F16 || precision == FUELG_PREC_SPLIT_BF16_SCALED) {
+  if (precision < FUELG_PREC_AUTO || precision > FUELG_PREC_F16 || precision == FUELG_PREC_SPLIT_BF16_SCALED) {
     set_error("unknown precision tier %d", precision);
     return ST_EINVAL;
   }
@@ -455,6 +555,8 @@ int fuelg_knn(fuelg_index* ix, const float* queries, int64_t m, int32_t k, int32
   FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
   int used = FUELG_PREC_FP32;
   int64_t rescored = 0;
+  if (precision == FUELG_PREC_AUTO)
+    FUELG_TRY(resolve_knn_precision(ix, Q, m, kk, dstat.as<int>(), s, &precision));
   FUELG_TRY(index_topk(ix, Q, m, kk, precision, keys.as<uint64_t>(), dstat.as<int>(), s, &used, &rescored));
   FUELG_TRY(finalize_knn(keys.as<uint64_t>(), m, kk, k, exclude_mode, static_cast<int64_t*>(oi.dptr),
                          static_cast<float*>(od.dptr), s));
@@ -520,7 +622,9 @@ int fuelg_knn_ties(fuelg_index* ix, const float* queries, int64_t m, int32_t k, 
     FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
     int used = FUELG_PREC_FP32;
     int64_t rescored = 0, range_rows = 0;
-    FUELG_TRY(index_topk(ix, Q, m, kk, precision, keys.as<uint64_t>(), dstat.as<int>(), s, &used, &rescored));
+    int prec = precision;
+    if (prec == FUELG_PREC_AUTO) FUELG_TRY(resolve_knn_precision(ix, Q, m, kk, dstat.as<int>(), s, &prec));
+    FUELG_TRY(index_topk(ix, Q, m, kk, prec, keys.as<uint64_t>(), dstat.as<int>(), s, &used, &rescored));
     ExactScanParams base;
     base.A = Q;
     base.m = m;
@@ -745,10 +849,14 @@ int fuelg_kmeans_lloyd(const float* data, int64_t n, int32_t d, int32_t k, const
     set_error("unknown summation order %d", order);
     return ST_EINVAL;
   }
-  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16) {
+  if (precision < FUELG_PREC_AUTO || precision > FUELG_PREC_SPLIT_BF16) {
     set_error("unknown precision tier %d", precision);
     return ST_EINVAL;
   }
+  // automatic tier: the split-BF16 screen (which also finds scaled-integer
+  // data) where it serves the shape and the pass is long enough to pay for
+  // its set-up; the plain CUDA-core scan otherwise
+  if (precision == FUELG_PREC_AUTO) precision = (d >= 32 && n >= 16384) ? FUELG_PREC_SPLIT_BF16 : FUELG_PREC_FP32;
   FUELG_TRY(begin_call());
   if (stats) memset(stats, 0, sizeof(*stats));
   cudaStream_t s;

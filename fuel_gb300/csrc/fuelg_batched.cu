@@ -731,10 +731,11 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     set_error("unknown summation order %d", order);
     return ST_EINVAL;
   }
-  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_SPLIT_BF16) {
+  if (precision < FUELG_PREC_AUTO || precision > FUELG_PREC_SPLIT_BF16) {
     set_error("unknown precision tier %d", precision);
     return ST_EINVAL;
   }
+  if (precision == FUELG_PREC_AUTO) precision = FUELG_PREC_SPLIT_BF16;  // the screen takes the problems it serves
   for (int p = 0; p < count; p++) {
     const fuelg_kmeans_problem& q = probs[p];
     if (q.n < 1 || q.d < 1 || q.k < 1 || !q.data || !q.init || !q.out_centers || !q.out_labels) {

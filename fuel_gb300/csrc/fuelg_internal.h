@@ -173,6 +173,11 @@ bool knn_tc_supported(int d, int kk, int tier);
 struct TcIndex;
 int knn_tc_index_build(const float* X32, int64_t n, int d, cudaStream_t stream, TcIndex** out);
 void knn_tc_index_free(TcIndex* t);
+// Value class of an index's data, which decides the cheapest exact tier:
+// integers with |v| <= 256 (the BF16 screen is exact), values within the FP16
+// range, or wider values.
+constexpr int TC_CLASS_INTEGER = 0, TC_CLASS_F16_RANGE = 1, TC_CLASS_WIDE = 2;
+int knn_tc_index_class(const TcIndex* t);
 int knn_tc_index_add_lo(TcIndex* t, const float* X32, cudaStream_t stream);
 // FP16 copy of the index; ST_ENOTSUP when a value lies outside the FP16 range.
 int knn_tc_index_add_f16(TcIndex* t, const float* X32, cudaStream_t stream);

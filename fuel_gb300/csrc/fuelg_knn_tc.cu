@@ -797,6 +797,11 @@ struct TcIndex {
   CUtensorMap tmX, tmXlo, tmXh;
 };
 
+int knn_tc_index_class(const TcIndex* t) {
+  if (t->integer) return TC_CLASS_INTEGER;
+  return t->vmax <= kF16Max ? TC_CLASS_F16_RANGE : TC_CLASS_WIDE;
+}
+
 void knn_tc_index_free(TcIndex* t) {
   if (!t) return;
   if (t->xb) cudaFree(t->xb);

@@ -253,7 +253,7 @@ int fuelg_server_create(fuelg_index* ix, int32_t precision, int64_t max_batch_qu
     return ST_EINVAL;
   }
   *out = nullptr;
-  if (precision < FUELG_PREC_FP32 || precision > FUELG_PREC_F16 || precision == FUELG_PREC_SPLIT_BF16_SCALED ||
+  if (precision < FUELG_PREC_AUTO || precision > FUELG_PREC_F16 || precision == FUELG_PREC_SPLIT_BF16_SCALED ||
       max_batch_queries < 1 ||
       budget_bytes < 1 || workers < 1 || workers > 16) {
     set_error("invalid server arguments (precision=%d max_batch=%lld budget=%lld workers=%d)", precision,
@@ -261,6 +261,15 @@ int fuelg_server_create(fuelg_index* ix, int32_t precision, int64_t max_batch_qu
     return ST_EINVAL;
   }
   IndexView v;
+  if (precision == FUELG_PREC_AUTO) {
+    // by the index's value class: the exact BF16 screen for small integers,
+    // FP16 (one product) within its range, split BF16 otherwise
+    FUELG_TRY(index_view_get(ix, TC_BF16, &v));
+    precision = !v.tc ? FUELG_PREC_FP32
+                : knn_tc_index_class(v.tc) == TC_CLASS_INTEGER   ? FUELG_PREC_BF16
+                : knn_tc_index_class(v.tc) == TC_CLASS_F16_RANGE ? FUELG_PREC_F16
+                                                                 : FUELG_PREC_SPLIT_BF16;
+  }
   const int want = precision == FUELG_PREC_FP32         ? -1
                    : precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT
                    : precision == FUELG_PREC_F16        ? TC_F16

@@ -73,9 +73,11 @@ class SearchIndex:
     """Persistent linear-scan index held in GB300 memory.
 
     Parameters mirror ``fuel.search.SearchIndex`` (python/fuel/search.py:230).
-    ``precision`` ('fp32' | 'bf16' | 'split_bf16' | 'fp16') picks the tier
-    (every tier returns the exact reference answer; the tensor-core tiers
-    screen in BF16, hi+lo BF16 or FP16 and re-score) and
+    ``precision`` (None / 'auto' | 'fp32' | 'bf16' | 'split_bf16' | 'fp16')
+    picks the tier (every tier returns the exact reference answer; the
+    tensor-core tiers screen in BF16, hi+lo BF16 or FP16 and re-score); the
+    default lets the engine choose per (d, n, k, value class) bucket, timing
+    the eligible tiers the first time a bucket is seen, and
     ``order`` ('arm' | 'x86') the summation profile to reproduce (default: the
     profile fuel compiles on this host).  ``precompute=K`` builds, on the GPU,
     the tie-inclusive kNN table of every indexed point to ``min(K, n)``
@@ -89,7 +91,7 @@ class SearchIndex:
     that is not reproduced.)
     """
 
-    def __init__(self, data, *, distance="euclidean", tree=None, seed=None, precompute=None, precision="fp32",
+    def __init__(self, data, *, distance="euclidean", tree=None, seed=None, precompute=None, precision=None,
                  order=None):
         data = _ensure_float(data)
         if data.ndim != 2:
@@ -108,6 +110,7 @@ class SearchIndex:
                 f"tree '{tree}' is not served by the GB300 engine; only the exact linear scan is accelerated")
         self._metric = _parse_distance(distance)
         _require_f32(data, "data")
+        precision = "auto" if precision is None else precision
         if precision not in _lib.PRECISION:
             raise ValueError(f"precision must be one of {sorted(_lib.PRECISION)}")
         self.precision = precision

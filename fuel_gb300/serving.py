@@ -38,7 +38,7 @@ class Request:
 
 
 class Server:
-    def __init__(self, index: SearchIndex, *, precision: str = "bf16", max_batch_queries: int = 8192,
+    def __init__(self, index: SearchIndex, *, precision: str = "auto", max_batch_queries: int = 8192,
                  budget_bytes: int = 8 << 30, workers: int = 2):
         if not isinstance(index, SearchIndex):
             raise TypeError("index must be a fuel_gb300.SearchIndex")

@@ -62,6 +62,17 @@ extern "C" {
    a wider proof margin) + exact FP32 re-score; values must lie within the FP16
    range (|v| <= 65504), otherwise the plain FP32 tier answers.               */
 #define FUELG_PREC_F16 4
+/* Let the engine pick the tier (every tier returns the same bits).  kNN /
+   range / serving: d outside [32, 256] -> FP32; integer data with |v| <= 256
+   -> BF16 (its screen is exact); otherwise the fastest of the eligible
+   tensor-core tiers, timed on the call's first (up to) 4096 query rows the
+   first time a (d, log2 n, log2 k, value class) bucket is seen, and kept for
+   the process -- and in the file named by FUELG_TUNE_CACHE when that variable
+   is set, one line per bucket.  k-means: the split-BF16 tier where its screen
+   serves the shape (d >= 32) and the problem is large enough (n >= 16384),
+   else FP32; batched k-means: split-BF16 for the problems it serves.
+   fuelg_stats.precision_used reports what ran. */
+#define FUELG_PREC_AUTO (-1)
 
 #define FUELG_LLOYD_FIXED_ITERS 1 /* run exactly max_iter iterations (ignore changed==0 stop) */
 

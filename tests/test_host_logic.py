@@ -61,3 +61,13 @@ def test_kmeans_init_parsing():
         cluster._init_centers(X, 3, "kmeans++", None)
     with pytest.raises(ValueError):
         cluster._init_centers(X, 3, "bogus", None)
+
+
+def test_precision_names():
+    from fuel_gb300 import _lib
+    assert _lib.PRECISION["auto"] == -1 and _lib.PRECISION["fp32"] == 0
+    X = np.zeros((4, 3), np.float32)
+    with pytest.raises(ValueError):
+        cluster.kmeans(X, k=2, variant="lloyd", init="first", precision="fp16")
+    with pytest.raises(ValueError):
+        cluster.kmeans(X, k=2, variant="lloyd", init="first", precision="tf32")
