@@ -75,3 +75,11 @@ def test_argument_validation_before_any_device_work(lib):
     assert lib.fuelg_lloyd_assign(None, 0, 1, None, 1, 0, 0, None, None, None) == _lib.EINVAL
     assert lib.fuelg_range_free(None) == _lib.OK
     assert lib.fuelg_index_destroy(None) == _lib.OK
+
+
+def test_rust_bindings_declare_every_header_function():
+    """rust/fuel-gb300-sys declares exactly the functions of include/fuelg.h."""
+    import re
+    src = open(os.path.join(ROOT, "rust", "fuel-gb300-sys", "src", "lib.rs")).read()
+    rust = set(re.findall(r"pub fn (fuelg_\w+)\(", src))
+    assert rust == set(declared_functions())
