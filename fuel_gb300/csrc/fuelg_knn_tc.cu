@@ -67,6 +67,7 @@ struct KnnTcArgs {
   uint32_t idesc;
   int* status;
   const volatile int* cancel;
+  uint64_t wait_ns;  // limit of the pipeline waits (pipeline_wait_ns)
 };
 
 
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
       for (int p = pb; p < pe && !*abort_flag; p++) {
         const int li = p - pb;
         const int q0 = a.piece_qb[p] * QM;
-        if (li > 0 && !mbar_wait(aempty, (uint32_t)((li - 1) & 1), abort_flag)) {
+        if (li > 0 && !mbar_wait(aempty, (uint32_t)((li - 1) & 1), abort_flag, a.wait_ns)) {
           if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
           *abort_flag = 1;
           break;
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
             break;
           }
           for (int j = 0; j < nb; j++) {
-            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+            if (!mbar_wait(&empty[stage], phase ^ 1, abort_flag, a.wait_ns)) {
               if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
               *abort_flag = 1;
               break;
@@ -401,7 +402,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
       bool ok = true;
       for (int p = pb; ok && p < pe && !*abort_flag; p++) {
         const int li = p - pb;
-        if (!mbar_wait(afull, (uint32_t)(li & 1), abort_flag)) {
+        if (!mbar_wait(afull, (uint32_t)(li & 1), abort_flag, a.wait_ns)) {
           if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
           *abort_flag = 1;
           break;
@@ -409,7 +410,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
         tc_fence_after();
         for (int64_t t = a.piece_t0[p]; ok && t < a.piece_t1[p] && !*abort_flag; t++, gt++) {
           const uint32_t buf = (uint32_t)(gt & 1), accph = (uint32_t)((gt >> 1) & 1);
-          if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag)) {
+          if (!mbar_wait(&acce[buf], accph ^ 1, abort_flag, a.wait_ns)) {
             if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
             *abort_flag = 1;
             ok = false;
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           tc_fence_after();
           const uint32_t d_tmem = tmem_base + buf * XN;
           for (int j = 0; j < nb; j++) {
-            if (!mbar_wait(&full[stage], phase, abort_flag)) {
+            if (!mbar_wait(&full[stage], phase, abort_flag, a.wait_ns)) {
               if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
               *abort_flag = 1;
               ok = false;
@@ -516,7 +517,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
         float* nsm = nsm_w + b * XN;
         reinterpret_cast<float4*>(nsm)[lane] = pn;
         if (t + 1 < t1) pn = __ldg(reinterpret_cast<const float4*>(a.xn2 + p0 + XN) + lane);
-        bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag);
+        bool ok = !*abort_flag && mbar_wait(&accf[b], accph, abort_flag, a.wait_ns);
         if (!ok) {
           if (!*abort_flag) atomicOr(a.status, DEV_TIMEOUT);
           *abort_flag = 1;
@@ -668,8 +669,8 @@ __global__ void knn_prep_kernel(const float* __restrict__ X, int64_t rows, int64
 // D~ >= D~_last, so its reference distance is >= D~_last - E_max.  Queries that
 // fail the proof are flagged for the exact scan.
 template <int ORDER>
-__global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __restrict__ X, int d, int64_t m,
-                                   int kk, int kk2, const int32_t* __restrict__ row_k, int margin_mode,
+__global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __restrict__ X, int64_t n, int d,
+                                   int64_t m, int kk, int kk2, const int32_t* __restrict__ row_k, int margin_mode,
                                    int metric, const uint64_t* __restrict__ keys_in,
                                    uint64_t* __restrict__ keys_out, const float* __restrict__ qn2, float xmax_norm,
                                    float xmax_n2, float alpha, float beta, float gamma, float abs_a,
@@ -693,7 +694,9 @@ __global__ void knn_rescore_kernel(const float* __restrict__ Q, const float* __r
   for (int c0 = 0; c0 < kk2q; c0 += 4) {
     const int c = c0 + grp;
     const uint64_t sk = c < kk2q ? kin[c] : KEY_NONE;
-    const bool real = sk != KEY_NONE;
+    // a key that names no index row (never produced by a completed screen)
+    // is treated as empty, so no read leaves X
+    const bool real = sk != KEY_NONE && (int64_t)key_idx(sk) < n;
     const uint32_t idx = real ? key_idx(sk) : 0u;
     const float* x = X + (int64_t)idx * d;
     const int sd = d & ~7;
@@ -1101,6 +1104,7 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
               ((uint32_t)(QM >> 4) << 24);
     a.status = dev_status;
     a.cancel = cancel_word_device();
+    a.wait_ns = pipeline_wait_ns();
     // the query map addresses rows b0.. through the y coordinate
     CUtensorMap tmQb, tmQl;
     FUELG_TRY(make_map_bf16(&tmQb, qb.as<__nv_bfloat16>() + b0 * dp, mpad - b0, dp, QM));
@@ -1135,13 +1139,13 @@ int knn_tc_topk(const TcIndex* ti, const float* Q32, int64_t m, const float* X32
     const size_t rsm = (size_t)8 * (d + 4) * sizeof(float);
     const unsigned rg = (unsigned)((mcur * 32 + 255) / 256);
     if (order == ORDER_X86)
-      knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2,
+      knn_rescore_kernel<ORDER_X86><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, n, d, mcur, kk, kk2,
                                                               row_k != nullptr ? row_k + b0 : nullptr, mmode, metric,
                                                               kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,
                                                               gamma, abs_a, redo.as<int32_t>(), nredo.as<int32_t>());
     else
-      knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, d, mcur, kk, kk2,
+      knn_rescore_kernel<ORDER_ARM><<<rg, 256, rsm, stream>>>(Q32 + b0 * d, X32, n, d, mcur, kk, kk2,
                                                               row_k != nullptr ? row_k + b0 : nullptr, mmode, metric,
                                                               kept, kept2.as<uint64_t>(),
                                                               qn2.as<float>() + b0, xmax_norm, xmax_n2, alpha, beta,

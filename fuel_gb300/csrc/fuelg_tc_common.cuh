@@ -2,6 +2,7 @@
 // tcgen05 kernels: mbarriers with bounded waits, TMA tile loads, UMMA shared
 // memory descriptors, tcgen05.mma / commit / ld, and tensor-map encoding.
 #pragma once
+#include <cstdlib>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -42,18 +43,32 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false when the barrier did not complete within kWaitNs or the
-// CTA is aborting.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+// Bounded wait: false when the barrier did not complete within limit_ns
+// (default kWaitNs) or the CTA is aborting.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
+                                          uint64_t limit_ns = kWaitNs) {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = globaltimer();
+  // a shortened limit is checked on every retry, the default one every 256
+  const bool short_limit = limit_ns < kWaitNs;
   for (uint32_t it = 1;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((it & 255) == 0) {
+    if ((it & 255) == 0 || short_limit) {
       if (*abort_flag) return false;
-      if (globaltimer() - t0 > kWaitNs) return false;
+      if (globaltimer() - t0 > limit_ns) return false;
     }
   }
+}
+// Limit of the pipeline waits of one launch: kWaitNs, or FUELG_WAIT_LIMIT_NS
+// when set (clamped to [1, kWaitNs]; a short limit makes the waits run out and
+// the kernel take its abort path -- tests use it).  The drain waits that keep a
+// CTA from exiting with copies or MMAs in flight always use kWaitNs.
+inline uint64_t pipeline_wait_ns() {
+  if (const char* e = getenv("FUELG_WAIT_LIMIT_NS")) {
+    const long long v = atoll(e);
+    if (v >= 1) return (uint64_t)v < kWaitNs ? (uint64_t)v : kWaitNs;
+  }
+  return kWaitNs;
 }
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
   asm volatile(
