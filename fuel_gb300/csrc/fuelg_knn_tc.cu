@@ -536,7 +536,7 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
           for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
           tmem_ld_wait();
           // shifted screen values f = |x|^2 - 2 q.x (in place) and each group's
-          // minimum as a 4-level tree (short dependency chains, four groups interleaved)
+          // minimum (short dependency chains, four groups interleaved)
           float mnh[4];
 #pragma unroll
           for (int h = 0; h < 4; h++) {
@@ -544,17 +544,18 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
 #pragma unroll
             for (int v = 0; v < 4; v++) {
               const float4 q4 = n4[v];
-              r[h][4 * v] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v]), q4.x));
-              r[h][4 * v + 1] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 1]), q4.y));
-              r[h][4 * v + 2] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 2]), q4.z));
-              r[h][4 * v + 3] = __float_as_uint(fmaf(-2.0f, __uint_as_float(r[h][4 * v + 3]), q4.w));
+              // f = fma(-2, q.x, |x|^2), two columns per paired instruction
+              fma2_rn(r[h][4 * v], r[h][4 * v + 1], -2.0f, q4.x, q4.y);
+              fma2_rn(r[h][4 * v + 2], r[h][4 * v + 3], -2.0f, q4.z, q4.w);
             }
-            float m8[8];
+            // minimum of the 16 columns with three-input minima (16 -> 6 -> 2 -> 1)
+            float m6[6];
 #pragma unroll
-            for (int j = 0; j < 8; j++) m8[j] = fminf(__uint_as_float(r[h][2 * j]), __uint_as_float(r[h][2 * j + 1]));
-#pragma unroll
-            for (int j = 0; j < 4; j++) m8[j] = fminf(m8[2 * j], m8[2 * j + 1]);
-            mnh[h] = fminf(fminf(m8[0], m8[1]), fminf(m8[2], m8[3]));
+            for (int j = 0; j < 5; j++)
+              m6[j] = min3_f32(__uint_as_float(r[h][3 * j]), __uint_as_float(r[h][3 * j + 1]),
+                               __uint_as_float(r[h][3 * j + 2]));
+            m6[5] = __uint_as_float(r[h][15]);
+            mnh[h] = fminf(min3_f32(m6[0], m6[1], m6[2]), min3_f32(m6[3], m6[4], m6[5]));
           }
 #pragma unroll
           for (int h = 0; h < 4; h++) {

@@ -43,6 +43,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// Two IEEE fused multiply-adds in one paired instruction: (a0, a1) <-
+// (fma(a0, b, c0), fma(a1, b, c1)).  Each half is exactly the scalar fmaf.
+__device__ __forceinline__ void fma2_rn(uint32_t& a0, uint32_t& a1, float b, float c0, float c1) {
+  unsigned long long x, y, z;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "r"(a0), "r"(a1));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(y) : "f"(b), "f"(b));
+  asm("mov.b64 %0, {%1, %2};" : "=l"(z) : "f"(c0), "f"(c1));
+  asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(z) : "l"(x), "l"(y));
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(a0), "=r"(a1) : "l"(z));
+}
+// Smallest of three floats in one instruction (a NaN operand is ignored, as
+// fminf ignores it).
+__device__ __forceinline__ float min3_f32(float a, float b, float c) {
+  float r;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Bounded wait: false when the barrier did not complete within limit_ns
 // (default kWaitNs) or the CTA is aborting.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
