@@ -360,6 +360,7 @@ constexpr int kTcRows = 128;
 struct BTcArgs {
   const int32_t* tcp;         // problem ids served here
   const int32_t* item_begin;  // [ntc + 1] first 128-row item of each
+  const int64_t* cta_begin;   // [grid + 1] first item of each CTA (ranges of equal estimated cost)
   int ntc, items;
   float alpha;                // operand + accumulation error per |x||c|
   int* status;
@@ -387,35 +388,72 @@ __device__ __forceinline__ float norm2_blocked(F v, int d) {
   return ((p[0] + p[1]) + (p[2] + p[3])) + ((p[4] + p[5]) + (p[6] + p[7]));
 }
 
+// Warp-specialised persistent screen over a list of 128-row items:
+//   warps 0-3  loaders: item rows -> BF16 hi / lo tile (SW128) and |x|^2, one
+//              row per thread, into one of two A buffers; on a problem change
+//              they also stage the problem's centres (hi / lo, SW128) and
+//              norms into one of two centre slots
+//   warp 4     TMEM owner; lane 0 issues the three products per K step
+//              (x_hi c_hi + x_hi c_lo + x_lo c_hi) into one of two 256-column
+//              accumulators and commits
+//   warps 5-8  epilogue: screen, labels, sums of changed rows
+// so the loads and conversions of item t+1, the MMAs and the epilogue of item
+// t overlap.  Barriers: a_full[b] (128 loader arrivals), acc_full[b] (the MMA
+// commit), item_done[b] (128 epilogue arrivals: A[b], TMEM[b], the item's
+// metadata and its centre slot are free again).  Every wait is bounded.
+constexpr int kTcThreads = 288;
+constexpr uint32_t kTcA = 32768;        // one A buffer: hi 16 KB + lo 16 KB
+constexpr uint32_t kTcB = 65536;        // one centre slot: hi 32 KB + lo 32 KB (256 centres)
+constexpr uint32_t kTcSmall = 2 * kTcA + 2 * kTcB;
+// + norms (2 x 2 x 256 floats), maxima (4), row norms (2 x 128), metadata (2 x 16 B),
+// 7 mbarriers, TMEM address and abort word, 1 KB alignment
+constexpr size_t kTcSmem = 1024 + kTcSmall + 4 * 2 * 2 * 256 + 4 * 4 + 4 * 2 * 128 + 16 * 2 + 8 * 7 + 8 + 64;
+
+// Every loader thread (warps 0-3, named barrier 1) learns whether all of
+// them passed `v`.
+__device__ __forceinline__ bool loaders_all(bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, 128, q;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(r)
+      : "r"((uint32_t)v)
+      : "memory");
+  return r != 0;
+}
+
 template <int KIND, int ORDER>
-__global__ void __launch_bounds__(kTcRows, 2) batched_tc_assign_kernel(
+__global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
     const BProb* __restrict__ probs, BTcArgs ta, const float* __restrict__ X, const float* __restrict__ C,
     int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs, int32_t* __restrict__ counts,
     int32_t* __restrict__ pchg, int first) {
   extern __shared__ __align__(1024) unsigned char smem_t[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_t) + 1023) & ~(uintptr_t)1023);
-  unsigned char* sAh = base;                 // [128 rows][64] bf16, SW128
-  unsigned char* sAl = base + 16384;
-  unsigned char* sBh = base + 32768;         // [256 centres][64] bf16, SW128
-  unsigned char* sBl = base + 65536;
-  float* cn2 = reinterpret_cast<float*>(base + 98304);  // [256] |c|^2
-  float* cn = cn2 + 256;                                 // [256] |c|
-  float* xn2 = cn + 256;                                 // [128] |x|^2
-  float* cmax = xn2 + 128;                               // [2] max |c|^2, max |c| of the problem
-  uint64_t* bar = reinterpret_cast<uint64_t*>(cmax + 2);
-  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bar + 1);
-  int* s_flag = reinterpret_cast<int*>(tmem_holder + 1);  // [0] change count, [1] abort
-  const int tid = threadIdx.x, warp = tid >> 5;
+  float* cn2s = reinterpret_cast<float*>(base + kTcSmall);  // [2 slots][256] |c|^2
+  float* cns = cn2s + 2 * 256;                               // [2 slots][256] |c|
+  float* cmaxs = cns + 2 * 256;                              // [2 slots][2] max |c|^2 (bits), spare
+  float* xn2s = cmaxs + 4;                                   // [2 buffers][128] |x|^2
+  int4* meta = reinterpret_cast<int4*>(xn2s + 2 * 128);     // [2 buffers] {problem, slot, first row, kp}
+  uint64_t* a_full = reinterpret_cast<uint64_t*>(meta + 2);
+  uint64_t* acc_full = a_full + 2;
+  uint64_t* item_done = acc_full + 2;
+  uint64_t* fin = item_done + 2;
+  uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    tcx::mbar_init(bar, 1);
-    s_flag[0] = 0;
-    s_flag[1] = 0;
+    for (int b = 0; b < 2; b++) {
+      tcx::mbar_init(&a_full[b], kTcRows);
+      tcx::mbar_init(&acc_full[b], 1);
+      tcx::mbar_init(&item_done[b], kTcRows);
+    }
+    tcx::mbar_init(fin, 1);
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 4) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(tcx::smem_u32(tmem_holder)),
-                 "r"(256)
+                 "r"(512)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -423,22 +461,12 @@ __global__ void __launch_bounds__(kTcRows, 2) batched_tc_assign_kernel(
   __syncthreads();
   tcx::tc_fence_after();
   const uint32_t tmem = *tmem_holder;
-  const int64_t it0 = (int64_t)ta.items * blockIdx.x / gridDim.x;
-  const int64_t it1 = (int64_t)ta.items * (blockIdx.x + 1) / gridDim.x;
-  const double u24 = 5.9604644775390625e-08;
-  int q = -1, p = -1, kp = 0;
-  BProb pr{};
-  float beta = 0.0f, gamma = 0.0f;
-  uint32_t phase = 0;
-  auto flush_chg = [&]() {
-    __syncthreads();
-    if (tid == 0 && p >= 0 && s_flag[0]) atomicAdd(&pchg[p], s_flag[0]);
-    __syncthreads();
-    if (tid == 0) s_flag[0] = 0;
-  };
-  for (int64_t item = it0; item < it1; item++) {
-    if (q < 0 || (q + 1 < ta.ntc && item >= ta.item_begin[q + 1])) {
-      flush_chg();
+  // this CTA's items: a contiguous range of equal estimated cost
+  const int64_t it0 = ta.cta_begin[blockIdx.x], it1 = ta.cta_begin[blockIdx.x + 1];
+  const int64_t nlt = it1 - it0;
+  auto problem_of = [&](int64_t item, int q0) {
+    int q = q0 < 0 ? 0 : q0;
+    if (q0 < 0 || item >= ta.item_begin[q + 1]) {
       int lo = 0, hi = ta.ntc;
       while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
@@ -446,13 +474,37 @@ __global__ void __launch_bounds__(kTcRows, 2) batched_tc_assign_kernel(
         else hi = mid;
       }
       q = lo;
-      p = ta.tcp[q];
-      pr = probs[p];
-      kp = (pr.k + 15) & ~15;
-      beta = (float)(((pr.d + 7) / 8 + 3 + 9) * u24 * 1.01);
-      gamma = (float)((pr.d + 4) * u24 * 1.01);
-      if (pr.active) {
-        // centres -> BF16 hi / lo in the SW128 layout (zero padded), FP32 norms
+    }
+    return q;
+  };
+
+  if (warp < 4) {
+    // ---- loaders ----------------------------------------------------------
+    int q = -1, cur_p = -1, slot = 1;
+    for (int64_t lt = 0; lt < nlt; lt++) {
+      const int b = (int)(lt & 1);
+      const uint32_t ph = (uint32_t)((lt >> 1) & 1);
+      // item lt-2 fully retired: its A buffer, accumulator, metadata and slot.
+      // The loaders leave together (a vote on their named barrier), so the
+      // barrier of a problem change below never waits for a loader that left.
+      bool ok = !*abort_flag && tcx::mbar_wait(&item_done[b], ph ^ 1u, abort_flag);
+      if (!ok && !*abort_flag) atomicOr(ta.status, DEV_TIMEOUT);
+      if (!loaders_all(ok)) {
+        *abort_flag = 1;
+        break;
+      }
+      const int64_t item = it0 + lt;
+      q = problem_of(item, q);
+      const int p = ta.tcp[q];
+      const BProb pr = probs[p];
+      const int kp = (pr.k + 15) & ~15;
+      if (p != cur_p) {
+        // a new problem: its centres into the other slot (the last item that
+        // used that slot retired before item lt-1 started: see item_done)
+        cur_p = p;
+        slot ^= 1;
+        unsigned char* sBh = base + 2 * kTcA + (uint32_t)slot * kTcB;
+        unsigned char* sBl = sBh + kTcB / 2;
         for (int e = tid; e < kp * 8; e += kTcRows) {
           const int j = e >> 3, ch = e & 7;
           uint32_t hw[4], lw[4];
@@ -471,172 +523,237 @@ __global__ void __launch_bounds__(kTcRows, 2) batched_tc_assign_kernel(
           *reinterpret_cast<uint4*>(sBh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
           *reinterpret_cast<uint4*>(sBl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         }
-        if (tid == 0) cmax[0] = cmax[1] = 0.0f;
-        __syncthreads();
+        if (tid == 0) cmaxs[2 * slot] = 0.0f;
+        asm volatile("bar.sync 1, %0;" ::"n"(kTcRows) : "memory");  // loaders only
         float m2 = 0.0f;
         for (int j = tid; j < pr.k; j += kTcRows) {
           const float* cj = C + pr.c_off + (int64_t)j * pr.d;
           const float v = norm2_blocked([&](int t) { return cj[t]; }, pr.d);
-          cn2[j] = v;
-          cn[j] = sqrtf(v);
+          cn2s[slot * 256 + j] = v;
+          cns[slot * 256 + j] = sqrtf(v);
           m2 = fmaxf(m2, v);
         }
         // non-negative floats order like their bit patterns
-        atomicMax(reinterpret_cast<int*>(cmax), __float_as_int(m2));
-        __syncthreads();
-        if (tid == 0) cmax[1] = sqrtf(cmax[0]);
+        atomicMax(reinterpret_cast<int*>(cmaxs + 2 * slot), __float_as_int(m2));
       }
-      __syncthreads();
-    }
-    if (!pr.active) continue;
-    // rows -> BF16 hi / lo (zero padded), FP32 norms; thread = row
-    const int64_t i = (item - ta.item_begin[q]) * kTcRows + tid;
-    const bool live = i < pr.n;
-    const float* xr = X + pr.x_off + (live ? i : 0) * pr.d;
-    // 8 chunks of 8 values: BF16 hi / lo packed into 16-byte stores at the
-    // swizzled chunk position; |x|^2 accumulated in the blocked order
-    float pn[8];
+      // rows -> BF16 hi / lo (zero padded), FP32 norms; thread = row
+      unsigned char* sAh = base + (uint32_t)b * kTcA;
+      unsigned char* sAl = sAh + kTcA / 2;
+      const int64_t i0 = (item - ta.item_begin[q]) * kTcRows;
+      const int64_t i = i0 + tid;
+      const bool live = pr.active && i < pr.n;
+      const float* xr = X + pr.x_off + (live ? i : 0) * pr.d;
+      float pn[8];
 #pragma unroll
-    for (int l = 0; l < 8; l++) pn[l] = 0.0f;
-    const bool vec = ((pr.d & 3) == 0) && ((pr.x_off & 3) == 0);
-#pragma unroll 2
-    for (int j = 0; j < 8; j++) {
-      float x[8];
-      if (live && vec && 8 * j + 7 < pr.d) {
-        const float4 a4 = __ldg(reinterpret_cast<const float4*>(xr + 8 * j));
-        const float4 b4 = __ldg(reinterpret_cast<const float4*>(xr + 8 * j + 4));
-        x[0] = a4.x, x[1] = a4.y, x[2] = a4.z, x[3] = a4.w, x[4] = b4.x, x[5] = b4.y, x[6] = b4.z, x[7] = b4.w;
+      for (int l = 0; l < 8; l++) pn[l] = 0.0f;
+      const bool vec = ((pr.d & 3) == 0) && ((pr.x_off & 3) == 0);
+      float xv[64];
+      // every load of the row first (one round trip), then the conversions
+      if (live && vec && pr.d == 64) {
+#pragma unroll
+        for (int j = 0; j < 16; j++) {
+          const float4 a4 = __ldg(reinterpret_cast<const float4*>(xr) + j);
+          xv[4 * j] = a4.x, xv[4 * j + 1] = a4.y, xv[4 * j + 2] = a4.z, xv[4 * j + 3] = a4.w;
+        }
+      } else if (live && vec && pr.d == 32) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          const float4 a4 = __ldg(reinterpret_cast<const float4*>(xr) + j);
+          xv[4 * j] = a4.x, xv[4 * j + 1] = a4.y, xv[4 * j + 2] = a4.z, xv[4 * j + 3] = a4.w;
+        }
+#pragma unroll
+        for (int j = 32; j < 64; j++) xv[j] = 0.0f;
       } else {
 #pragma unroll
-        for (int l = 0; l < 8; l++) x[l] = (live && 8 * j + l < pr.d) ? __ldg(xr + 8 * j + l) : 0.0f;
+        for (int j = 0; j < 64; j++) xv[j] = (live && j < pr.d) ? __ldg(xr + j) : 0.0f;
       }
-      uint32_t hw[4], lw[4];
 #pragma unroll
-      for (int l = 0; l < 8; l += 2) {
-        const __nv_bfloat162 h = __floats2bfloat162_rn(x[l], x[l + 1]);
-        const float2 hf = __bfloat1622float2(h);
-        const __nv_bfloat162 lo = __floats2bfloat162_rn(x[l] - hf.x, x[l + 1] - hf.y);
-        hw[l / 2] = *reinterpret_cast<const uint32_t*>(&h);
-        lw[l / 2] = *reinterpret_cast<const uint32_t*>(&lo);
-        pn[l] = fmaf(x[l], x[l], pn[l]);
-        pn[l + 1] = fmaf(x[l + 1], x[l + 1], pn[l + 1]);
+      for (int j = 0; j < 8; j++) {
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int l = 0; l < 8; l += 2) {
+          const float x0 = xv[8 * j + l], x1 = xv[8 * j + l + 1];
+          const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+          const float2 hf = __bfloat1622float2(h);
+          const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+          hw[l / 2] = *reinterpret_cast<const uint32_t*>(&h);
+          lw[l / 2] = *reinterpret_cast<const uint32_t*>(&lo);
+          pn[l] = fmaf(x0, x0, pn[l]);
+          pn[l + 1] = fmaf(x1, x1, pn[l + 1]);
+        }
+        const uint32_t off = (uint32_t)tid * 128u + ((uint32_t)(j ^ (tid & 7)) << 4);
+        *reinterpret_cast<uint4*>(sAh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(sAl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
       }
-      const uint32_t off = (uint32_t)tid * 128u + ((uint32_t)(j ^ (tid & 7)) << 4);
-      *reinterpret_cast<uint4*>(sAh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-      *reinterpret_cast<uint4*>(sAl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+      xn2s[b * 128 + tid] = ((pn[0] + pn[1]) + (pn[2] + pn[3])) + ((pn[4] + pn[5]) + (pn[6] + pn[7]));
+      if (tid == 0) meta[b] = make_int4(p, slot, (int)i0, pr.active ? kp : 0);
+      // generic-proxy smem writes -> visible to the tensor core's async proxy
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tcx::mbar_arrive(&a_full[b]);
     }
-    const float nx = ((pn[0] + pn[1]) + (pn[2] + pn[3])) + ((pn[4] + pn[5]) + (pn[6] + pn[7]));
-    xn2[tid] = nx;
-    // generic-proxy smem writes -> visible to the tensor core's async proxy
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tcx::tc_fence_before();
-    __syncthreads();
-    tcx::tc_fence_after();
-    if (tid == 0) {
-      const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kp >> 3) << 17) |
-                             ((uint32_t)(kTcRows >> 4) << 24);
-      const uint64_t ah = tcx::smem_desc_sw128(tcx::smem_u32(sAh)), al = tcx::smem_desc_sw128(tcx::smem_u32(sAl));
-      const uint64_t bh = tcx::smem_desc_sw128(tcx::smem_u32(sBh)), bl = tcx::smem_desc_sw128(tcx::smem_u32(sBl));
-      // K steps of 16 that hold data (the zero columns past d add nothing)
-      const int nks = (pr.d + 15) >> 4;
+  } else if (warp == 4) {
+    // ---- MMA issuer ---------------------------------------------------------
+    if (lane == 0) {
+      for (int64_t lt = 0; lt < nlt && !*abort_flag; lt++) {
+        const int b = (int)(lt & 1);
+        const uint32_t ph = (uint32_t)((lt >> 1) & 1);
+        if (!tcx::mbar_wait(&a_full[b], ph, abort_flag)) {
+          if (!*abort_flag) atomicOr(ta.status, DEV_TIMEOUT);
+          *abort_flag = 1;
+          break;
+        }
+        tcx::tc_fence_after();
+        const int4 mt = meta[b];
+        const int kp = mt.w;
+        if (kp > 0) {
+          const BProb& pr = probs[mt.x];
+          unsigned char* sAh = base + (uint32_t)b * kTcA;
+          unsigned char* sBh = base + 2 * kTcA + (uint32_t)mt.y * kTcB;
+          const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kp >> 3) << 17) |
+                                 ((uint32_t)(kTcRows >> 4) << 24);
+          const uint64_t ah = tcx::smem_desc_sw128(tcx::smem_u32(sAh));
+          const uint64_t al = tcx::smem_desc_sw128(tcx::smem_u32(sAh + kTcA / 2));
+          const uint64_t bh = tcx::smem_desc_sw128(tcx::smem_u32(sBh));
+          const uint64_t bl = tcx::smem_desc_sw128(tcx::smem_u32(sBh + kTcB / 2));
+          const uint32_t d_tmem = tmem + (uint32_t)b * 256u;
+          // K steps of 16 that hold data (the zero columns past d add nothing)
+          const int nks = (pr.d + 15) >> 4;
 #pragma unroll
-      for (int kk = 0; kk < 4; kk++)
-        if (kk < nks) tcx::umma_bf16(tmem, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : 0u);
+          for (int kk = 0; kk < 4; kk++)
+            if (kk < nks) tcx::umma_bf16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : 0u);
 #pragma unroll
-      for (int kk = 0; kk < 4; kk++)
-        if (kk < nks) tcx::umma_bf16(tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
+          for (int kk = 0; kk < 4; kk++)
+            if (kk < nks) tcx::umma_bf16(d_tmem, ah + 2 * kk, bl + 2 * kk, idesc, 1u);
 #pragma unroll
-      for (int kk = 0; kk < 4; kk++)
-        if (kk < nks) tcx::umma_bf16(tmem, al + 2 * kk, bh + 2 * kk, idesc, 1u);
-      tcx::umma_commit(bar);
+          for (int kk = 0; kk < 4; kk++)
+            if (kk < nks) tcx::umma_bf16(d_tmem, al + 2 * kk, bh + 2 * kk, idesc, 1u);
+        }
+        tcx::umma_commit(&acc_full[b]);
+      }
+      // every MMA issued here has completed before TMEM is freed
+      tcx::umma_commit(fin);
+      volatile int never = 0;
+      if (!tcx::mbar_wait(fin, 0, &never)) atomicOr(ta.status, DEV_TIMEOUT);
     }
-    const bool ok = tcx::mbar_wait(bar, phase, reinterpret_cast<volatile int*>(s_flag + 1));
-    phase ^= 1;
-    if (__syncthreads_or(!ok)) {
-      if (tid == 0) atomicOr(ta.status, DEV_TIMEOUT);
-      break;
-    }
-    tcx::tc_fence_after();
-    // screen: best centre, then every centre whose lower bound reaches its
-    // upper bound; TMEM read 64 columns per wait
-    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
-    const float xl = sqrtf(nx);
-    float best = __int_as_float(0x7f800000);
-    int bj = 0;
-    for (int c0 = 0; c0 < kp; c0 += 64) {
-      uint32_t r[4][16];
+  } else {
+    // ---- epilogue: warp w reads TMEM lanes 32 * (w % 4) .. +32 ---------------
+    const int g = warp & 3;
+    const int row = g * 32 + lane;
+    const double u24 = 5.9604644775390625e-08;
+    for (int64_t lt = 0; lt < nlt; lt++) {
+      const int b = (int)(lt & 1);
+      const uint32_t ph = (uint32_t)((lt >> 1) & 1);
+      bool ok = !*abort_flag && tcx::mbar_wait(&acc_full[b], ph, abort_flag);
+      if (!ok) {
+        if (!*abort_flag) atomicOr(ta.status, DEV_TIMEOUT);
+        *abort_flag = 1;
+      }
+      if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
+      tcx::tc_fence_after();
+      const int4 mt = meta[b];
+      const int p = mt.x, slot = mt.y, kp = mt.w;
+      const BProb pr = probs[p];
+      const float* cn2 = cn2s + slot * 256;
+      const float* cn = cns + slot * 256;
+      const float cmax0 = cmaxs[2 * slot];
+      const float nx = xn2s[b * 128 + row];
+      const int64_t i = (int64_t)mt.z + row;
+      const bool live = kp > 0 && i < pr.n;
+      const float beta = (float)(((pr.d + 7) / 8 + 3 + 9) * u24 * 1.01);
+      const float gamma = (float)((pr.d + 4) * u24 * 1.01);
+      const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)b * 256u;
+      const float xl = sqrtf(nx);
+      float best = __int_as_float(0x7f800000);
+      int bj = 0;
+      bool undecided = false;
+      if (kp > 0) {
+        // screen: best centre, then every centre whose lower bound reaches its
+        // upper bound; TMEM read 64 columns per wait
+        for (int c0 = 0; c0 < kp; c0 += 64) {
+          uint32_t r[4][16];
 #pragma unroll
-      for (int h = 0; h < 4; h++) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
-      tcx::tmem_ld_wait();
+          for (int h = 0; h < 4; h++)
+            if (c0 + 16 * h < kp) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+          tcx::tmem_ld_wait();
 #pragma unroll
-      for (int h = 0; h < 4; h++)
+          for (int h = 0; h < 4; h++)
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int col = c0 + 16 * h + j;
-          if (col < pr.k) {
-            const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
-            if (dt < best) {
-              best = dt;
-              bj = col;
+            for (int j = 0; j < 16; j++) {
+              const int col = c0 + 16 * h + j;
+              if (col < pr.k) {
+                const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
+                if (dt < best) {
+                  best = dt;
+                  bj = col;
+                }
+              }
             }
-          }
         }
-    }
-    const float hi_b = best + (ta.alpha * xl * cn[bj] + beta * (nx + cn2[bj])) * (1.0f + gamma) + gamma * fabsf(best);
-    // columns above T cannot reach hi_b even with the largest error of the
-    // problem (norm maxima); only the others get the exact per-column test
-    const float amax = (ta.alpha * xl * cmax[1] + beta * (nx + cmax[0])) * (1.0f + gamma);
-    const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
-    bool undecided = false;
-    for (int c0 = 0; c0 < kp; c0 += 64) {
-      uint32_t r[4][16];
+        const float hi_b =
+            best + (ta.alpha * xl * cn[bj] + beta * (nx + cn2[bj])) * (1.0f + gamma) + gamma * fabsf(best);
+        // columns above T cannot reach hi_b even with the largest error of the
+        // problem (norm maxima); only the others get the exact per-column test
+        const float amax = (ta.alpha * xl * sqrtf(cmax0) + beta * (nx + cmax0)) * (1.0f + gamma);
+        const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
+        for (int c0 = 0; c0 < kp; c0 += 64) {
+          uint32_t r[4][16];
 #pragma unroll
-      for (int h = 0; h < 4; h++) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
-      tcx::tmem_ld_wait();
+          for (int h = 0; h < 4; h++)
+            if (c0 + 16 * h < kp) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+          tcx::tmem_ld_wait();
 #pragma unroll
-      for (int h = 0; h < 4; h++)
+          for (int h = 0; h < 4; h++)
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const int col = c0 + 16 * h + j;
-          const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col < 256 ? col : 0]);
-          if (col < pr.k && col != bj && (!(T > 0.0f) || !(dt > T))) {
-            const float e = (ta.alpha * xl * cn[col] + beta * (nx + cn2[col])) * (1.0f + gamma) + gamma * fabsf(dt);
-            if (!(dt - e > hi_b)) undecided = true;
-          }
+            for (int j = 0; j < 16; j++) {
+              const int col = c0 + 16 * h + j;
+              if (col < pr.k && col != bj) {
+                const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
+                if (!(T > 0.0f) || !(dt > T)) {
+                  const float e =
+                      (ta.alpha * xl * cn[col] + beta * (nx + cn2[col])) * (1.0f + gamma) + gamma * fabsf(dt);
+                  if (!(dt - e > hi_b)) undecided = true;
+                }
+              }
+            }
         }
-    }
-    tcx::tc_fence_before();
-    int lab = bj;
-    {
-      const unsigned um = __ballot_sync(0xffffffffu, live && undecided);
-      if ((tid & 31) == 0 && um) atomicAdd(ta.undecided, (unsigned long long)__popc(um));
-    }
-    if (live && undecided) {
-      // the exact re-score kernel decides this row
-      const int u = atomicAdd(ta.und_n, 1);
-      ta.und_p[u] = p;
-      ta.und_i[u] = (int32_t)i;
-    }
-    const int old = live ? (first ? -1 : labels[pr.lab_off + i]) : -1;
-    if (live && !undecided && lab != old) {
-      labels[pr.lab_off + i] = lab;
-      if (!first) atomicAdd(&s_flag[0], 1);
-      atomicAdd(&counts[pr.cnt_off + lab], 1);
-      if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
-      for (int t = 0; t < pr.d; t++) {
-        const float xv = __ldg(xr + t);
-        add_coord(limbs + pr.limb_off + ((int64_t)lab * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
-        if (old >= 0) add_coord(limbs + pr.limb_off + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+      }
+      // the item's accumulator, tile, metadata and centre slot are no longer read
+      tcx::tc_fence_before();
+      tcx::mbar_arrive(&item_done[b]);
+      if (kp == 0) continue;
+      const int lab = bj;
+      {
+        const unsigned um = __ballot_sync(0xffffffffu, live && undecided);
+        if (lane == 0 && um) atomicAdd(ta.undecided, (unsigned long long)__popc(um));
+      }
+      if (live && undecided) {
+        // the exact re-score kernel decides this row
+        const int u = atomicAdd(ta.und_n, 1);
+        ta.und_p[u] = p;
+        ta.und_i[u] = (int32_t)i;
+      }
+      const int old = live ? (first ? -1 : labels[pr.lab_off + i]) : -1;
+      const bool chg = live && !undecided && lab != old;
+      const unsigned cm = __ballot_sync(0xffffffffu, chg);
+      if (!first && lane == 0 && cm) atomicAdd(&pchg[p], __popc(cm));
+      if (chg) {
+        labels[pr.lab_off + i] = lab;
+        atomicAdd(&counts[pr.cnt_off + lab], 1);
+        if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
+        const float* xr = X + pr.x_off + i * pr.d;
+        for (int t = 0; t < pr.d; t++) {
+          const float xv = __ldg(xr + t);
+          add_coord(limbs + pr.limb_off + ((int64_t)lab * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
+          if (old >= 0) add_coord(limbs + pr.limb_off + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+        }
       }
     }
-    __syncthreads();  // TMEM and the A tile are reused by the next item
   }
-  flush_chg();
   tcx::tc_fence_before();
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 4) {
     tcx::tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
   }
 }
 
@@ -828,7 +945,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     return ST_ENOTSUP;
   }
   DevBuf dX, dC, dLab, dCnt, dOff, dRb, dRange, dProbs, dKdb, dPchg, dConv, dLast, dIter, dInert, dLimbs, dTcp,
-      dTcb, dSt, dUnd;
+      dTcb, dSt, dUnd, dCtaB;
   FUELG_TRY(dX.alloc(sizeof(float) * xs));
   FUELG_TRY(dC.alloc(sizeof(float) * cs));
   FUELG_TRY(dLab.alloc(sizeof(int32_t) * ls));
@@ -913,7 +1030,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
                                          : batched_tc_assign_kernel<KIND_PAIRWISE, ORDER_ARM>;
   auto t_iter = order == FUELG_ORDER_X86 ? batched_tc_assign_kernel<KIND_SQDIST, ORDER_X86>
                                          : batched_tc_assign_kernel<KIND_SQDIST, ORDER_ARM>;
-  const size_t tsmem = 1024 + 98304 + sizeof(float) * (256 * 2 + 128 + 2) + 64;
+  const size_t tsmem = kTcSmem;
   FUELG_CUDA(cudaFuncSetAttribute(t_init, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
   FUELG_CUDA(cudaFuncSetAttribute(t_iter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsmem));
   BTcArgs ta{};
@@ -953,7 +1070,35 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     if (it != g_tuned.end()) bps = it->second.blocks_per_sm;
   }
   auto grid_for = [&](int b) { return (unsigned)std::max<int64_t>(1, std::min<int64_t>(items, (int64_t)sms * b)); };
-  const unsigned tc_grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tc_items, (int64_t)sms * 2));
+  // one persistent screen CTA per SM, each over a contiguous range of items of
+  // equal estimated cost (row loads + an epilogue that grows with the centres)
+  const unsigned tc_grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(tc_items, (int64_t)sms));
+  {
+    std::vector<double> icost(ntc);
+    double total = 0.0;
+    for (int q = 0; q < ntc; q++) {
+      const int kp = (hp[tcp[q]].k + 15) & ~15;
+      icost[q] = 64.0 + 2.0 * kp;
+      total += icost[q] * (tc_begin[q + 1] - tc_begin[q]);
+    }
+    std::vector<int64_t> cb(tc_grid + 1, 0);
+    cb[tc_grid] = tc_items;
+    double acc = 0.0;
+    int q = 0;
+    for (unsigned c = 1; c < tc_grid; c++) {
+      const double target = total * c / tc_grid;
+      while (q < ntc && acc + icost[q] * (tc_begin[q + 1] - tc_begin[q]) < target) {
+        acc += icost[q] * (tc_begin[q + 1] - tc_begin[q]);
+        q++;
+      }
+      int64_t at = tc_items;
+      if (q < ntc) at = std::min<int64_t>(tc_begin[q + 1], tc_begin[q] + (int64_t)std::ceil((target - acc) / icost[q]));
+      cb[c] = std::max(cb[c - 1], at);
+    }
+    FUELG_TRY(dCtaB.alloc(sizeof(int64_t) * (tc_grid + 1)));
+    FUELG_CUDA(cudaMemcpyAsync(dCtaB.p, cb.data(), sizeof(int64_t) * (tc_grid + 1), cudaMemcpyHostToDevice, s));
+    ta.cta_begin = dCtaB.as<int64_t>();
+  }
   const unsigned mean_grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((kd + 255) / 256, (int64_t)sms * 8));
   const int fixed = (flags & FUELG_LLOYD_FIXED_ITERS) ? 1 : 0;
   (void)fixed;  // every pass runs; the reported count follows the changed == 0 stop unless fixed
@@ -971,7 +1116,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
       note_launch();
     }
     if (tc_items > 0) {
-      (first ? t_init : t_iter)<<<tc_grid, kTcRows, tsmem, s>>>(dProbs.as<BProb>(), ta, dX.as<float>(),
+      (first ? t_init : t_iter)<<<tc_grid, kTcThreads, tsmem, s>>>(dProbs.as<BProb>(), ta, dX.as<float>(),
                                                                  dC.as<float>(), dLab.as<int32_t>(),
                                                                  dLimbs.as<unsigned long long>(),
                                                                  dCnt.as<int32_t>(), dPchg.as<int32_t>(),
