@@ -668,7 +668,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       bool undecided = false;
       if (kp > 0) {
         // screen: best centre, then every centre whose lower bound reaches its
-        // upper bound; TMEM read 64 columns per wait
+        // upper bound; TMEM read 64 columns per wait.  The best centre is the
+        // first minimum (strict <), kept as four independent running minima over
+        // the columns of each residue mod 4 and merged by (distance, column):
+        // the same centre as one scan in column order, with a quarter of the
+        // dependency chain.
+        float b4[4] = {best, best, best, best};
+        int j4[4] = {0, 0, 0, 0};
         for (int c0 = 0; c0 < kp; c0 += 64) {
           uint32_t r[4][16];
 #pragma unroll
@@ -676,19 +682,27 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
             if (c0 + 16 * h < kp) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
           tcx::tmem_ld_wait();
 #pragma unroll
+          for (int h = 0; h < 4; h++) tcx::tmem_regs_ready(r[h]);
+#pragma unroll
           for (int h = 0; h < 4; h++)
 #pragma unroll
             for (int j = 0; j < 16; j++) {
               const int col = c0 + 16 * h + j;
               if (col < pr.k) {
                 const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
-                if (dt < best) {
-                  best = dt;
-                  bj = col;
+                if (dt < b4[j & 3]) {
+                  b4[j & 3] = dt;
+                  j4[j & 3] = col;
                 }
               }
             }
         }
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (b4[u] < best || (b4[u] == best && j4[u] < bj)) {
+            best = b4[u];
+            bj = j4[u];
+          }
         const float hi_b =
             best + (ta.alpha * xl * cn[bj] + beta * (nx + cn2[bj])) * (1.0f + gamma) + gamma * fabsf(best);
         // columns above T cannot reach hi_b even with the largest error of the
@@ -701,6 +715,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
           for (int h = 0; h < 4; h++)
             if (c0 + 16 * h < kp) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
           tcx::tmem_ld_wait();
+#pragma unroll
+          for (int h = 0; h < 4; h++) tcx::tmem_regs_ready(r[h]);
 #pragma unroll
           for (int h = 0; h < 4; h++)
 #pragma unroll
@@ -740,11 +756,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         labels[pr.lab_off + i] = lab;
         atomicAdd(&counts[pr.cnt_off + lab], 1);
         if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
-        const float* xr = X + pr.x_off + i * pr.d;
-        for (int t = 0; t < pr.d; t++) {
+      }
+      // the changed rows' coordinates into the exact sums, one row at a time by
+      // the whole warp: the lanes take consecutive coordinates, so each atomic
+      // instruction covers adjacent counters of one cluster
+      unsigned pend = cm;
+      while (pend) {
+        const int src = __ffs(pend) - 1;
+        pend &= pend - 1;
+        const int64_t is = __shfl_sync(0xffffffffu, i, src);
+        const int ls = __shfl_sync(0xffffffffu, lab, src);
+        const int os = __shfl_sync(0xffffffffu, old, src);
+        const float* xr = X + pr.x_off + is * pr.d;
+        for (int t = lane; t < pr.d; t += 32) {
           const float xv = __ldg(xr + t);
-          add_coord(limbs + pr.limb_off + ((int64_t)lab * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
-          if (old >= 0) add_coord(limbs + pr.limb_off + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+          add_coord(limbs + pr.limb_off + ((int64_t)ls * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
+          if (os >= 0) add_coord(limbs + pr.limb_off + ((int64_t)os * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
         }
       }
     }

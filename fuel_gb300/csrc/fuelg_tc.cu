@@ -447,6 +447,11 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             }
           tmem_ld_wait();
 #pragma unroll
+          for (int h = 0; h < 2; h++) {
+            tmem_regs_ready(rh[h]);
+            if (BLO && a.sep_lo) tmem_regs_ready(rl[h]);
+          }
+#pragma unroll
           for (int h = 0; h < 2; h++)
 #pragma unroll
             for (int j = 0; j < 16; j++) {
