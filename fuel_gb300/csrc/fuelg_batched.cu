@@ -389,25 +389,38 @@ __device__ __forceinline__ float norm2_blocked(F v, int d) {
 }
 
 // Warp-specialised persistent screen over a list of 128-row items:
-//   warps 0-3  loaders: item rows -> BF16 hi / lo tile (SW128) and |x|^2, one
-//              row per thread, into one of two A buffers; on a problem change
-//              they also stage the problem's centres (hi / lo, SW128) and
-//              norms into one of two centre slots
+//   warps 0-3  loaders: thread 0 copies the NEXT item's rows (contiguous in
+//              memory) into one of two staging buffers with one bulk copy; all
+//              128 convert the current item's rows from staging into BF16 hi /
+//              lo (SW128) and |x|^2, one row per thread, into one of two A
+//              buffers; on a problem change they stage the problem's centres
+//              (hi / lo, SW128), norms and parameters
 //   warp 4     TMEM owner; lane 0 issues the three products per K step
 //              (x_hi c_hi + x_hi c_lo + x_lo c_hi) into one of two 256-column
 //              accumulators and commits
 //   warps 5-8  epilogue: screen, labels, sums of changed rows
-// so the loads and conversions of item t+1, the MMAs and the epilogue of item
-// t overlap.  Barriers: a_full[b] (128 loader arrivals), acc_full[b] (the MMA
-// commit), item_done[b] (128 epilogue arrivals: A[b], TMEM[b], the item's
-// metadata and its centre slot are free again).  Every wait is bounded.
+// so the row copy of item t+1, its conversion, the MMAs and the epilogue of
+// item t overlap.  Barriers: stage_full[s] (bulk copy bytes), a_full[b] (128
+// loader arrivals), acc_full[b] (the MMA commit), item_done[b] (128 epilogue
+// arrivals: A[b], TMEM[b] and the item's parameters are free again).  On a
+// problem change the loaders first wait for the previous item to retire, so
+// the single centre buffer is never replaced under a reader.  Every wait is
+// bounded.
 constexpr int kTcThreads = 288;
-constexpr uint32_t kTcA = 32768;        // one A buffer: hi 16 KB + lo 16 KB
-constexpr uint32_t kTcB = 65536;        // one centre slot: hi 32 KB + lo 32 KB (256 centres)
-constexpr uint32_t kTcSmall = 2 * kTcA + 2 * kTcB;
-// + norms (2 x 2 x 256 floats), maxima (4), row norms (2 x 128), metadata (2 x 16 B),
-// 7 mbarriers, TMEM address and abort word, 1 KB alignment
-constexpr size_t kTcSmem = 1024 + kTcSmall + 4 * 2 * 2 * 256 + 4 * 4 + 4 * 2 * 128 + 16 * 2 + 8 * 7 + 8 + 64;
+constexpr uint32_t kTcA = 32768;   // one A buffer: hi 16 KB + lo 16 KB
+constexpr uint32_t kTcB = 65536;   // the centre buffer: hi 32 KB + lo 32 KB (256 centres)
+constexpr uint32_t kTcS = 32768;   // one staging buffer: 128 rows x 64 f32
+constexpr uint32_t kTcOffB = 2 * kTcA, kTcOffS = kTcOffB + kTcB, kTcSmall = kTcOffS + 2 * kTcS;
+
+struct ItemMeta {  // one item's problem parameters, written by the loaders
+  int64_t n, lab_off, limb_off, x_off;
+  int32_t p, i0, kp, d, k, L, e_lo, cnt_off;
+};
+
+// + norms (2 x 256 floats), maxima (4), row norms (2 x 128), metadata (2), 9 mbarriers,
+// TMEM address and abort word, 1 KB alignment
+constexpr size_t kTcSmem =
+    1024 + kTcSmall + 4 * 2 * 256 + 4 * 4 + 4 * 2 * 128 + sizeof(ItemMeta) * 2 + 8 * 9 + 8 + 64;
 
 // Every loader thread (warps 0-3, named barrier 1) learns whether all of
 // them passed `v`.
@@ -429,12 +442,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
   extern __shared__ __align__(1024) unsigned char smem_t[];
   unsigned char* base =
       reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_t) + 1023) & ~(uintptr_t)1023);
-  float* cn2s = reinterpret_cast<float*>(base + kTcSmall);  // [2 slots][256] |c|^2
-  float* cns = cn2s + 2 * 256;                               // [2 slots][256] |c|
-  float* cmaxs = cns + 2 * 256;                              // [2 slots][2] max |c|^2 (bits), spare
+  unsigned char* sBh = base + kTcOffB;
+  unsigned char* sBl = sBh + kTcB / 2;
+  float* cn2s = reinterpret_cast<float*>(base + kTcSmall);  // [256] |c|^2 of the staged problem
+  float* cns = cn2s + 256;                                   // [256] |c|
+  float* cmaxs = cns + 256;                                  // [0] max |c|^2 (bits), spare
   float* xn2s = cmaxs + 4;                                   // [2 buffers][128] |x|^2
-  int4* meta = reinterpret_cast<int4*>(xn2s + 2 * 128);     // [2 buffers] {problem, slot, first row, kp}
-  uint64_t* a_full = reinterpret_cast<uint64_t*>(meta + 2);
+  ItemMeta* meta = reinterpret_cast<ItemMeta*>(xn2s + 2 * 128);
+  uint64_t* stage_full = reinterpret_cast<uint64_t*>(meta + 2);
+  uint64_t* a_full = stage_full + 2;
   uint64_t* acc_full = a_full + 2;
   uint64_t* item_done = acc_full + 2;
   uint64_t* fin = item_done + 2;
@@ -443,6 +459,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
     for (int b = 0; b < 2; b++) {
+      tcx::mbar_init(&stage_full[b], 1);
       tcx::mbar_init(&a_full[b], kTcRows);
       tcx::mbar_init(&acc_full[b], 1);
       tcx::mbar_init(&item_done[b], kTcRows);
@@ -477,16 +494,37 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
     }
     return q;
   };
+  // bytes of an item's rows that one bulk copy brings in (0: the direct-load path)
+  auto bulk_bytes = [&](const BProb& pr, int64_t i0) -> uint32_t {
+    if (!pr.active || (pr.d & 3) != 0 || (pr.x_off & 3) != 0 || pr.d > 64) return 0u;
+    const int64_t rows = min((int64_t)kTcRows, pr.n - i0);
+    return (uint32_t)(rows * pr.d * 4);
+  };
 
   if (warp < 4) {
     // ---- loaders ----------------------------------------------------------
-    int q = -1, cur_p = -1, slot = 1;
+    int q = -1, cur_p = -1, qn = -1;
+    int issued[2] = {0, 0};  // copies (or plain arrivals) armed per staging buffer, thread 0
+    // the first item's rows
+    if (tid == 0 && nlt > 0) {
+      issued[0] = 1;
+      qn = problem_of(it0, -1);
+      const BProb pn = probs[ta.tcp[qn]];
+      const int64_t i0n = (it0 - ta.item_begin[qn]) * kTcRows;
+      const uint32_t by = bulk_bytes(pn, i0n);
+      if (by) {
+        tcx::mbar_expect_tx(&stage_full[0], by);
+        tcx::bulk_load(base + kTcOffS, X + pn.x_off + i0n * pn.d, by, &stage_full[0]);
+      } else {
+        tcx::mbar_arrive(&stage_full[0]);
+      }
+    }
     for (int64_t lt = 0; lt < nlt; lt++) {
       const int b = (int)(lt & 1);
       const uint32_t ph = (uint32_t)((lt >> 1) & 1);
-      // item lt-2 fully retired: its A buffer, accumulator, metadata and slot.
+      // item lt-2 retired: its A buffer, accumulator and parameters are free.
       // The loaders leave together (a vote on their named barrier), so the
-      // barrier of a problem change below never waits for a loader that left.
+      // barriers below never wait for a loader that left.
       bool ok = !*abort_flag && tcx::mbar_wait(&item_done[b], ph ^ 1u, abort_flag);
       if (!ok && !*abort_flag) atomicOr(ta.status, DEV_TIMEOUT);
       if (!loaders_all(ok)) {
@@ -498,13 +536,19 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       const int p = ta.tcp[q];
       const BProb pr = probs[p];
       const int kp = (pr.k + 15) & ~15;
+      const int64_t i0 = (item - ta.item_begin[q]) * kTcRows;
       if (p != cur_p) {
-        // a new problem: its centres into the other slot (the last item that
-        // used that slot retired before item lt-1 started: see item_done)
+        // a new problem: the previous item must retire before its centres go
+        if (lt > 0) {
+          const int pb = (int)((lt - 1) & 1);
+          ok = !*abort_flag && tcx::mbar_wait(&item_done[pb], (uint32_t)(((lt - 1) >> 1) & 1), abort_flag);
+          if (!ok && !*abort_flag) atomicOr(ta.status, DEV_TIMEOUT);
+          if (!loaders_all(ok)) {
+            *abort_flag = 1;
+            break;
+          }
+        }
         cur_p = p;
-        slot ^= 1;
-        unsigned char* sBh = base + 2 * kTcA + (uint32_t)slot * kTcB;
-        unsigned char* sBl = sBh + kTcB / 2;
         for (int e = tid; e < kp * 8; e += kTcRows) {
           const int j = e >> 3, ch = e & 7;
           uint32_t hw[4], lw[4];
@@ -523,73 +567,117 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
           *reinterpret_cast<uint4*>(sBh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
           *reinterpret_cast<uint4*>(sBl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
         }
-        if (tid == 0) cmaxs[2 * slot] = 0.0f;
+        if (tid == 0) cmaxs[0] = 0.0f;
         asm volatile("bar.sync 1, %0;" ::"n"(kTcRows) : "memory");  // loaders only
         float m2 = 0.0f;
-        for (int j = tid; j < pr.k; j += kTcRows) {
-          const float* cj = C + pr.c_off + (int64_t)j * pr.d;
-          const float v = norm2_blocked([&](int t) { return cj[t]; }, pr.d);
-          cn2s[slot * 256 + j] = v;
-          cns[slot * 256 + j] = sqrtf(v);
+        for (int j = tid; j < 256; j += kTcRows) {
+          float v = 0.0f;
+          if (j < pr.k) {
+            const float* cj = C + pr.c_off + (int64_t)j * pr.d;
+            v = norm2_blocked([&](int t) { return cj[t]; }, pr.d);
+          }
+          cn2s[j] = v;  // zero past k: the epilogue reads them four at a time
+          cns[j] = sqrtf(v);
           m2 = fmaxf(m2, v);
         }
         // non-negative floats order like their bit patterns
-        atomicMax(reinterpret_cast<int*>(cmaxs + 2 * slot), __float_as_int(m2));
+        atomicMax(reinterpret_cast<int*>(cmaxs), __float_as_int(m2));
       }
-      // rows -> BF16 hi / lo (zero padded), FP32 norms; thread = row
+      // the next item's rows into the other staging buffer: its previous
+      // contents (item lt-1) were converted before every loader passed the
+      // vote above
+      if (tid == 0 && lt + 1 < nlt) {
+        const int s = (int)((lt + 1) & 1);
+        issued[s]++;
+        qn = problem_of(item + 1, qn);
+        const BProb pn = probs[ta.tcp[qn]];
+        const int64_t i0n = (item + 1 - ta.item_begin[qn]) * kTcRows;
+        const uint32_t by = bulk_bytes(pn, i0n);
+        if (by) {
+          tcx::mbar_expect_tx(&stage_full[s], by);
+          tcx::bulk_load(base + kTcOffS + (uint32_t)s * kTcS, X + pn.x_off + i0n * pn.d, by, &stage_full[s]);
+        } else {
+          tcx::mbar_arrive(&stage_full[s]);
+        }
+      }
+      // this item's rows -> BF16 hi / lo (zero padded), FP32 norms; thread = row
       unsigned char* sAh = base + (uint32_t)b * kTcA;
       unsigned char* sAl = sAh + kTcA / 2;
-      const int64_t i0 = (item - ta.item_begin[q]) * kTcRows;
       const int64_t i = i0 + tid;
       const bool live = pr.active && i < pr.n;
+      ok = !*abort_flag && tcx::mbar_wait(&stage_full[b], ph, abort_flag);
+      if (!ok && !*abort_flag) atomicOr(ta.status, DEV_TIMEOUT);
+      if (!loaders_all(ok)) {
+        *abort_flag = 1;
+        break;
+      }
+      const bool bulk = bulk_bytes(pr, i0) != 0;
+      const float* srow = reinterpret_cast<const float*>(base + kTcOffS + (uint32_t)b * kTcS) + tid * pr.d;
       const float* xr = X + pr.x_off + (live ? i : 0) * pr.d;
       float pn[8];
 #pragma unroll
       for (int l = 0; l < 8; l++) pn[l] = 0.0f;
-      const bool vec = ((pr.d & 3) == 0) && ((pr.x_off & 3) == 0);
-      float xv[64];
-      // every load of the row first (one round trip), then the conversions
-      if (live && vec && pr.d == 64) {
+      // chunks of 8 values in a per-row rotated order (row t starts at chunk
+      // t & 7), so the staging reads of a warp spread over the banks; the
+      // norm keeps its 8 interleaved chains of ceil(d/8) terms and 3-level tree
+#pragma unroll 2
+      for (int jj = 0; jj < 8; jj++) {
+        const int j = (jj + tid) & 7;
+        float x[8];
+        if (live && bulk && 8 * j + 7 < pr.d) {
+          const float4 a4 = *reinterpret_cast<const float4*>(srow + 8 * j);
+          const float4 b4 = *reinterpret_cast<const float4*>(srow + 8 * j + 4);
+          x[0] = a4.x, x[1] = a4.y, x[2] = a4.z, x[3] = a4.w, x[4] = b4.x, x[5] = b4.y, x[6] = b4.z, x[7] = b4.w;
+        } else if (live && bulk) {
 #pragma unroll
-        for (int j = 0; j < 16; j++) {
-          const float4 a4 = __ldg(reinterpret_cast<const float4*>(xr) + j);
-          xv[4 * j] = a4.x, xv[4 * j + 1] = a4.y, xv[4 * j + 2] = a4.z, xv[4 * j + 3] = a4.w;
+          for (int l = 0; l < 8; l++) x[l] = 8 * j + l < pr.d ? srow[8 * j + l] : 0.0f;
+        } else {
+#pragma unroll
+          for (int l = 0; l < 8; l++) x[l] = (live && 8 * j + l < pr.d) ? __ldg(xr + 8 * j + l) : 0.0f;
         }
-      } else if (live && vec && pr.d == 32) {
-#pragma unroll
-        for (int j = 0; j < 8; j++) {
-          const float4 a4 = __ldg(reinterpret_cast<const float4*>(xr) + j);
-          xv[4 * j] = a4.x, xv[4 * j + 1] = a4.y, xv[4 * j + 2] = a4.z, xv[4 * j + 3] = a4.w;
-        }
-#pragma unroll
-        for (int j = 32; j < 64; j++) xv[j] = 0.0f;
-      } else {
-#pragma unroll
-        for (int j = 0; j < 64; j++) xv[j] = (live && j < pr.d) ? __ldg(xr + j) : 0.0f;
-      }
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
         uint32_t hw[4], lw[4];
 #pragma unroll
         for (int l = 0; l < 8; l += 2) {
-          const float x0 = xv[8 * j + l], x1 = xv[8 * j + l + 1];
-          const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+          const __nv_bfloat162 h = __floats2bfloat162_rn(x[l], x[l + 1]);
           const float2 hf = __bfloat1622float2(h);
-          const __nv_bfloat162 lo = __floats2bfloat162_rn(x0 - hf.x, x1 - hf.y);
+          const __nv_bfloat162 lo = __floats2bfloat162_rn(x[l] - hf.x, x[l + 1] - hf.y);
           hw[l / 2] = *reinterpret_cast<const uint32_t*>(&h);
           lw[l / 2] = *reinterpret_cast<const uint32_t*>(&lo);
-          pn[l] = fmaf(x0, x0, pn[l]);
-          pn[l + 1] = fmaf(x1, x1, pn[l + 1]);
+          pn[l] = fmaf(x[l], x[l], pn[l]);
+          pn[l + 1] = fmaf(x[l + 1], x[l + 1], pn[l + 1]);
         }
         const uint32_t off = (uint32_t)tid * 128u + ((uint32_t)(j ^ (tid & 7)) << 4);
         *reinterpret_cast<uint4*>(sAh + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
         *reinterpret_cast<uint4*>(sAl + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
       }
       xn2s[b * 128 + tid] = ((pn[0] + pn[1]) + (pn[2] + pn[3])) + ((pn[4] + pn[5]) + (pn[6] + pn[7]));
-      if (tid == 0) meta[b] = make_int4(p, slot, (int)i0, pr.active ? kp : 0);
+      if (tid == 0) {
+        ItemMeta m;
+        m.n = pr.n;
+        m.lab_off = pr.lab_off;
+        m.limb_off = pr.limb_off;
+        m.x_off = pr.x_off;
+        m.p = p;
+        m.i0 = (int32_t)i0;
+        m.kp = pr.active ? kp : 0;
+        m.d = pr.d;
+        m.k = pr.k;
+        m.L = pr.L;
+        m.e_lo = pr.e_lo;
+        m.cnt_off = pr.cnt_off;
+        meta[b] = m;
+      }
       // generic-proxy smem writes -> visible to the tensor core's async proxy
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       tcx::mbar_arrive(&a_full[b]);
+    }
+    // a copy still in flight must not outlive the CTA: the last one armed on
+    // each staging buffer lands before the exit (also after an abort)
+    if (tid == 0) {
+      volatile int never = 0;
+      for (int s = 0; s < 2; s++)
+        if (issued[s] > 0 && !tcx::mbar_wait(&stage_full[s], (uint32_t)((issued[s] - 1) & 1), &never))
+          atomicOr(ta.status, DEV_TIMEOUT);
     }
   } else if (warp == 4) {
     // ---- MMA issuer ---------------------------------------------------------
@@ -603,21 +691,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
           break;
         }
         tcx::tc_fence_after();
-        const int4 mt = meta[b];
-        const int kp = mt.w;
+        const int kp = meta[b].kp;
         if (kp > 0) {
-          const BProb& pr = probs[mt.x];
           unsigned char* sAh = base + (uint32_t)b * kTcA;
-          unsigned char* sBh = base + 2 * kTcA + (uint32_t)mt.y * kTcB;
           const uint32_t idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(kp >> 3) << 17) |
                                  ((uint32_t)(kTcRows >> 4) << 24);
           const uint64_t ah = tcx::smem_desc_sw128(tcx::smem_u32(sAh));
           const uint64_t al = tcx::smem_desc_sw128(tcx::smem_u32(sAh + kTcA / 2));
           const uint64_t bh = tcx::smem_desc_sw128(tcx::smem_u32(sBh));
-          const uint64_t bl = tcx::smem_desc_sw128(tcx::smem_u32(sBh + kTcB / 2));
+          const uint64_t bl = tcx::smem_desc_sw128(tcx::smem_u32(sBl));
           const uint32_t d_tmem = tmem + (uint32_t)b * 256u;
           // K steps of 16 that hold data (the zero columns past d add nothing)
-          const int nks = (pr.d + 15) >> 4;
+          const int nks = (meta[b].d + 15) >> 4;
 #pragma unroll
           for (int kk = 0; kk < 4; kk++)
             if (kk < nks) tcx::umma_bf16(d_tmem, ah + 2 * kk, bh + 2 * kk, idesc, kk ? 1u : 0u);
@@ -650,17 +735,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       }
       if (!__all_sync(0xffffffffu, ok)) break;  // warp-uniform exit
       tcx::tc_fence_after();
-      const int4 mt = meta[b];
-      const int p = mt.x, slot = mt.y, kp = mt.w;
-      const BProb pr = probs[p];
-      const float* cn2 = cn2s + slot * 256;
-      const float* cn = cns + slot * 256;
-      const float cmax0 = cmaxs[2 * slot];
+      const ItemMeta mt = meta[b];
+      const int kp = mt.kp;
+      const int64_t i = (int64_t)mt.i0 + row;
+      const bool live = kp > 0 && i < mt.n;
+      // the row's current label, fetched while the screen runs
+      const int old = live ? (first ? -1 : labels[mt.lab_off + i]) : -1;
+      const float cmax0 = cmaxs[0];
       const float nx = xn2s[b * 128 + row];
-      const int64_t i = (int64_t)mt.z + row;
-      const bool live = kp > 0 && i < pr.n;
-      const float beta = (float)(((pr.d + 7) / 8 + 3 + 9) * u24 * 1.01);
-      const float gamma = (float)((pr.d + 4) * u24 * 1.01);
+      const float beta = (float)(((mt.d + 7) / 8 + 3 + 9) * u24 * 1.01);
+      const float gamma = (float)((mt.d + 4) * u24 * 1.01);
       const uint32_t taddr = tmem + ((uint32_t)(g * 32) << 16) + (uint32_t)b * 256u;
       const float xl = sqrtf(nx);
       float best = __int_as_float(0x7f800000);
@@ -668,31 +752,34 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       bool undecided = false;
       if (kp > 0) {
         // screen: best centre, then every centre whose lower bound reaches its
-        // upper bound; TMEM read 64 columns per wait.  The best centre is the
+        // upper bound; TMEM read 32 columns per wait.  The best centre is the
         // first minimum (strict <), kept as four independent running minima over
         // the columns of each residue mod 4 and merged by (distance, column):
         // the same centre as one scan in column order, with a quarter of the
         // dependency chain.
         float b4[4] = {best, best, best, best};
         int j4[4] = {0, 0, 0, 0};
-        for (int c0 = 0; c0 < kp; c0 += 64) {
-          uint32_t r[4][16];
+        for (int c0 = 0; c0 < kp; c0 += 32) {
+          uint32_t r[2][16];
 #pragma unroll
-          for (int h = 0; h < 4; h++)
+          for (int h = 0; h < 2; h++)
             if (c0 + 16 * h < kp) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
           tcx::tmem_ld_wait();
 #pragma unroll
-          for (int h = 0; h < 4; h++) tcx::tmem_regs_ready(r[h]);
+          for (int h = 0; h < 2; h++) tcx::tmem_regs_ready(r[h]);
 #pragma unroll
-          for (int h = 0; h < 4; h++)
+          for (int h = 0; h < 2; h++)
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const int col = c0 + 16 * h + j;
-              if (col < pr.k) {
-                const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
-                if (dt < b4[j & 3]) {
-                  b4[j & 3] = dt;
-                  j4[j & 3] = col;
+            for (int v = 0; v < 4; v++) {
+              const float4 c4 = *reinterpret_cast<const float4*>(cn2s + c0 + 16 * h + 4 * v);
+              const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+              for (int u = 0; u < 4; u++) {
+                const int col = c0 + 16 * h + 4 * v + u;
+                const float dt = fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]);
+                if (col < mt.k && dt < b4[u]) {
+                  b4[u] = dt;
+                  j4[u] = col;
                 }
               }
             }
@@ -704,39 +791,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
             bj = j4[u];
           }
         const float hi_b =
-            best + (ta.alpha * xl * cn[bj] + beta * (nx + cn2[bj])) * (1.0f + gamma) + gamma * fabsf(best);
+            best + (ta.alpha * xl * cns[bj] + beta * (nx + cn2s[bj])) * (1.0f + gamma) + gamma * fabsf(best);
         // columns above T cannot reach hi_b even with the largest error of the
         // problem (norm maxima); only the others get the exact per-column test
         const float amax = (ta.alpha * xl * sqrtf(cmax0) + beta * (nx + cmax0)) * (1.0f + gamma);
         const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
-        for (int c0 = 0; c0 < kp; c0 += 64) {
-          uint32_t r[4][16];
+        for (int c0 = 0; c0 < kp; c0 += 32) {
+          uint32_t r[2][16];
 #pragma unroll
-          for (int h = 0; h < 4; h++)
+          for (int h = 0; h < 2; h++)
             if (c0 + 16 * h < kp) tcx::tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
           tcx::tmem_ld_wait();
 #pragma unroll
-          for (int h = 0; h < 4; h++) tcx::tmem_regs_ready(r[h]);
+          for (int h = 0; h < 2; h++) tcx::tmem_regs_ready(r[h]);
 #pragma unroll
-          for (int h = 0; h < 4; h++)
+          for (int h = 0; h < 2; h++)
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const int col = c0 + 16 * h + j;
-              if (col < pr.k && col != bj) {
-                const float dt = fmaf(-2.0f, __uint_as_float(r[h][j]), nx + cn2[col]);
-                if (!(T > 0.0f) || !(dt > T)) {
+            for (int v = 0; v < 4; v++) {
+              const float4 c4 = *reinterpret_cast<const float4*>(cn2s + c0 + 16 * h + 4 * v);
+              const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+              for (int u = 0; u < 4; u++) {
+                const int col = c0 + 16 * h + 4 * v + u;
+                const float dt = fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]);
+                if (col < mt.k && col != bj && (!(T > 0.0f) || !(dt > T))) {
                   const float e =
-                      (ta.alpha * xl * cn[col] + beta * (nx + cn2[col])) * (1.0f + gamma) + gamma * fabsf(dt);
+                      (ta.alpha * xl * cns[col] + beta * (nx + cc[u])) * (1.0f + gamma) + gamma * fabsf(dt);
                   if (!(dt - e > hi_b)) undecided = true;
                 }
               }
             }
         }
       }
-      // the item's accumulator, tile, metadata and centre slot are no longer read
+      // the item's accumulator, tile and parameters are no longer read
       tcx::tc_fence_before();
       tcx::mbar_arrive(&item_done[b]);
       if (kp == 0) continue;
+      const int p = mt.p;
       const int lab = bj;
       {
         const unsigned um = __ballot_sync(0xffffffffu, live && undecided);
@@ -748,14 +839,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         ta.und_p[u] = p;
         ta.und_i[u] = (int32_t)i;
       }
-      const int old = live ? (first ? -1 : labels[pr.lab_off + i]) : -1;
       const bool chg = live && !undecided && lab != old;
       const unsigned cm = __ballot_sync(0xffffffffu, chg);
       if (!first && lane == 0 && cm) atomicAdd(&pchg[p], __popc(cm));
       if (chg) {
-        labels[pr.lab_off + i] = lab;
-        atomicAdd(&counts[pr.cnt_off + lab], 1);
-        if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
+        labels[mt.lab_off + i] = lab;
+        atomicAdd(&counts[mt.cnt_off + lab], 1);
+        if (old >= 0) atomicAdd(&counts[mt.cnt_off + old], -1);
       }
       // the changed rows' coordinates into the exact sums, one row at a time by
       // the whole warp: the lanes take consecutive coordinates, so each atomic
@@ -767,11 +857,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         const int64_t is = __shfl_sync(0xffffffffu, i, src);
         const int ls = __shfl_sync(0xffffffffu, lab, src);
         const int os = __shfl_sync(0xffffffffu, old, src);
-        const float* xr = X + pr.x_off + is * pr.d;
-        for (int t = lane; t < pr.d; t += 32) {
+        const float* xr = X + mt.x_off + is * mt.d;
+        for (int t = lane; t < mt.d; t += 32) {
           const float xv = __ldg(xr + t);
-          add_coord(limbs + pr.limb_off + ((int64_t)ls * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
-          if (os >= 0) add_coord(limbs + pr.limb_off + ((int64_t)os * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
+          add_coord(limbs + mt.limb_off + ((int64_t)ls * mt.d + t) * mt.L, xv, mt.e_lo, mt.L, false);
+          if (os >= 0) add_coord(limbs + mt.limb_off + ((int64_t)os * mt.d + t) * mt.L, xv, mt.e_lo, mt.L, true);
         }
       }
     }

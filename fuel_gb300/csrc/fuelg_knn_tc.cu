@@ -529,16 +529,19 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
         __syncwarp();
         tc_fence_after();
         const uint32_t taddr = tmem_base + ((uint32_t)(g * 32) << 16) + b * XN;
-        // 32-column chunks, software pipelined: the TMEM loads of chunk c+1 are in
-        // flight while chunk c is screened; the log check (which may call the
-        // selection) runs only after they completed.  Exact data: a column equal
-        // to the threshold cannot enter (the piece's tiles come in ascending
-        // index order, so it would follow every held key of that distance).
-        const bool strict = a.exact != 0;
-        auto screen32 = [&](uint32_t (&r)[2][16], int c0) {
-          float mnh[2];
+#pragma unroll 1
+        for (int c0 = 0; c0 < XN; c0 += 64) {
+          uint32_t r[4][16];
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
+          for (int h = 0; h < 4; h++) tmem_ld16_nowait(taddr + c0 + 16 * h, r[h]);
+          tmem_ld_wait();
+#pragma unroll
+          for (int h = 0; h < 4; h++) tmem_regs_ready(r[h]);
+          // shifted screen values f = |x|^2 - 2 q.x (in place) and each group's
+          // minimum (short dependency chains, four groups interleaved)
+          float mnh[4];
+#pragma unroll
+          for (int h = 0; h < 4; h++) {
             const float4* n4 = reinterpret_cast<const float4*>(nsm + c0 + 16 * h);
 #pragma unroll
             for (int v = 0; v < 4; v++) {
@@ -557,16 +560,20 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
             mnh[h] = fminf(min3_f32(m6[0], m6[1], m6[2]), min3_f32(m6[3], m6[4], m6[5]));
           }
 #pragma unroll
-          for (int h = 0; h < 2; h++) {
-            if (strict ? mnh[h] < thr : mnh[h] <= thr) {
+          for (int h = 0; h < 4; h++) {
+            if (mnh[h] <= thr) {
               // the few passing columns, one loop trip each; the screened
               // distance is D~ = |q|^2 + (|x|^2 - 2 q.x) in f32
               float f[16];
 #pragma unroll
               for (int j = 0; j < 16; j++) f[j] = __uint_as_float(r[h][j]);
-              unsigned mask = 0;
+              unsigned b8[8];
 #pragma unroll
-              for (int j = 0; j < 16; j++) mask |= (strict ? f[j] < thr : f[j] <= thr) ? (1u << j) : 0u;
+              for (int j = 0; j < 8; j++)
+                b8[j] = (f[2 * j] <= thr ? 1u : 0u) | (f[2 * j + 1] <= thr ? 2u : 0u);
+#pragma unroll
+              for (int j = 0; j < 4; j++) b8[j] = b8[2 * j] | (b8[2 * j + 1] << 2);
+              unsigned mask = (b8[0] | (b8[1] << 4)) | ((b8[2] | (b8[3] << 4)) << 8);
               while (mask) {
                 const int j = __ffs(mask) - 1;
                 mask &= mask - 1;
@@ -580,42 +587,12 @@ __global__ void __launch_bounds__(kThreadsKT, kCtasPerSm)
               }
             }
           }
-        };
-        // at most 32 appends per lane per chunk: compact before the log can overflow
-        auto check_log = [&]() {
-          const unsigned full = __ballot_sync(0xffffffffu, na > kApp - 32);
+          // at most 64 appends per lane per chunk: compact before the log can overflow
+          const unsigned full = __ballot_sync(0xffffffffu, na > kApp - 64);
           if (full) {
             flush_rows(full);
             thr = threshold();
           }
-        };
-        static_assert(XN % 64 == 0, "chunk pairs");
-        uint32_t ra[2][16], rb[2][16];
-        tmem_ld16_nowait(taddr, ra[0]);
-        tmem_ld16_nowait(taddr + 16, ra[1]);
-        tmem_ld_wait();
-        tmem_regs_ready(ra[0]);
-        tmem_regs_ready(ra[1]);
-#pragma unroll 1
-        for (int c0 = 0; c0 < XN; c0 += 64) {
-          tmem_ld16_nowait(taddr + c0 + 32, rb[0]);
-          tmem_ld16_nowait(taddr + c0 + 48, rb[1]);
-          screen32(ra, c0);
-          tmem_ld_wait();
-          tmem_regs_ready(rb[0]);
-          tmem_regs_ready(rb[1]);
-          check_log();
-          if (c0 + 64 < XN) {
-            tmem_ld16_nowait(taddr + c0 + 64, ra[0]);
-            tmem_ld16_nowait(taddr + c0 + 80, ra[1]);
-          }
-          screen32(rb, c0 + 32);
-          tmem_ld_wait();
-          if (c0 + 64 < XN) {
-            tmem_regs_ready(ra[0]);
-            tmem_regs_ready(ra[1]);
-          }
-          check_log();
         }
         tc_fence_before();
         __syncwarp();
