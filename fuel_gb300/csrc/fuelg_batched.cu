@@ -847,21 +847,44 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         atomicAdd(&counts[mt.cnt_off + lab], 1);
         if (old >= 0) atomicAdd(&counts[mt.cnt_off + old], -1);
       }
-      // the changed rows' coordinates into the exact sums, one row at a time by
-      // the whole warp: the lanes take consecutive coordinates, so each atomic
-      // instruction covers adjacent counters of one cluster
-      unsigned pend = cm;
-      while (pend) {
-        const int src = __ffs(pend) - 1;
-        pend &= pend - 1;
-        const int64_t is = __shfl_sync(0xffffffffu, i, src);
-        const int ls = __shfl_sync(0xffffffffu, lab, src);
-        const int os = __shfl_sync(0xffffffffu, old, src);
-        const float* xr = X + mt.x_off + is * mt.d;
-        for (int t = lane; t < mt.d; t += 32) {
-          const float xv = __ldg(xr + t);
-          add_coord(limbs + mt.limb_off + ((int64_t)ls * mt.d + t) * mt.L, xv, mt.e_lo, mt.L, false);
-          if (os >= 0) add_coord(limbs + mt.limb_off + ((int64_t)os * mt.d + t) * mt.L, xv, mt.e_lo, mt.L, true);
+      // the changed rows' coordinates into the exact sums: the warp takes the
+      // rows that enter one cluster (or leave one) together -- lanes over
+      // consecutive coordinates, the group's 32-bit slices summed in 64-bit
+      // registers (at most 32 slices: no overflow), one atomic per counter --
+      // which gives the counters the same values as one add per row, since the
+      // counters add modulo 2^64
+      for (int dir = 0; dir < 2; dir++) {
+        const bool mine = chg && (dir == 0 || old >= 0);
+        const int key = dir == 0 ? lab : old;
+        unsigned pend = __ballot_sync(0xffffffffu, mine);
+        while (pend) {
+          const int src = __ffs(pend) - 1;
+          const int ks = __shfl_sync(0xffffffffu, key, src);
+          const unsigned grp = __ballot_sync(0xffffffffu, mine && key == ks);
+          pend &= ~grp;
+          unsigned long long* dst = limbs + mt.limb_off + (int64_t)ks * mt.d * mt.L;
+          for (int tb = 0; tb < mt.d; tb += 32) {
+            const int t = tb + lane;
+            const bool tv = t < mt.d;
+            unsigned long long acc[4] = {0ull, 0ull, 0ull, 0ull};
+            unsigned gm = grp;
+            while (gm) {
+              const int r = __ffs(gm) - 1;
+              gm &= gm - 1;
+              const int64_t is = __shfl_sync(0xffffffffu, i, r);
+              if (tv) {
+                const unsigned __int128 v = fixed_of(__ldg(X + mt.x_off + is * mt.d + t), mt.e_lo, dir == 1);
+#pragma unroll
+                for (int l = 0; l < 4; l++)
+                  if (l < mt.L) acc[l] += (unsigned long long)((v >> (32 * l)) & 0xffffffffu);
+              }
+            }
+            if (tv) {
+#pragma unroll
+              for (int l = 0; l < 4; l++)
+                if (l < mt.L && acc[l]) atomicAdd(dst + (int64_t)t * mt.L + l, acc[l]);
+            }
+          }
         }
       }
     }
