@@ -5,7 +5,7 @@ search and Lloyd k-means hot path.
 ``fuel.cluster.kmeans``; the compute runs in libfuelg.so (hand-written
 sm_103a CUDA behind the C ABI of include/fuelg.h).
 """
-from .search import SearchIndex, knn_search, pairwise_distances, range_search  # noqa: F401
+from .search import SearchIndex, knn_batched, knn_search, pairwise_distances, range_search  # noqa: F401
 from .cluster import KMeansResult, kmeans, kmeans_batched, lloyd_assign  # noqa: F401
 
 __version__ = "0.1.0"

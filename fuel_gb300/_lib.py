@@ -52,6 +52,14 @@ class ErrorReport(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class KnnSet(ctypes.Structure):
+    """fuelg_knn_set (include/fuelg.h)."""
+    _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_int64), ("d", ctypes.c_int32), ("metric", ctypes.c_int32),
+                ("queries", ctypes.c_void_p), ("m", ctypes.c_int64), ("k", ctypes.c_int32),
+                ("exclude_mode", ctypes.c_int32), ("out_idx", ctypes.c_void_p), ("out_dist", ctypes.c_void_p),
+                ("status", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class KMeansProblem(ctypes.Structure):
     """fuelg_kmeans_problem (include/fuelg.h)."""
     _fields_ = [("data", ctypes.c_void_p), ("n", ctypes.c_int64), ("d", ctypes.c_int32), ("k", ctypes.c_int32),
@@ -74,6 +82,7 @@ SIGNATURES = {
                                         ctypes.POINTER(_i32)]),
     "fuelg_knn": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
     "fuelg_knn_ties": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _i32, _pp, ctypes.POINTER(Stats)]),
+    "fuelg_knn_batched": (ctypes.c_int, [_vp, _i32, _i32, _i32, ctypes.POINTER(Stats)]),
     "fuelg_knn_error": (ctypes.c_int, [_vp, _vp, _i64, _i32, _vp, _vp, ctypes.POINTER(ErrorReport)]),
     "fuelg_fp32_rate": (ctypes.c_int, [ctypes.POINTER(_dbl)]),
     "fuelg_range": (ctypes.c_int, [_vp, _vp, _i64, _dbl, _i32, _pp, ctypes.POINTER(Stats)]),

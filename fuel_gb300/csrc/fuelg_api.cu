@@ -5,6 +5,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "../../include/fuelg.h"
 #include "fuelg_common.cuh"
@@ -654,6 +655,85 @@ int fuelg_knn_ties(fuelg_index* ix, const float* queries, int64_t m, int32_t k, 
     return st;
   }
   *out = r;
+  return ST_OK;
+}
+
+int fuelg_knn_batched(fuelg_knn_set* sets, int32_t count, int32_t order, int32_t precision, fuelg_stats* stats) {
+  if (count < 0 || (count > 0 && !sets)) {
+    set_error("invalid batched kNN arguments count=%d", count);
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  if (precision != FUELG_PREC_FP32 && precision != FUELG_PREC_AUTO) {
+    set_error("batched kNN runs the exact FP32 scan (precision %d requested)", precision);
+    return ST_ENOTSUP;
+  }
+  int bad = 0;
+  for (int i = 0; i < count; i++) {
+    fuelg_knn_set& t = sets[i];
+    t.status = ST_OK;
+    const bool ok = t.n >= 0 && t.d >= 1 && t.d <= 1024 && t.m >= 0 && t.k >= 0 && t.k <= 4095 &&
+                    (t.metric == FUELG_METRIC_SQEUCLIDEAN || t.metric == FUELG_METRIC_EUCLIDEAN) &&
+                    t.exclude_mode >= FUELG_EXCLUDE_NONE && t.exclude_mode <= FUELG_EXCLUDE_KPLUS1 &&
+                    (t.n == 0 || t.data) && (t.m == 0 || t.queries) &&
+                    (t.m == 0 || t.k == 0 || (t.out_idx && t.out_dist));
+    if (!ok) {
+      t.status = ST_EINVAL;
+      if (!bad) set_error("set %d: invalid shape or arguments (n=%lld d=%d m=%lld k=%d)", i, (long long)t.n, t.d,
+                          (long long)t.m, t.k);
+      bad = 1;
+    }
+  }
+  if (bad) return ST_EINVAL;
+  FUELG_TRY(begin_call());
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaStream_t s;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  CallMeter meter;
+  Timer tm(s);
+  std::vector<InBuf> xs(count), qs(count);
+  std::vector<OutBuf> ois(count), ods(count);
+  std::vector<KnnSetDev> dev(count);
+  Scratch dstat;
+  FUELG_TRY(dstat.alloc(sizeof(int), s));
+  FUELG_CUDA(cudaMemsetAsync(dstat.p, 0, sizeof(int), s));
+  int64_t h2d = 0, evals = 0;
+  for (int i = 0; i < count; i++) {
+    const fuelg_knn_set& t = sets[i];
+    const int64_t mk = (t.m > 0 && t.k > 0) ? t.m : 0;
+    FUELG_TRY(xs[i].init(t.data, mk ? (size_t)t.n * t.d * sizeof(float) : 0, s));
+    FUELG_TRY(qs[i].init(t.queries, mk ? (size_t)t.m * t.d * sizeof(float) : 0, s));
+    FUELG_TRY(ois[i].init(t.out_idx, (size_t)mk * t.k * sizeof(int64_t), s));
+    FUELG_TRY(ods[i].init(t.out_dist, (size_t)mk * t.k * sizeof(float), s));
+    h2d += xs[i].h2d + qs[i].h2d;
+    evals += mk * t.n;
+    dev[i] = KnnSetDev{static_cast<const float*>(qs[i].dptr), mk, static_cast<const float*>(xs[i].dptr), t.n, t.d,
+                       t.metric, t.k, t.exclude_mode, static_cast<int64_t*>(ois[i].dptr),
+                       static_cast<float*>(ods[i].dptr)};
+  }
+  FUELG_TRY(exact_knn_sets(dev.data(), count, order, dstat.as<int>(), s));
+  int64_t d2h = 0;
+  for (int i = 0; i < count; i++) {
+    FUELG_TRY(ois[i].flush(s, &d2h));
+    FUELG_TRY(ods[i].flush(s, &d2h));
+  }
+  const double ms = tm.stop();
+  FUELG_TRY(read_dev_status(dstat.as<int>(), s));
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = evals;
+    stats->precision_used = FUELG_PREC_FP32;
+    meter.fill(stats);
+  }
   return ST_OK;
 }
 

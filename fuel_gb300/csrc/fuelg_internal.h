@@ -157,6 +157,25 @@ int exact_topk(const ExactScanParams& p, uint64_t* out_keys, int* dev_status, cu
 int finalize_knn(const uint64_t* keys, int64_t m, int kk, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
                  cudaStream_t stream);
 
+// Many independent kNN query sets (device buffers), each with its own data,
+// n, d, k, metric and exclude rule, scanned in one launch over a list of
+// (set, query block, index split) items, merged and finalized in a second.
+struct KnnSetDev {
+  const float* A;  // queries [m, d]
+  int64_t m;
+  const float* B;  // points [n, d]
+  int64_t n;
+  int d, metric, k, mode;
+  int64_t* out_idx;  // [m, k]
+  float* out_dist;
+};
+struct KnnSetOut {
+  int64_t* out_idx;
+  float* out_dist;
+  int32_t k, mode;
+};
+int exact_knn_sets(const KnnSetDev* sets, int count, int order, int* dev_status, cudaStream_t stream);
+
 // Top-k + finalize with every temporary inside the caller-provided scratch
 // region (no allocation; queries are batched to fit; no cancellation).
 int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int64_t* out_idx, float* out_dist,

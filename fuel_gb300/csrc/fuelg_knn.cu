@@ -101,8 +101,9 @@ __device__ __forceinline__ uint64_t merge_buffer(uint64_t* __restrict__ buf, int
   return nxt[kk - 1];
 }
 
+// The scan of one CTA: query block qb against index split sy of sgrid.
 template <int KIND, int ORDER, int NP, bool KK1>
-__global__ void __launch_bounds__(kThreads) scan_topk_kernel(ScanArgs a) {
+__device__ __forceinline__ void scan_topk_body(const ScanArgs& a, int64_t qb, int sy, int sgrid) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* qt = reinterpret_cast<float*>(smem_raw);
   float* xt = qt + a.qpb * a.qs;
@@ -112,11 +113,11 @@ __global__ void __launch_bounds__(kThreads) scan_topk_kernel(ScanArgs a) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int qgroup = warp / a.ws, wsplit = warp % a.ws;
   const int qloc = qgroup * 32 + lane;
-  const int64_t q0 = (int64_t)blockIdx.x * a.qpb;
+  const int64_t q0 = qb * a.qpb;
   const int64_t qi = q0 + qloc;
-  const int S = gridDim.y * a.ws;
-  const int s_total = blockIdx.y * a.ws + wsplit;
-  const int64_t p_begin = (int64_t)blockIdx.y * a.split_len;
+  const int S = sgrid * a.ws;
+  const int s_total = sy * a.ws + wsplit;
+  const int64_t p_begin = (int64_t)sy * a.split_len;
   const int64_t p_end = min(a.n, p_begin + a.split_len);
   const bool active = qi < a.m;
 
@@ -180,6 +181,27 @@ __global__ void __launch_bounds__(kThreads) scan_topk_kernel(ScanArgs a) {
   }
 }
 
+template <int KIND, int ORDER, int NP, bool KK1>
+__global__ void __launch_bounds__(kThreads) scan_topk_kernel(ScanArgs a) {
+  scan_topk_body<KIND, ORDER, NP, KK1>(a, blockIdx.x, blockIdx.y, gridDim.y);
+}
+
+// Many independent kNN query sets in one launch: CTA b runs work item b, a
+// (set, query block, index split) of its set's own scan arguments -- each set
+// with its own data, n, d, k and metric.
+struct SetItem {
+  int32_t set, sy;
+  int64_t qb;
+};
+template <int ORDER>
+__global__ void __launch_bounds__(kThreads) scan_sets_kernel(const ScanArgs* __restrict__ sets,
+                                                             const int32_t* __restrict__ sgrid,
+                                                             const SetItem* __restrict__ items) {
+  const SetItem it = items[blockIdx.x];
+  const ScanArgs a = sets[it.set];
+  scan_topk_body<KIND_KNN, ORDER, 4, false>(a, it.qb, it.sy, sgrid[it.set]);
+}
+
 __device__ __forceinline__ uint64_t warp_min_u64(uint64_t v) {
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
@@ -234,13 +256,8 @@ __global__ void min_splits_kernel(const uint64_t* __restrict__ best, int64_t m, 
 //              to k.  With the k+1 smallest keys c[0..k]: drop self, and use
 //              c[k] only if its distance equals the k-th distance.
 //  2 kplus1    python/search.rs:1163-1170 -- search k+1, drop self, take k.
-__global__ void finalize_kernel(const uint64_t* __restrict__ keys, int64_t m, int kk, int k, int mode,
-                                int64_t* __restrict__ out_idx, float* __restrict__ out_dist) {
-  const int64_t qi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (qi >= m) return;
-  const uint64_t* c = keys + qi * kk;
-  int64_t* oi = out_idx + qi * k;
-  float* od = out_dist + qi * k;
+__device__ __forceinline__ void finalize_row(const uint64_t* __restrict__ c, int64_t qi, int kk, int k, int mode,
+                                             int64_t* __restrict__ oi, float* __restrict__ od) {
   int w = 0;
   if (mode == 0) {
     for (; w < k && w < kk; w++) {
@@ -265,6 +282,13 @@ __global__ void finalize_kernel(const uint64_t* __restrict__ keys, int64_t m, in
     oi[w] = -1;
     od[w] = __int_as_float(0x7f800000);
   }
+}
+
+__global__ void finalize_kernel(const uint64_t* __restrict__ keys, int64_t m, int kk, int k, int mode,
+                                int64_t* __restrict__ out_idx, float* __restrict__ out_dist) {
+  const int64_t qi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (qi >= m) return;
+  finalize_row(keys + qi * kk, qi, kk, k, mode, out_idx + qi * k, out_dist + qi * k);
 }
 
 int vec4_ok(const float* p, int d) { return (d % 4 == 0) && ((reinterpret_cast<uintptr_t>(p) & 15) == 0); }
@@ -393,6 +417,165 @@ int exact_topk(const ExactScanParams& p, uint64_t* out_keys, int* dev_status, cu
     }
     FUELG_CUDA(cudaGetLastError());
   }
+  return ST_OK;
+}
+
+namespace {
+
+// Set of global query q: the last set whose first query is <= q.
+__device__ __forceinline__ int set_of(const int64_t* __restrict__ qbegin, int count, int64_t q) {
+  int lo = 0, hi = count;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (qbegin[mid] <= q) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// One warp per query of every set: k-way merge of its set's S sorted split
+// lists (S <= 32), then the set's exclude rule and padding into its outputs.
+__global__ void merge_sets_kernel(const ScanArgs* __restrict__ sets, const int32_t* __restrict__ nsplit,
+                                  const int64_t* __restrict__ qbegin, int count, const KnnSetOut* __restrict__ outs,
+                                  uint64_t* __restrict__ keys, const int64_t* __restrict__ koff) {
+  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (q >= qbegin[count]) return;
+  const int st = set_of(qbegin, count, q);
+  const int64_t qi = q - qbegin[st];
+  const int S = nsplit[st];
+  const int kk = sets[st].kk;
+  const uint64_t* L = sets[st].lists + ((uint64_t)qi * S + lane) * 2ull * kk;
+  uint64_t* o = keys + koff[st] + qi * kk;
+  int p = 0;
+  uint64_t cur = lane < S ? L[0] : KEY_NONE;
+  for (int j = 0; j < kk; j++) {
+    const uint64_t mn = warp_min_u64(cur);
+    if (lane == 0) o[j] = mn;
+    if (mn != KEY_NONE && cur == mn) {
+      p++;
+      cur = p < kk ? L[p] : KEY_NONE;
+    }
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const KnnSetOut& so = outs[st];
+    finalize_row(o, qi, kk, so.k, so.mode, so.out_idx + qi * so.k, so.out_dist + qi * so.k);
+  }
+}
+
+}  // namespace
+
+int exact_knn_sets(const KnnSetDev* sets, int count, int order, int* dev_status, cudaStream_t stream) {
+  std::vector<ScanArgs> args;
+  std::vector<int32_t> nsplit, sgrid;
+  std::vector<int64_t> qbegin(1, 0), koff;
+  std::vector<KnnSetOut> outs;
+  std::vector<SetItem> items;
+  size_t smem = 0, list_words = 0, key_words = 0;
+  std::vector<size_t> list_off;
+  for (int i = 0; i < count; i++) {
+    const KnnSetDev& t = sets[i];
+    if (t.m == 0 || t.k == 0) continue;
+    ExactScanParams p;
+    p.A = t.A;
+    p.m = t.m;
+    p.B = t.B;
+    p.n = t.n;
+    p.d = t.d;
+    p.kind = KIND_KNN;
+    p.order = order;
+    p.metric = t.metric;
+    p.kk = t.mode == 0 ? t.k : t.k + 1;
+    if (t.n == 0) {  // no points: every row padded
+      Scratch none;
+      FUELG_TRY(none.alloc((size_t)t.m * p.kk * 8, stream));
+      FUELG_CUDA(cudaMemsetAsync(none.p, 0xff, (size_t)t.m * p.kk * 8, stream));
+      FUELG_TRY(finalize_knn(none.as<uint64_t>(), t.m, p.kk, t.k, t.mode, t.out_idx, t.out_dist, stream));
+      FUELG_CUDA(cudaStreamSynchronize(stream));
+      continue;
+    }
+    if (t.n >= 0xffffffffll) {
+      set_error("set %d: index too large: n=%lld (limit 2^32-2)", i, (long long)t.n);
+      return ST_ENOTSUP;
+    }
+    Plan pl;
+    FUELG_TRY(make_plan(p, false, 4, &pl));
+    ScanArgs a{};
+    a.A = t.A;
+    a.m = t.m;
+    a.B = t.B;
+    a.n = t.n;
+    a.d = t.d;
+    a.kk = p.kk;
+    a.metric = t.metric;
+    a.split_len = pl.split_len;
+    a.ws = pl.ws;
+    a.qpb = pl.qpb;
+    a.pt = pl.pt;
+    a.qs = pl.qs;
+    a.xs = pl.xs;
+    a.status = dev_status;
+    a.cancel = cancel_word_device();
+    a.a_vec4 = vec4_ok(a.A, a.d);
+    a.b_vec4 = vec4_ok(a.B, a.d);
+    const int S = pl.S_grid * pl.ws;
+    list_off.push_back(list_words);
+    list_words += (size_t)t.m * S * 2 * p.kk;
+    koff.push_back((int64_t)key_words);
+    key_words += (size_t)t.m * p.kk;
+    const int si = (int)args.size();
+    const int64_t qblocks = (t.m + pl.qpb - 1) / pl.qpb;
+    for (int64_t qb = 0; qb < qblocks; qb++)
+      for (int sy = 0; sy < pl.S_grid; sy++) items.push_back(SetItem{si, sy, qb});
+    args.push_back(a);
+    nsplit.push_back(S);
+    sgrid.push_back(pl.S_grid);
+    qbegin.push_back(qbegin.back() + t.m);
+    outs.push_back(KnnSetOut{t.out_idx, t.out_dist, t.k, t.mode});
+    smem = std::max(smem, pl.smem);
+  }
+  const int ns = (int)args.size();
+  if (ns == 0) return ST_OK;
+  if (items.size() >= (1u << 31) || list_words * 8 > (size_t(6) << 30)) {
+    set_error("batched kNN: the sets' split lists need %zu bytes (limit 6 GiB); submit fewer or smaller sets",
+              list_words * 8);
+    return ST_ENOTSUP;
+  }
+  Scratch dlists, dkeys, dargs, dsplit, dsgrid, dqb, dko, douts, ditems;
+  FUELG_TRY(dlists.alloc(list_words * 8, stream));
+  FUELG_TRY(dkeys.alloc(key_words * 8, stream));
+  for (int i = 0; i < ns; i++) args[i].lists = dlists.as<uint64_t>() + list_off[i];
+  FUELG_TRY(dargs.alloc(sizeof(ScanArgs) * ns, stream));
+  FUELG_TRY(dsplit.alloc(sizeof(int32_t) * ns, stream));
+  FUELG_TRY(dsgrid.alloc(sizeof(int32_t) * ns, stream));
+  FUELG_TRY(dqb.alloc(sizeof(int64_t) * (ns + 1), stream));
+  FUELG_TRY(dko.alloc(sizeof(int64_t) * ns, stream));
+  FUELG_TRY(douts.alloc(sizeof(KnnSetOut) * ns, stream));
+  FUELG_TRY(ditems.alloc(sizeof(SetItem) * items.size(), stream));
+  FUELG_CUDA(cudaMemcpyAsync(dargs.p, args.data(), sizeof(ScanArgs) * ns, cudaMemcpyHostToDevice, stream));
+  FUELG_CUDA(cudaMemcpyAsync(dsplit.p, nsplit.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, stream));
+  FUELG_CUDA(cudaMemcpyAsync(dsgrid.p, sgrid.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, stream));
+  FUELG_CUDA(cudaMemcpyAsync(dqb.p, qbegin.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice, stream));
+  FUELG_CUDA(cudaMemcpyAsync(dko.p, koff.data(), sizeof(int64_t) * ns, cudaMemcpyHostToDevice, stream));
+  FUELG_CUDA(cudaMemcpyAsync(douts.p, outs.data(), sizeof(KnnSetOut) * ns, cudaMemcpyHostToDevice, stream));
+  FUELG_CUDA(cudaMemcpyAsync(ditems.p, items.data(), sizeof(SetItem) * items.size(), cudaMemcpyHostToDevice, stream));
+  auto kern = order == ORDER_X86 ? scan_sets_kernel<ORDER_X86> : scan_sets_kernel<ORDER_ARM>;
+  FUELG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  HotTimer* ht = hot_timer();
+  if (ht) ht->begin(stream);
+  kern<<<(unsigned)items.size(), kThreads, smem, stream>>>(dargs.as<ScanArgs>(), dsgrid.as<int32_t>(),
+                                                           ditems.as<SetItem>());
+  note_launch();
+  if (ht) ht->end(stream);
+  FUELG_CUDA(cudaGetLastError());
+  const int64_t qtot = qbegin.back();
+  merge_sets_kernel<<<(unsigned)((qtot * 32 + 255) / 256), 256, 0, stream>>>(
+      dargs.as<ScanArgs>(), dsplit.as<int32_t>(), dqb.as<int64_t>(), ns, douts.as<KnnSetOut>(), dkeys.as<uint64_t>(),
+      dko.as<int64_t>());
+  note_launch();
+  FUELG_CUDA(cudaGetLastError());
+  FUELG_CUDA(cudaStreamSynchronize(stream));  // the tables above are freed on return
   return ST_OK;
 }
 

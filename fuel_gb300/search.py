@@ -369,6 +369,56 @@ def range_search(data, query, radius, *, exclude_self=None, distance="euclidean"
     return index.radius_search(query, radius, exclude_self=exclude_self)
 
 
+def knn_batched(sets, *, order=None):
+    """Many independent exact kNN query sets in one engine call.
+
+    ``sets``: iterable of ``(data float32[n, d], queries float32[m, d], k)`` or
+    ``(data, queries, k, options)`` with ``options`` a dict of ``distance``
+    ('euclidean' default, or 'sqeuclidean') and ``exclude`` ('none' default,
+    'linear' -- the linear index's exclude-self rule, python/search.rs:485-488
+    -- or 'kplus1', the precomputed / tree rule, :1163-1170; query row i is
+    matched against point i of the same set).  Returns a list of
+    ``(int64[m, k], float32[m, k])`` -- for each set exactly what
+    ``SearchIndex(data, distance=..., tree='linear', precision='fp32').knn``
+    returns -- computed by one scan launch over all sets (each with its own n,
+    d and k) and one merge launch.  No reference counterpart: fuel answers one
+    call at a time.
+    """
+    order = order or _lib.default_order()
+    if order not in _lib.ORDER:
+        raise ValueError(f"order must be one of {sorted(_lib.ORDER)}")
+    modes = {"none": _lib.EXCLUDE_NONE, "linear": _lib.EXCLUDE_LINEAR, "kplus1": _lib.EXCLUDE_KPLUS1}
+    keep, descs, outs = [], [], []
+    for item in sets:
+        data, queries, k = item[0], item[1], int(item[2])
+        opts = item[3] if len(item) > 3 else {}
+        X = np.ascontiguousarray(data, np.float32)
+        Q = np.ascontiguousarray(queries, np.float32)
+        if X.ndim != 2 or Q.ndim != 2 or X.shape[1] != Q.shape[1]:
+            raise ValueError("each set needs data [n, d] and queries [m, d]")
+        if k < 0:
+            raise ValueError("k must be non-negative")
+        metric = _parse_distance(opts.get("distance", "euclidean"))
+        exclude = opts.get("exclude", "none")
+        if exclude not in modes:
+            raise ValueError(f"exclude must be one of {sorted(modes)}")
+        idx = np.empty((Q.shape[0], k), np.int64)
+        dist = np.empty((Q.shape[0], k), np.float32)
+        keep += [X, Q]
+        descs.append(_lib.KnnSet(X.ctypes.data if X.size else None, X.shape[0], X.shape[1], _lib.METRIC[metric],
+                                 Q.ctypes.data if Q.size else None, Q.shape[0], k, modes[exclude],
+                                 idx.ctypes.data, dist.ctypes.data, 0, 0))
+        outs.append((idx, dist))
+    if not descs:
+        return []
+    arr = (_lib.KnnSet * len(descs))(*descs)
+    st = _lib.Stats()
+    _lib.check(_lib.load().fuelg_knn_batched(ctypes.cast(arr, ctypes.c_void_p), len(descs), _lib.ORDER[order],
+                                             _lib.PRECISION["fp32"], ctypes.byref(st)))
+    knn_batched.last_stats = st.as_dict()
+    return outs
+
+
 def _condensed_n(length: int) -> int:
     """n with n*(n-1)/2 == length (python/fuel/search.py:50-57)."""
     import math

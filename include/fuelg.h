@@ -135,6 +135,35 @@ int fuelg_knn(fuelg_index *index, const float *queries, int64_t m, int32_t k, in
 int fuelg_knn_ties(fuelg_index *index, const float *queries, int64_t m, int32_t k, int32_t exclude_mode,
                    int32_t precision, fuelg_range_result **out, fuelg_stats *stats);
 
+/* Many independent kNN query sets in one call.  No single counterpart in the
+ * reference (fuel answers one SearchIndex::knn at a time,
+ * python/search.rs:560-568); each set gets exactly what fuelg_knn returns for
+ * a linear index built from its `data` (same metric and summation order,
+ * FUELG_PREC_FP32) with its queries, k and exclude rule -- bit-identical
+ * indices and distances.  All sets are scanned by one launch over a list of
+ * (set, query block, index split) items with their own n, d and k, then
+ * merged and finalized by a second launch.  Inputs and outputs are host or
+ * device arrays.  precision: FUELG_PREC_FP32 or FUELG_PREC_AUTO (both run the
+ * exact CUDA-core scan; the tensor-core tiers serve one index per fuelg_knn
+ * call).  Per-set failures (bad shape, d beyond the scan's limit) are written
+ * to the set's status and the call returns FUELG_EINVAL; nothing is computed
+ * then. */
+typedef struct {
+  const float *data;    /* [n, d] */
+  int64_t n;
+  int32_t d;
+  int32_t metric;       /* FUELG_METRIC_* */
+  const float *queries; /* [m, d] */
+  int64_t m;
+  int32_t k;
+  int32_t exclude_mode; /* FUELG_EXCLUDE_*: query row i vs point i of this set */
+  int64_t *out_idx;     /* [m, k] */
+  float *out_dist;      /* [m, k] */
+  int32_t status;       /* FUELG_OK or the set's error */
+  int32_t reserved;
+} fuelg_knn_set;
+int fuelg_knn_batched(fuelg_knn_set *sets, int32_t count, int32_t order, int32_t precision, fuelg_stats *stats);
+
 /* Accuracy of returned kNN rows against FP64.  No counterpart in the
  * reference (fuel's distances are f32 throughout); it checks results of
  * fuelg_knn / fuelg_server_* against distances formed in double: for every

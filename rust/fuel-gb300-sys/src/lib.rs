@@ -87,6 +87,23 @@ pub struct fuelg_kmeans_problem {
     pub out_inertia: f64,
 }
 
+#[repr(C)]
+#[derive(Debug, Clone, Copy)]
+pub struct fuelg_knn_set {
+    pub data: *const f32,
+    pub n: i64,
+    pub d: i32,
+    pub metric: i32,
+    pub queries: *const f32,
+    pub m: i64,
+    pub k: i32,
+    pub exclude_mode: i32,
+    pub out_idx: *mut i64,
+    pub out_dist: *mut f32,
+    pub status: i32,
+    pub reserved: i32,
+}
+
 #[link(name = "fuelg")]
 unsafe extern "C" {
     pub fn fuelg_last_error() -> *const c_char;
@@ -103,6 +120,8 @@ unsafe extern "C" {
                      precision: i32, out_idx: *mut i64, out_dist: *mut f32, stats: *mut fuelg_stats) -> c_int;
     pub fn fuelg_knn_ties(index: *mut fuelg_index, queries: *const f32, m: i64, k: i32, exclude_mode: i32,
                           precision: i32, out: *mut *mut fuelg_range_result, stats: *mut fuelg_stats) -> c_int;
+    pub fn fuelg_knn_batched(sets: *mut fuelg_knn_set, count: i32, order: i32, precision: i32,
+                             stats: *mut fuelg_stats) -> c_int;
     pub fn fuelg_knn_error(index: *mut fuelg_index, queries: *const f32, m: i64, k: i32, idx: *const i64,
                            dist: *const f32, out: *mut fuelg_error_report) -> c_int;
     pub fn fuelg_fp32_rate(tera_fma_per_s: *mut f64) -> c_int;
