@@ -31,6 +31,9 @@
 
 namespace fuelg {
 
+// Middle Lloyd passes captured into one CUDA graph (see lloyd_run).
+constexpr int kPassesPerGraph = 8;
+
 struct TcLloydState;
 TcLloydState* lloyd_tc_new();
 void lloyd_tc_delete(TcLloydState*);
@@ -338,7 +341,8 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
 
   Scratch keys, lab_new, changed, frob, cold, inert_part, inert;
   FUELG_TRY(lab_new.alloc(sizeof(int32_t) * n, stream));
-  FUELG_TRY(changed.alloc(sizeof(int32_t) * 2, stream));
+  // one changed-count slot (2 words apart) per pass of a multi-pass graph
+  FUELG_TRY(changed.alloc(sizeof(int32_t) * 2 * (kPassesPerGraph + 1), stream));
   FUELG_TRY(frob.alloc(sizeof(double) * 2, stream));
   if (p.tol > 0) FUELG_TRY(cold.alloc(sizeof(float) * k * d, stream));
   const int inert_blocks = 4 * 152;
@@ -346,7 +350,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   FUELG_TRY(inert.alloc(sizeof(double), stream));
 
   int32_t* h_changed = nullptr;
-  FUELG_CUDA(cudaMallocHost(&h_changed, sizeof(int32_t)));
+  FUELG_CUDA(cudaMallocHost(&h_changed, sizeof(int32_t) * 2 * kPassesPerGraph));
   struct HostFree {
     void* p;
     ~HostFree() {
@@ -419,65 +423,94 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   if (tc) cprep = lloyd_tc_centre_prep(tc);
   SumsCommit scv{};
   if (exact) exact_sums_commit_view(es, &scv);
-  auto pass = [&](bool first, bool write_centers) -> int {
+  auto pass = [&](bool first, bool write_centers, int32_t* chg) -> int {
     const bool fused = tc && exact && !first && d <= 1024;
     if (fused) FUELG_TRY(lloyd_tc_pass_fused(p, tc, C, labels, scv, dev_status, stream));
     else FUELG_TRY(assign(first));
     if (p.tol > 0 && write_centers)
       FUELG_CUDA(cudaMemcpyAsync(cold.p, C, sizeof(float) * k * d, cudaMemcpyDeviceToDevice, stream));
-    if (fused) return exact_sums_update(es, p.X, write_centers, C, changed.as<int32_t>(), &cprep, stream, true);
+    if (fused) return exact_sums_update(es, p.X, write_centers, C, chg, &cprep, stream, true);
     if (exact)
-      return exact_sums_step(es, p.X, lab_new.as<int32_t>(), labels, first, write_centers, C, changed.as<int32_t>(),
-                             dev_status, stream, tc ? &cprep : nullptr);
-    FUELG_CUDA(cudaMemsetAsync(changed.p, 0, sizeof(int32_t), stream));
+      return exact_sums_step(es, p.X, lab_new.as<int32_t>(), labels, first, write_centers, C, chg, dev_status, stream,
+                             tc ? &cprep : nullptr);
+    FUELG_CUDA(cudaMemsetAsync(chg, 0, sizeof(int32_t), stream));
     post_assign_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(lab_new.as<int32_t>(), n, labels,
-                                                                       first ? 1 : 0, changed.as<int32_t>()); ::fuelg::note_launch();
+                                                                       first ? 1 : 0, chg); ::fuelg::note_launch();
     FUELG_CUDA(cudaGetLastError());
     if (write_centers) FUELG_TRY(fp64_sums_update(&fs, p.X, labels, C, stream));
     return ST_OK;
   };
 
-  // Middle passes (another pass follows) replay one captured CUDA graph of a
-  // pass from the fourth iteration on; the first ones run as plain launches so
-  // the screen kernel's launches are timed individually.
-  cudaGraphExec_t gexec = nullptr;
+  // Middle passes (another pass follows) replay captured CUDA graphs from the
+  // fourth iteration on -- kPassesPerGraph consecutive passes per graph where
+  // that many middle passes remain (and no tol check runs between passes), so
+  // the screen of each pass can start its point loads while the centre update
+  // of the previous one finishes; one pass per graph otherwise.  The first
+  // passes run as plain launches so the screen kernel's launches are timed
+  // individually.  Pass j of a graph writes its changed count to slot 2j: a
+  // pass that changed nothing leaves sums, centres and labels as they were,
+  // so the passes after it in the same graph repeat it exactly and the loop
+  // stops at the first such pass (lloyd.rs:197).
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // one pass / kPassesPerGraph passes
   struct GraphFree {
-    cudaGraphExec_t& g;
+    cudaGraphExec_t* g;
     ~GraphFree() {
-      if (g) cudaGraphExecDestroy(g);
+      for (int i = 0; i < 2; i++)
+        if (g[i]) cudaGraphExecDestroy(g[i]);
     }
   } gf{gexec};
-  int64_t graph_launches = 0;
-  auto graph_pass = [&]() -> int {
-    if (!gexec) {
+  int64_t graph_launches[2] = {0, 0};
+  auto graph_pass = [&](int npass) -> int {
+    const int gi = npass == 1 ? 0 : 1;
+    if (!gexec[gi]) {
       HotTimer* saved = hot_timer();
       hot_timer() = nullptr;
       cudaGraph_t g = nullptr;
       FUELG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
       const int64_t l0 = launch_count();
-      const int rc = pass(false, true);
+      int rc = ST_OK;
+      for (int j = 0; j < npass && rc == ST_OK; j++) rc = pass(false, true, changed.as<int32_t>() + 2 * j);
       const cudaError_t ce = cudaStreamEndCapture(stream, &g);
       hot_timer() = saved;
-      graph_launches = launch_count() - l0;
-      note_launch((int)-graph_launches);  // counted per replay
+      graph_launches[gi] = launch_count() - l0;
+      note_launch((int)-graph_launches[gi]);  // counted per replay
       if (rc != ST_OK) {
         if (g) cudaGraphDestroy(g);
         return rc;
       }
       FUELG_CUDA(ce);
-      const cudaError_t ie = cudaGraphInstantiate(&gexec, g, 0);
+      const cudaError_t ie = cudaGraphInstantiate(&gexec[gi], g, 0);
       cudaGraphDestroy(g);
       FUELG_CUDA(ie);
     }
-    FUELG_CUDA(cudaGraphLaunch(gexec, stream));
-    note_launch((int)graph_launches);
+    FUELG_CUDA(cudaGraphLaunch(gexec[gi], stream));
+    note_launch((int)graph_launches[gi]);
     return ST_OK;
   };
 
   const float* inertia_centers = C;
-  FUELG_TRY(pass(true, p.max_iter > 1));
+  FUELG_TRY(pass(true, p.max_iter > 1, changed.as<int32_t>()));
   int iters = 1;
   while (iters < p.max_iter) {
+    if (p.tol <= 0 && iters + 1 >= 4 && iters + kPassesPerGraph < p.max_iter) {
+      // kPassesPerGraph middle passes in one graph
+      FUELG_TRY(graph_pass(kPassesPerGraph));
+      const int before = iters;
+      iters += kPassesPerGraph;
+      if (!p.fixed_iters) {
+        FUELG_CUDA(cudaMemcpyAsync(h_changed, changed.p, sizeof(int32_t) * 2 * kPassesPerGraph,
+                                   cudaMemcpyDeviceToHost, stream));
+        FUELG_CUDA(cudaStreamSynchronize(stream));
+        int stop = -1;
+        for (int j = 0; j < kPassesPerGraph && stop < 0; j++)
+          if (h_changed[2 * j] == 0) stop = j;
+        if (stop >= 0) {
+          iters = before + stop + 1;
+          break;
+        }
+      }
+      continue;
+    }
     iters++;
     if (p.tol > 0) {
       frob_kernel<<<1, 256, 0, stream>>>(cold.as<float>(), C, (int64_t)k * d, frob.as<double>()); ::fuelg::note_launch();
@@ -494,8 +527,8 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
         break;
       }
     }
-    if (iters >= 4 && iters < p.max_iter) FUELG_TRY(graph_pass());
-    else FUELG_TRY(pass(false, iters < p.max_iter));
+    if (iters >= 4 && iters < p.max_iter) FUELG_TRY(graph_pass(1));
+    else FUELG_TRY(pass(false, iters < p.max_iter, changed.as<int32_t>()));
     if (!p.fixed_iters) {
       FUELG_CUDA(cudaMemcpyAsync(h_changed, changed.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
       FUELG_CUDA(cudaStreamSynchronize(stream));
