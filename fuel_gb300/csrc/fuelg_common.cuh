@@ -42,6 +42,12 @@ __device__ __forceinline__ float sq_rn(float x) { return __fmul_rn(x, x); }
 // griddep_wait() before touching any memory the predecessor (or an earlier
 // kernel) reads or writes.  Without the launch attribute this is a no-op.
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next kernel of the stream (launched with the same attribute) be
+// scheduled once every CTA of this grid has passed here or exited; its CTAs
+// then run up to their own griddep_wait(), which still waits for this whole
+// grid to complete.  Called right after griddep_wait(): the successor is
+// scheduled only once this kernel's own predecessors have completed.
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
 // Per-pair distances, NP point rows against one query row, all in shared

@@ -134,6 +134,7 @@ __global__ void commit_changes_kernel(const int32_t* __restrict__ lab_new, int64
   __shared__ int32_t h_in[kSmemK], h_out[kSmemK];
   __shared__ unsigned s_last;
   griddep_wait();
+  griddep_launch();
   commit_body(blockIdx.x, gridDim.x, h_in, h_out, lab_new, n, first, k, labels, chg_i, chg_old, chg_new, nchg, cin,
               cout);
   __threadfence();
@@ -209,6 +210,7 @@ __global__ void bucket_scatter_kernel(const int32_t* __restrict__ chg_i, const i
   __shared__ int32_t c_in[kSmemK], c_out[kSmemK];
   __shared__ int32_t s_off[2 * kPlanMaxK];
   griddep_wait();
+  griddep_launch();
   const int32_t* oin = off_in;
   const int32_t* oout = off_out;
   if (plan) {
@@ -301,6 +303,7 @@ __global__ void __launch_bounds__(256) accumulate_kernel(const float* __restrict
                                                          unsigned long long* __restrict__ limbs) {
   __shared__ int32_t rid[kRows];
   griddep_wait();
+  griddep_launch();
   accumulate_body<L>(blockIdx.x, gridDim.x, ty, rid, X, d, k, e_lo, chunk_off, chunk_info, cin, cout, off_in, off_out,
                      bucket_in, bucket_out, limbs);
 }
@@ -364,6 +367,7 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
                             int32_t* __restrict__ nchg, int32_t* __restrict__ changed, int32_t* __restrict__ zero4k,
                             int nzero) {
   griddep_wait();
+  griddep_launch();
   mean_handoff(blockIdx.x, gridDim.x, nchg, changed, zero4k, nzero);
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < kd; e += (int64_t)gridDim.x * blockDim.x)
     mean_elem<L>(limbs, e, d, e_lo, counts, centers, write_centers);
@@ -383,6 +387,7 @@ __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __re
                                                         int nzero, CentrePrep cp) {
   __shared__ float part[8];
   griddep_wait();
+  griddep_launch();
   mean_handoff(blockIdx.x, gridDim.x, nchg, changed, zero4k, nzero);
   if (cp.zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *cp.zero_word = 0;
   const int j = blockIdx.x;

@@ -212,6 +212,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   float* scn = snc + a.kp;
   int32_t* h_in = reinterpret_cast<int32_t*>(scn + a.kp);  // fused: per-CTA in/out histograms
   int32_t* h_out = h_in + a.kp;
+  // the centre norms again, 16-byte aligned, +inf past k up to a multiple of 64
+  float* sncd = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(h_out + a.kp) + 15) & ~(uintptr_t)15);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t ntiles = (a.n + BM - 1) / BM;
@@ -264,17 +266,32 @@ __global__ void __launch_bounds__(kTcThreads, 2)
     }
   }
   griddep_wait();
+  griddep_launch();
   // The centre norms and the per-CTA histograms belong to the epilogue: its
   // warps stage them behind their own barrier, so the producer's first
   // centre chunk goes out without waiting for these loads.
+  // Per CTA, for the epilogue's uniform bound: the largest centre norms and
+  // whether every norm is finite and below 2^124.
+  float sncmax = 0.0f, scnmax = 0.0f;
+  bool cta_finite = true;
   if (warp >= 2) {
-    for (int j = threadIdx.x - 64; j < a.kp; j += BM) {
-      snc[j] = a.nc[j];
-      scn[j] = a.cn[j];
-      h_in[j] = 0;
-      h_out[j] = 0;
+    const int kp64 = (a.kp + 63) & ~63;
+    for (int j = threadIdx.x - 64; j < kp64; j += BM) {
+      if (j < a.kp) {
+        snc[j] = a.nc[j];
+        scn[j] = a.cn[j];
+        h_in[j] = 0;
+        h_out[j] = 0;
+      }
+      sncd[j] = j < a.k ? a.nc[j] : __int_as_float(0x7f800000);
     }
     named_bar_sync(1, BM);
+    for (int j = 0; j < a.k; j++) {
+      const float s2 = snc[j], c1 = scn[j];
+      cta_finite = cta_finite && s2 < 0x1p124f && c1 < 0x1p62f;
+      sncmax = fmaxf(sncmax, s2);
+      scnmax = fmaxf(scnmax, c1);
+    }
   }
 
   if (warp == 0) {
@@ -433,17 +450,21 @@ __global__ void __launch_bounds__(kTcThreads, 2)
       int bj = 0;
       uint64_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
       if (a.kp <= 64) {
-        // The row's kp <= 64 dot products in registers: two TMEM round trips,
-        // then the accumulator is released before the screen arithmetic.
-        float v[64];
+        // Pass 1 without branches, per 32 columns (TMEM -> registers): the
+        // screen values dt_c = fma(-2, v_c, nxi + snc_c) (padding columns: +inf
+        // through sncd) reduced by a tree that keeps the smallest value, its
+        // first index and dot product, and the second smallest value (the left
+        // operand wins ties, so the first index wins, as in a scan).
+        float second = __int_as_float(0x7f800000), vmax = 0.0f;
 #pragma unroll
-        for (int h0 = 0; h0 < 4; h0 += 2) {
+        for (int r = 0; r < 2; r++) {
+          if (32 * r >= a.kp) break;
           uint32_t rh[2][16], rl[2][16];
 #pragma unroll
           for (int h = 0; h < 2; h++)
-            if (16 * (h0 + h) < a.kp) {
-              tmem_ld16_nowait(taddr + 16 * (h0 + h), rh[h]);
-              if (BLO && a.sep_lo) tmem_ld16_nowait(taddr + a.kp + 16 * (h0 + h), rl[h]);
+            if (32 * r + 16 * h < a.kp) {
+              tmem_ld16_nowait(taddr + 32 * r + 16 * h, rh[h]);
+              if (BLO && a.sep_lo) tmem_ld16_nowait(taddr + a.kp + 32 * r + 16 * h, rl[h]);
             }
           tmem_ld_wait();
 #pragma unroll
@@ -451,41 +472,118 @@ __global__ void __launch_bounds__(kTcThreads, 2)
             tmem_regs_ready(rh[h]);
             if (BLO && a.sep_lo) tmem_regs_ready(rl[h]);
           }
+          float v[32], m[32], dv[32], s2[16];
+          int id[32];
 #pragma unroll
-          for (int h = 0; h < 2; h++)
+          for (int h = 0; h < 2; h++) {
+            const bool ld = 32 * r + 16 * h < a.kp;
 #pragma unroll
             for (int j = 0; j < 16; j++) {
-              float x = 16 * (h0 + h) < a.kp ? __uint_as_float(rh[h][j]) : 0.0f;
-              if (BLO && a.sep_lo && 16 * (h0 + h) < a.kp) x += __uint_as_float(rl[h][j]);
-              v[16 * (h0 + h) + j] = x;
+              float x = ld ? __uint_as_float(rh[h][j]) : 0.0f;
+              if (BLO && a.sep_lo && ld) x += __uint_as_float(rl[h][j]);
+              v[16 * h + j] = x;
             }
+          }
+          const float4* sd4 = reinterpret_cast<const float4*>(sncd + 32 * r);
+#pragma unroll
+          for (int q = 0; q < 8; q++) {
+            const float4 s4 = sd4[q];
+            m[4 * q + 0] = fmaf(-2.0f, v[4 * q + 0], nxi + s4.x);
+            m[4 * q + 1] = fmaf(-2.0f, v[4 * q + 1], nxi + s4.y);
+            m[4 * q + 2] = fmaf(-2.0f, v[4 * q + 2], nxi + s4.z);
+            m[4 * q + 3] = fmaf(-2.0f, v[4 * q + 3], nxi + s4.w);
+          }
+#pragma unroll
+          for (int c = 0; c < 32; c++) {
+            dv[c] = v[c];
+            id[c] = 32 * r + c;
+          }
+#pragma unroll
+          for (int c = 0; c < 32; c += 2) {
+            const bool rt = m[c + 1] < m[c];
+            s2[c >> 1] = rt ? m[c] : m[c + 1];
+            m[c] = rt ? m[c + 1] : m[c];
+            id[c] = rt ? id[c + 1] : id[c];
+            dv[c] = rt ? dv[c + 1] : dv[c];
+          }
+#pragma unroll
+          for (int w = 2; w < 32; w <<= 1)
+#pragma unroll
+            for (int c = 0; c < 32; c += 2 * w) {
+              const bool rt = m[c + w] < m[c];
+              const float lose = rt ? m[c] : m[c + w];
+              s2[c >> 1] = min3_f32(lose, s2[c >> 1], s2[(c + w) >> 1]);
+              m[c] = rt ? m[c + w] : m[c];
+              id[c] = rt ? id[c + w] : id[c];
+              dv[c] = rt ? dv[c + w] : dv[c];
+            }
+          if (r == 0) {
+            best = m[0];
+            bj = id[0];
+            best_dot = dv[0];
+            second = s2[0];
+          } else {
+            const bool rt = m[0] < best;
+            second = min3_f32(rt ? best : m[0], second, s2[0]);
+            best = rt ? m[0] : best;
+            bj = rt ? id[0] : bj;
+            best_dot = rt ? dv[0] : best_dot;
+          }
+          if (nonneg) {
+            float mx = vmax;
+#pragma unroll
+            for (int c = 0; c < 32; c += 2) mx = max3_f32(mx, v[c], v[c + 1]);
+            vmax = mx;
+          }
+        }
+        const float sb = nonneg ? fmaxf(best_dot, 0.0f) * a.s_scale : xni * scn[bj];
+        const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
+        const float hi = best + eb;
+        // Every other column j has dt_j >= second, and its rounded bound e_j
+        // (at most five roundings of non-negative terms) stays below
+        // (C + gamma |dt_j|)(1 + 2^-24)^5, C = the bound's other terms at the
+        // largest S_j and snc_j; t - gamma' |t| grows with t, so with
+        // tb >= (C + gamma |second|)(1 + 2^-18) a value second - tb two ulps
+        // above hi makes the per-column test below pass for every j.  Finite
+        // norms below 2^124 keep every dt finite.
+        constexpr float kInfl = 1.0f + 0x1p-18f;
+        const float smax = nonneg ? fmaxf(vmax, 0.0f) * a.s_scale : xni * scnmax;
+        const float cmax = (a.alpha * smax + a.beta * (nxi + sncmax)) * (1.0f + a.gamma) * kInfl;
+        const float tb = fmaf(a.gamma * kInfl, fabsf(second), cmax);
+        const float hu = __fadd_ru(__fmaf_ru(fabsf(hi), 0x1p-22f, hi), 0x1p-125f);
+        const bool easy = cta_finite && nxi < 0x1p124f && (second - tb) >= hu;
+        if (__any_sync(0xffffffffu, !easy)) {
+          // pass 2: every other centre whose lower bound reaches the best's
+          // upper bound (the columns re-read from TMEM, 16 at a time)
+          uint32_t blo = 0, bhi = 0;
+#pragma unroll
+          for (int c0 = 0; c0 < 64; c0 += 16) {
+            if (c0 >= a.kp) break;
+            uint32_t rh[16], rl[16];
+            tmem_ld16_nowait(taddr + c0, rh);
+            if (BLO && a.sep_lo) tmem_ld16_nowait(taddr + a.kp + c0, rl);
+            tmem_ld_wait();
+            tmem_regs_ready(rh);
+            if (BLO && a.sep_lo) tmem_regs_ready(rl);
+#pragma unroll
+            for (int j = 0; j < 16; j++) {
+              const int col = c0 + j;
+              float x = __uint_as_float(rh[j]);
+              if (BLO && a.sep_lo) x += __uint_as_float(rl[j]);
+              const float dt = fmaf(-2.0f, x, nxi + snc[col]);
+              const float sj = nonneg ? fmaxf(x, 0.0f) * a.s_scale : xni * scn[col];
+              const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
+              const uint32_t cb = !(dt - e > hi) ? 1u : 0u;
+              if (col < 32) blo |= cb << col;
+              else bhi |= cb << (col - 32);
+            }
+          }
+          const uint64_t kmask = a.k >= 64 ? ~0ull : ((1ull << a.k) - 1ull);
+          m0 = ((((uint64_t)bhi) << 32) | blo) & kmask & ~(1ull << bj);
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&acce[buf]);
-        // pass 1: screened argmin (first index wins ties)
-#pragma unroll
-        for (int col = 0; col < 64; col++)
-          if (col < a.k) {
-            const float dt = fmaf(-2.0f, v[col], nxi + snc[col]);
-            if (dt < best) {
-              best = dt;
-              bj = col;
-              best_dot = v[col];
-            }
-          }
-        const float sb = nonneg ? fmaxf(best_dot, 0.0f) * a.s_scale : xni * scn[bj];
-        const float eb = (a.alpha * sb + a.beta * (nxi + snc[bj])) * (1.0f + a.gamma) + a.gamma * fabsf(best);
-        const float hi = best + eb;
-        // pass 2: every other centre whose lower bound reaches the best's upper bound
-#pragma unroll
-        for (int col = 0; col < 64; col++)
-          if (col < a.k && col != bj) {
-            const float dt = fmaf(-2.0f, v[col], nxi + snc[col]);
-            const float sj = nonneg ? fmaxf(v[col], 0.0f) * a.s_scale : xni * scn[col];
-            const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
-            if (!(dt - e > hi)) m0 |= 1ull << col;
-          }
       } else {
       // pass 1: screened argmin (first index wins ties)
       for (int c0 = 0; c0 < a.kp; c0 += 16) {
@@ -595,6 +693,7 @@ __global__ void prep_rows_kernel(const float* __restrict__ X, int64_t rows, int6
                                  float* __restrict__ nrm2, float* __restrict__ nrm, int* __restrict__ neg_flag,
                                  int32_t* __restrict__ zero_word, float scale) {
   griddep_wait();
+  griddep_launch();
   if (zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *zero_word = 0;
   bool anyneg = false;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
@@ -721,6 +820,7 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
   constexpr int PER = 32 / G;
   extern __shared__ __align__(16) float rs_smem[];
   griddep_wait();
+  griddep_launch();
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   float* xs = rs_smem + (size_t)wib * (PER + 1) * ds;
   float* cs = xs + ds;
@@ -898,7 +998,8 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   }
   st->ctas_per_sm = per_sm;
   st->stages = stages;
-  st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 16 * st->kp + 16;
+  st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 16 * st->kp + 16 +
+              4 * ((st->kp + 63) / 64 * 64) + 16;
   if (st->smem > 227 * 1024) {
     set_error("tensor-core Lloyd tile does not fit shared memory (k=%d)", p.k);
     return ST_ENOTSUP;

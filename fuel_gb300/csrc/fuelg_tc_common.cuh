@@ -61,6 +61,13 @@ __device__ __forceinline__ float min3_f32(float a, float b, float c) {
   return r;
 }
 
+// Largest of three floats in one instruction (a NaN operand is ignored).
+__device__ __forceinline__ float max3_f32(float a, float b, float c) {
+  float r;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+  return r;
+}
+
 // Bounded wait: false when the barrier did not complete within limit_ns
 // (default kWaitNs) or the CTA is aborting.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag,
