@@ -723,6 +723,7 @@ def batched_rate(reps=1, count=BATCH_PROBLEMS, plain=True):
             "problem_iters_per_s": pi / (t / 1e3), "plain_per_problem_ms": plain_ms,
             "plain_problem_iters_per_s": pi / (plain_ms / 1e3), "batched_vs_plain": plain_ms / t,
             "kernel_launches": kmeans_batched.last_stats["kernel_launches"],
+            "rescored_rows": kmeans_batched.last_stats.get("rescored"),
             "roofline": {"bound": "hbm", "achieved": ach, "peak": pk.get("hbm_gbs", 6800.0), "unit": "GB/s",
                          "frac": ach / pk.get("hbm_gbs", 6800.0), "alg_bytes_per_iteration": bytes_it,
                          "flops_per_iteration": flops_it,

@@ -367,6 +367,8 @@ struct BTcArgs {
   unsigned long long* undecided;  // rows re-scored exactly (count over the call)
   int32_t* und_p;                 // this pass's undecided rows: problem, row
   int32_t* und_i;
+  uint32_t* und_m;                // and their candidate centres: und_w bit words per row
+  int und_w;
   int* und_n;
 };
 
@@ -750,6 +752,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       float best = __int_as_float(0x7f800000);
       int bj = 0;
       bool undecided = false;
+      // candidate centres of an undecided row: 32-column words (bit w of
+      // cm_set: word w holds candidates)
+      uint32_t cmask[8];
+      uint32_t cm_set = 0;
       if (kp > 0) {
         // screen: best centre, then every centre whose lower bound reaches its
         // upper bound; TMEM read 32 columns per wait.  The best centre is the
@@ -757,7 +763,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         // the columns of each residue mod 4 and merged by (distance, column):
         // the same centre as one scan in column order, with a quarter of the
         // dependency chain.
-        float b4[4] = {best, best, best, best};
+        float b4[4] = {best, best, best, best}, s4[4] = {best, best, best, best};
         int j4[4] = {0, 0, 0, 0};
         for (int c0 = 0; c0 < kp; c0 += 32) {
           uint32_t r[2][16];
@@ -777,26 +783,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
               for (int u = 0; u < 4; u++) {
                 const int col = c0 + 16 * h + 4 * v + u;
                 const float dt = fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]);
-                if (col < mt.k && dt < b4[u]) {
-                  b4[u] = dt;
-                  j4[u] = col;
+                if (col < mt.k) {
+                  // second smallest of the chain, then its smallest (first wins)
+                  s4[u] = fminf(s4[u], fmaxf(b4[u], dt));
+                  if (dt < b4[u]) {
+                    b4[u] = dt;
+                    j4[u] = col;
+                  }
                 }
               }
             }
         }
+        int wu = 0;
 #pragma unroll
         for (int u = 0; u < 4; u++)
           if (b4[u] < best || (b4[u] == best && j4[u] < bj)) {
             best = b4[u];
             bj = j4[u];
+            wu = u;
           }
+        // the smallest screen value of every other column
+        float second = fminf(fminf(s4[0], s4[1]), fminf(s4[2], s4[3]));
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+          if (u != wu) second = fminf(second, b4[u]);
         const float hi_b =
             best + (ta.alpha * xl * cns[bj] + beta * (nx + cn2s[bj])) * (1.0f + gamma) + gamma * fabsf(best);
         // columns above T cannot reach hi_b even with the largest error of the
         // problem (norm maxima); only the others get the exact per-column test
         const float amax = (ta.alpha * xl * sqrtf(cmax0) + beta * (nx + cmax0)) * (1.0f + gamma);
         const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
+        // every other column's screen value is >= second: when second > T the
+        // per-column test below skips them all, so a warp whose rows all pass
+        // this skips the second TMEM pass
+        const bool clear = T > 0.0f && second > T;
+        if (!__all_sync(0xffffffffu, clear))
         for (int c0 = 0; c0 < kp; c0 += 32) {
+          uint32_t bits = 0;
           uint32_t r[2][16];
 #pragma unroll
           for (int h = 0; h < 2; h++)
@@ -817,10 +840,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
                 if (col < mt.k && col != bj && (!(T > 0.0f) || !(dt > T))) {
                   const float e =
                       (ta.alpha * xl * cns[col] + beta * (nx + cc[u])) * (1.0f + gamma) + gamma * fabsf(dt);
-                  if (!(dt - e > hi_b)) undecided = true;
+                  if (!(dt - e > hi_b)) bits |= 1u << (16 * h + 4 * v + u);
                 }
               }
             }
+          if (bits) {
+            undecided = true;
+            cmask[c0 >> 5] = bits;
+            cm_set |= 1u << (c0 >> 5);
+          }
         }
       }
       // the item's accumulator, tile and parameters are no longer read
@@ -834,10 +862,17 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         if (lane == 0 && um) atomicAdd(ta.undecided, (unsigned long long)__popc(um));
       }
       if (live && undecided) {
-        // the exact re-score kernel decides this row
+        // the exact re-score kernel decides this row among its candidates
+        // and the screen's best
         const int u = atomicAdd(ta.und_n, 1);
         ta.und_p[u] = p;
         ta.und_i[u] = (int32_t)i;
+        uint32_t* um = ta.und_m + (int64_t)u * ta.und_w;
+        for (int w = 0; w < ta.und_w; w++) {
+          uint32_t m = ((cm_set >> w) & 1u) ? cmask[w] : 0u;
+          if (w == (bj >> 5)) m |= 1u << (bj & 31);
+          um[w] = m;
+        }
       }
       const bool chg = live && !undecided && lab != old;
       const unsigned cm = __ballot_sync(0xffffffffu, chg);
@@ -904,7 +939,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
 template <int KIND, int ORDER>
 __global__ void __launch_bounds__(256) batched_rescore_kernel(
     const BProb* __restrict__ probs, const int32_t* __restrict__ und_p, const int32_t* __restrict__ und_i,
-    const int* __restrict__ und_n, const float* __restrict__ X, const float* __restrict__ C,
+    const uint32_t* __restrict__ und_m, int und_w, const int* __restrict__ und_n, const float* __restrict__ X,
+    const float* __restrict__ C,
     int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs, int32_t* __restrict__ counts,
     int32_t* __restrict__ pchg, int first) {
   const int lane = threadIdx.x & 31;
@@ -916,10 +952,27 @@ __global__ void __launch_bounds__(256) batched_rescore_kernel(
     const BProb& pr = probs[p];
     const float* xr = X + pr.x_off + i * pr.d;
     uint64_t best = ~0ull;
-    for (int c = lane; c < pr.k; c += 32) {
-      const float dv = exact_dist_scalar<KIND, ORDER>(xr, C + pr.c_off + (int64_t)c * pr.d, pr.d);
-      const uint64_t key = ((uint64_t)__float_as_uint(dv) << 32) | (uint32_t)c;
-      best = key < best ? key : best;
+    // the candidates (every centre whose lower bound reached the screen
+    // best's upper bound, and that best): lane t scores the t-th of each 32
+    const uint32_t* um = und_m + (int64_t)u * und_w;
+    int w = 0;
+    uint32_t m = um[0];
+    for (;;) {
+      int c = -1, got = 0;
+      while (got < 32) {
+        while (m == 0 && w + 1 < und_w) m = um[++w];
+        if (m == 0) break;
+        const int b = __ffs(m) - 1;
+        m &= m - 1;
+        if (got == lane) c = w * 32 + b;
+        got++;
+      }
+      if (c >= 0 && c < pr.k) {
+        const float dv = exact_dist_scalar<KIND, ORDER>(xr, C + pr.c_off + (int64_t)c * pr.d, pr.d);
+        const uint64_t key = ((uint64_t)__float_as_uint(dv) << 32) | (uint32_t)c;
+        best = key < best ? key : best;
+      }
+      if (got < 32) break;
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -1040,6 +1093,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   int64_t work = 0;
   std::vector<int32_t> tcp, tc_begin;  // tensor-core problems and their 128-row item starts
   int64_t tc_items = 0, tc_rows = 0;
+  int tc_kmax = 1;
   int64_t rb = 0;
   for (int p = 0; p < P; p++) {
     const fuelg_kmeans_problem& q = probs[p];
@@ -1064,6 +1118,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
       tc_begin.push_back((int32_t)tc_items);
       tc_items += (q.n + kTcRows - 1) / kTcRows;
       tc_rows += q.n;
+      tc_kmax = std::max(tc_kmax, q.k);
     }
     xoff[p] = xs;
     kdb[p] = kd;
@@ -1186,9 +1241,11 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   ta.status = dSt.as<int>();
   ta.undecided = reinterpret_cast<unsigned long long*>(dSt.as<int>() + 2);
   ta.und_n = dSt.as<int>() + 1;
-  FUELG_TRY(dUnd.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, tc_rows)));
+  ta.und_w = (tc_kmax + 31) / 32;
+  FUELG_TRY(dUnd.alloc(sizeof(int32_t) * (2 + ta.und_w) * std::max<int64_t>(1, tc_rows)));
   ta.und_p = dUnd.as<int32_t>();
   ta.und_i = dUnd.as<int32_t>() + std::max<int64_t>(1, tc_rows);
+  ta.und_m = reinterpret_cast<uint32_t*>(dUnd.as<int32_t>() + 2 * std::max<int64_t>(1, tc_rows));
   auto r_init = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_PAIRWISE, ORDER_X86>
                                          : batched_rescore_kernel<KIND_PAIRWISE, ORDER_ARM>;
   auto r_iter = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_SQDIST, ORDER_X86>
@@ -1262,7 +1319,8 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
                                                                  dCnt.as<int32_t>(), dPchg.as<int32_t>(),
                                                                  first ? 1 : 0);
       note_launch();
-      (first ? r_init : r_iter)<<<sms * 8, 256, 0, s>>>(dProbs.as<BProb>(), ta.und_p, ta.und_i, ta.und_n,
+      (first ? r_init : r_iter)<<<sms * 8, 256, 0, s>>>(dProbs.as<BProb>(), ta.und_p, ta.und_i, ta.und_m, ta.und_w,
+                                                        ta.und_n,
                                                         dX.as<float>(), dC.as<float>(), dLab.as<int32_t>(),
                                                         dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
                                                         dPchg.as<int32_t>(), first ? 1 : 0);
