@@ -763,7 +763,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         // the columns of each residue mod 4 and merged by (distance, column):
         // the same centre as one scan in column order, with a quarter of the
         // dependency chain.
-        float b4[4] = {best, best, best, best}, s4[4] = {best, best, best, best};
+        float b4[4] = {best, best, best, best};
         int j4[4] = {0, 0, 0, 0};
         for (int c0 = 0; c0 < kp; c0 += 32) {
           uint32_t r[2][16];
@@ -783,41 +783,25 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
               for (int u = 0; u < 4; u++) {
                 const int col = c0 + 16 * h + 4 * v + u;
                 const float dt = fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]);
-                if (col < mt.k) {
-                  // second smallest of the chain, then its smallest (first wins)
-                  s4[u] = fminf(s4[u], fmaxf(b4[u], dt));
-                  if (dt < b4[u]) {
-                    b4[u] = dt;
-                    j4[u] = col;
-                  }
+                if (col < mt.k && dt < b4[u]) {
+                  b4[u] = dt;
+                  j4[u] = col;
                 }
               }
             }
         }
-        int wu = 0;
 #pragma unroll
         for (int u = 0; u < 4; u++)
           if (b4[u] < best || (b4[u] == best && j4[u] < bj)) {
             best = b4[u];
             bj = j4[u];
-            wu = u;
           }
-        // the smallest screen value of every other column
-        float second = fminf(fminf(s4[0], s4[1]), fminf(s4[2], s4[3]));
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-          if (u != wu) second = fminf(second, b4[u]);
         const float hi_b =
             best + (ta.alpha * xl * cns[bj] + beta * (nx + cn2s[bj])) * (1.0f + gamma) + gamma * fabsf(best);
         // columns above T cannot reach hi_b even with the largest error of the
         // problem (norm maxima); only the others get the exact per-column test
         const float amax = (ta.alpha * xl * sqrtf(cmax0) + beta * (nx + cmax0)) * (1.0f + gamma);
         const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
-        // every other column's screen value is >= second: when second > T the
-        // per-column test below skips them all, so a warp whose rows all pass
-        // this skips the second TMEM pass
-        const bool clear = T > 0.0f && second > T;
-        if (!__all_sync(0xffffffffu, clear))
         for (int c0 = 0; c0 < kp; c0 += 32) {
           uint32_t bits = 0;
           uint32_t r[2][16];
