@@ -129,10 +129,10 @@ template <int KIND, int ORDER>
 __global__ void __launch_bounds__(kItemRows) batched_assign_kernel(
     const BProb* __restrict__ probs, int P, int items_total, const float* __restrict__ X,
     const float* __restrict__ C, int32_t* __restrict__ labels, unsigned long long* __restrict__ limbs,
-    int32_t* __restrict__ counts, int32_t* __restrict__ pchg, int first, int64_t work_total) {
+    int32_t* __restrict__ counts, int32_t* __restrict__ pchg, int first, int64_t work_total, int ccap) {
   extern __shared__ __align__(16) unsigned char smem_b[];
-  float* cs = reinterpret_cast<float*>(smem_b);                                           // [kCentreCap]
-  unsigned long long* agg = reinterpret_cast<unsigned long long*>(cs + kCentreCap);      // [kAggCap]
+  float* cs = reinterpret_cast<float*>(smem_b);                                           // [ccap]
+  unsigned long long* agg = reinterpret_cast<unsigned long long*>(cs + ccap);            // [kAggCap]
   int* aggc = reinterpret_cast<int*>(agg + kAggCap);                                      // [256]
   __shared__ int s_chg;
   const int64_t it0 = item_at_cost(probs, P, items_total, (int64_t)((__int128)work_total * blockIdx.x / gridDim.x));
@@ -168,7 +168,7 @@ __global__ void __launch_bounds__(kItemRows) batched_assign_kernel(
       __syncthreads();
       p = lo;
       pr = probs[p];
-      staged = pr.k * pr.d <= kCentreCap;
+      staged = pr.k * pr.d <= ccap;
       use_agg = pr.k * pr.d * pr.L <= kAggCap && pr.k <= 256;
       if (pr.active) {
         if (staged)
@@ -1198,7 +1198,13 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   FUELG_CUDA(cudaMemsetAsync(dIter.p, 0, sizeof(int32_t), s));
   FUELG_CUDA(cudaMemsetAsync(dInert.p, 0, sizeof(double) * P, s));
 
-  const size_t smem = sizeof(float) * kCentreCap + sizeof(unsigned long long) * kAggCap + sizeof(int) * 256;
+  // centre staging sized for the problems this kernel serves (those without
+  // the tensor-core screen): more resident CTAs when their centres are small
+  int ccap = 4;
+  for (int p = 0; p < P; p++)
+    if (!hp[p].tc) ccap = std::max<int64_t>(ccap, std::min<int64_t>(kCentreCap, (int64_t)hp[p].k * hp[p].d));
+  ccap = (ccap + 3) & ~3;
+  const size_t smem = sizeof(float) * ccap + sizeof(unsigned long long) * kAggCap + sizeof(int) * 256;
   auto k_init = order == FUELG_ORDER_X86 ? batched_assign_kernel<KIND_PAIRWISE, ORDER_X86>
                                          : batched_assign_kernel<KIND_PAIRWISE, ORDER_ARM>;
   auto k_iter = order == FUELG_ORDER_X86 ? batched_assign_kernel<KIND_SQDIST, ORDER_X86>
@@ -1289,11 +1295,11 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
       if (first)
         k_init<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
                                              dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                             dPchg.as<int32_t>(), 1, work);
+                                             dPchg.as<int32_t>(), 1, work, ccap);
       else
         k_iter<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
                                              dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
-                                             dPchg.as<int32_t>(), 0, work);
+                                             dPchg.as<int32_t>(), 0, work, ccap);
       note_launch();
     }
     if (tc_items > 0) {
@@ -1329,7 +1335,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   if (!bps && max_iter > 2) {
     float best_ms = 1e30f;
     int best_b = 3;
-    for (int b : {2, 3, 4}) {
+    for (int b : {2, 4, 8}) {
       if (done >= max_iter - 1) break;
       cudaEvent_t t0, t1;
       cudaEventCreate(&t0);
