@@ -442,12 +442,13 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   };
 
   // Middle passes (another pass follows) replay captured CUDA graphs from the
-  // fourth iteration on -- kPassesPerGraph consecutive passes per graph where
+  // second iteration on -- kPassesPerGraph consecutive passes per graph where
   // that many middle passes remain (and no tol check runs between passes), so
   // the screen of each pass can start its point loads while the centre update
   // of the previous one finishes; one pass per graph otherwise.  The first
-  // passes run as plain launches so the screen kernel's launches are timed
-  // individually.  Pass j of a graph writes its changed count to slot 2j: a
+  // pass and the last few run as plain launches, so the screen kernel's
+  // launches are timed individually in the steady state.  Pass j of a graph
+  // writes its changed count to slot 2j: a
   // pass that changed nothing leaves sums, centres and labels as they were,
   // so the passes after it in the same graph repeat it exactly and the loop
   // stops at the first such pass (lloyd.rs:197).
@@ -491,8 +492,12 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   const float* inertia_centers = C;
   FUELG_TRY(pass(true, p.max_iter > 1, changed.as<int32_t>()));
   int iters = 1;
+  // The last kTimedPasses passes before the final one (and the final one)
+  // run as plain launches: their screen launches are the ones timed
+  // individually (events around a launch inside a graph are not possible).
+  constexpr int kTimedPasses = 3;
   while (iters < p.max_iter) {
-    if (p.tol <= 0 && iters + 1 >= 4 && iters + kPassesPerGraph < p.max_iter) {
+    if (p.tol <= 0 && iters + kPassesPerGraph + kTimedPasses < p.max_iter) {
       // kPassesPerGraph middle passes in one graph
       FUELG_TRY(graph_pass(kPassesPerGraph));
       const int before = iters;
@@ -527,7 +532,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
         break;
       }
     }
-    if (iters >= 4 && iters < p.max_iter) FUELG_TRY(graph_pass(1));
+    if (iters + kTimedPasses < p.max_iter) FUELG_TRY(graph_pass(1));
     else FUELG_TRY(pass(false, iters < p.max_iter, changed.as<int32_t>()));
     if (!p.fixed_iters) {
       FUELG_CUDA(cudaMemcpyAsync(h_changed, changed.p, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
