@@ -866,6 +866,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
         atomicAdd(&counts[mt.cnt_off + lab], 1);
         if (old >= 0) atomicAdd(&counts[mt.cnt_off + old], -1);
       }
+      // the first pass's sums (every row enters) are made after the pass by
+      // the bucketed kernels below
+      if (first) continue;
       // the changed rows' coordinates into the exact sums: the warp takes the
       // rows that enter one cluster (or leave one) together -- lanes over
       // consecutive coordinates, the group's 32-bit slices summed in 64-bit
@@ -973,12 +976,122 @@ __global__ void __launch_bounds__(256) batched_rescore_kernel(
       atomicAdd(&counts[pr.cnt_off + lab], 1);
       if (old >= 0) atomicAdd(&counts[pr.cnt_off + old], -1);
     }
+    if (first) continue;  // the first pass's sums: tc_first_sum_kernel
     for (int t = lane; t < pr.d; t += 32) {
       const float xv = __ldg(xr + t);
       add_coord(limbs + pr.limb_off + ((int64_t)lab * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, false);
       if (old >= 0) add_coord(limbs + pr.limb_off + ((int64_t)old * pr.d + t) * pr.L, xv, pr.e_lo, pr.L, true);
     }
   }
+}
+
+// The first pass's exact sums of the tensor-core problems, after every row
+// has its label (so a warp sums runs of rows of one cluster in registers
+// instead of one atomic per row and counter): bucket offsets per cluster (one
+// warp per problem: exclusive prefix of its final counts, from the problem's
+// first row of the bucket array), the rows scattered into their clusters'
+// buckets, then one warp per 32 bucket entries.
+__global__ void tc_first_offsets_kernel(const BProb* __restrict__ probs, const int32_t* __restrict__ tcp, int ntc,
+                                        const int64_t* __restrict__ row_base, const int32_t* __restrict__ counts,
+                                        int64_t* __restrict__ boff, int32_t* __restrict__ cursor) {
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= ntc) return;
+  const BProb pr = probs[tcp[q]];
+  int64_t carry = row_base[q];
+  for (int j0 = 0; j0 < pr.k; j0 += 32) {
+    const int j = j0 + lane;
+    const int c = j < pr.k ? counts[pr.cnt_off + j] : 0;
+    int a = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, a, o);
+      if (lane >= o) a += u;
+    }
+    if (j < pr.k) {
+      boff[pr.cnt_off + j] = carry + a - c;
+      cursor[pr.cnt_off + j] = 0;
+    }
+    carry += __shfl_sync(0xffffffffu, a, 31);
+  }
+}
+
+__global__ void __launch_bounds__(kTcRows) tc_first_scatter_kernel(
+    const BProb* __restrict__ probs, const int32_t* __restrict__ tcp, const int32_t* __restrict__ item_begin,
+    int ntc, const int32_t* __restrict__ labels, const int64_t* __restrict__ boff, int32_t* __restrict__ cursor,
+    int32_t* __restrict__ b_row, int32_t* __restrict__ b_gc) {
+  const int item = blockIdx.x;
+  int lo = 0, hi = ntc;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (item_begin[mid] <= item) lo = mid;
+    else hi = mid;
+  }
+  const BProb pr = probs[tcp[lo]];
+  const int64_t i = (int64_t)(item - item_begin[lo]) * kTcRows + threadIdx.x;
+  const bool live = pr.active && i < pr.n;
+  const int gc = live ? pr.cnt_off + labels[pr.lab_off + i] : -1;
+  // one reservation per cluster among the warp's rows
+  const unsigned grp = __match_any_sync(0xffffffffu, gc);
+  const int lead = __ffs(grp) - 1;
+  int at = 0;
+  if (live && (int)(threadIdx.x & 31) == lead) at = atomicAdd(&cursor[gc], __popc(grp));
+  at = __shfl_sync(0xffffffffu, at, lead) + __popc(grp & ((1u << (threadIdx.x & 31)) - 1u));
+  if (live) {
+    const int64_t e = boff[gc] + at;
+    b_row[e] = (int32_t)i;
+    b_gc[e] = gc;
+  }
+}
+
+__global__ void __launch_bounds__(256) tc_first_sum_kernel(const BProb* __restrict__ probs,
+                                                           const int32_t* __restrict__ gc_prob, int64_t entries,
+                                                           const int32_t* __restrict__ b_row,
+                                                           const int32_t* __restrict__ b_gc,
+                                                           const float* __restrict__ X,
+                                                           unsigned long long* __restrict__ limbs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32;
+  if (w0 >= entries) return;
+  const int64_t e = w0 + lane;
+  const int myrow = e < entries ? b_row[e] : 0;
+  const int mygc = e < entries ? b_gc[e] : -1;
+  int cur = -1;
+  BProb pr{};
+  unsigned long long a0[4] = {0ull, 0ull, 0ull, 0ull}, a1[4] = {0ull, 0ull, 0ull, 0ull};
+  auto flush = [&]() {
+    if (cur < 0) return;
+    unsigned long long* dst = limbs + pr.limb_off + (int64_t)(cur - pr.cnt_off) * pr.d * pr.L;
+    for (int l = 0; l < pr.L; l++) {
+      if (lane < pr.d && a0[l]) atomicAdd(dst + (int64_t)lane * pr.L + l, a0[l]);
+      if (lane + 32 < pr.d && a1[l]) atomicAdd(dst + (int64_t)(lane + 32) * pr.L + l, a1[l]);
+      a0[l] = 0ull;
+      a1[l] = 0ull;
+    }
+  };
+#pragma unroll 4
+  for (int t = 0; t < 32; t++) {
+    const int gc = __shfl_sync(0xffffffffu, mygc, t);
+    if (gc < 0) break;
+    const int row = __shfl_sync(0xffffffffu, myrow, t);
+    if (gc != cur) {
+      flush();
+      cur = gc;
+      pr = probs[gc_prob[gc]];
+    }
+    const float* xr = X + pr.x_off + (int64_t)row * pr.d;
+    const float x0 = lane < pr.d ? __ldg(xr + lane) : 0.0f;
+    const float x1 = lane + 32 < pr.d ? __ldg(xr + lane + 32) : 0.0f;
+    const unsigned __int128 v0 = fixed_of(x0, pr.e_lo, false), v1 = fixed_of(x1, pr.e_lo, false);
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+      if (l < pr.L) {
+        a0[l] += (unsigned long long)((v0 >> (32 * l)) & 0xffffffffu);
+        a1[l] += (unsigned long long)((v1 >> (32 * l)) & 0xffffffffu);
+      }
+    }
+  }
+  flush();
 }
 
 struct DevBuf {
@@ -1236,6 +1349,28 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   ta.und_p = dUnd.as<int32_t>();
   ta.und_i = dUnd.as<int32_t>() + std::max<int64_t>(1, tc_rows);
   ta.und_m = reinterpret_cast<uint32_t*>(dUnd.as<int32_t>() + 2 * std::max<int64_t>(1, tc_rows));
+  // the first pass's bucketed sums of the tensor-core problems: the bucket
+  // array (row, cluster) reuses the undecided list's memory once the first
+  // re-score is done; rows of each active problem from row_base[q]
+  DevBuf dBoff, dCur, dGcp, dRowB;
+  int64_t tc_entries = 0;
+  if (tc_items > 0) {
+    std::vector<int64_t> rowb(ntc + 1);
+    for (int q = 0; q < ntc; q++) {
+      rowb[q] = tc_entries;
+      if (hp[tcp[q]].active) tc_entries += hp[tcp[q]].n;
+    }
+    rowb[ntc] = tc_entries;
+    std::vector<int32_t> gcp(std::max<int64_t>(1, ks));
+    for (int p = 0; p < P; p++)
+      for (int j = 0; j < hp[p].k; j++) gcp[hp[p].cnt_off + j] = p;
+    FUELG_TRY(dBoff.alloc(sizeof(int64_t) * std::max<int64_t>(1, ks)));
+    FUELG_TRY(dCur.alloc(sizeof(int32_t) * std::max<int64_t>(1, ks)));
+    FUELG_TRY(dGcp.alloc(sizeof(int32_t) * std::max<int64_t>(1, ks)));
+    FUELG_TRY(dRowB.alloc(sizeof(int64_t) * (ntc + 1)));
+    FUELG_CUDA(cudaMemcpyAsync(dGcp.p, gcp.data(), sizeof(int32_t) * gcp.size(), cudaMemcpyHostToDevice, s));
+    FUELG_CUDA(cudaMemcpyAsync(dRowB.p, rowb.data(), sizeof(int64_t) * (ntc + 1), cudaMemcpyHostToDevice, s));
+  }
   auto r_init = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_PAIRWISE, ORDER_X86>
                                          : batched_rescore_kernel<KIND_PAIRWISE, ORDER_ARM>;
   auto r_iter = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_SQDIST, ORDER_X86>
@@ -1315,6 +1450,24 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
                                                         dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
                                                         dPchg.as<int32_t>(), first ? 1 : 0);
       note_launch();
+      if (first) {
+        int32_t* b_row = dUnd.as<int32_t>();
+        int32_t* b_gc = b_row + std::max<int64_t>(1, tc_rows);
+        tc_first_offsets_kernel<<<(unsigned)((ntc * 32 + 255) / 256), 256, 0, s>>>(
+            dProbs.as<BProb>(), ta.tcp, ntc, dRowB.as<int64_t>(), dCnt.as<int32_t>(), dBoff.as<int64_t>(),
+            dCur.as<int32_t>());
+        note_launch();
+        tc_first_scatter_kernel<<<(unsigned)tc_items, kTcRows, 0, s>>>(dProbs.as<BProb>(), ta.tcp, ta.item_begin, ntc,
+                                                                       dLab.as<int32_t>(), dBoff.as<int64_t>(),
+                                                                       dCur.as<int32_t>(), b_row, b_gc);
+        note_launch();
+        if (tc_entries > 0) {
+          tc_first_sum_kernel<<<(unsigned)((tc_entries + 255) / 256), 256, 0, s>>>(
+              dProbs.as<BProb>(), dGcp.as<int32_t>(), tc_entries, b_row, b_gc, dX.as<float>(),
+              dLimbs.as<unsigned long long>());
+          note_launch();
+        }
+      }
     }
     // canonical counters every pass; new centres only when another pass follows
     batched_mean_kernel<<<mean_grid, 256, 0, s>>>(dProbs.as<BProb>(), P, dKdb.as<int64_t>(), kd,
