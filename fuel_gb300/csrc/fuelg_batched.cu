@@ -370,6 +370,12 @@ struct BTcArgs {
   uint32_t* und_m;                // and their candidate centres: und_w bit words per row
   int und_w;
   int* und_n;
+  // passes after the first: changed rows (row, new and old global cluster)
+  // listed for the bucketed sums while the list has room, and the per-key
+  // counts (key 2 gc: rows entering cluster gc, 2 gc + 1: rows leaving it)
+  int32_t *chg_row, *chg_new, *chg_old, *hist;
+  int* chg_n;
+  int chg_cap;
 };
 
 
@@ -869,14 +875,33 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       // the first pass's sums (every row enters) are made after the pass by
       // the bucketed kernels below
       if (first) continue;
-      // the changed rows' coordinates into the exact sums: the warp takes the
+      // later passes: the changed rows go to the change list (bucketed and
+      // summed after the pass) while it has room
+      bool listed = false;
+      {
+        const unsigned cmw = __ballot_sync(0xffffffffu, chg);
+        if (cmw) {
+          int at = 0;
+          if (lane == 0) at = atomicAdd(ta.chg_n, __popc(cmw));
+          at = __shfl_sync(0xffffffffu, at, 0) + __popc(cmw & ((1u << lane) - 1u));
+          if (chg && at < ta.chg_cap) {
+            listed = true;
+            ta.chg_row[at] = (int32_t)i;
+            ta.chg_new[at] = mt.cnt_off + lab;
+            ta.chg_old[at] = mt.cnt_off + old;
+            atomicAdd(&ta.hist[2 * (mt.cnt_off + lab)], 1);
+            atomicAdd(&ta.hist[2 * (mt.cnt_off + old) + 1], 1);
+          }
+        }
+      }
+      // the others' coordinates into the exact sums: the warp takes the
       // rows that enter one cluster (or leave one) together -- lanes over
       // consecutive coordinates, the group's 32-bit slices summed in 64-bit
       // registers (at most 32 slices: no overflow), one atomic per counter --
       // which gives the counters the same values as one add per row, since the
       // counters add modulo 2^64
       for (int dir = 0; dir < 2; dir++) {
-        const bool mine = chg && (dir == 0 || old >= 0);
+        const bool mine = chg && !listed && (dir == 0 || old >= 0);
         const int key = dir == 0 ? lab : old;
         unsigned pend = __ballot_sync(0xffffffffu, mine);
         while (pend) {
@@ -1092,6 +1117,137 @@ __global__ void __launch_bounds__(256) tc_first_sum_kernel(const BProb* __restri
     }
   }
   flush();
+}
+
+// Passes after the first: the listed changes' exact sums.  Bucket offsets per
+// key (one warp per problem: its keys' exclusive prefix, the problem's region
+// taken from a global counter; the counts and cursors are cleared for the next
+// pass), the listed rows scattered under their keys (one reservation per key
+// among a warp's rows), then one warp per 32 bucket entries sums runs of one
+// key in registers (rows leaving a cluster negated).  ctl: [0] listed rows,
+// [1] region counter, [2] bucket entries of the pass.
+__global__ void chg_offsets_kernel(const BProb* __restrict__ probs, const int32_t* __restrict__ tcp, int ntc,
+                                   int32_t* __restrict__ hist, int64_t* __restrict__ boff,
+                                   int32_t* __restrict__ cursor, int* __restrict__ ctl) {
+  const int lane = threadIdx.x & 31;
+  const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (q >= ntc) return;
+  const BProb pr = probs[tcp[q]];
+  const int nk = 2 * pr.k, k0 = 2 * pr.cnt_off;
+  int tot = 0;
+  for (int j0 = 0; j0 < nk; j0 += 32) tot += (j0 + lane < nk) ? hist[k0 + j0 + lane] : 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+  if (tot == 0) return;
+  int base = 0;
+  if (lane == 0) base = atomicAdd(&ctl[1], tot);
+  int64_t carry = __shfl_sync(0xffffffffu, base, 0);
+  for (int j0 = 0; j0 < nk; j0 += 32) {
+    const int j = j0 + lane;
+    const int c = j < nk ? hist[k0 + j] : 0;
+    int a = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, a, o);
+      if (lane >= o) a += u;
+    }
+    if (j < nk) {
+      boff[k0 + j] = carry + a - c;
+      cursor[k0 + j] = 0;
+      hist[k0 + j] = 0;
+    }
+    carry += __shfl_sync(0xffffffffu, a, 31);
+  }
+}
+
+__global__ void __launch_bounds__(256) chg_scatter_kernel(const int32_t* __restrict__ chg_row,
+                                                          const int32_t* __restrict__ chg_new,
+                                                          const int32_t* __restrict__ chg_old, int cap,
+                                                          const int64_t* __restrict__ boff,
+                                                          int32_t* __restrict__ cursor, int32_t* __restrict__ b_row,
+                                                          int32_t* __restrict__ b_key, int* __restrict__ ctl) {
+  const int lane = threadIdx.x & 31;
+  const int n = min(ctl[0], cap);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    ctl[2] = ctl[1];  // this pass's bucket entries
+    ctl[1] = 0;
+  }
+  const int stride = gridDim.x * blockDim.x;
+  for (int e0 = blockIdx.x * blockDim.x; e0 < n; e0 += stride) {
+    const int e = e0 + threadIdx.x;
+    const bool v = e < n;
+    const int row = v ? chg_row[e] : 0;
+#pragma unroll
+    for (int dir = 0; dir < 2; dir++) {
+      const int key = v ? 2 * (dir ? chg_old[e] : chg_new[e]) + dir : -1;
+      const unsigned grp = __match_any_sync(0xffffffffu, key);
+      const int lead = __ffs(grp) - 1;
+      int at = 0;
+      if (v && lane == lead) at = atomicAdd(&cursor[key], __popc(grp));
+      at = __shfl_sync(0xffffffffu, at, lead) + __popc(grp & ((1u << lane) - 1u));
+      if (v) {
+        const int64_t b = boff[key] + at;
+        b_row[b] = row;
+        b_key[b] = key;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) chg_sum_kernel(const BProb* __restrict__ probs,
+                                                      const int32_t* __restrict__ gc_prob,
+                                                      const int32_t* __restrict__ b_row,
+                                                      const int32_t* __restrict__ b_key, const float* __restrict__ X,
+                                                      unsigned long long* __restrict__ limbs, int* __restrict__ ctl) {
+  const int lane = threadIdx.x & 31;
+  const int64_t entries = ctl[2];
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl[0] = 0;  // the list, for the next pass
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w0 = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; w0 < entries; w0 += nw * 32) {
+    const int64_t e = w0 + lane;
+    const int myrow = e < entries ? b_row[e] : 0;
+    const int mykey = e < entries ? b_key[e] : -1;
+    int cur = -1;
+    BProb pr{};
+    unsigned long long a0[4] = {0ull, 0ull, 0ull, 0ull}, a1[4] = {0ull, 0ull, 0ull, 0ull};
+    auto flush = [&]() {
+      if (cur < 0) return;
+      unsigned long long* dst = limbs + pr.limb_off + (int64_t)((cur >> 1) - pr.cnt_off) * pr.d * pr.L;
+#pragma unroll
+      for (int l = 0; l < 4; l++) {
+        if (l < pr.L) {
+          if (lane < pr.d && a0[l]) atomicAdd(dst + (int64_t)lane * pr.L + l, a0[l]);
+          if (lane + 32 < pr.d && a1[l]) atomicAdd(dst + (int64_t)(lane + 32) * pr.L + l, a1[l]);
+        }
+        a0[l] = 0ull;
+        a1[l] = 0ull;
+      }
+    };
+#pragma unroll 4
+    for (int t = 0; t < 32; t++) {
+      const int key = __shfl_sync(0xffffffffu, mykey, t);
+      if (key < 0) break;
+      const int row = __shfl_sync(0xffffffffu, myrow, t);
+      if (key != cur) {
+        flush();
+        cur = key;
+        pr = probs[gc_prob[key >> 1]];
+      }
+      const float* xr = X + pr.x_off + (int64_t)row * pr.d;
+      const bool neg = (key & 1) != 0;
+      const float x0 = lane < pr.d ? __ldg(xr + lane) : 0.0f;
+      const float x1 = lane + 32 < pr.d ? __ldg(xr + lane + 32) : 0.0f;
+      const unsigned __int128 v0 = fixed_of(x0, pr.e_lo, neg), v1 = fixed_of(x1, pr.e_lo, neg);
+#pragma unroll
+      for (int l = 0; l < 4; l++) {
+        if (l < pr.L) {
+          a0[l] += (unsigned long long)((v0 >> (32 * l)) & 0xffffffffu);
+          a1[l] += (unsigned long long)((v1 >> (32 * l)) & 0xffffffffu);
+        }
+      }
+    }
+    flush();
+  }
 }
 
 struct DevBuf {
@@ -1371,6 +1527,27 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     FUELG_CUDA(cudaMemcpyAsync(dGcp.p, gcp.data(), sizeof(int32_t) * gcp.size(), cudaMemcpyHostToDevice, s));
     FUELG_CUDA(cudaMemcpyAsync(dRowB.p, rowb.data(), sizeof(int64_t) * (ntc + 1), cudaMemcpyHostToDevice, s));
   }
+  // later passes: the change list (room for half the tensor-core rows; the
+  // rest of a pass's changes take the epilogue's direct sums), its per-key
+  // counts, offsets and cursors, the buckets and three control words
+  DevBuf dChg, dHist, dKoff, dKcur, dBk, dCtl;
+  const int chg_cap = (int)std::max<int64_t>(1, tc_rows / 2);
+  if (tc_items > 0) {
+    FUELG_TRY(dChg.alloc(sizeof(int32_t) * 3 * (size_t)chg_cap));
+    FUELG_TRY(dHist.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks)));
+    FUELG_TRY(dKoff.alloc(sizeof(int64_t) * 2 * std::max<int64_t>(1, ks)));
+    FUELG_TRY(dKcur.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks)));
+    FUELG_TRY(dBk.alloc(sizeof(int32_t) * 4 * (size_t)chg_cap));
+    FUELG_TRY(dCtl.alloc(sizeof(int) * 4));
+    FUELG_CUDA(cudaMemsetAsync(dHist.p, 0, sizeof(int32_t) * 2 * std::max<int64_t>(1, ks), s));
+    FUELG_CUDA(cudaMemsetAsync(dCtl.p, 0, sizeof(int) * 4, s));
+    ta.chg_row = dChg.as<int32_t>();
+    ta.chg_new = ta.chg_row + chg_cap;
+    ta.chg_old = ta.chg_new + chg_cap;
+    ta.hist = dHist.as<int32_t>();
+    ta.chg_n = dCtl.as<int>();
+    ta.chg_cap = chg_cap;
+  }
   auto r_init = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_PAIRWISE, ORDER_X86>
                                          : batched_rescore_kernel<KIND_PAIRWISE, ORDER_ARM>;
   auto r_iter = order == FUELG_ORDER_X86 ? batched_rescore_kernel<KIND_SQDIST, ORDER_X86>
@@ -1467,6 +1644,21 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
               dLimbs.as<unsigned long long>());
           note_launch();
         }
+      } else {
+        int32_t* b_row = dBk.as<int32_t>();
+        int32_t* b_key = b_row + 2 * (size_t)chg_cap;
+        chg_offsets_kernel<<<(unsigned)((ntc * 32 + 255) / 256), 256, 0, s>>>(
+            dProbs.as<BProb>(), ta.tcp, ntc, dHist.as<int32_t>(), dKoff.as<int64_t>(), dKcur.as<int32_t>(),
+            dCtl.as<int>());
+        note_launch();
+        chg_scatter_kernel<<<(unsigned)(sms * 4), 256, 0, s>>>(ta.chg_row, ta.chg_new, ta.chg_old, chg_cap,
+                                                               dKoff.as<int64_t>(), dKcur.as<int32_t>(), b_row, b_key,
+                                                               dCtl.as<int>());
+        note_launch();
+        chg_sum_kernel<<<(unsigned)(sms * 8), 256, 0, s>>>(dProbs.as<BProb>(), dGcp.as<int32_t>(), b_row, b_key,
+                                                           dX.as<float>(), dLimbs.as<unsigned long long>(),
+                                                           dCtl.as<int>());
+        note_launch();
       }
     }
     // canonical counters every pass; new centres only when another pass follows
