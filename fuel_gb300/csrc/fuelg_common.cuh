@@ -48,6 +48,13 @@ __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wa
 // grid to complete.  Called right after griddep_wait(): the successor is
 // scheduled only once this kernel's own predecessors have completed.
 __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte
+// aligned); cp_async_wait_all() waits for the calling thread's copies.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
 // Per-pair distances, NP point rows against one query row, all in shared

@@ -373,12 +373,14 @@ __global__ void mean_kernel(unsigned long long* __restrict__ limbs, int64_t kd, 
     mean_elem<L>(limbs, e, d, e_lo, counts, centers, write_centers);
 }
 
-// The same update, one block per centre row, which also writes the row's
-// BF16 copies (of fl(scale * c)) and norms for the next pass's tensor-core
-// screen (block j >= k: a zero padding row of the copies).  Every thread
-// converts the coordinates it computed; the squared norm is a per-thread FP32
-// sum of ceil(dp/256) terms and an 8-level tree, within (ceil(d/32) + 9) 2^-24
-// relative -- the beta term of the screen's bound.
+// The same update, two blocks per centre row (each one half of its columns),
+// which also writes the row's BF16 copies (of fl(scale * c)) and squared-norm
+// halves for the next pass's tensor-core screen (rows j >= k: zero padding
+// rows of the copies).  Every thread converts the coordinates it computed;
+// each half's squared norm is a per-thread FP32 sum of at most ceil(dp/512)
+// terms and an 8-level tree, stored at nrm2[h * kp + j]; the screen adds the
+// two halves: within (ceil(d/32) + 9) 2^-24 relative -- the beta term of the
+// screen's bound.
 template <int L, bool SPLIT>
 __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __restrict__ limbs, int k, int d,
                                                         int e_lo, const int32_t* __restrict__ counts,
@@ -390,7 +392,9 @@ __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __re
   griddep_launch();
   mean_handoff(blockIdx.x, gridDim.x, nchg, changed, zero4k, nzero);
   if (cp.zero_word != nullptr && blockIdx.x == 0 && threadIdx.x == 0) *cp.zero_word = 0;
-  const int j = blockIdx.x;
+  const int j = blockIdx.x >> 1, half = blockIdx.x & 1;
+  const int cpb = ((cp.dp + 1) / 2 + 255) & ~255;  // columns of the first half
+  const int c_lo = half * cpb, c_hi = min(cp.dp, c_lo + cpb);
   float acc = 0.0f;
   // the limbs, old centre values and count this thread needs, loaded before
   // any is used (one memory round trip for rows of up to kPer * 256 columns)
@@ -400,8 +404,8 @@ __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __re
   const int cnt = j < k ? counts[j] : 0;
 #pragma unroll
   for (int u = 0; u < kPer; u++) {
-    const int c = threadIdx.x + u * 256;
-    const bool v = j < k && c < d;
+    const int c = c_lo + threadIdx.x + u * 256;
+    const bool v = j < k && c < d && c < c_hi;
     const int64_t e = (int64_t)j * d + c;
 #pragma unroll
     for (int l = 0; l < L; l++) lv[u][l] = v ? limbs[e * L + l] : 0ull;
@@ -416,13 +420,13 @@ __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __re
   };
 #pragma unroll
   for (int u = 0; u < kPer; u++) {
-    const int c = threadIdx.x + u * 256;
-    if (c >= cp.dp) break;
+    const int c = c_lo + threadIdx.x + u * 256;
+    if (c >= c_hi) break;
     const int64_t e = (int64_t)j * d + c;
     const float v = (j < k && c < d) ? mean_of<L>(limbs + e * L, lv[u], cnt, e_lo, centers + e, oldc[u], 1) : 0.0f;
     emit(c, v);
   }
-  for (int c = threadIdx.x + kPer * 256; c < cp.dp; c += blockDim.x) {
+  for (int c = c_lo + threadIdx.x + kPer * 256; c < c_hi; c += blockDim.x) {
     const float v = (j < k && c < d) ? mean_elem<L>(limbs, (int64_t)j * d + c, d, e_lo, counts, centers, 1) : 0.0f;
     emit(c, v);
   }
@@ -433,8 +437,7 @@ __global__ void __launch_bounds__(256) mean_prep_kernel(unsigned long long* __re
   if (threadIdx.x == 0) {
     const float a01 = part[0] + part[1], a23 = part[2] + part[3], a45 = part[4] + part[5], a67 = part[6] + part[7];
     const float nn = (a01 + a23) + (a45 + a67);
-    cp.nrm2[j] = nn;
-    cp.nrm[j] = sqrtf(nn);
+    cp.nrm2[half * cp.kp + j] = nn;
   }
 }
 
@@ -560,7 +563,7 @@ int exact_sums_update(ExactSums* s, const float* X, bool write_centers, float* c
                          (const int32_t*)s->bucket_out.as<int32_t>(), s->limbs.as<unsigned long long>()));
     if (prep) {
       auto mk = cp->lo != nullptr ? mean_prep_kernel<LL, true> : mean_prep_kernel<LL, false>;
-      FUELG_TRY(launch_pdl(mk, dim3((unsigned)cp->kp), dim3(256), 0, stream, s->limbs.as<unsigned long long>(), k, d,
+      FUELG_TRY(launch_pdl(mk, dim3((unsigned)(2 * cp->kp)), dim3(256), 0, stream, s->limbs.as<unsigned long long>(), k, d,
                            s->e_lo, (const int32_t*)s->counts.as<int32_t>(), centers, s->nchg.as<int32_t>(), changed,
                            cin, 4 * k, *cp));
     } else {

@@ -277,13 +277,15 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   if (warp >= 2) {
     const int kp64 = (a.kp + 63) & ~63;
     for (int j = threadIdx.x - 64; j < kp64; j += BM) {
+      // squared norms: the sum of the two halves the centre update wrote
+      const float nc2 = j < a.kp ? a.nc[j] + a.nc[a.kp + j] : 0.0f;
       if (j < a.kp) {
-        snc[j] = a.nc[j];
-        scn[j] = a.cn[j];
+        snc[j] = nc2;
+        scn[j] = sqrtf(nc2);
         h_in[j] = 0;
         h_out[j] = 0;
       }
-      sncd[j] = j < a.k ? a.nc[j] : __int_as_float(0x7f800000);
+      sncd[j] = j < a.k ? nc2 : __int_as_float(0x7f800000);
     }
     named_bar_sync(1, BM);
     for (int j = 0; j < a.k; j++) {
@@ -840,8 +842,10 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
     const int32_t old = (commit && lane == 0) ? labels[i] : 0;
     const float* x = X + i * d;
     __syncwarp();
+    // 16-byte rows by asynchronous copies: the point row and the first group
+    // of candidate rows below arrive in one round trip
     if (v4)
-      for (int e = lane; e < d / 4; e += 32) reinterpret_cast<float4*>(xs)[e] = __ldg(reinterpret_cast<const float4*>(x) + e);
+      for (int e = lane; e < d / 4; e += 32) cp_async16(xs + 4 * e, x + 4 * e);
     else
       for (int e = lane; e < d; e += 32) xs[e] = __ldg(x + e);
     uint64_t best = KEY_NONE;
@@ -866,11 +870,11 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
         const float* c = C + (int64_t)js[t] * d;
         float* dst = cs + (size_t)t * ds;
         if (v4)
-          for (int e = lane; e < d / 4; e += 32)
-            reinterpret_cast<float4*>(dst)[e] = __ldg(reinterpret_cast<const float4*>(c) + e);
+          for (int e = lane; e < d / 4; e += 32) cp_async16(dst + 4 * e, c + 4 * e);
         else
           for (int e = lane; e < d; e += 32) dst[e] = __ldg(c + e);
       }
+      cp_async_wait_all();
       __syncwarp();
       const bool mine = slot < got;
       if (!mine) j = 0;
@@ -881,6 +885,7 @@ __global__ void __launch_bounds__(128) rescore_smem_kernel(const float* __restri
       }
       if (got < PER) break;
     }
+    cp_async_wait_all();  // (every row has a candidate: nothing is left in flight)
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       const uint64_t o = __shfl_xor_sync(0xffffffffu, best, off);
@@ -1008,7 +1013,10 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   const size_t cb = (size_t)st->kp * st->dp * 2;
   FUELG_TRY(st->chi.alloc(cb, stream));
   if (blo) FUELG_TRY(st->clo.alloc(cb, stream));
-  FUELG_TRY(st->cnrm2.alloc(sizeof(float) * st->kp, stream));
+  // [2][kp]: the centre update writes the squared norm in two halves (the
+  // first-pass preparation writes the first, the second stays zero)
+  FUELG_TRY(st->cnrm2.alloc(sizeof(float) * 2 * st->kp, stream));
+  FUELG_CUDA(cudaMemsetAsync(st->cnrm2.p, 0, sizeof(float) * 2 * st->kp, stream));
   FUELG_TRY(st->cnrm.alloc(sizeof(float) * st->kp, stream));
   FUELG_TRY(st->ulist.alloc(sizeof(int32_t) * n, stream));
   FUELG_TRY(st->umask.alloc(sizeof(uint64_t) * n * st->mw, stream));
