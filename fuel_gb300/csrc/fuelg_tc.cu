@@ -208,7 +208,8 @@ __global__ void __launch_bounds__(kTcThreads, 2)
   uint64_t* fin = acce + 2;
   uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(fin + 1);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_holder + 1);
-  float* snc = reinterpret_cast<float*>(tmem_holder + 4);
+  // centre norms (16-byte aligned: pass 2 reads them four at a time)
+  float* snc = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(tmem_holder + 4) + 15) & ~(uintptr_t)15);
   float* scn = snc + a.kp;
   int32_t* h_in = reinterpret_cast<int32_t*>(scn + a.kp);  // fused: per-CTA in/out histograms
   int32_t* h_out = h_in + a.kp;
@@ -556,29 +557,47 @@ __global__ void __launch_bounds__(kTcThreads, 2)
         const bool easy = cta_finite && nxi < 0x1p124f && (second - tb) >= hu;
         if (__any_sync(0xffffffffu, !easy)) {
           // pass 2: every other centre whose lower bound reaches the best's
-          // upper bound (the columns re-read from TMEM, 16 at a time)
+          // upper bound (the columns re-read from TMEM, 32 per wait)
           uint32_t blo = 0, bhi = 0;
 #pragma unroll
-          for (int c0 = 0; c0 < 64; c0 += 16) {
-            if (c0 >= a.kp) break;
-            uint32_t rh[16], rl[16];
-            tmem_ld16_nowait(taddr + c0, rh);
-            if (BLO && a.sep_lo) tmem_ld16_nowait(taddr + a.kp + c0, rl);
-            tmem_ld_wait();
-            tmem_regs_ready(rh);
-            if (BLO && a.sep_lo) tmem_regs_ready(rl);
+          for (int r = 0; r < 2; r++) {
+            if (32 * r >= a.kp) break;
+            uint32_t rh[2][16], rl[2][16];
 #pragma unroll
-            for (int j = 0; j < 16; j++) {
-              const int col = c0 + j;
-              float x = __uint_as_float(rh[j]);
-              if (BLO && a.sep_lo) x += __uint_as_float(rl[j]);
-              const float dt = fmaf(-2.0f, x, nxi + snc[col]);
-              const float sj = nonneg ? fmaxf(x, 0.0f) * a.s_scale : xni * scn[col];
-              const float e = (a.alpha * sj + a.beta * (nxi + snc[col])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
-              const uint32_t cb = !(dt - e > hi) ? 1u : 0u;
-              if (col < 32) blo |= cb << col;
-              else bhi |= cb << (col - 32);
+            for (int h = 0; h < 2; h++)
+              if (32 * r + 16 * h < a.kp) {
+                tmem_ld16_nowait(taddr + 32 * r + 16 * h, rh[h]);
+                if (BLO && a.sep_lo) tmem_ld16_nowait(taddr + a.kp + 32 * r + 16 * h, rl[h]);
+              }
+            tmem_ld_wait();
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              tmem_regs_ready(rh[h]);
+              if (BLO && a.sep_lo) tmem_regs_ready(rl[h]);
             }
+            uint32_t bits = 0;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+              if (32 * r + 16 * h >= a.kp) break;
+#pragma unroll
+              for (int q = 0; q < 4; q++) {
+                const int c4 = 32 * r + 16 * h + 4 * q;
+                const float4 n4 = *reinterpret_cast<const float4*>(snc + c4);
+                const float4 s4 = *reinterpret_cast<const float4*>(scn + c4);
+                const float nn[4] = {n4.x, n4.y, n4.z, n4.w}, ss[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                  float x = __uint_as_float(rh[h][4 * q + u]);
+                  if (BLO && a.sep_lo) x += __uint_as_float(rl[h][4 * q + u]);
+                  const float dt = fmaf(-2.0f, x, nxi + nn[u]);
+                  const float sj = nonneg ? fmaxf(x, 0.0f) * a.s_scale : xni * ss[u];
+                  const float e = (a.alpha * sj + a.beta * (nxi + nn[u])) * (1.0f + a.gamma) + a.gamma * fabsf(dt);
+                  bits |= (!(dt - e > hi) ? 1u : 0u) << (16 * h + 4 * q + u);
+                }
+              }
+            }
+            if (r == 0) blo = bits;
+            else bhi = bits;
           }
           const uint64_t kmask = a.k >= 64 ? ~0ull : ((1ull << a.k) - 1ull);
           m0 = ((((uint64_t)bhi) << 32) | blo) & kmask & ~(1ull << bj);
@@ -1003,7 +1022,7 @@ int lloyd_tc_prepare(const LloydParams& p, TcLloydState* st, cudaStream_t stream
   }
   st->ctas_per_sm = per_sm;
   st->stages = stages;
-  st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 16 * st->kp + 16 +
+  st->smem = 1024 + stages * stage_bytes + 8 * (2 * stages + 5) + 16 + 16 + 16 * st->kp + 16 +
               4 * ((st->kp + 63) / 64 * 64) + 16;
   if (st->smem > 227 * 1024) {
     set_error("tensor-core Lloyd tile does not fit shared memory (k=%d)", p.k);
