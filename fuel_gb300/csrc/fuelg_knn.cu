@@ -28,7 +28,8 @@ namespace fuelg {
 namespace {
 
 constexpr int kThreads = 128;
-constexpr int kCB = 16;  // candidate buffer entries per thread
+constexpr int kCB = 16;  // candidate buffer entries per thread, at most (kCbSmallK for small k)
+constexpr int kCbSmallK = 8;  // for kk <= 16: a smaller buffer leaves room for more resident CTAs
 
 struct ScanArgs {
   const float* A;
@@ -48,6 +49,7 @@ struct ScanArgs {
   int a_vec4, b_vec4; // rows may be staged with 16-byte loads (d % 4 == 0 and 16-byte aligned base)
   int* status;
   const volatile int* cancel;
+  int kcb;            // candidate buffer entries per thread (<= kCB)
 };
 
 __device__ __forceinline__ void stage_rows(float* __restrict__ dst, int dstride, const float* __restrict__ src,
@@ -165,7 +167,7 @@ __device__ __forceinline__ void scan_topk_body(const ScanArgs& a, int64_t qb, in
           }
         }
       }
-      if (!KK1 && cnt > kCB - NP) {
+      if (!KK1 && cnt > a.kcb - NP) {
         tau = merge_buffer(buf + tid, cnt, list, half, a.kk);
         cnt = 0;
       }
@@ -297,6 +299,7 @@ struct Plan {
   int ws, qpb, pt, qs, xs, np, S_grid;
   int64_t split_len;
   size_t smem;
+  int kcb;
 };
 
 int make_plan(const ExactScanParams& p, bool kk1, int np, Plan* pl) {
@@ -315,7 +318,8 @@ int make_plan(const ExactScanParams& p, bool kk1, int np, Plan* pl) {
   int pt = (int)((24 * 1024) / qrow);
   pt = std::max(unit, std::min(128, pt));
   pt = (pt / unit) * unit;
-  size_t smem = (size_t)qpb * qrow + (size_t)pt * qrow + (kk1 ? 0 : (size_t)kThreads * kCB * 8);
+  const int kcb = p.kk <= 16 ? kCbSmallK : kCB;
+  size_t smem = (size_t)qpb * qrow + (size_t)pt * qrow + (kk1 ? 0 : (size_t)kThreads * kcb * 8);
   const int64_t qblocks = (p.m + qpb - 1) / qpb;
   int64_t want = (8 * 152 + qblocks - 1) / qblocks;
   int64_t tiles = (p.n + pt - 1) / pt;
@@ -324,7 +328,7 @@ int make_plan(const ExactScanParams& p, bool kk1, int np, Plan* pl) {
   split_len = ((split_len + pt - 1) / pt) * pt;
   if (split_len == 0) split_len = pt;
   S_grid = std::max<int64_t>(1, (p.n + split_len - 1) / split_len);
-  *pl = Plan{ws, qpb, pt, qs, qs, np, (int)S_grid, split_len, smem};
+  *pl = Plan{ws, qpb, pt, qs, qs, np, (int)S_grid, split_len, smem, kcb};
   return ST_OK;
 }
 
@@ -385,6 +389,7 @@ int exact_topk(const ExactScanParams& p, uint64_t* out_keys, int* dev_status, cu
     a.ws = pl.ws;
     a.qpb = pl.qpb;
     a.pt = pl.pt;
+    a.kcb = pl.kcb;
     a.qs = pl.qs;
     a.xs = pl.xs;
     a.lists = kk1 ? nullptr : lists.as<uint64_t>();
@@ -513,6 +518,7 @@ int exact_knn_sets(const KnnSetDev* sets, int count, int order, int* dev_status,
     a.ws = pl.ws;
     a.qpb = pl.qpb;
     a.pt = pl.pt;
+    a.kcb = pl.kcb;
     a.qs = pl.qs;
     a.xs = pl.xs;
     a.status = dev_status;
@@ -695,6 +701,7 @@ int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int6
     a.ws = pl.ws;
     a.qpb = pl.qpb;
     a.pt = pl.pt;
+    a.kcb = pl.kcb;
     a.qs = pl.qs;
     a.xs = pl.xs;
     a.lists = kk1 ? nullptr : lists;
@@ -844,6 +851,7 @@ int exact_range(const ExactScanParams& p, float radius, int exclude_self, int64_
   a.ws = pl.ws;
   a.qpb = pl.qpb;
   a.pt = pl.pt;
+  a.kcb = pl.kcb;
   a.qs = pl.qs;
   a.xs = pl.xs;
   a.a_vec4 = vec4_ok(a.A, a.d);
