@@ -70,3 +70,32 @@ def test_batched_config_sample(gpu):
     for (X, init), g in zip(probs, got):
         ref = kmeans(X, k=init.shape[0], variant="lloyd", init=init, max_iter=8, fixed_iters=True)
         _same(g, ref)
+
+
+@pytest.mark.gpu
+def test_batched_change_list_overflow(gpu):
+    """A pass in which most tensor-core rows change: the first update moves
+    centre 0 away from the majority, which then moves to centre 1 (75% of
+    the rows).  The change list holds half of the tensor-core rows, so the
+    rest of the pass takes the screen epilogue's direct sums; the result must
+    still equal the single-problem call and the exact-mean oracle."""
+    from oracle import oracle
+    rng = np.random.default_rng(21)
+    n, d = 4096, 32
+    X = rng.normal(scale=0.01, size=(n, d)).astype(np.float32)
+    X[: 3 * n // 4, 0] += 0.0          # majority near x0 = 0
+    X[3 * n // 4:, 0] += 100.0         # minority near x0 = 100
+    init = np.zeros((2, d), np.float32)
+    init[0, 0] = 1.0                   # pass 1: every row nearest centre 0
+    init[1, 0] = -1.5                  # pass 2: centre 0 at ~25 -> the majority moves here
+    small = workloads.batched_kmeans_data((300, 8, 3, 7))  # a CUDA-core problem alongside
+    probs = [(X, init), small]
+    got = kmeans_batched(probs, max_iter=6, fixed_iters=True, precision="split_bf16")
+    ref = kmeans(X, k=2, variant="lloyd", init=init, max_iter=6, fixed_iters=True)
+    _same(got[0], ref)
+    rc, rl, rit, _ = oracle.lloyd_exact(X, 2, init, max_iter=6, fixed_iters=True)
+    np.testing.assert_array_equal(got[0].centers.view(np.uint32), rc.view(np.uint32))
+    np.testing.assert_array_equal(got[0].labels, rl)
+    assert (rl == 1).sum() >= n // 2, "most rows must have moved to centre 1"
+    rs = kmeans(small[0], k=small[1].shape[0], variant="lloyd", init=small[1], max_iter=6, fixed_iters=True)
+    _same(got[1], rs)
