@@ -584,7 +584,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
             const float* cj = C + pr.c_off + (int64_t)j * pr.d;
             v = norm2_blocked([&](int t) { return cj[t]; }, pr.d);
           }
-          cn2s[j] = v;  // zero past k: the epilogue reads them four at a time
+          // +inf past k: the epilogue reads them four at a time, and a padding
+          // column's screen value is then +inf (never the minimum)
+          cn2s[j] = j < pr.k ? v : __int_as_float(0x7f800000);
           cns[j] = sqrtf(v);
           m2 = fmaxf(m2, v);
         }
@@ -763,14 +765,16 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
       uint32_t cmask[8];
       uint32_t cm_set = 0;
       if (kp > 0) {
-        // screen: best centre, then every centre whose lower bound reaches its
-        // upper bound; TMEM read 32 columns per wait.  The best centre is the
-        // first minimum (strict <), kept as four independent running minima over
-        // the columns of each residue mod 4 and merged by (distance, column):
-        // the same centre as one scan in column order, with a quarter of the
-        // dependency chain.
+        // screen, two passes over the TMEM columns (32 per wait).  Pass 1: the
+        // smallest screen value (four independent running minima over the
+        // columns of each residue mod 4; the padding columns past k read +inf
+        // norms).  The best centre's upper bound is taken with the problem's
+        // norm maxima (at least its own error term), so it needs no column
+        // index.  Pass 2: the first column holding the smallest value is the
+        // best centre (first index wins ties, as in a scan), and every other
+        // column whose lower bound reaches the bound is a candidate; columns
+        // above T cannot reach it with the largest error of the problem.
         float b4[4] = {best, best, best, best};
-        int j4[4] = {0, 0, 0, 0};
         for (int c0 = 0; c0 < kp; c0 += 32) {
           uint32_t r[2][16];
 #pragma unroll
@@ -780,34 +784,23 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
 #pragma unroll
           for (int h = 0; h < 2; h++) tcx::tmem_regs_ready(r[h]);
 #pragma unroll
-          for (int h = 0; h < 2; h++)
+          for (int h = 0; h < 2; h++) {
+            if (c0 + 16 * h >= kp) break;
 #pragma unroll
             for (int v = 0; v < 4; v++) {
               const float4 c4 = *reinterpret_cast<const float4*>(cn2s + c0 + 16 * h + 4 * v);
               const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
 #pragma unroll
-              for (int u = 0; u < 4; u++) {
-                const int col = c0 + 16 * h + 4 * v + u;
-                const float dt = fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]);
-                if (col < mt.k && dt < b4[u]) {
-                  b4[u] = dt;
-                  j4[u] = col;
-                }
-              }
+              for (int u = 0; u < 4; u++)
+                b4[u] = fminf(b4[u], fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]));
             }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; u++)
-          if (b4[u] < best || (b4[u] == best && j4[u] < bj)) {
-            best = b4[u];
-            bj = j4[u];
           }
-        const float hi_b =
-            best + (ta.alpha * xl * cns[bj] + beta * (nx + cn2s[bj])) * (1.0f + gamma) + gamma * fabsf(best);
-        // columns above T cannot reach hi_b even with the largest error of the
-        // problem (norm maxima); only the others get the exact per-column test
+        }
+        best = fminf(fminf(b4[0], b4[1]), fminf(b4[2], b4[3]));
         const float amax = (ta.alpha * xl * sqrtf(cmax0) + beta * (nx + cmax0)) * (1.0f + gamma);
+        const float hi_b = best + amax + gamma * fabsf(best);
         const float T = (hi_b + amax) * (1.0f + 2.0f * gamma) * (1.0f + 9.5367431640625e-07f);
+        bool found = false;
         for (int c0 = 0; c0 < kp; c0 += 32) {
           uint32_t bits = 0;
           uint32_t r[2][16];
@@ -818,7 +811,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
 #pragma unroll
           for (int h = 0; h < 2; h++) tcx::tmem_regs_ready(r[h]);
 #pragma unroll
-          for (int h = 0; h < 2; h++)
+          for (int h = 0; h < 2; h++) {
+            if (c0 + 16 * h >= kp) break;
 #pragma unroll
             for (int v = 0; v < 4; v++) {
               const float4 c4 = *reinterpret_cast<const float4*>(cn2s + c0 + 16 * h + 4 * v);
@@ -827,18 +821,29 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
               for (int u = 0; u < 4; u++) {
                 const int col = c0 + 16 * h + 4 * v + u;
                 const float dt = fmaf(-2.0f, __uint_as_float(r[h][4 * v + u]), nx + cc[u]);
-                if (col < mt.k && col != bj && (!(T > 0.0f) || !(dt > T))) {
+                if (!found && dt == best) {
+                  found = true;
+                  bj = col;
+                } else if (col < mt.k && (!(T > 0.0f) || !(dt > T))) {
                   const float e =
                       (ta.alpha * xl * cns[col] + beta * (nx + cc[u])) * (1.0f + gamma) + gamma * fabsf(dt);
                   if (!(dt - e > hi_b)) bits |= 1u << (16 * h + 4 * v + u);
                 }
               }
             }
+          }
           if (bits) {
             undecided = true;
             cmask[c0 >> 5] = bits;
             cm_set |= 1u << (c0 >> 5);
           }
+        }
+        // no column equal to the minimum (a NaN screen value): the re-score
+        // decides among every centre
+        if (!found) {
+          undecided = true;
+          for (int w = 0; w < (kp + 31) / 32; w++) cmask[w] = 0xffffffffu;
+          cm_set = (1u << ((kp + 31) / 32)) - 1u;
         }
       }
       // the item's accumulator, tile and parameters are no longer read
