@@ -304,12 +304,19 @@ __device__ __forceinline__ float exact_dist_fn(QF q, XF x) {
   constexpr bool lane8 = (KIND == KIND_KNN) || (KIND == KIND_SQDIST && ORDER == ORDER_ARM);
   constexpr bool fma8 = (KIND == KIND_KNN && ORDER == ORDER_X86);
   if constexpr (lane8) {
+    // A lane's first term is added to +0: the sum is the square itself
+    // (x*x >= +0, NaN stays the canonical NaN), so it is taken as is.
     float acc[8];
-#pragma unroll
-    for (int l = 0; l < 8; l++) acc[l] = 0.0f;
     constexpr int sd = D & ~7;
+    if constexpr (sd >= 8) {
 #pragma unroll
-    for (int i = 0; i < sd; i += 8) {
+      for (int l = 0; l < 8; l++) acc[l] = sq_rn(__fsub_rn(q(l), x(l)));
+    } else {
+#pragma unroll
+      for (int l = 0; l < 8; l++) acc[l] = 0.0f;
+    }
+#pragma unroll
+    for (int i = 8; i < sd; i += 8) {
 #pragma unroll
       for (int l = 0; l < 8; l++) {
         const float df = __fsub_rn(q(i + l), x(i + l));
@@ -322,7 +329,7 @@ __device__ __forceinline__ float exact_dist_fn(QF q, XF x) {
 #pragma unroll
     for (int i = sd; i < D; i++) {
       const float df = __fsub_rn(q(i), x(i));
-      s = fma8 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df));
+      s = (sd == 0 && i == 0) ? sq_rn(df) : (fma8 ? __fmaf_rn(df, df, s) : __fadd_rn(s, sq_rn(df)));
     }
     return s;
   } else if constexpr (KIND == KIND_SQDIST) {  // x86 avx2::sqdist_f32
