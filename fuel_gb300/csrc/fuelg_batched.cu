@@ -1536,7 +1536,8 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   // rest of a pass's changes take the epilogue's direct sums), its per-key
   // counts, offsets and cursors, the buckets and three control words
   DevBuf dChg, dHist, dKoff, dKcur, dBk, dCtl;
-  const int chg_cap = (int)std::max<int64_t>(1, tc_rows / 2);
+  // (bucket positions and the region counter are 32-bit: at most 2^29 listed rows)
+  const int chg_cap = (int)std::max<int64_t>(1, std::min<int64_t>(tc_rows / 2, 1ll << 29));
   if (tc_items > 0) {
     FUELG_TRY(dChg.alloc(sizeof(int32_t) * 3 * (size_t)chg_cap));
     FUELG_TRY(dHist.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks)));
