@@ -1323,6 +1323,20 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     cudaStream_t s;
     ~SG() { cudaStreamDestroy(s); }
   } sg{s};
+  // the CUDA-core kernel's stream (forked from s and joined back every pass)
+  cudaStream_t s2;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+  SG sg2{s2};
+  cudaEvent_t ev_fork, ev_join;
+  FUELG_CUDA(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  FUELG_CUDA(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  struct EG2 {
+    cudaEvent_t a, b;
+    ~EG2() {
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+    }
+  } eg2{ev_fork, ev_join};
   const int64_t launches0 = launch_count();
   cudaEvent_t ev0, ev1, evh0, evh1;
   cudaEventCreate(&ev0);
@@ -1478,6 +1492,12 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   for (int p = 0; p < P; p++)
     if (!hp[p].tc) ccap = std::max<int64_t>(ccap, std::min<int64_t>(kCentreCap, (int64_t)hp[p].k * hp[p].d));
   ccap = (ccap + 3) & ~3;
+  // With tensor-core problems in the batch the CUDA-core kernel runs beside the
+  // screen (its own stream, joined before the centre update): with the centres
+  // of the problems it serves (d < 32) one of its CTAs fits beside the
+  // screen's on every SM, and its warps use the issue slots the screen's
+  // epilogue leaves.
+  const bool concurrent = items > 0 && tc_items > 0;
   const size_t smem = sizeof(float) * ccap + sizeof(unsigned long long) * kAggCap + sizeof(int) * 256;
   auto k_init = order == FUELG_ORDER_X86 ? batched_assign_kernel<KIND_PAIRWISE, ORDER_X86>
                                          : batched_assign_kernel<KIND_PAIRWISE, ORDER_ARM>;
@@ -1609,13 +1629,19 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   (void)fixed;  // every pass runs; the reported count follows the changed == 0 stop unless fixed
 
   auto pass = [&](bool first, bool write, unsigned grid) -> int {
+    cudaStream_t sc = s;
+    if (concurrent) {
+      FUELG_CUDA(cudaEventRecord(ev_fork, s));
+      FUELG_CUDA(cudaStreamWaitEvent(s2, ev_fork, 0));
+      sc = s2;
+    }
     if (items > 0) {
       if (first)
-        k_init<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
+        k_init<<<grid, kItemRows, smem, sc>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
                                              dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
                                              dPchg.as<int32_t>(), 1, work, ccap);
       else
-        k_iter<<<grid, kItemRows, smem, s>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
+        k_iter<<<grid, kItemRows, smem, sc>>>(dProbs.as<BProb>(), P, (int)items, dX.as<float>(), dC.as<float>(),
                                              dLab.as<int32_t>(), dLimbs.as<unsigned long long>(), dCnt.as<int32_t>(),
                                              dPchg.as<int32_t>(), 0, work, ccap);
       note_launch();
@@ -1666,6 +1692,10 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
                                                            dCtl.as<int>());
         note_launch();
       }
+    }
+    if (concurrent) {
+      FUELG_CUDA(cudaEventRecord(ev_join, s2));
+      FUELG_CUDA(cudaStreamWaitEvent(s, ev_join, 0));
     }
     // canonical counters every pass; new centres only when another pass follows
     batched_mean_kernel<<<mean_grid, 256, 0, s>>>(dProbs.as<BProb>(), P, dKdb.as<int64_t>(), kd,
