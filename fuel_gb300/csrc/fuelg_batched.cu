@@ -824,7 +824,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) batched_tc_assign_kernel(
                 if (!found && dt == best) {
                   found = true;
                   bj = col;
-                } else if (col < mt.k && (!(T > 0.0f) || !(dt > T))) {
+                } else if (!(T > 0.0f) || !(dt > T)) {  // padding columns (+inf) only when T <= 0
                   const float e =
                       (ta.alpha * xl * cns[col] + beta * (nx + cc[u])) * (1.0f + gamma) + gamma * fabsf(dt);
                   if (!(dt - e > hi_b)) bits |= 1u << (16 * h + 4 * v + u);
