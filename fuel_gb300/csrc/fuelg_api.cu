@@ -35,6 +35,31 @@ void note_launch(int count) { g_launches += count; }
 int64_t launch_count() { return g_launches; }
 HotTimer*& hot_timer() { return g_hot; }
 
+cudaMemPool_t lib_pool() {
+  static std::mutex mu;
+  static std::map<int, cudaMemPool_t> pools;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = pools.find(dev);
+  if (it != pools.end()) return it->second;
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+    uint64_t keep = 16ull << 30;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  } else {
+    cudaGetLastError();
+    cudaDeviceGetDefaultMemPool(&pool, dev);
+  }
+  pools[dev] = pool;
+  return pool;
+}
+
 static int ensure_cancel_word() {
   std::lock_guard<std::mutex> lk(g_cancel_mu);
   if (g_cancel_host) return ST_OK;

@@ -1257,11 +1257,13 @@ __global__ void __launch_bounds__(256) chg_sum_kernel(const BProb* __restrict__ 
 
 struct DevBuf {
   void* p = nullptr;
+  cudaStream_t s = nullptr;
   ~DevBuf() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, s);
   }
-  int alloc(size_t b) {
-    if (cudaMalloc(&p, b ? b : 16) != cudaSuccess) {
+  int alloc(size_t b, cudaStream_t st) {
+    s = st;
+    if (cudaMallocFromPoolAsync(&p, b ? b : 16, lib_pool(), st) != cudaSuccess) {
       cudaGetLastError();
       p = nullptr;
       set_error("device allocation of %zu bytes failed", b);
@@ -1413,13 +1415,13 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   }
   DevBuf dX, dC, dLab, dCnt, dOff, dRb, dRange, dProbs, dKdb, dPchg, dConv, dLast, dIter, dInert, dLimbs, dTcp,
       dTcb, dSt, dUnd, dCtaB;
-  FUELG_TRY(dX.alloc(sizeof(float) * xs));
-  FUELG_TRY(dC.alloc(sizeof(float) * cs));
-  FUELG_TRY(dLab.alloc(sizeof(int32_t) * ls));
-  FUELG_TRY(dCnt.alloc(sizeof(int32_t) * ks));
-  FUELG_TRY(dOff.alloc(sizeof(int64_t) * (P + 1)));
-  FUELG_TRY(dRb.alloc(sizeof(int32_t) * (P + 1)));
-  FUELG_TRY(dRange.alloc(sizeof(int) * 3 * P));
+  FUELG_TRY(dX.alloc(sizeof(float) * xs, s));
+  FUELG_TRY(dC.alloc(sizeof(float) * cs, s));
+  FUELG_TRY(dLab.alloc(sizeof(int32_t) * ls, s));
+  FUELG_TRY(dCnt.alloc(sizeof(int32_t) * ks, s));
+  FUELG_TRY(dOff.alloc(sizeof(int64_t) * (P + 1), s));
+  FUELG_TRY(dRb.alloc(sizeof(int32_t) * (P + 1), s));
+  FUELG_TRY(dRange.alloc(sizeof(int) * 3 * P, s));
   FUELG_CUDA(cudaMemsetAsync(dX.p, 0, sizeof(float) * xs, s));  // alignment padding between problems reads as 0
   for (int p = 0; p < P; p++) {
     FUELG_CUDA(cudaMemcpyAsync(dX.as<float>() + hp[p].x_off, probs[p].data, sizeof(float) * probs[p].n * probs[p].d,
@@ -1462,19 +1464,19 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     hp[p].limb_off = limbs_total;
     limbs_total += (int64_t)hp[p].k * hp[p].d * hp[p].L;
   }
-  FUELG_TRY(dLimbs.alloc(sizeof(unsigned long long) * limbs_total));
-  FUELG_TRY(dProbs.alloc(sizeof(BProb) * P));
-  FUELG_TRY(dKdb.alloc(sizeof(int64_t) * (P + 1)));
-  FUELG_TRY(dPchg.alloc(sizeof(int32_t) * P));
-  FUELG_TRY(dConv.alloc(sizeof(int32_t) * P));
-  FUELG_TRY(dLast.alloc(sizeof(int32_t) * P));
-  FUELG_TRY(dIter.alloc(sizeof(int32_t)));
-  FUELG_TRY(dInert.alloc(sizeof(double) * P));
+  FUELG_TRY(dLimbs.alloc(sizeof(unsigned long long) * limbs_total, s));
+  FUELG_TRY(dProbs.alloc(sizeof(BProb) * P, s));
+  FUELG_TRY(dKdb.alloc(sizeof(int64_t) * (P + 1), s));
+  FUELG_TRY(dPchg.alloc(sizeof(int32_t) * P, s));
+  FUELG_TRY(dConv.alloc(sizeof(int32_t) * P, s));
+  FUELG_TRY(dLast.alloc(sizeof(int32_t) * P, s));
+  FUELG_TRY(dIter.alloc(sizeof(int32_t), s));
+  FUELG_TRY(dInert.alloc(sizeof(double) * P, s));
   FUELG_CUDA(cudaMemcpyAsync(dProbs.p, hp.data(), sizeof(BProb) * P, cudaMemcpyHostToDevice, s));
   const int ntc = (int)tcp.size();
-  FUELG_TRY(dTcp.alloc(sizeof(int32_t) * std::max(1, ntc)));
-  FUELG_TRY(dTcb.alloc(sizeof(int32_t) * (ntc + 1)));
-  FUELG_TRY(dSt.alloc(sizeof(int) * 4));
+  FUELG_TRY(dTcp.alloc(sizeof(int32_t) * std::max(1, ntc), s));
+  FUELG_TRY(dTcb.alloc(sizeof(int32_t) * (ntc + 1), s));
+  FUELG_TRY(dSt.alloc(sizeof(int) * 4, s));
   if (ntc) FUELG_CUDA(cudaMemcpyAsync(dTcp.p, tcp.data(), sizeof(int32_t) * ntc, cudaMemcpyHostToDevice, s));
   FUELG_CUDA(cudaMemcpyAsync(dTcb.p, tc_begin.data(), sizeof(int32_t) * (ntc + 1), cudaMemcpyHostToDevice, s));
   FUELG_CUDA(cudaMemsetAsync(dSt.p, 0, sizeof(int) * 4, s));
@@ -1526,7 +1528,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   ta.undecided = reinterpret_cast<unsigned long long*>(dSt.as<int>() + 2);
   ta.und_n = dSt.as<int>() + 1;
   ta.und_w = (tc_kmax + 31) / 32;
-  FUELG_TRY(dUnd.alloc(sizeof(int32_t) * (2 + ta.und_w) * std::max<int64_t>(1, tc_rows)));
+  FUELG_TRY(dUnd.alloc(sizeof(int32_t) * (2 + ta.und_w) * std::max<int64_t>(1, tc_rows), s));
   ta.und_p = dUnd.as<int32_t>();
   ta.und_i = dUnd.as<int32_t>() + std::max<int64_t>(1, tc_rows);
   ta.und_m = reinterpret_cast<uint32_t*>(dUnd.as<int32_t>() + 2 * std::max<int64_t>(1, tc_rows));
@@ -1545,10 +1547,10 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
     std::vector<int32_t> gcp(std::max<int64_t>(1, ks));
     for (int p = 0; p < P; p++)
       for (int j = 0; j < hp[p].k; j++) gcp[hp[p].cnt_off + j] = p;
-    FUELG_TRY(dBoff.alloc(sizeof(int64_t) * std::max<int64_t>(1, ks)));
-    FUELG_TRY(dCur.alloc(sizeof(int32_t) * std::max<int64_t>(1, ks)));
-    FUELG_TRY(dGcp.alloc(sizeof(int32_t) * std::max<int64_t>(1, ks)));
-    FUELG_TRY(dRowB.alloc(sizeof(int64_t) * (ntc + 1)));
+    FUELG_TRY(dBoff.alloc(sizeof(int64_t) * std::max<int64_t>(1, ks), s));
+    FUELG_TRY(dCur.alloc(sizeof(int32_t) * std::max<int64_t>(1, ks), s));
+    FUELG_TRY(dGcp.alloc(sizeof(int32_t) * std::max<int64_t>(1, ks), s));
+    FUELG_TRY(dRowB.alloc(sizeof(int64_t) * (ntc + 1), s));
     FUELG_CUDA(cudaMemcpyAsync(dGcp.p, gcp.data(), sizeof(int32_t) * gcp.size(), cudaMemcpyHostToDevice, s));
     FUELG_CUDA(cudaMemcpyAsync(dRowB.p, rowb.data(), sizeof(int64_t) * (ntc + 1), cudaMemcpyHostToDevice, s));
   }
@@ -1559,12 +1561,12 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   // (bucket positions and the region counter are 32-bit: at most 2^29 listed rows)
   const int chg_cap = (int)std::max<int64_t>(1, std::min<int64_t>(tc_rows / 2, 1ll << 29));
   if (tc_items > 0) {
-    FUELG_TRY(dChg.alloc(sizeof(int32_t) * 3 * (size_t)chg_cap));
-    FUELG_TRY(dHist.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks)));
-    FUELG_TRY(dKoff.alloc(sizeof(int64_t) * 2 * std::max<int64_t>(1, ks)));
-    FUELG_TRY(dKcur.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks)));
-    FUELG_TRY(dBk.alloc(sizeof(int32_t) * 4 * (size_t)chg_cap));
-    FUELG_TRY(dCtl.alloc(sizeof(int) * 4));
+    FUELG_TRY(dChg.alloc(sizeof(int32_t) * 3 * (size_t)chg_cap, s));
+    FUELG_TRY(dHist.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks), s));
+    FUELG_TRY(dKoff.alloc(sizeof(int64_t) * 2 * std::max<int64_t>(1, ks), s));
+    FUELG_TRY(dKcur.alloc(sizeof(int32_t) * 2 * std::max<int64_t>(1, ks), s));
+    FUELG_TRY(dBk.alloc(sizeof(int32_t) * 4 * (size_t)chg_cap, s));
+    FUELG_TRY(dCtl.alloc(sizeof(int) * 4, s));
     FUELG_CUDA(cudaMemsetAsync(dHist.p, 0, sizeof(int32_t) * 2 * std::max<int64_t>(1, ks), s));
     FUELG_CUDA(cudaMemsetAsync(dCtl.p, 0, sizeof(int) * 4, s));
     ta.chg_row = dChg.as<int32_t>();
@@ -1620,7 +1622,7 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
       if (q < ntc) at = std::min<int64_t>(tc_begin[q + 1], tc_begin[q] + (int64_t)std::ceil((target - acc) / icost[q]));
       cb[c] = std::max(cb[c - 1], at);
     }
-    FUELG_TRY(dCtaB.alloc(sizeof(int64_t) * (tc_grid + 1)));
+    FUELG_TRY(dCtaB.alloc(sizeof(int64_t) * (tc_grid + 1), s));
     FUELG_CUDA(cudaMemcpyAsync(dCtaB.p, cb.data(), sizeof(int64_t) * (tc_grid + 1), cudaMemcpyHostToDevice, s));
     ta.cta_begin = dCtaB.as<int64_t>();
   }

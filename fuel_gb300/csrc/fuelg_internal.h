@@ -42,6 +42,12 @@ const char* last_error();
   } while (0)
 
 // Stream-ordered scratch allocations (cudaMallocAsync pool) freed on scope exit.
+// The stream-ordered memory pool of this library's temporaries on the current
+// device: it keeps up to 16 GB cached between calls, where the device's default
+// pool hands its memory back at every synchronisation and the next call maps it
+// again.
+cudaMemPool_t lib_pool();
+
 struct Scratch {
   void* p = nullptr;
   cudaStream_t s = nullptr;
@@ -54,7 +60,7 @@ struct Scratch {
   int alloc(size_t bytes, cudaStream_t stream) {
     s = stream;
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMallocAsync(&p, bytes, stream);
+    cudaError_t e = cudaMallocFromPoolAsync(&p, bytes, lib_pool(), stream);
     if (e != cudaSuccess) {
       p = nullptr;
       set_error("device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(e));
