@@ -452,18 +452,36 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   // pass that changed nothing leaves sums, centres and labels as they were,
   // so the passes after it in the same graph repeat it exactly and the loop
   // stops at the first such pass (lloyd.rs:197).
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // one pass / kPassesPerGraph passes
-  struct GraphFree {
-    cudaGraphExec_t* g;
-    ~GraphFree() {
+  // one pass / kPassesPerGraph passes.  The instantiated graphs are kept per
+  // thread and device between calls: a later call captures its passes again
+  // (their arguments differ) and updates the kept graph in place, which costs
+  // far less than instantiating it; a graph of another shape is replaced.
+  struct KeptGraphs {
+    int dev = -1;
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    ~KeptGraphs() {
       for (int i = 0; i < 2; i++)
         if (g[i]) cudaGraphExecDestroy(g[i]);
     }
-  } gf{gexec};
+  };
+  thread_local KeptGraphs kept;
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (kept.dev != dev) {
+      for (int i = 0; i < 2; i++)
+        if (kept.g[i]) {
+          cudaGraphExecDestroy(kept.g[i]);
+          kept.g[i] = nullptr;
+        }
+      kept.dev = dev;
+    }
+  }
+  bool ready[2] = {false, false};  // captured and updated for this call
   int64_t graph_launches[2] = {0, 0};
   auto graph_pass = [&](int npass) -> int {
     const int gi = npass == 1 ? 0 : 1;
-    if (!gexec[gi]) {
+    if (!ready[gi]) {
       HotTimer* saved = hot_timer();
       hot_timer() = nullptr;
       cudaGraph_t g = nullptr;
@@ -480,11 +498,23 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
         return rc;
       }
       FUELG_CUDA(ce);
-      const cudaError_t ie = cudaGraphInstantiate(&gexec[gi], g, 0);
+      bool updated = false;
+      if (kept.g[gi]) {
+        cudaGraphExecUpdateResultInfo info;
+        updated = cudaGraphExecUpdate(kept.g[gi], g, &info) == cudaSuccess;
+        if (!updated) {
+          cudaGetLastError();
+          cudaGraphExecDestroy(kept.g[gi]);
+          kept.g[gi] = nullptr;
+        }
+      }
+      cudaError_t ie = cudaSuccess;
+      if (!updated) ie = cudaGraphInstantiate(&kept.g[gi], g, 0);
       cudaGraphDestroy(g);
       FUELG_CUDA(ie);
+      ready[gi] = true;
     }
-    FUELG_CUDA(cudaGraphLaunch(gexec[gi], stream));
+    FUELG_CUDA(cudaGraphLaunch(kept.g[gi], stream));
     note_launch((int)graph_launches[gi]);
     return ST_OK;
   };
