@@ -41,13 +41,13 @@ const char* last_error();
     if (s_ != ::fuelg::ST_OK) return s_; \
   } while (0)
 
-// Stream-ordered scratch allocations (cudaMallocAsync pool) freed on scope exit.
 // The stream-ordered memory pool of this library's temporaries on the current
 // device: it keeps up to 16 GB cached between calls, where the device's default
 // pool hands its memory back at every synchronisation and the next call maps it
 // again.
 cudaMemPool_t lib_pool();
 
+// Stream-ordered scratch allocations (from lib_pool) freed on scope exit.
 struct Scratch {
   void* p = nullptr;
   cudaStream_t s = nullptr;

@@ -452,7 +452,7 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   // pass that changed nothing leaves sums, centres and labels as they were,
   // so the passes after it in the same graph repeat it exactly and the loop
   // stops at the first such pass (lloyd.rs:197).
-  // one pass / kPassesPerGraph passes.  The instantiated graphs are kept per
+  // The two instantiated graphs (one pass, kPassesPerGraph passes) are kept per
   // thread and device between calls: a later call captures its passes again
   // (their arguments differ) and updates the kept graph in place, which costs
   // far less than instantiating it; a graph of another shape is replaced.
