@@ -92,8 +92,7 @@ __device__ __forceinline__ bool prep_row(const float* __restrict__ xr, int64_t r
 struct CentrePrep {
   __nv_bfloat16* hi = nullptr;  // nullptr: no copies to write
   __nv_bfloat16* lo = nullptr;  // split tier only
-  float* nrm2 = nullptr;
-  float* nrm = nullptr;
+  float* nrm2 = nullptr;  // ||c||^2 as two halves: nrm2[j] + nrm2[kp + j]
   int dp = 0, kp = 0;
   int32_t* zero_word = nullptr;  // cleared for the next pass (the screen's undecided-point counter)
   float scale = 1.0f;            // the copies hold fl(scale * c)

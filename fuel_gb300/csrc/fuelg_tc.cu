@@ -158,8 +158,7 @@ struct TcArgs {
   int d, k, kp, kc, stages;
   const float* nx;  // ||x||^2 per point (f32 of an FP64 sum)
   const float* xn;  // ||x||
-  const float* nc;  // ||c||^2 per (padded) centre
-  const float* cn;  // ||c||
+  const float* nc;  // ||c||^2 per (padded) centre, as two halves: nc[j] + nc[kp + j]
   int32_t* lab_new;
   int32_t* ulist;
   uint64_t* umask;
@@ -1090,7 +1089,6 @@ int tc_pass(const LloydParams& p, TcLloydState* st, const float* centers, bool f
   a.nx = st->xnrm2.as<float>();
   a.xn = st->xnrm.as<float>();
   a.nc = st->cnrm2.as<float>();
-  a.cn = st->cnrm.as<float>();
   a.lab_new = lab_new;
   a.ulist = st->ulist.as<int32_t>();
   a.umask = st->umask.as<uint64_t>();
@@ -1227,7 +1225,6 @@ CentrePrep lloyd_tc_centre_prep(TcLloydState* st) {
   cp.hi = st->chi.as<__nv_bfloat16>();
   cp.lo = st->split ? st->clo.as<__nv_bfloat16>() : nullptr;
   cp.nrm2 = st->cnrm2.as<float>();
-  cp.nrm = st->cnrm.as<float>();
   cp.dp = st->dp;
   cp.kp = st->kp;
   cp.zero_word = st->ucount.as<int32_t>();
