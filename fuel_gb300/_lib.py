@@ -103,6 +103,7 @@ SIGNATURES = {
     "fuelg_knn_noalloc": (ctypes.c_int, [_vp, _i64, _i32, _vp, _i64, _i32, _i32, _i32, _i32, _vp, _vp, _vp]),
     "fuelg_cancel": (ctypes.c_int, []),
     "fuelg_reset_cancel": (ctypes.c_int, []),
+    "fuelg_release": (ctypes.c_int, []),
 }
 
 
@@ -159,6 +160,14 @@ def device_count() -> int:
     n = ctypes.c_int32(0)
     check(load().fuelg_device_count(ctypes.byref(n)))
     return int(n.value)
+
+
+def release():
+    """Free what the engine keeps between calls (fuelg_release): its memory
+    pool, the Lloyd loop's kept CUDA graphs, the cancellation word.  Call it
+    with no call in flight and every index and server closed, e.g. before
+    resetting the device; ValueError while a server is open."""
+    check(load().fuelg_release())
 
 
 def ptr(a) -> ctypes.c_void_p:

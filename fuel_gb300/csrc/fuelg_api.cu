@@ -2,8 +2,10 @@
 // buffers, status codes, cancellation and per-call measurements.
 #include <cstdarg>
 #include <cstring>
+#include <atomic>
 #include <map>
 #include <mutex>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -35,30 +37,88 @@ void note_launch(int count) { g_launches += count; }
 int64_t launch_count() { return g_launches; }
 HotTimer*& hot_timer() { return g_hot; }
 
+namespace {
+// Memory pools made by lib_pool, per device (a device whose pool could not be
+// made uses its default pool, which is not destroyed on release).
+struct PoolEntry {
+  cudaMemPool_t pool = nullptr;
+  bool created = false;
+};
+std::mutex g_pool_mu;
+std::map<int, PoolEntry>& pools() {
+  static auto* m = new std::map<int, PoolEntry>();  // never destroyed: threads may outlive static teardown
+  return *m;
+}
+
+// Every thread's kept graph executables, and the release generation.
+struct GraphRegistry {
+  std::mutex mu;
+  std::set<cudaGraphExec_t> graphs;
+  std::atomic<uint64_t> gen{1};
+};
+GraphRegistry& graph_registry() {
+  static auto* r = new GraphRegistry();
+  return *r;
+}
+
+std::atomic<int> g_open_servers{0};
+}  // namespace
+
 cudaMemPool_t lib_pool() {
-  static std::mutex mu;
-  static std::map<int, cudaMemPool_t> pools;
   int dev = 0;
   cudaGetDevice(&dev);
-  std::lock_guard<std::mutex> lk(mu);
-  auto it = pools.find(dev);
-  if (it != pools.end()) return it->second;
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  auto it = pools().find(dev);
+  if (it != pools().end()) return it->second.pool;
   cudaMemPoolProps props = {};
   props.allocType = cudaMemAllocationTypePinned;
   props.handleTypes = cudaMemHandleTypeNone;
   props.location.type = cudaMemLocationTypeDevice;
   props.location.id = dev;
-  cudaMemPool_t pool = nullptr;
-  if (cudaMemPoolCreate(&pool, &props) == cudaSuccess) {
+  PoolEntry e;
+  if (cudaMemPoolCreate(&e.pool, &props) == cudaSuccess) {
     uint64_t keep = 16ull << 30;
-    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    cudaMemPoolSetAttribute(e.pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    e.created = true;
   } else {
     cudaGetLastError();
-    cudaDeviceGetDefaultMemPool(&pool, dev);
+    e.pool = nullptr;
+    cudaDeviceGetDefaultMemPool(&e.pool, dev);
   }
-  pools[dev] = pool;
-  return pool;
+  pools()[dev] = e;
+  return e.pool;
 }
+
+CUcontext current_context() {
+  using Fn = CUresult (*)(CUcontext*);
+  static Fn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      return reinterpret_cast<Fn>(p);
+    cudaGetLastError();
+    return (Fn) nullptr;
+  }();
+  CUcontext ctx = nullptr;
+  if (!fn || fn(&ctx) != CUDA_SUCCESS) return nullptr;
+  return ctx;
+}
+
+void keep_graph(cudaGraphExec_t g) {
+  GraphRegistry& r = graph_registry();
+  std::lock_guard<std::mutex> lk(r.mu);
+  r.graphs.insert(g);
+}
+void drop_graph(cudaGraphExec_t g) {
+  GraphRegistry& r = graph_registry();
+  std::lock_guard<std::mutex> lk(r.mu);
+  if (r.graphs.erase(g)) cudaGraphExecDestroy(g);
+}
+uint64_t cache_generation() { return graph_registry().gen.load(); }
+
+void server_opened() { g_open_servers++; }
+void server_closed() { g_open_servers--; }
 
 static int ensure_cancel_word() {
   std::lock_guard<std::mutex> lk(g_cancel_mu);
@@ -276,6 +336,37 @@ int fuelg_cancel(void) {
 }
 int fuelg_reset_cancel(void) {
   if (g_cancel_host) *(volatile int*)g_cancel_host = 0;
+  return ST_OK;
+}
+
+int fuelg_release(void) {
+  if (g_open_servers.load() > 0) {
+    set_error("%d serving handle(s) still open: destroy them before fuelg_release", g_open_servers.load());
+    return ST_EINVAL;
+  }
+  {
+    GraphRegistry& r = graph_registry();
+    std::lock_guard<std::mutex> lk(r.mu);
+    for (cudaGraphExec_t g : r.graphs) cudaGraphExecDestroy(g);
+    r.graphs.clear();
+    r.gen++;
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    // a pool with allocations still out is freed once they are returned
+    for (auto& kv : pools())
+      if (kv.second.created) cudaMemPoolDestroy(kv.second.pool);
+    pools().clear();
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_cancel_mu);
+    int* h = g_cancel_host;
+    g_cancel_host = nullptr;
+    g_cancel_dev = nullptr;
+    if (h) cudaFreeHost(h);
+  }
+  noalloc_forget();
+  cudaGetLastError();  // a context already gone makes the destroys fail: nothing is left to free then
   return ST_OK;
 }
 

@@ -6,6 +6,7 @@
 #include <string>
 #include <utility>
 #include <vector>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace fuelg {
@@ -46,6 +47,24 @@ const char* last_error();
 // pool hands its memory back at every synchronisation and the next call maps it
 // again.
 cudaMemPool_t lib_pool();
+
+// The calling thread's current CUDA context (nullptr when it has none), read
+// through the driver's cuCtxGetCurrent.
+CUcontext current_context();
+
+// State kept between calls is released by fuelg_release.  The Lloyd loop's
+// instantiated graphs are kept per host thread: keep_graph registers one so
+// that a release destroys every thread's, drop_graph destroys a registered one
+// (once), and cache_generation() changes at every release, after which a
+// thread's own handles are stale and must be forgotten, not destroyed.
+void keep_graph(cudaGraphExec_t g);
+void drop_graph(cudaGraphExec_t g);
+uint64_t cache_generation();
+// Forgets the allocation-free kNN path's resolved scratch addresses.
+void noalloc_forget();
+// Open serving handles (a release is refused while one is open).
+void server_opened();
+void server_closed();
 
 // Stream-ordered scratch allocations (from lib_pool) freed on scope exit.
 struct Scratch {

@@ -456,25 +456,38 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
   // thread and device between calls: a later call captures its passes again
   // (their arguments differ) and updates the kept graph in place, which costs
   // far less than instantiating it; a graph of another shape is replaced.
+  // They belong to the device and context they were made in, and
+  // fuelg_release destroys every thread's (a new generation: this thread's
+  // handles are then forgotten).
   struct KeptGraphs {
     int dev = -1;
+    CUcontext ctx = nullptr;
+    uint64_t gen = 0;
     cudaGraphExec_t g[2] = {nullptr, nullptr};
+    void drop() {
+      for (int i = 0; i < 2; i++) {
+        if (g[i]) drop_graph(g[i]);
+        g[i] = nullptr;
+      }
+    }
     ~KeptGraphs() {
-      for (int i = 0; i < 2; i++)
-        if (g[i]) cudaGraphExecDestroy(g[i]);
+      if (gen == cache_generation()) drop();
     }
   };
   thread_local KeptGraphs kept;
   {
     int dev = 0;
     cudaGetDevice(&dev);
-    if (kept.dev != dev) {
-      for (int i = 0; i < 2; i++)
-        if (kept.g[i]) {
-          cudaGraphExecDestroy(kept.g[i]);
-          kept.g[i] = nullptr;
-        }
+    const CUcontext ctx = current_context();
+    const uint64_t gen = cache_generation();
+    if (kept.gen != gen) {
+      kept.g[0] = kept.g[1] = nullptr;
+      kept.gen = gen;
+    }
+    if (kept.dev != dev || kept.ctx != ctx) {
+      kept.drop();
       kept.dev = dev;
+      kept.ctx = ctx;
     }
   }
   bool ready[2] = {false, false};  // captured and updated for this call
@@ -504,12 +517,18 @@ int lloyd_run(const LloydParams& p, LloydResult* r, int* dev_status, cudaStream_
         updated = cudaGraphExecUpdate(kept.g[gi], g, &info) == cudaSuccess;
         if (!updated) {
           cudaGetLastError();
-          cudaGraphExecDestroy(kept.g[gi]);
+          drop_graph(kept.g[gi]);
           kept.g[gi] = nullptr;
         }
       }
       cudaError_t ie = cudaSuccess;
-      if (!updated) ie = cudaGraphInstantiate(&kept.g[gi], g, 0);
+      if (!updated) {
+        ie = cudaGraphInstantiate(&kept.g[gi], g, 0);
+        if (ie == cudaSuccess)
+          keep_graph(kept.g[gi]);
+        else
+          kept.g[gi] = nullptr;
+      }
       cudaGraphDestroy(g);
       FUELG_CUDA(ie);
       ready[gi] = true;

@@ -32,21 +32,6 @@ struct ScratchSlot {
 };
 ScratchSlot g_scratch[kMaxDevices];
 
-// cuCtxGetCurrent through the runtime's driver entry point (no link-time
-// dependency on libcuda).
-using CtxGetCurrentFn = CUresult (*)(CUcontext*);
-CtxGetCurrentFn ctx_get_current() {
-  static CtxGetCurrentFn fn = nullptr;
-  if (!fn) {
-    void* p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<CtxGetCurrentFn>(p);
-  }
-  return fn;
-}
-
 // Device address of g_noalloc_scratch for the current device and context.  It
 // is looked up with cudaGetSymbolAddress on the first call on a device (host
 // code must not use the symbol itself: on the host it is only a stand-in, not a
@@ -60,17 +45,12 @@ int noalloc_scratch(void** out) {
     set_error("device ordinal %d outside the supported range", dev);
     return ST_ENOTSUP;
   }
-  CtxGetCurrentFn get_ctx = ctx_get_current();
-  if (!get_ctx) {
-    set_error("cuCtxGetCurrent is unavailable from the driver");
-    return ST_ECUDA;
-  }
-  CUcontext ctx = nullptr;
-  if (get_ctx(&ctx) == CUDA_SUCCESS && ctx == nullptr) {
+  CUcontext ctx = current_context();
+  if (ctx == nullptr) {
     // no context yet on this thread: cudaSetDevice makes the device's primary
     // context current (a context the caller made current is left alone)
     FUELG_CUDA(cudaSetDevice(dev));
-    get_ctx(&ctx);
+    ctx = current_context();
   }
   if (ctx == nullptr) {
     set_error("no current CUDA context on device %d", dev);
@@ -109,6 +89,12 @@ bool device_accessible(const void* p, int dev) {
 }
 
 }  // namespace
+
+void noalloc_forget() {
+  std::lock_guard<std::mutex> lk(g_scratch_mu);
+  for (ScratchSlot& slot : g_scratch) slot = ScratchSlot{};
+}
+
 }  // namespace fuelg
 
 using namespace fuelg;

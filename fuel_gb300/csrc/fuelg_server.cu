@@ -281,6 +281,7 @@ int fuelg_server_create(fuelg_index* ix, int32_t precision, int64_t max_batch_qu
   sv->max_batch = max_batch_queries;
   sv->budget = budget_bytes;
   for (int i = 0; i < workers; i++) sv->workers.emplace_back(worker_main, sv);
+  server_opened();
   *out = sv;
   return ST_OK;
 }
@@ -380,6 +381,7 @@ int fuelg_server_destroy(fuelg_server* sv) {
   for (auto& t : sv->workers) t.join();
   for (auto& kv : sv->reqs) delete kv.second;
   delete sv;
+  server_closed();
   return ST_OK;
 }
 

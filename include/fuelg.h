@@ -327,6 +327,17 @@ int fuelg_knn_noalloc(const float *data, int64_t n, int32_t d, const float *quer
 int fuelg_cancel(void);
 int fuelg_reset_cancel(void);
 
+/* Frees what the library keeps between calls: its stream-ordered memory pool
+ * of temporaries (up to 16 GB cached per device), the instantiated CUDA graphs
+ * of the Lloyd loop (kept per host thread), the host-mapped cancellation word
+ * and the resolved scratch addresses of fuelg_knn_noalloc.  Later calls set
+ * them up again.  Indexes and range results stay valid across a release
+ * (they own their device memory); FUELG_EINVAL while a server is open.  Call
+ * it with no library call in flight on any thread: before cudaDeviceReset, or
+ * before destroying a CUDA context the library ran in (after destroying the
+ * handles made in it). */
+int fuelg_release(void);
+
 #ifdef __cplusplus
 }
 #endif

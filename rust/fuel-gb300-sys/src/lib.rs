@@ -163,6 +163,7 @@ unsafe extern "C" {
 
     pub fn fuelg_cancel() -> c_int;
     pub fn fuelg_reset_cancel() -> c_int;
+    pub fn fuelg_release() -> c_int;
 }
 
 /// The message of the calling thread's last failing call.

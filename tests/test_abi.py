@@ -75,6 +75,7 @@ def test_argument_validation_before_any_device_work(lib):
     assert lib.fuelg_lloyd_assign(None, 0, 1, None, 1, 0, 0, None, None, None) == _lib.EINVAL
     assert lib.fuelg_range_free(None) == _lib.OK
     assert lib.fuelg_index_destroy(None) == _lib.OK
+    assert lib.fuelg_release() == _lib.OK  # nothing kept yet: a no-op
 
 
 def test_rust_bindings_declare_every_header_function():
