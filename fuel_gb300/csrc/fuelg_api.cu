@@ -429,7 +429,7 @@ namespace fuelg {
 int index_view_get(fuelg_index* ix, int want_tier, IndexView* out) {
   std::lock_guard<std::mutex> lk(ix->mu);
   cudaSetDevice(ix->device);
-  if (want_tier >= 0 && !ix->tc && ix->n > 0 && knn_tc_supported(ix->d, 1, TC_BF16))
+  if (want_tier >= 0 && !ix->tc && ix->n > 0 && knn_tc_supported(ix->n, ix->d, 1, TC_BF16))
     FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, ix->stream, &ix->tc));
   if (want_tier == TC_SPLIT && ix->tc) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, ix->stream));
   out->f16 = false;
@@ -496,7 +496,7 @@ int index_topk(fuelg_index* ix, const float* Q, int64_t m, int kk, int precision
   *used = FUELG_PREC_FP32;
   *rescored = 0;
   const int tier = precision == FUELG_PREC_SPLIT_BF16 ? TC_SPLIT : precision == FUELG_PREC_F16 ? TC_F16 : TC_BF16;
-  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->d, kk, tier) && ix->n > 0) {
+  if (precision != FUELG_PREC_FP32 && knn_tc_supported(ix->n, ix->d, kk, tier) && ix->n > 0) {
     int exact = 0;
     if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
     if (tier == TC_SPLIT) FUELG_TRY(knn_tc_index_add_lo(ix->tc, ix->X, s));
@@ -568,7 +568,7 @@ void tune_store_locked(const TuneKey& key, int tier) {
 int resolve_knn_precision(fuelg_index* ix, const float* Q, int64_t m, int kk, int* dstat, cudaStream_t s,
                           int* out) {
   *out = FUELG_PREC_FP32;
-  if (ix->n == 0 || !knn_tc_supported(ix->d, kk, TC_BF16)) return ST_OK;
+  if (ix->n == 0 || !knn_tc_supported(ix->n, ix->d, kk, TC_BF16)) return ST_OK;
   if (!ix->tc) FUELG_TRY(knn_tc_index_build(ix->X, ix->n, ix->d, s, &ix->tc));
   const int cls = knn_tc_index_class(ix->tc);
   if (cls == TC_CLASS_INTEGER) {

@@ -1409,7 +1409,8 @@ extern "C" int fuelg_kmeans_batched(fuelg_kmeans_problem* probs, int32_t count, 
   kdb[P] = kd;
   rblk[P] = (int32_t)rb;
   tc_begin.push_back((int32_t)tc_items);
-  if (all_items >= (1ll << 31) || tc_items >= (1ll << 31)) {
+  // 32-bit item starts; centre keys 2 gc + 1 (gc < ks) of the change list are 32-bit
+  if (all_items >= (1ll << 31) || tc_items >= (1ll << 31) || ks >= (1ll << 30)) {
     set_error("batch too large");
     return ST_ENOTSUP;
   }

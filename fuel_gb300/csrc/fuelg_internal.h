@@ -211,7 +211,7 @@ int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int6
 // Operand tiers: BF16 (one product, error ~2^-8), split BF16 (hi + lo, three
 // products, ~2^-16), FP16 (one product, ~2^-11; values within the FP16 range).
 constexpr int TC_BF16 = 0, TC_SPLIT = 1, TC_F16 = 2;
-bool knn_tc_supported(int d, int kk, int tier);
+bool knn_tc_supported(int64_t n, int d, int kk, int tier);
 // Resident tensor-core form of an index: BF16 copy padded to whole tiles, FP32
 // norms, integer census and the index-side bounds; built once per handle.
 struct TcIndex;

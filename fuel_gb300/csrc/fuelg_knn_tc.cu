@@ -781,8 +781,10 @@ size_t knn_tc_fixed_smem(int d, int split) {
 int margin_mode_of(int tier) { return tier == TC_F16 ? 2 : 1; }
 }  // namespace
 
-bool knn_tc_supported(int d, int kk, int tier) {
+bool knn_tc_supported(int64_t n, int d, int kk, int tier) {
   if (d < 32 || d > 256 || kk < 1) return false;
+  // TMA row coordinates are signed 32-bit: the padded index must stay below 2^31 rows
+  if (n >= (1ll << 31) - 4096) return false;
   // kept keys per query are selected 8 per lane by one warp
   if (kk2_of(kk, margin_mode_of(tier)) > 32 * kSel) return false;
   return knn_tc_fixed_smem(d, tier == TC_SPLIT) + 2 * (size_t)XN * BK * 2 <= kSmemPerCta;

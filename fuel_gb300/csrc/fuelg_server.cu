@@ -112,7 +112,7 @@ int run_batch(fuelg_server* sv, std::vector<Request*>& batch, cudaStream_t s, fl
                                                         : TC_BF16;
   int rc = ST_ENOTSUP;
   if (sv->precision != FUELG_PREC_FP32 && ix.tc && (tier != TC_F16 || ix.f16) &&
-      knn_tc_supported(ix.d, kmax, tier)) {
+      knn_tc_supported(ix.n, ix.d, kmax, tier)) {
     // one launch for the mixed batch: every row selects only its own k (plus margin)
     int64_t rescored = 0;
     int exact = 0;
