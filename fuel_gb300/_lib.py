@@ -21,7 +21,8 @@ EXCLUDE_NONE, EXCLUDE_LINEAR, EXCLUDE_KPLUS1 = 0, 1, 2
 # fp16: kNN / serving only (tcgen05 FP16 screen; values within the FP16 range)
 PRECISION = {"auto": -1, "fp32": 0, "bf16": 1, "split_bf16": 2, "fp16": 4}
 # stats["precision_used"] may also be 3: split_bf16 on scaled-integer data
-PRECISION_NAMES = {0: "fp32", 1: "bf16", 2: "split_bf16", 3: "split_bf16_scaled", 4: "fp16"}
+# and 5: the exact FP64 scan of float64 data (the _f64 calls)
+PRECISION_NAMES = {0: "fp32", 1: "bf16", 2: "split_bf16", 3: "split_bf16_scaled", 4: "fp16", 5: "fp64"}
 LLOYD_FIXED_ITERS = 1
 
 
@@ -104,6 +105,12 @@ SIGNATURES = {
     "fuelg_cancel": (ctypes.c_int, []),
     "fuelg_reset_cancel": (ctypes.c_int, []),
     "fuelg_release": (ctypes.c_int, []),
+    "fuelg_index_create_f64": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _pp]),
+    "fuelg_knn_f64": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _vp, _vp, ctypes.POINTER(Stats)]),
+    "fuelg_knn_ties_f64": (ctypes.c_int, [_vp, _vp, _i64, _i32, _i32, _pp, ctypes.POINTER(Stats)]),
+    "fuelg_range_f64": (ctypes.c_int, [_vp, _vp, _i64, _dbl, _i32, _pp, ctypes.POINTER(Stats)]),
+    "fuelg_range_copy_f64": (ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    "fuelg_pairwise_f64": (ctypes.c_int, [_vp, _i64, _i32, _i32, _i32, _i32, _vp, ctypes.POINTER(Stats)]),
 }
 
 

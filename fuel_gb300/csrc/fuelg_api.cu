@@ -164,6 +164,8 @@ struct fuelg_index {
   int32_t order = 0;
   float* X = nullptr;  // device copy [n, d]
   TcIndex* tc = nullptr;  // tensor-core form, built on the first tensor-core call
+  bool f64 = false;       // a float64 index (fuelg_index_create_f64): X64 instead of X
+  double* X64 = nullptr;  // device copy [n, d]
   cudaStream_t stream = nullptr;
   std::mutex mu;  // calls on one handle are serialised
 };
@@ -173,6 +175,10 @@ struct fuelg_range_result {
   int64_t* off = nullptr;  // device
   int64_t* idx = nullptr;
   float* dist = nullptr;
+  // float64 lists (fuelg_knn_ties_f64 / fuelg_range_f64) are kept in host memory
+  bool f64 = false;
+  std::vector<int64_t> h_off, h_idx;
+  std::vector<double> h_dist;
 };
 
 namespace {
@@ -370,7 +376,12 @@ int fuelg_release(void) {
   return ST_OK;
 }
 
-int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, int32_t order, fuelg_index** out) {
+}  // extern "C"
+
+namespace {
+
+int index_create_impl(const void* data, bool f64, int64_t n, int32_t d, int32_t metric, int32_t order,
+                      fuelg_index** out) {
   if (!out) {
     set_error("out is NULL");
     return ST_EINVAL;
@@ -388,9 +399,14 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
     set_error("unknown summation order %d", order);
     return ST_EINVAL;
   }
+  if (f64 && n > (1ll << 32) - 2) {
+    set_error("float64 index too large: n=%lld (limit 2^32-2)", (long long)n);
+    return ST_ENOTSUP;
+  }
   FUELG_TRY(begin_call());
   fuelg_index* ix = new fuelg_index();
   cudaGetDevice(&ix->device);
+  ix->f64 = f64;
   ix->n = n;
   ix->d = d;
   ix->metric = metric;
@@ -400,19 +416,22 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
     set_error("cannot create a stream");
     return ST_ECUDA;
   }
-  const size_t bytes = (size_t)n * d * sizeof(float);
+  const size_t bytes = (size_t)n * d * (f64 ? sizeof(double) : sizeof(float));
   if (bytes) {
-    if (cudaMalloc(&ix->X, bytes) != cudaSuccess) {
+    void* dst = nullptr;
+    if (cudaMalloc(&dst, bytes) != cudaSuccess) {
       cudaGetLastError();
       cudaStreamDestroy(ix->stream);
       delete ix;
       set_error("cannot allocate %zu bytes for the index", bytes);
       return ST_ENOMEM;
     }
-    cudaError_t e = cudaMemcpyAsync(ix->X, data, bytes, cudaMemcpyDefault, ix->stream);
+    if (f64) ix->X64 = static_cast<double*>(dst);
+    else ix->X = static_cast<float*>(dst);
+    cudaError_t e = cudaMemcpyAsync(dst, data, bytes, cudaMemcpyDefault, ix->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ix->stream);
     if (e != cudaSuccess) {
-      cudaFree(ix->X);
+      cudaFree(dst);
       cudaStreamDestroy(ix->stream);
       delete ix;
       set_error("index upload failed: %s", cudaGetErrorString(e));
@@ -423,10 +442,27 @@ int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, 
   return ST_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+int fuelg_index_create(const float* data, int64_t n, int32_t d, int32_t metric, int32_t order, fuelg_index** out) {
+  return index_create_impl(data, false, n, d, metric, order, out);
+}
+
+int fuelg_index_create_f64(const double* data, int64_t n, int32_t d, int32_t metric, int32_t order,
+                           fuelg_index** out) {
+  return index_create_impl(data, true, n, d, metric, order, out);
+}
+
 }  // extern "C"
 
 namespace fuelg {
 int index_view_get(fuelg_index* ix, int want_tier, IndexView* out) {
+  if (ix->f64) {
+    set_error("the index holds float64 data: this call serves float32 indexes");
+    return ST_EINVAL;
+  }
   std::lock_guard<std::mutex> lk(ix->mu);
   cudaSetDevice(ix->device);
   if (want_tier >= 0 && !ix->tc && ix->n > 0 && knn_tc_supported(ix->n, ix->d, 1, TC_BF16))
@@ -457,6 +493,7 @@ int fuelg_index_destroy(fuelg_index* ix) {
   if (ix->stream) cudaStreamSynchronize(ix->stream);
   knn_tc_index_free(ix->tc);
   if (ix->X) cudaFree(ix->X);
+  if (ix->X64) cudaFree(ix->X64);
   if (ix->stream) cudaStreamDestroy(ix->stream);
   delete ix;
   return ST_OK;
@@ -618,6 +655,10 @@ int check_knn_args(fuelg_index* ix, const float* queries, int64_t m, int32_t k, 
                    int32_t precision) {
   if (!ix) {
     set_error("index is NULL");
+    return ST_EINVAL;
+  }
+  if (ix->f64) {
+    set_error("the index holds float64 data: use the _f64 calls");
     return ST_EINVAL;
   }
   if (m < 0 || k < 0 || (m > 0 && !queries && m != ix->n)) {
@@ -859,6 +900,10 @@ int fuelg_knn_error(fuelg_index* ix, const float* queries, int64_t m, int32_t k,
     set_error("invalid knn_error arguments");
     return ST_EINVAL;
   }
+  if (ix->f64) {
+    set_error("the index holds float64 data: the error report serves float32 indexes");
+    return ST_EINVAL;
+  }
   memset(out, 0, sizeof(*out));
   std::lock_guard<std::mutex> lk(ix->mu);
   FUELG_TRY(begin_call());
@@ -951,6 +996,10 @@ int fuelg_range(fuelg_index* ix, const float* queries, int64_t m, double radius,
     set_error("invalid range arguments m=%lld", (long long)m);
     return ST_EINVAL;
   }
+  if (ix->f64) {
+    set_error("the index holds float64 data: use fuelg_range_f64");
+    return ST_EINVAL;
+  }
   std::lock_guard<std::mutex> lk(ix->mu);
   FUELG_TRY(begin_call());
   cudaSetDevice(ix->device);
@@ -1008,6 +1057,10 @@ int fuelg_range_copy(const fuelg_range_result* r, int64_t* offsets, int64_t* idx
     set_error("range result is NULL");
     return ST_EINVAL;
   }
+  if (r->f64) {
+    set_error("float64 lists: read them with fuelg_range_copy_f64");
+    return ST_EINVAL;
+  }
   if (offsets) FUELG_CUDA(cudaMemcpy(offsets, r->off, sizeof(int64_t) * (r->m + 1), cudaMemcpyDefault));
   if (r->total) {
     if (idx) FUELG_CUDA(cudaMemcpy(idx, r->idx, sizeof(int64_t) * r->total, cudaMemcpyDefault));
@@ -1022,6 +1075,239 @@ int fuelg_range_free(fuelg_range_result* r) {
   if (r->idx) cudaFree(r->idx);
   if (r->dist) cudaFree(r->dist);
   delete r;
+  return ST_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+int check_f64_index(fuelg_index* ix) {
+  if (!ix) {
+    set_error("index is NULL");
+    return ST_EINVAL;
+  }
+  if (!ix->f64) {
+    set_error("the index holds float32 data: use the float32 calls");
+    return ST_EINVAL;
+  }
+  return ST_OK;
+}
+
+F64Scan f64_view(const fuelg_index* ix) {
+  F64Scan x;
+  x.X = ix->X64;
+  x.n = ix->n;
+  x.d = ix->d;
+  x.metric = ix->metric;
+  x.order = ix->order;
+  return x;
+}
+
+// fuelg_knn_ties_f64 / fuelg_range_f64: host-side CSR lists into a result handle.
+int f64_lists_call(fuelg_index* ix, const double* queries, int64_t m, bool range, int64_t kq, bool drop_self,
+                   double radius, fuelg_range_result** out, fuelg_stats* stats) {
+  std::lock_guard<std::mutex> lk(ix->mu);
+  FUELG_TRY(begin_call());
+  cudaSetDevice(ix->device);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  cudaStream_t s = ix->stream;
+  CallMeter meter;
+  Timer tm(s);
+  InBuf q;
+  if (queries) FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(double), s));
+  const double* Q = queries ? static_cast<const double*>(q.dptr) : ix->X64;
+  fuelg_range_result* r = new fuelg_range_result();
+  r->m = m;
+  r->f64 = true;
+  int64_t d2h = 0;
+  const int st = f64_lists(f64_view(ix), Q, m, range, kq, drop_self, radius, &r->h_off, &r->h_idx, &r->h_dist,
+                           &d2h, s);
+  const double ms = tm.stop();
+  if (st != ST_OK) {
+    delete r;
+    return st;
+  }
+  r->total = r->h_off.empty() ? 0 : r->h_off.back();
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = q.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = m * ix->n;
+    stats->precision_used = FUELG_PREC_FP64;
+    meter.fill(stats);
+  }
+  *out = r;
+  return ST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fuelg_knn_f64(fuelg_index* ix, const double* queries, int64_t m, int32_t k, int32_t exclude_mode,
+                  int64_t* out_idx, double* out_dist, fuelg_stats* stats) {
+  FUELG_TRY(check_f64_index(ix));
+  if (m < 0 || k < 0 || (m > 0 && !queries && m != ix->n)) {
+    set_error("invalid knn arguments m=%lld k=%d (queries may be NULL only for the index's own %lld rows)",
+              (long long)m, k, (long long)ix->n);
+    return ST_EINVAL;
+  }
+  if (exclude_mode < FUELG_EXCLUDE_NONE || exclude_mode > FUELG_EXCLUDE_KPLUS1) {
+    set_error("unknown exclude mode %d", exclude_mode);
+    return ST_EINVAL;
+  }
+  if (k > 4095) {
+    set_error("k=%d exceeds the supported maximum of 4095", k);
+    return ST_ENOTSUP;
+  }
+  if (m > 0 && k > 0 && (!out_idx || !out_dist)) {
+    set_error("invalid knn arguments: output buffers are NULL");
+    return ST_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(ix->mu);
+  FUELG_TRY(begin_call());
+  cudaSetDevice(ix->device);
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (m == 0 || k == 0) return ST_OK;
+  cudaStream_t s = ix->stream;
+  CallMeter meter;
+  Timer tm(s);
+  InBuf q;
+  if (queries) FUELG_TRY(q.init(queries, (size_t)m * ix->d * sizeof(double), s));
+  const double* Q = queries ? static_cast<const double*>(q.dptr) : ix->X64;
+  OutBuf oi, od;
+  FUELG_TRY(oi.init(out_idx, (size_t)m * k * sizeof(int64_t), s));
+  FUELG_TRY(od.init(out_dist, (size_t)m * k * sizeof(double), s));
+  FUELG_TRY(f64_knn(f64_view(ix), Q, m, k, exclude_mode, static_cast<int64_t*>(oi.dptr),
+                    static_cast<double*>(od.dptr), s));
+  int64_t d2h = 0;
+  FUELG_TRY(oi.flush(s, &d2h));
+  FUELG_TRY(od.flush(s, &d2h));
+  const double ms = tm.stop();
+  FUELG_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = q.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = m * ix->n;
+    stats->precision_used = FUELG_PREC_FP64;
+    meter.fill(stats);
+  }
+  return ST_OK;
+}
+
+int fuelg_knn_ties_f64(fuelg_index* ix, const double* queries, int64_t m, int32_t k, int32_t exclude_mode,
+                       fuelg_range_result** out, fuelg_stats* stats) {
+  if (!out) {
+    set_error("out is NULL");
+    return ST_EINVAL;
+  }
+  *out = nullptr;
+  FUELG_TRY(check_f64_index(ix));
+  if (m < 0 || k < 0 || (m > 0 && !queries && m != ix->n)) {
+    set_error("invalid knn arguments m=%lld k=%d (queries may be NULL only for the index's own %lld rows)",
+              (long long)m, k, (long long)ix->n);
+    return ST_EINVAL;
+  }
+  if (exclude_mode < FUELG_EXCLUDE_NONE || exclude_mode > FUELG_EXCLUDE_KPLUS1) {
+    set_error("unknown exclude mode %d", exclude_mode);
+    return ST_EINVAL;
+  }
+  if (k > 4095) {
+    set_error("k=%d exceeds the supported maximum of 4095", k);
+    return ST_ENOTSUP;
+  }
+  // the linear-index rule searches k, the k+1 rule k+1; both drop self afterwards
+  const int64_t kq = exclude_mode == FUELG_EXCLUDE_KPLUS1 ? (int64_t)k + 1 : k;
+  return f64_lists_call(ix, queries, m, false, kq, exclude_mode != FUELG_EXCLUDE_NONE, 0.0, out, stats);
+}
+
+int fuelg_range_f64(fuelg_index* ix, const double* queries, int64_t m, double radius, int32_t exclude_self,
+                    fuelg_range_result** out, fuelg_stats* stats) {
+  if (!out) {
+    set_error("out is NULL");
+    return ST_EINVAL;
+  }
+  *out = nullptr;
+  FUELG_TRY(check_f64_index(ix));
+  if (m < 0 || (m > 0 && !queries)) {
+    set_error("invalid range arguments m=%lld", (long long)m);
+    return ST_EINVAL;
+  }
+  return f64_lists_call(ix, queries, m, true, 0, exclude_self != 0, radius, out, stats);
+}
+
+int fuelg_range_copy_f64(const fuelg_range_result* r, int64_t* offsets, int64_t* idx, double* dist) {
+  if (!r) {
+    set_error("range result is NULL");
+    return ST_EINVAL;
+  }
+  if (!r->f64) {
+    set_error("float32 lists: read them with fuelg_range_copy");
+    return ST_EINVAL;
+  }
+  if (offsets && !r->h_off.empty())
+    FUELG_CUDA(cudaMemcpy(offsets, r->h_off.data(), sizeof(int64_t) * r->h_off.size(), cudaMemcpyDefault));
+  if (r->total) {
+    if (idx) FUELG_CUDA(cudaMemcpy(idx, r->h_idx.data(), sizeof(int64_t) * r->total, cudaMemcpyDefault));
+    if (dist) FUELG_CUDA(cudaMemcpy(dist, r->h_dist.data(), sizeof(double) * r->total, cudaMemcpyDefault));
+  }
+  return ST_OK;
+}
+
+int fuelg_pairwise_f64(const double* X, int64_t n, int32_t d, int32_t metric, int32_t order, int32_t form,
+                       double* out, fuelg_stats* stats) {
+  if (n < 0 || d < 1 || (n > 0 && !X)) {
+    set_error("invalid pairwise arguments n=%lld d=%d", (long long)n, d);
+    return ST_EINVAL;
+  }
+  if (metric != FUELG_METRIC_SQEUCLIDEAN && metric != FUELG_METRIC_EUCLIDEAN) {
+    set_error("unknown metric %d", metric);
+    return ST_EINVAL;
+  }
+  if (order != FUELG_ORDER_ARM && order != FUELG_ORDER_X86) {
+    set_error("unknown summation order %d", order);
+    return ST_EINVAL;
+  }
+  if (form != FUELG_PAIRWISE_CONDENSED && form != FUELG_PAIRWISE_SQUARE) {
+    set_error("unknown pairwise form %d", form);
+    return ST_EINVAL;
+  }
+  const int64_t outs = form == FUELG_PAIRWISE_CONDENSED ? n * (n - 1) / 2 : n * n;
+  if (outs > 0 && !out) {
+    set_error("out is NULL");
+    return ST_EINVAL;
+  }
+  FUELG_TRY(begin_call());
+  if (stats) memset(stats, 0, sizeof(*stats));
+  if (outs <= 0) return ST_OK;
+  cudaStream_t s;
+  FUELG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct StreamGuard {
+    cudaStream_t s;
+    ~StreamGuard() { cudaStreamDestroy(s); }
+  } sg{s};
+  CallMeter meter;
+  Timer tm(s);
+  InBuf xb;
+  FUELG_TRY(xb.init(X, (size_t)n * d * sizeof(double), s));
+  OutBuf ob;
+  FUELG_TRY(ob.init(out, (size_t)outs * sizeof(double), s));
+  FUELG_TRY(f64_pairwise(static_cast<const double*>(xb.dptr), n, d, metric, order, form,
+                         static_cast<double*>(ob.dptr), s));
+  int64_t d2h = 0;
+  FUELG_TRY(ob.flush(s, &d2h));
+  const double ms = tm.stop();
+  FUELG_CUDA(cudaStreamSynchronize(s));
+  if (stats) {
+    stats->device_ms = ms;
+    stats->h2d_bytes = xb.h2d;
+    stats->d2h_bytes = d2h;
+    stats->distance_evals = form == FUELG_PAIRWISE_CONDENSED ? outs : n * n;
+    stats->precision_used = FUELG_PREC_FP64;
+    meter.fill(stats);
+  }
   return ST_OK;
 }
 

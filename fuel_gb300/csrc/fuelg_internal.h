@@ -206,6 +206,25 @@ int exact_knn_sets(const KnnSetDev* sets, int count, int order, int* dev_status,
 int exact_knn_in_scratch(const ExactScanParams& p, int k, int exclude_mode, int64_t* out_idx, float* out_dist,
                          void* scratch, size_t scratch_bytes, cudaStream_t stream);
 
+// The exact FP64 scan (fuelg_f64.cu) over a float64 index X [n, d] (n <= 2^32 - 2).
+struct F64Scan {
+  const double* X = nullptr;
+  int64_t n = 0;
+  int d = 0;
+  int metric = 0;
+  int order = 0;
+};
+// Truncated kNN rows [m, k] (device outputs) under an exclude rule (FUELG_EXCLUDE_*).
+int f64_knn(const F64Scan& x, const double* Q, int64_t m, int k, int mode, int64_t* out_idx, double* out_dist,
+            cudaStream_t s);
+// CSR lists in host memory: tie-inclusive kNN lists of kq (range false), or
+// every point within radius (range true); drop_self leaves point i out of row i.
+int f64_lists(const F64Scan& x, const double* Q, int64_t m, bool range, int64_t kq, bool drop_self, double radius,
+              std::vector<int64_t>* off, std::vector<int64_t>* idx, std::vector<double>* dist, int64_t* d2h,
+              cudaStream_t s);
+// All pairwise distances of X (FUELG_PAIRWISE_* layouts), device output.
+int f64_pairwise(const double* X, int64_t n, int d, int metric, int order, int form, double* out, cudaStream_t s);
+
 // Tensor-core kNN (fuelg_knn_tc.cu): top-kk keys per query [m, kk] via a
 // tcgen05 screen; exact for integer data, otherwise re-scored and proven.
 // Operand tiers: BF16 (one product, error ~2^-8), split BF16 (hi + lo, three

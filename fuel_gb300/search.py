@@ -6,10 +6,12 @@ validation, return types and exclude-self rules.  The scan itself runs in
 libfuelg.so; distances are bit-identical to fuel's f32 distances for the
 chosen summation profile (``order``).
 
-What is served: float32 data, distances ``euclidean``/``l2`` and
-``sqeuclidean``/``squared_euclidean``, the linear scan (``tree`` = ``None``,
-``'auto'``, ``'linear'``, ``'brute'``, ``'bruteforce'``).  Anything else
-raises ``NotImplementedError`` rather than silently running elsewhere.
+What is served: float32 data and float64 data (every other input dtype
+becomes float64, as in fuel; float64 runs the exact FP64 scan with fuel's f64
+distances), distances ``euclidean``/``l2`` and ``sqeuclidean``/
+``squared_euclidean``, the linear scan (``tree`` = ``None``, ``'auto'``,
+``'linear'``, ``'brute'``, ``'bruteforce'``).  Anything else raises
+``NotImplementedError`` rather than silently running elsewhere.
 """
 from __future__ import annotations
 
@@ -63,12 +65,6 @@ def _parse_distance(distance: str) -> str:
         "squared_euclidean)")
 
 
-def _require_f32(arr, what):
-    if arr.dtype != np.float32:
-        raise NotImplementedError(
-            f"{what} has dtype {arr.dtype}; the GB300 engine serves float32 (cast with .astype(np.float32))")
-
-
 class SearchIndex:
     """Persistent linear-scan index held in GB300 memory.
 
@@ -109,10 +105,13 @@ class SearchIndex:
             raise NotImplementedError(
                 f"tree '{tree}' is not served by the GB300 engine; only the exact linear scan is accelerated")
         self._metric = _parse_distance(distance)
-        _require_f32(data, "data")
+        self._f64 = data.dtype == np.float64
         precision = "auto" if precision is None else precision
         if precision not in _lib.PRECISION:
             raise ValueError(f"precision must be one of {sorted(_lib.PRECISION)}")
+        if self._f64 and precision not in ("auto", "fp32"):
+            raise NotImplementedError(
+                f"precision '{precision}' applies to float32 data; float64 data runs the exact FP64 scan")
         self.precision = precision
         self.order = order or _lib.default_order()
         if self.order not in _lib.ORDER:
@@ -123,8 +122,9 @@ class SearchIndex:
         lib = _lib.load()
         host = np.ascontiguousarray(data)
         handle = ctypes.c_void_p()
-        _lib.check(lib.fuelg_index_create(_lib.ptr(host), host.shape[0], host.shape[1], _lib.METRIC[self._metric],
-                                          _lib.ORDER[self.order], ctypes.byref(handle)))
+        create = lib.fuelg_index_create_f64 if self._f64 else lib.fuelg_index_create
+        _lib.check(create(_lib.ptr(host), host.shape[0], host.shape[1], _lib.METRIC[self._metric],
+                          _lib.ORDER[self.order], ctypes.byref(handle)))
         self._handle = handle
         self.index = self
         self.last_stats = None
@@ -162,7 +162,7 @@ class SearchIndex:
         return query, bool(exclude_self)
 
     def knn(self, query, k, *, exclude_self=None):
-        """(int64[m, k] indices, float32[m, k] distances), -1 / inf padded."""
+        """(int64[m, k] indices, [m, k] distances of the index dtype), -1 / inf padded."""
         query, exclude_self = self._prepare_query(query, exclude_self)
         k = int(k)
         if k < 0:
@@ -174,34 +174,43 @@ class SearchIndex:
             return self._knn_from_table(m, k, exclude_self)
         q = np.ascontiguousarray(query)
         idx = np.empty((m, k), np.int64)
-        dist = np.empty((m, k), np.float32)
+        dist = np.empty((m, k), self.dtype)
         if exclude_self:
             mode = _lib.EXCLUDE_KPLUS1 if self.precompute is not None else _lib.EXCLUDE_LINEAR
         else:
             mode = _lib.EXCLUDE_NONE
         st = _lib.Stats()
-        _lib.check(_lib.load().fuelg_knn(self._handle, _lib.ptr(q), m, k, mode, _lib.PRECISION[self.precision],
-                                         _lib.ptr(idx), _lib.ptr(dist), ctypes.byref(st)))
+        lib = _lib.load()
+        if self._f64:
+            _lib.check(lib.fuelg_knn_f64(self._handle, _lib.ptr(q), m, k, mode, _lib.ptr(idx), _lib.ptr(dist),
+                                         ctypes.byref(st)))
+        else:
+            _lib.check(lib.fuelg_knn(self._handle, _lib.ptr(q), m, k, mode, _lib.PRECISION[self.precision],
+                                     _lib.ptr(idx), _lib.ptr(dist), ctypes.byref(st)))
         self.last_stats = st.as_dict()
         return idx, dist
 
     def _ties_csr(self, q, m, k, mode):
-        """fuelg_knn_ties -> (offsets int64[m+1], idx int64[], dist float32[]);
-        q None: the index's own rows are the queries."""
+        """fuelg_knn_ties -> (offsets int64[m+1], idx int64[], dist[] of the index
+        dtype); q None: the index's own rows are the queries."""
         lib = _lib.load()
         res = ctypes.c_void_p()
         st = _lib.Stats()
-        _lib.check(lib.fuelg_knn_ties(self._handle, None if q is None else _lib.ptr(q), m, k, mode,
-                                      _lib.PRECISION[self.precision], ctypes.byref(res), ctypes.byref(st)))
+        qp = None if q is None else _lib.ptr(q)
+        if self._f64:
+            _lib.check(lib.fuelg_knn_ties_f64(self._handle, qp, m, k, mode, ctypes.byref(res), ctypes.byref(st)))
+        else:
+            _lib.check(lib.fuelg_knn_ties(self._handle, qp, m, k, mode, _lib.PRECISION[self.precision],
+                                          ctypes.byref(res), ctypes.byref(st)))
         try:
-            off, idx, dist = _take_csr(lib, res, m)
+            off, idx, dist = _take_csr(lib, res, m, self._f64)
         finally:
             lib.fuelg_range_free(res)
         self.last_stats = st.as_dict()
         return off, idx, dist
 
     def knn_with_ties(self, query, k, *, exclude_self=None):
-        """Tie-inclusive kNN lists: ([int64 arrays], [float32 arrays]) per
+        """Tie-inclusive kNN lists: ([int64 arrays], [distance arrays]) per
         query row -- the k nearest points plus every point tied with the k-th
         distance, sorted by (distance, index), as KNNHeap::into_vec returns
         them (src/api/search.rs:80-151); exclude_self drops index i from row i
@@ -242,17 +251,18 @@ class SearchIndex:
         return np.ascontiguousarray(gi[:, :k]), np.ascontiguousarray(gd[:, :k])
 
     def radius_search(self, query, radius, *, exclude_self=None):
-        """([int64 arrays], [float32 arrays]) per query row, sorted by (distance, index)."""
+        """([int64 arrays], [distance arrays]) per query row, sorted by (distance, index)."""
         query, exclude_self = self._prepare_query(query, exclude_self)
         q = np.ascontiguousarray(query)
         m = q.shape[0]
         lib = _lib.load()
         res = ctypes.c_void_p()
         st = _lib.Stats()
-        _lib.check(lib.fuelg_range(self._handle, _lib.ptr(q), m, float(radius), int(exclude_self),
-                                   ctypes.byref(res), ctypes.byref(st)))
+        call = lib.fuelg_range_f64 if self._f64 else lib.fuelg_range
+        _lib.check(call(self._handle, _lib.ptr(q), m, float(radius), int(exclude_self), ctypes.byref(res),
+                        ctypes.byref(st)))
         try:
-            off, idx, dist = _take_csr(lib, res, m)
+            off, idx, dist = _take_csr(lib, res, m, self._f64)
         finally:
             lib.fuelg_range_free(res)
         self.last_stats = st.as_dict()
@@ -270,14 +280,15 @@ class SearchIndex:
         return f"<SearchIndex tree={self.tree!r} dtype={self.dtype!r} shape={self.shape!r}>"
 
 
-def _take_csr(lib, res, m):
+def _take_csr(lib, res, m, f64=False):
     """Copy a fuelg_range_result to host arrays (offsets[m+1], idx[], dist[])."""
     mm, tot = ctypes.c_int64(), ctypes.c_int64()
     _lib.check(lib.fuelg_range_size(res, ctypes.byref(mm), ctypes.byref(tot)))
     off = np.empty(m + 1, np.int64)
     idx = np.empty(max(1, tot.value), np.int64)
-    dist = np.empty(max(1, tot.value), np.float32)
-    _lib.check(lib.fuelg_range_copy(res, _lib.ptr(off), _lib.ptr(idx), _lib.ptr(dist)))
+    dist = np.empty(max(1, tot.value), np.float64 if f64 else np.float32)
+    copy = lib.fuelg_range_copy_f64 if f64 else lib.fuelg_range_copy
+    _lib.check(copy(res, _lib.ptr(off), _lib.ptr(idx), _lib.ptr(dist)))
     return off, idx[:tot.value], dist[:tot.value]
 
 
@@ -295,20 +306,21 @@ class PrioritySearcher:
             raise ValueError(f"query must have {index.shape[1]} coordinates")
         self._index = index
         self._query = q
+        self._ft = index.dtype.type  # cutoff and skip compare in the index dtype
         self.reset()
 
     def reset(self):
         self._cand = None
         self._pos = 0
-        self.cutoff = np.float32(np.inf)
-        self.skip = np.float32(0.0)
+        self.cutoff = self._ft(np.inf)
+        self.skip = self._ft(0.0)
 
     def reset_with_limits(self, cutoff, skip):
         if not skip >= 0 or not cutoff >= skip:
             raise ValueError("need 0 <= skip <= cutoff")
         self.reset()
-        self.cutoff = np.float32(cutoff)
-        self.skip = np.float32(skip)
+        self.cutoff = self._ft(cutoff)
+        self.skip = self._ft(skip)
 
     def _ensure(self):
         if self._cand is not None:
@@ -350,7 +362,7 @@ class PrioritySearcher:
     def decrease_cutoff(self, threshold):
         if threshold > self.cutoff:
             raise ValueError("thresholds must only decrease")
-        self.cutoff = np.float32(threshold)
+        self.cutoff = self._ft(threshold)
 
 
 def knn_search(data, query, k, *, exclude_self=None, distance="euclidean", tree="auto", seed=None, **kw):
@@ -435,9 +447,10 @@ def pairwise_distances(data, distance="euclidean", form="condensed", *, order=No
 
     ``form='condensed'``: the lower triangle as one vector, pair (i, j) with
     j < i at ``i*(i-1)//2 + j``; ``form='square'``: the symmetric matrix.
-    Raw float32 points with distance ``euclidean``/``l2`` or
-    ``sqeuclidean``/``squared_euclidean`` run on the GPU (fuelg_pairwise),
-    bit-identical to fuel's distance in the chosen summation ``order``;
+    Raw float32 or float64 points with distance ``euclidean``/``l2`` or
+    ``sqeuclidean``/``squared_euclidean`` run on the GPU (fuelg_pairwise /
+    fuelg_pairwise_f64), bit-identical to fuel's distance of that dtype in the
+    chosen summation ``order``;
     ``distance='precomputed'`` converts between the forms as fuel does (a 1-D
     input is a scipy ``pdist`` vector, pairs (a, b) with a < b).
     """
@@ -467,7 +480,6 @@ def pairwise_distances(data, distance="euclidean", form="condensed", *, order=No
     if data.ndim != 2:
         raise ValueError("data must be a 2D array of observations when distance is not 'precomputed'")
     metric = _parse_distance(distance)
-    _require_f32(data, "data")
     order = order or _lib.default_order()
     if order not in _lib.ORDER:
         raise ValueError(f"order must be one of {sorted(_lib.ORDER)}")
@@ -475,10 +487,12 @@ def pairwise_distances(data, distance="euclidean", form="condensed", *, order=No
     n, d = X.shape
     square = form == "square"
     if d == 0:  # every distance between empty rows is 0
-        return np.zeros((n, n) if square else n * (n - 1) // 2, dtype=np.float32)
-    out = np.empty(n * n if square else n * (n - 1) // 2, dtype=np.float32)
+        return np.zeros((n, n) if square else n * (n - 1) // 2, dtype=X.dtype)
+    out = np.empty(n * n if square else n * (n - 1) // 2, dtype=X.dtype)
     st = _lib.Stats()
-    _lib.check(_lib.load().fuelg_pairwise(_lib.ptr(X), n, d, _lib.METRIC[metric], _lib.ORDER[order],
-                                          1 if square else 0, _lib.ptr(out), ctypes.byref(st)))
+    lib = _lib.load()
+    call = lib.fuelg_pairwise_f64 if X.dtype == np.float64 else lib.fuelg_pairwise
+    _lib.check(call(_lib.ptr(X), n, d, _lib.METRIC[metric], _lib.ORDER[order], 1 if square else 0, _lib.ptr(out),
+                    ctypes.byref(st)))
     pairwise_distances.last_stats = st.as_dict()
     return out.reshape(n, n) if square else out

@@ -73,6 +73,9 @@ extern "C" {
    else FP32; batched k-means: split-BF16 for the problems it serves.
    fuelg_stats.precision_used reports what ran. */
 #define FUELG_PREC_AUTO (-1)
+/* Reported in fuelg_stats.precision_used by the float64 calls (the exact FP64
+   scan); not a request value. */
+#define FUELG_PREC_FP64 5
 
 #define FUELG_LLOYD_FIXED_ITERS 1 /* run exactly max_iter iterations (ignore changed==0 stop) */
 
@@ -213,6 +216,37 @@ int fuelg_range_free(fuelg_range_result *res);
 #define FUELG_PAIRWISE_SQUARE 1
 int fuelg_pairwise(const float *X, int64_t n, int32_t d, int32_t metric, int32_t order, int32_t form, float *out,
                    fuelg_stats *stats);
+
+/* ---- float64 data ----------------------------------------------------------
+ * fuel builds a float64 index for every input that is not float32
+ * (python/fuel/_dispatch.py:8-19; build_linear_scan_f64, python/search.rs:
+ * 1371-1389) and compares f64 distances in its f64 operation order
+ * (src/distance/squared_euclidean.rs:44-67 on x86 AVX + FMA builds, :99-133
+ * elsewhere; Euclidean = f64 sqrt).  These calls run the exact FP64 scan:
+ * every (query, point) distance in that order, (distance, index) order and
+ * the same tie, exclude and padding rules as the float32 calls.  A float64
+ * index (n <= 2^32 - 2) serves only the _f64 calls, a float32 index only the
+ * float32 calls (FUELG_EINVAL otherwise).  Distances are f64 (+inf padding);
+ * fuelg_stats.precision_used reports FUELG_PREC_FP64. */
+int fuelg_index_create_f64(const double *data, int64_t n, int32_t d, int32_t metric, int32_t order,
+                           fuelg_index **out);
+/* As fuelg_knn: out_idx / out_dist [m, k] (int64 / f64); queries NULL = the
+ * index's own rows (m = n). */
+int fuelg_knn_f64(fuelg_index *index, const double *queries, int64_t m, int32_t k, int32_t exclude_mode,
+                  int64_t *out_idx, double *out_dist, fuelg_stats *stats);
+/* As fuelg_knn_ties; read the lists with fuelg_range_copy_f64. */
+int fuelg_knn_ties_f64(fuelg_index *index, const double *queries, int64_t m, int32_t k, int32_t exclude_mode,
+                       fuelg_range_result **out, fuelg_stats *stats);
+/* As fuelg_range with an f64 radius (linear_scan_range on f64 data); read the
+ * lists with fuelg_range_copy_f64. */
+int fuelg_range_f64(fuelg_index *index, const double *queries, int64_t m, double radius, int32_t exclude_self,
+                    fuelg_range_result **out, fuelg_stats *stats);
+/* offsets [m+1]; idx / dist [total] of a float64 result. */
+int fuelg_range_copy_f64(const fuelg_range_result *res, int64_t *offsets, int64_t *idx, double *dist);
+/* As fuelg_pairwise on float64 points (_compute_pairwise_distances[_condensed]_f64,
+ * python/mod.rs:74-124). */
+int fuelg_pairwise_f64(const double *X, int64_t n, int32_t d, int32_t metric, int32_t order, int32_t form,
+                       double *out, fuelg_stats *stats);
 
 /* Lloyd k-means with fixed initial centres.  Replaces lloyd_f32
  * (python/kmeans.rs:188-218, 355) -> cluster::kmeans::lloyd

@@ -914,9 +914,9 @@ int fo_lloyd_f32(const float *X, int64_t n, int64_t d, int64_t k, const float *i
 /* linear_scan_knn for one query row WITHOUT the marshaller's truncation: the
  * full tie-inclusive KNNHeap::into_vec list (src/api/search.rs:145-150).
  * Writes up to `cap` pairs, returns the list length. */
-int64_t fo_knn_ties_f32(const float *X, int64_t n, int64_t d, const float *q, int64_t k, int metric, int order,
-                        int64_t cap, int64_t *out_idx, float *out_dist) {
-    fo_knn_ctx c = {0, X, q, n, d, 1, k, metric, order, 0, NULL, NULL};
+static int64_t fo_knn_ties_any(int is64, const void *X, int64_t n, int64_t d, const void *q, int64_t k, int metric,
+                               int order, int64_t cap, int64_t *out_idx, void *out_dist) {
+    fo_knn_ctx c = {is64, X, q, n, d, 1, k, metric, order, 0, NULL, NULL};
     if (k <= 0 || n <= 0) return 0;
     fo_knnheap h;
     memset(&h, 0, sizeof(h));
@@ -934,10 +934,19 @@ int64_t fo_knn_ties_f32(const float *X, int64_t n, int64_t d, const float *q, in
     qsort(res, nres, sizeof(fo_pair), fo_pair_qcmp);
     for (int64_t j = 0; j < nres && j < cap; j++) {
         out_idx[j] = res[j].idx;
-        out_dist[j] = (float)res[j].dist;
+        if (is64) ((double *)out_dist)[j] = res[j].dist;
+        else ((float *)out_dist)[j] = (float)res[j].dist;
     }
     free(res);
     free(h.heap);
     free(h.ties);
     return nres;
+}
+int64_t fo_knn_ties_f32(const float *X, int64_t n, int64_t d, const float *q, int64_t k, int metric, int order,
+                        int64_t cap, int64_t *out_idx, float *out_dist) {
+    return fo_knn_ties_any(0, X, n, d, q, k, metric, order, cap, out_idx, out_dist);
+}
+int64_t fo_knn_ties_f64(const double *X, int64_t n, int64_t d, const double *q, int64_t k, int metric, int order,
+                        int64_t cap, int64_t *out_idx, double *out_dist) {
+    return fo_knn_ties_any(1, X, n, d, q, k, metric, order, cap, out_idx, out_dist);
 }

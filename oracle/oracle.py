@@ -302,15 +302,16 @@ def knn_with_ties(X, q, k: int, metric: str = "sqeuclidean", order: str | None =
     """The full tie-inclusive linear_scan_knn list for one query (no truncation)."""
     lib = load()
     order = order or host_order()
-    X = _f(X, np.float32)
-    q = _f(q, np.float32).ravel()
-    fn = lib.fo_knn_ties_f32
+    dt = np.float64 if np.asarray(X).dtype == np.float64 else np.float32
+    X = _f(X, dt)
+    q = _f(q, dt).ravel()
+    fn = lib.fo_knn_ties_f64 if dt == np.float64 else lib.fo_knn_ties_f32
     fn.restype = ctypes.c_int64
     fn.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                    ctypes.c_int, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p]
     cap = X.shape[0]
     idx = np.empty(cap, np.int64)
-    dd = np.empty(cap, np.float32)
+    dd = np.empty(cap, dt)
     cnt = fn(_p(X), X.shape[0], X.shape[1], _p(q), k, METRICS[metric], ORDERS[order], cap, _p(idx), _p(dd))
     return idx[:cnt].copy(), dd[:cnt].copy()
 
@@ -320,7 +321,8 @@ def knn_ties(X, Q, k: int, metric: str = "sqeuclidean", order: str | None = None
     linear_scan_knn's KNNHeap::into_vec list (k, or k+1 for exclude='kplus1'),
     then index i dropped from row i for exclude 'linear' / 'kplus1'
     (python/search.rs:485-488, 1163-1170)."""
-    Q = _f(Q, np.float32)
+    dt = np.float64 if np.asarray(X).dtype == np.float64 else np.float32
+    Q = _f(Q, dt)
     kq = k + 1 if exclude == "kplus1" else k
     offs, ids, ds = [0], [], []
     for i in range(Q.shape[0]):
@@ -332,7 +334,7 @@ def knn_ties(X, Q, k: int, metric: str = "sqeuclidean", order: str | None = None
         ds.append(dd)
         offs.append(offs[-1] + len(ii))
     cat = (lambda parts, dt: np.concatenate(parts).astype(dt) if parts else np.empty(0, dt))
-    return np.array(offs, np.int64), cat(ids, np.int64), cat(ds, np.float32)
+    return np.array(offs, np.int64), cat(ids, np.int64), cat(ds, dt)
 
 
 # --------------------------------------------------------------------------

@@ -27,6 +27,8 @@ pub const FUELG_PREC_BF16: i32 = 1;
 pub const FUELG_PREC_SPLIT_BF16: i32 = 2;
 pub const FUELG_PREC_SPLIT_BF16_SCALED: i32 = 3;
 pub const FUELG_PREC_F16: i32 = 4;
+/// Reported by the float64 calls (the exact FP64 scan); not a request value.
+pub const FUELG_PREC_FP64: i32 = 5;
 pub const FUELG_LLOYD_FIXED_ITERS: i32 = 1;
 pub const FUELG_PAIRWISE_CONDENSED: i32 = 0;
 pub const FUELG_PAIRWISE_SQUARE: i32 = 1;
@@ -135,6 +137,20 @@ unsafe extern "C" {
 
     pub fn fuelg_pairwise(x: *const f32, n: i64, d: i32, metric: i32, order: i32, form: i32, out: *mut f32,
                           stats: *mut fuelg_stats) -> c_int;
+
+    // float64 data (build_linear_scan_f64, python/search.rs:1371-1389): the exact FP64 scan
+    pub fn fuelg_index_create_f64(data: *const f64, n: i64, d: i32, metric: i32, order: i32,
+                                  out: *mut *mut fuelg_index) -> c_int;
+    pub fn fuelg_knn_f64(index: *mut fuelg_index, queries: *const f64, m: i64, k: i32, exclude_mode: i32,
+                         out_idx: *mut i64, out_dist: *mut f64, stats: *mut fuelg_stats) -> c_int;
+    pub fn fuelg_knn_ties_f64(index: *mut fuelg_index, queries: *const f64, m: i64, k: i32, exclude_mode: i32,
+                              out: *mut *mut fuelg_range_result, stats: *mut fuelg_stats) -> c_int;
+    pub fn fuelg_range_f64(index: *mut fuelg_index, queries: *const f64, m: i64, radius: f64, exclude_self: i32,
+                           out: *mut *mut fuelg_range_result, stats: *mut fuelg_stats) -> c_int;
+    pub fn fuelg_range_copy_f64(res: *const fuelg_range_result, offsets: *mut i64, idx: *mut i64,
+                                dist: *mut f64) -> c_int;
+    pub fn fuelg_pairwise_f64(x: *const f64, n: i64, d: i32, metric: i32, order: i32, form: i32, out: *mut f64,
+                              stats: *mut fuelg_stats) -> c_int;
 
     pub fn fuelg_kmeans_lloyd(data: *const f32, n: i64, d: i32, k: i32, init_centers: *const f32,
                               max_iter: i32, tol: f64, precision: i32, order: i32, flags: i32,

@@ -58,9 +58,13 @@ def test_no_cpu_fallback_without_gpu(lib):
     rc = lib.fuelg_index_create(_lib.ptr(X), 4, 3, 0, 0, ctypes.byref(h))
     assert rc == _lib.ENODEV
     assert "no CUDA device" in _lib.last_error()
+    X64 = X.astype(np.float64)
+    assert lib.fuelg_index_create_f64(_lib.ptr(X64), 4, 3, 0, 0, ctypes.byref(h)) == _lib.ENODEV
     import fuel_gb300
     with pytest.raises(RuntimeError):
         fuel_gb300.SearchIndex(X, tree="linear")
+    with pytest.raises(RuntimeError):
+        fuel_gb300.SearchIndex(X64, tree="linear")
     with pytest.raises(RuntimeError):
         fuel_gb300.kmeans(X, k=2, variant="lloyd", init="first")
 
@@ -76,6 +80,12 @@ def test_argument_validation_before_any_device_work(lib):
     assert lib.fuelg_range_free(None) == _lib.OK
     assert lib.fuelg_index_destroy(None) == _lib.OK
     assert lib.fuelg_release() == _lib.OK  # nothing kept yet: a no-op
+    assert lib.fuelg_index_create_f64(None, 4, 3, 0, 0, ctypes.byref(h)) == _lib.EINVAL
+    assert lib.fuelg_knn_f64(None, None, 0, 1, 0, None, None, None) == _lib.EINVAL
+    assert lib.fuelg_knn_ties_f64(None, None, 0, 1, 0, None, None) == _lib.EINVAL
+    assert lib.fuelg_range_f64(None, None, 0, 1.0, 0, None, None) == _lib.EINVAL
+    assert lib.fuelg_range_copy_f64(None, None, None, None) == _lib.EINVAL
+    assert lib.fuelg_pairwise_f64(None, 3, 0, 0, 0, 0, None, None) == _lib.EINVAL
 
 
 def test_rust_bindings_declare_every_header_function():

@@ -32,8 +32,9 @@ def test_non_linear_trees_are_not_silently_served():
 
 def test_float64_is_not_silently_downcast():
     X = np.zeros((4, 3), np.float64)
+    # float64 search runs the exact FP64 scan; the tensor-core tiers serve float32 data
     with pytest.raises(NotImplementedError):
-        search.SearchIndex(X, tree="linear")
+        search.SearchIndex(X, tree="linear", precision="bf16")
     with pytest.raises(NotImplementedError):
         cluster.kmeans(X, k=2, variant="lloyd", init="first")
 
