@@ -12,6 +12,10 @@
 //!   many queries in one call: the batch drivers of python/search.rs:471-514
 //!   and the table `PrecomputedKnnSearcher::new` builds
 //!   (src/search/precomputed.rs:36-55).
+//! * [`GpuLinearScanF64`] does the same for float64 data (fuel's
+//!   `build_linear_scan_f64`, python/search.rs:1371-1389) through the exact
+//!   FP64 scan (`fuelg_knn_ties_f64`, `fuelg_range_f64`): distances
+//!   bit-identical to fuel's own f64 distances.
 //! * [`lloyd_gpu`] has the signature of `cluster::kmeans::lloyd`
 //!   (src/cluster/kmeans/lloyd.rs:118-125) and runs it through
 //!   `fuelg_kmeans_lloyd` with the centres the `Initialization` chooses.
@@ -189,6 +193,150 @@ where
 {
     /// `linear_scan_range` (src/api/search.rs:154-166).
     fn search_range(&self, query: &Q, radius: f32) -> Vec<DistPair<f32>> {
+        if self.n == 0 {
+            return Vec::new();
+        }
+        let q = self.coords(query);
+        self.range_batch(&q, radius, false)
+            .map(|mut rows| rows.pop().unwrap_or_default())
+            .unwrap_or_else(|e| panic!("GPU range search failed: {e}"))
+    }
+}
+
+/// Tie-inclusive / range lists of a float64 batch, one `Vec<DistPair>` per query row.
+fn take_lists_f64(res: *mut sys::fuelg_range_result, m: usize) -> Result<Vec<Vec<DistPair<f64>>>, String> {
+    struct Guard(*mut sys::fuelg_range_result);
+    impl Drop for Guard {
+        fn drop(&mut self) {
+            unsafe {
+                sys::fuelg_range_free(self.0);
+            }
+        }
+    }
+    let _g = Guard(res);
+    let (mut mm, mut total) = (0i64, 0i64);
+    sys::check(unsafe { sys::fuelg_range_size(res, &mut mm, &mut total) })?;
+    let mut off = vec![0i64; m + 1];
+    let mut idx = vec![0i64; total.max(1) as usize];
+    let mut dist = vec![0f64; total.max(1) as usize];
+    sys::check(unsafe { sys::fuelg_range_copy_f64(res, off.as_mut_ptr(), idx.as_mut_ptr(), dist.as_mut_ptr()) })?;
+    Ok((0..m)
+        .map(|r| {
+            (off[r] as usize..off[r + 1] as usize).map(|e| DistPair::new(dist[e], idx[e] as usize)).collect()
+        })
+        .collect())
+}
+
+/// A float64 linear-scan index resident in GPU memory: fuel's
+/// `build_linear_scan_f64` (python/search.rs:1371-1389) on the exact FP64 scan.
+pub struct GpuLinearScanF64 {
+    ix: *mut sys::fuelg_index,
+    n: usize,
+    d: usize,
+}
+
+unsafe impl Send for GpuLinearScanF64 {}
+unsafe impl Sync for GpuLinearScanF64 {}
+
+impl Drop for GpuLinearScanF64 {
+    fn drop(&mut self) {
+        unsafe {
+            sys::fuelg_index_destroy(self.ix);
+        }
+    }
+}
+
+impl GpuLinearScanF64 {
+    /// Upload `n` rows of `d` coordinates (row-major) and build the index.
+    pub fn new(data: &[f64], n: usize, d: usize, metric: Metric) -> Result<Self, String> {
+        if data.len() != n * d {
+            return Err(format!("data holds {} values, expected n*d = {}", data.len(), n * d));
+        }
+        let mut ix = ptr::null_mut();
+        sys::check(unsafe {
+            sys::fuelg_index_create_f64(data.as_ptr(), n as i64, d as i32, metric.code(), sys::FUELG_ORDER_HOST,
+                                        &mut ix)
+        })?;
+        Ok(GpuLinearScanF64 { ix, n, d })
+    }
+
+    /// Index every row of a fuel data set.
+    pub fn from_data<A: VectorData<f64>>(data: &A, metric: Metric) -> Result<Self, String> {
+        let (n, d) = (data.nrows(), data.ncols());
+        let mut rows = Vec::with_capacity(n * d);
+        for i in 0..n {
+            rows.extend_from_slice(data.point(i));
+        }
+        Self::new(&rows, n, d, metric)
+    }
+
+    pub fn len(&self) -> usize { self.n }
+    pub fn is_empty(&self) -> bool { self.n == 0 }
+    pub fn dims(&self) -> usize { self.d }
+
+    /// Tie-inclusive kNN lists of `m` query rows, exclude rules as
+    /// [`GpuLinearScan::knn_batch`].
+    pub fn knn_batch(&self, queries: &[f64], k: usize, exclude_mode: i32) -> Result<Vec<Vec<DistPair<f64>>>, String> {
+        let m = queries.len() / self.d.max(1);
+        let mut res = ptr::null_mut();
+        sys::check(unsafe {
+            sys::fuelg_knn_ties_f64(self.ix, queries.as_ptr(), m as i64, k as i32, exclude_mode, &mut res,
+                                    ptr::null_mut())
+        })?;
+        take_lists_f64(res, m)
+    }
+
+    /// The kNN table of every indexed point to `max_k` neighbours with ties.
+    pub fn precomputed_table(&self, max_k: usize) -> Result<Vec<Vec<DistPair<f64>>>, String> {
+        let max_k = max_k.min(self.n);
+        let mut res = ptr::null_mut();
+        sys::check(unsafe {
+            sys::fuelg_knn_ties_f64(self.ix, ptr::null(), self.n as i64, max_k as i32, sys::FUELG_EXCLUDE_NONE,
+                                    &mut res, ptr::null_mut())
+        })?;
+        take_lists_f64(res, self.n)
+    }
+
+    /// Sorted range lists of `m` query rows (f64 radius).
+    pub fn range_batch(&self, queries: &[f64], radius: f64, exclude_self: bool)
+        -> Result<Vec<Vec<DistPair<f64>>>, String> {
+        let m = queries.len() / self.d.max(1);
+        let mut res = ptr::null_mut();
+        sys::check(unsafe {
+            sys::fuelg_range_f64(self.ix, queries.as_ptr(), m as i64, radius, exclude_self as i32, &mut res,
+                                 ptr::null_mut())
+        })?;
+        take_lists_f64(res, m)
+    }
+
+    fn coords<Q: CoordinateSearch<f64, f64> + ?Sized>(&self, q: &Q) -> Vec<f64> {
+        (0..self.d).map(|axis| q.query_coordinate(axis)).collect()
+    }
+}
+
+impl<Q> KnnSearch<f64, Q> for GpuLinearScanF64
+where
+    Q: DistanceSearch<f64> + CoordinateSearch<f64, f64> + ?Sized,
+{
+    /// `linear_scan_knn` on f64 data: the k nearest plus every tie at the k-th
+    /// distance, sorted by (distance, index).
+    fn search_knn(&self, query: &Q, k: usize) -> Vec<DistPair<f64>> {
+        if k == 0 || self.n == 0 {
+            return Vec::new();
+        }
+        let q = self.coords(query);
+        self.knn_batch(&q, k, sys::FUELG_EXCLUDE_NONE)
+            .map(|mut rows| rows.pop().unwrap_or_default())
+            .unwrap_or_else(|e| panic!("GPU kNN failed: {e}"))
+    }
+}
+
+impl<Q> RangeSearch<f64, Q> for GpuLinearScanF64
+where
+    Q: DistanceSearch<f64> + CoordinateSearch<f64, f64> + ?Sized,
+{
+    /// `linear_scan_range` on f64 data.
+    fn search_range(&self, query: &Q, radius: f64) -> Vec<DistPair<f64>> {
         if self.n == 0 {
             return Vec::new();
         }
