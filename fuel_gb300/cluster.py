@@ -170,6 +170,11 @@ def kmeans_batched(problems, *, max_iter=300, order=None, fixed_iters=False, pre
     order = order or _lib.default_order()
     keep, descs, outs = [], [], []
     for data, init in problems:
+        data = np.asarray(data)
+        if data.dtype != np.float32:
+            # kmeans() serves float32 data too; a silent cast would change the answer
+            raise NotImplementedError(
+                f"data has dtype {data.dtype}; the GB300 engine serves float32 (cast with .astype(np.float32))")
         X = np.ascontiguousarray(data, np.float32)
         C0 = np.ascontiguousarray(init, np.float32)
         if X.ndim != 2 or C0.ndim != 2 or X.shape[1] != C0.shape[1]:

@@ -404,6 +404,10 @@ def knn_batched(sets, *, order=None):
     for item in sets:
         data, queries, k = item[0], item[1], int(item[2])
         opts = item[3] if len(item) > 3 else {}
+        if _ensure_float(data).dtype != np.float32 or _ensure_float(queries).dtype != np.float32:
+            # a silent cast would change the answer: fuel searches such data in float64
+            raise NotImplementedError("knn_batched serves float32 sets; search float64 data with SearchIndex "
+                                      "(the exact FP64 scan)")
         X = np.ascontiguousarray(data, np.float32)
         Q = np.ascontiguousarray(queries, np.float32)
         if X.ndim != 2 or Q.ndim != 2 or X.shape[1] != Q.shape[1]:

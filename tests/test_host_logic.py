@@ -39,6 +39,20 @@ def test_float64_is_not_silently_downcast():
         cluster.kmeans(X, k=2, variant="lloyd", init="first")
 
 
+def test_batched_knn_refuses_float64_sets():
+    X = np.zeros((4, 3), np.float64)
+    with pytest.raises(NotImplementedError):
+        search.knn_batched([(X, X, 2)])
+    with pytest.raises(NotImplementedError):
+        search.knn_batched([(X.astype(np.float32), X.astype(np.int32), 2)])
+
+
+def test_batched_kmeans_refuses_non_float32_data():
+    X = np.zeros((6, 3), np.float64)
+    with pytest.raises(NotImplementedError):
+        cluster.kmeans_batched([(X, X[:2])])
+
+
 def test_integer_input_becomes_float64_like_reference():
     assert search._ensure_float(np.zeros((2, 2), np.int32)).dtype == np.float64
 
