@@ -33,14 +33,15 @@ def test_pairwise_sqdist_f64_vectorized(oracle, order):
     assert got.tolist() == [0.0, 20.0, 30.0, 20.0, 0.0, 30.0, 30.0, 30.0, 0.0]
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("order", ORDERS)
-def test_linear_scan_knn_keeps_tie(oracle, order):
-    data = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0]], np.float32)
+def test_linear_scan_knn_keeps_tie(oracle, order, dtype):
+    data = np.array([[0.0, 0.0], [1.0, 0.0], [2.0, 0.0]], dtype)
     idx, dist = oracle.knn_with_ties(data, [1.0, 0.0], 2, metric="euclidean", order=order)
     assert idx.tolist() == [1, 0, 2]
-    assert dist[0] <= dist[1] <= dist[2]
+    assert dist.dtype == dtype and dist[0] <= dist[1] <= dist[2]
     # and the marshalled row is truncated to k (python/search.rs:1195-1216)
-    i2, d2 = oracle.knn(data, np.array([[1.0, 0.0]], np.float32), 2, metric="euclidean", order=order)
+    i2, d2 = oracle.knn(data, np.array([[1.0, 0.0]], dtype), 2, metric="euclidean", order=order)
     assert i2.tolist() == [[1, 0]]
 
 
@@ -52,9 +53,10 @@ def test_linear_scan_range(oracle, order):
     assert idx.tolist() == [0, 1]
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("order", ORDERS)
-def test_precomputed_tie_semantics(oracle, order):
-    pts = np.array([[0.0, 0.0], [0.0, 0.0], [1.0, 0.0], [1.0, 0.0], [2.0, 0.0]], np.float32)
+def test_precomputed_tie_semantics(oracle, order, dtype):
+    pts = np.array([[0.0, 0.0], [0.0, 0.0], [1.0, 0.0], [1.0, 0.0], [2.0, 0.0]], dtype)
     for i in range(len(pts)):
         for k in (1, 2):
             idx, dist = oracle.knn_with_ties(pts, pts[i], k, metric="euclidean", order=order)
