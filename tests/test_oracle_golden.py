@@ -2,6 +2,7 @@
 
 Sources (reference checkout paths):
   src/math/mod.rs:672-690          exact pairwise squared distances (f32 and f64)
+  src/math/mod.rs (tests)          vec_row_sqdist vs the plain sum, 1e-5 relative
   src/search/linear_scan.rs:247-262  k=2 with a tie returns 3 results [1, 0, 2]
   src/search/linear_scan.rs:264-275  range search radius 1.0 returns [0, 1]
   src/search/precomputed.rs:136-165  duplicate points: kNN lists keep all ties
@@ -88,3 +89,32 @@ def test_knn10_golden_f32(oracle):
     X = np.array(g["points"], np.float32)
     idx, dist = oracle.knn(X, X, 10, metric="euclidean", exclude="kplus1")
     assert np.max(np.abs(oracle.knn_outlier(dist.astype(np.float64)) - np.array(ref["KNN-10"]))) <= 1e-6
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("order", ORDERS)
+def test_row_sqdist_layout_cases(oracle, order, dtype):
+    """src/math/mod.rs tests check_row_sqdist_layouts (C-order rows) and
+    check_row_sqdist_strided: vec_row_sqdist -- math::sqdist per row, the
+    order of Lloyd's later passes -- within 1e-5 relative (to max(expected,
+    1)) of the plain sum of squared differences, on the reference's own value
+    ramps and (n, d) sizes."""
+    f64 = dtype == np.float64
+    sizes = [(64, 32), (65, 32), (13, 7) if f64 else (9, 5), (100, 16)]
+    for n, d in sizes:
+        center = (np.arange(d) * 0.1 + 0.5).astype(dtype)
+        pts = (np.arange(n * d) * 0.03 + 0.01).astype(dtype).reshape(n, d)
+        for j in range(n):
+            got = oracle.dist("sqdist", order, center, pts[j])
+            diff = center - pts[j]
+            want = (diff * diff).sum(dtype=dtype)
+            assert abs(got - want) / max(want, 1.0) < 1e-5, (n, d, j)
+    for n, d in [(17, 11), (64, 5)]:
+        center = (np.arange(d) * 0.2 + 0.25).astype(dtype)
+        base = (np.arange(n * d * 2) * 0.01 + 0.03).astype(dtype).reshape(n, 2 * d)
+        pts = np.ascontiguousarray(base[:, ::2])
+        for j in range(n):
+            got = oracle.dist("sqdist", order, center, pts[j])
+            diff = center - pts[j]
+            want = (diff * diff).sum(dtype=dtype)
+            assert abs(got - want) / max(want, 1.0) < 1e-5, (n, d, j)
